@@ -1,0 +1,110 @@
+"""The oracle pinned against the reference: its own golden U.ref files and fixtures produced by running it."""
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle.element import SmallStrainElements
+from oracle.mesh import BoxMesh
+from oracle.nist import NIST, Model, Step
+from oracle.system import csr_slot_map, csr_update, element_dofs, vij_pattern
+
+
+def _box_model(mesh, elType, material, props, dir_sets, nodeforces=(), bodyforce=None, dir_values=None):
+    els = SmallStrainElements(elType, mesh.coords[mesh.elements], material, props)
+    ed = element_dofs(mesh.elements)
+    dirs = []
+    for s, comps in dir_sets:
+        nodes = mesh.nodeSets[s]
+        d = (3 * nodes[:, None] + np.asarray(comps)[None]).ravel()
+        vals = np.tile(np.asarray(dir_values[s] if dir_values and s in dir_values else np.zeros(len(comps))), nodes.size)
+        dirs.append((d, vals))
+    nfs = []
+    for s, comp in nodeforces:
+        nodes = mesh.nodeSets[s]
+        nfs.append(((3 * nodes[:, None] + np.arange(3)[None]).ravel(), np.tile(comp, nodes.size)))
+    return Model(3 * mesh.nNodes, [(els, ed)], dirs, nfs, [(0, bodyforce)] if bodyforce is not None else [])
+
+
+UREF_CASES = {
+    # name: (nX, nY, nZ, lX, lY, lZ, elType, E, nu, dirichlet sets, node forces, body force)
+    "TensionBarHexa8": (4, 4, 30, 5, 5, 500, "C3D8", 1.8e4, 0.22, ["gen_front"], [("gen_back", [0, 0, -4.0])], None),
+    "SimpleBeamHexa8": (200, 2, 2, 2500, 50, 50, "C3D8", 210000, 0.22, ["gen_leftBack", "gen_rightBack"], [("gen_front", [0, 0, -4.16])], None),
+    "WallShearHexa8": (20, 20, 2, 1000, 1000, 5, "C3D8", 2.1e4, 0.22, ["gen_bottom"], [("gen_top", [1.0, 0, 0])], [0, -0.000077, 0]),
+    "WallShearHexa20": (10, 10, 1, 1000, 1000, 5, "C3D20", 2.1e4, 0.22, ["gen_bottom"], [("gen_top", [1.18868, 0, 0])], [0, -0.000077, 0]),
+}  # fmt: skip
+
+
+@pytest.mark.parametrize("name", sorted(UREF_CASES))
+def test_oracle_matches_reference_uref(name):
+    nX, nY, nZ, lX, lY, lZ, elType, E, nu, dsets, nf, bf = UREF_CASES[name]
+    mesh = BoxMesh(nX, nY, nZ, lX, lY, lZ, nNodesPerElement=20 if "20" in elType else 8)
+    model = _box_model(mesh, elType, "linearelastic", [E, nu], [(s, [0, 1, 2]) for s in dsets], nf, None if bf is None else np.array(bf, float))
+    s = NIST(model)
+    U, _ = s.solveStep(Step(maxInc=1.0, minInc=1e-9, maxIter=25, extrapolation="off"))
+    ref = golden(f"uref_{name}.npz")["U"]
+    # the reference runner's own tolerance is 1e-6 (_cli/_run_tests_edelweissfe.py:105)
+    assert np.max(np.abs(U - ref)) < 1e-12
+
+
+ELEM_FIXTURES = [
+    ("C3D8", "linearelastic"),
+    ("C3D8", "vonmises"),
+    ("C3D8", "vonmisesexp"),
+    ("C3D20", "linearelastic"),
+    ("C3D20", "vonmises"),
+]
+
+
+@pytest.mark.parametrize("elType,mat", ELEM_FIXTURES)
+def test_oracle_element_matches_reference(elType, mat):
+    g = golden(f"elem_{elType}_{mat}.npz")
+    els = SmallStrainElements(elType, g["coords"], "vonmises" if mat.startswith("vonmises") else mat, g["props"])
+    els.stateRef[:] = g["state0"]
+    Ke, Pe = els.compute_yourself(g["U"], g["dU"])
+    n = els.nDof
+    Kref = g["Kvij"].reshape(-1, n, n)
+    assert np.max(np.abs(Ke - Kref)) <= 1e-12 * np.max(np.abs(Kref))
+    assert np.max(np.abs(Pe - g["Pe"])) <= 1e-12 * np.max(np.abs(g["Pe"]))
+    s1 = g["state1"]
+    scale = np.max(np.abs(s1), axis=(0, 1)) + 1e-30
+    assert np.max(np.abs(els.stateTemp - s1) / scale) < 1e-12
+
+
+def test_oracle_csr_matches_reference_bitwise():
+    g = golden("csr_small.npz")
+    I, J = vij_pattern(element_dofs(g["elements"]))
+    assert np.array_equal(I, g["I"]) and np.array_equal(J, g["J"])
+    indptr, indices, x = csr_slot_map(I, J, int(g["nDof"]))
+    assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+    data = csr_update(g["V"], x, len(indices))
+    assert np.array_equal(data.view(np.uint64), g["data"].view(np.uint64))
+
+
+def test_oracle_nist_cantilever_matches_reference():
+    g = golden("nist_cantilever_20x4x4.npz")
+    mesh = BoxMesh(20, 4, 4, 10, 2, 2)
+    nf = [("gen_right", [0, 0, -0.25])]
+    nf += [(s, [0, 0, 0.125]) for s in ["gen_rightFront", "gen_rightBack", "gen_bottomRight", "gen_topRight"]]
+    nf += [(s, [0, 0, -0.0625]) for s in ["gen_bottomRightFront", "gen_bottomRightBack", "gen_topRightFront", "gen_topRightBack"]]
+    model = _box_model(mesh, "C3D8", "linearelastic", [210000.0, 0.3], [("gen_left", [0, 1, 2])], nf)
+    s = NIST(model)
+    U, _ = s.solveStep(Step(maxInc=1.0, minInc=1e-6, maxIter=25))
+    assert np.max(np.abs(U - g["U"])) < 1e-12
+    assert [it for _, it in s.history] == list(g["iters"])
+    assert abs(U.min() - (-4.65324e-3)) < 1e-8
+
+
+@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20"])
+def test_oracle_nist_j2_matches_reference(case):
+    g = golden(f"nist_{case}.npz")
+    elType = str(g["elType"])
+    mesh = BoxMesh(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]), nNodesPerElement=20 if "20" in elType else 8)
+    model = _box_model(
+        mesh, elType, "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0],
+        [("gen_left", [0, 1, 2]), ("gen_right", [0])], dir_values={"gen_right": [float(g["ux"])]},
+    )  # fmt: skip
+    s = NIST(model)
+    U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.history] == list(g["iters"])
+    assert np.max(np.abs(U - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
