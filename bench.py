@@ -1,0 +1,437 @@
+"""Benchmark of the GB300 hot path on the 160k-element hex8 J2 model (100x40x40 box).
+
+Workload (one "step" = one load increment of the Newton driver: element loop, 3x3-block
+assembly, Krylov solve, repeated until the reference's convergence test passes):
+  C3D8 box 100x40x40 on 10x4x4, J2 [E=210000, nu=0.3, fy=250, H=1000], x=0 clamped,
+  x=10 face pulled to u_x = 0.02 over 20 increments (maxInc 0.05).  The load history is
+  advanced (untimed) into the plastic regime; every timed step re-solves the same
+  plastic increment from the same committed state (the trial state is not accepted).
+  Inputs are resident and larger than L2 (BSR system 159 MB FP32, state 266 MB).
+
+value     : load-step seconds with the plain block-Jacobi PCG (FP32 inner, FP64 refinement)
+e2e       : the same through the public Python API with the step's inputs (U_n, dU) copied
+            from pinned host memory and the result (U, P) read back every step
+roofline  : the dominant kernel (persistent PCG), bytes per iteration / measured time
+cpu_baseline: the numpy oracle (restatement of the reference's CPU path) on a bounded sample
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nx 100 --ny 40 --nz 40]
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PROPS = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=100)
+    ap.add_argument("--ny", type=int, default=40)
+    ap.add_argument("--nz", type=int, default=40)
+    ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(a):
+    return {
+        "workload": f"hex8 J2 box {a.nx}x{a.ny}x{a.nz} (C3D8, 2x2x2 Gauss), pull 0.02 over 20 increments",
+        "elements": a.nx * a.ny * a.nz,
+        "dofs": 3 * (a.nx + 1) * (a.ny + 1) * (a.nz + 1),
+        "material": "J2 E=210000 nu=0.3 fy=250 H=1000",
+        "timed_increment": a.increment,
+        "l2": "inputs larger than L2 (BSR system and element state resident, > 129 MB)",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")  # fmt: skip
+
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits"],
+                                         capture_output=True, text=True, timeout=5).stdout.strip()  # fmt: skip
+                    if out:
+                        self.samples.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 2 + i and s[2 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}  # fmt: skip
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def build_solver(a, linsolver):
+    from edelweissfe_gb300.mesh import box_mesh
+    from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model
+    from edelweissfe_gb300.solver import NISTGPU
+
+    lX, lY, lZ = 0.1 * a.nx, 0.1 * a.ny, 0.1 * a.nz
+    m = box_mesh(a.nx, a.ny, a.nz, lX, lY, lZ)
+    model = Model(m["coords"], [ElementGroup("C3D8", m["elements"], "vonmises", np.array(PROPS))])
+    dirs = [DirichletBC(m["nodeSets"]["gen_left"], {0: 0.0, 1: 0.0, 2: 0.0}),
+            DirichletBC(m["nodeSets"]["gen_right"], {0: 0.002 * lX})]  # fmt: skip
+    return NISTGPU(model, dirs, linsolver=linsolver)
+
+
+def pcg_bytes_per_iteration(info, fp32=True):
+    """Algorithmic DRAM bytes of one PCG iteration on the BSR(3x3) system."""
+    s = 4 if fp32 else 8
+    nb, nn, nd = info.nBlocks, info.nNodes, info.nDof
+    spmv = nb * (9 * s + 4) + (nn + 1) * 4 + nd * s + nd * s  # values + columns + row pointers + p gather + q write
+    update = nd * s * (2 + 2 + 1 + 1) + nn * 9 * s + nd  # x rw, r rw, q r, z w; block inverses; mask
+    pupdate = nd * s * 3  # z r, p rw
+    return spmv + update + pupdate
+
+
+def assembly_bytes(info, nEl, fp32=True):
+    """Algorithmic DRAM bytes of one assembly (element kernel + condensation + BSR scatter)."""
+    s = 4 if fp32 else 8
+    nQP = 8
+    elem = nEl * (8 * 4 + nQP * 13 * 8 * 2 + 36 * 9 * s + 24 * 8) + info.nDof * 8 * 2  # node ids, state r/w, Ke, Pe, X+dU
+    cond = nEl * 24 * 8 + nEl * 8 * 8 + info.nDof * 8 * 2  # Pe read, map, P and F write
+    scatter = nEl * 36 * 9 * s + nEl * 64 * 8 + info.nBlocks * (9 * s + 8)  # Ke read, map, BSR write
+    return elem, cond, scatter
+
+
+def run_ours(a):
+    import torch
+
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300 import build as b
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, LinSolverOptions, Step
+
+    b.build()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    t0 = time.time()
+    s = build_solver(a, LinSolverOptions(rtol=1e-8, profile=True))
+    setup_s = time.time() - t0
+    info = s.info
+    stream = torch.cuda.current_stream()
+    step = Step(maxInc=0.05, minInc=1e-6, maxIter=25)
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+
+    # advance the load history (untimed) up to the increment that the steps re-solve
+    U = s._vec()
+    dU = s._vec()
+    P = s._vec()
+    prev = None
+    stepper = AdaptiveTimeStepper(0.0, 1.0, step.startInc, step.maxInc, step.minInc, step.maxNumInc)
+    history = []
+    target = None
+    for ts in stepper.generateTimeStep():
+        if ts.number == a.increment:
+            target = ts
+            break
+        U, dU, P, it = s.solveIncrement(U, dU, P, ts, prev, step)
+        _lib.check(s.lib.ef_accept_state(s.ctx), "accept")
+        history.append(it)
+        prev = ts
+    U_n, dU_n = U.clone(), dU.clone()
+
+    def one_step():
+        s.krylovIterations.clear()
+        d = dU_n.clone()
+        _, _, _, it = s.solveIncrement(U_n, d, s._vec(), target, prev, step)
+        return it
+
+    for _ in range(a.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    newton, krylov, kms, klaunch = [], [], 0.0, 0
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(a.steps):
+        s.linsolver.profile = True
+        newton.append(one_step())
+        krylov.append(list(s.krylovIterations))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    # per-solve kernel timing (the persistent PCG launches) from the last timed step
+    prof_ms, prof_it, prof_launch = 0.0, 0, 0
+    for _ in range(1):
+        s.krylovIterations.clear()
+        d = dU_n.clone()
+        infos = []
+        orig = s.linearSolve
+
+        def wrapped(R):
+            x = orig(R)
+            infos.append((s.lastSolveInfo.kernelMs, s.lastSolveInfo.iterations, s.lastSolveInfo.kernelLaunches))
+            return x
+
+        s.linearSolve = wrapped
+        s.solveIncrement(U_n, d, s._vec(), target, prev, step)
+        s.linearSolve = orig
+        prof_ms = sum(i[0] for i in infos)
+        prof_it = sum(i[1] for i in infos)
+        prof_launch = sum(i[2] for i in infos)
+    t_step = ms / 1e3 / a.steps
+    if world > 1:
+        t = torch.tensor([t_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+
+    # assembly timing: element kernel + condensation + BSR scatter on resident inputs
+    ts_ = target
+    t2 = np.array([ts_.stepTime, ts_.totalTime])
+    Pv, Fv = s._vec(), s._vec()
+    times = {"elements": [], "assemble": []}
+    for rep in range(6):
+        ea, eb, ec = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        ea.record(stream)
+        _lib.check(s.lib.ef_compute_elements(s.ctx, U_n.data_ptr(), dU_n.data_ptr(), t2.ctypes.data, ts_.timeIncrement,
+                                             Pv.data_ptr(), Fv.data_ptr(), stream.cuda_stream), "ce")  # fmt: skip
+        eb.record(stream)
+        _lib.check(s.lib.ef_assemble_bsr(s.ctx, stream.cuda_stream), "bsr")
+        ec.record(stream)
+        torch.cuda.synchronize()
+        if rep >= 2:
+            times["elements"].append(ea.elapsed_time(eb))
+            times["assemble"].append(eb.elapsed_time(ec))
+    s.lib.ef_element_status(s.ctx, stream.cuda_stream, None)
+    nEl = a.nx * a.ny * a.nz
+    b_elem, b_cond, b_scat = assembly_bytes(info, nEl)
+    t_el = float(np.median(times["elements"])) * 1e-3
+    t_as = float(np.median(times["assemble"])) * 1e-3
+    asm_gbs = (b_elem + b_cond + b_scat) / (t_el + t_as) / 1e9
+
+    # e2e through the public API: host inputs -> device, solve, results -> host
+    hU = U_n.cpu().pin_memory()
+    hdU = dU_n.cpu().pin_memory()
+    outU = torch.empty(s.nDof, dtype=torch.float64).pin_memory()
+    outP = torch.empty(s.nDof, dtype=torch.float64).pin_memory()
+    e2e_steps = max(1, min(a.steps, 3))
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        Ud = hU.to(dev, non_blocking=True)
+        dUd = hdU.to(dev, non_blocking=True)
+        Unp, _, Pd, _ = s.solveIncrement(Ud, dUd, s._vec(), target, prev, step)
+        outU.copy_(Unp, non_blocking=True)
+        outP.copy_(Pd, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = f0.elapsed_time(f1) / 1e3 / e2e_steps
+
+    peaks, peak_kind = measured_peaks()
+    bpi = pcg_bytes_per_iteration(info)
+    achieved = bpi * prof_it / (prof_ms * 1e-3) / 1e9 if prof_ms > 0 else None
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a, newton_per_step=float(np.mean(newton)),
+                           krylov_per_step=float(np.mean([sum(k) for k in krylov])))  # fmt: skip
+    line = {
+        "metric": "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s",
+        "value": t_step,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": t_step * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 residual/return map, f32 stiffness + Krylov inner, f64 refinement",
+        "data": "synthetic (structured box mesh, seeded parameters)",
+        "config": workload(a),
+        "solver": "block-Jacobi PCG (plain method)",
+        "newton_iterations_per_step": newton,
+        "krylov_iterations_per_step": [sum(k) for k in krylov],
+        "assembly": {"elements_ms": t_el * 1e3, "bsr_scatter_ms": t_as * 1e3, "GBps": asm_gbs,
+                     "frac_hbm": asm_gbs / peaks["hbm_gbs"], "bytes": b_elem + b_cond + b_scat},
+        "dof_iterations_per_s": info.nDof * prof_it / (prof_ms * 1e-3) if prof_ms > 0 else None,
+        "setup_s": setup_s,
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.nDof, "d2h_bytes_per_step": 2 * 8 * s.nDof},
+        "gpu_launches": None,
+        "roofline": {"bound": "hbm", "kernel": "pcg_persistent_kernel<float>", "achieved": achieved,
+                     "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"] if achieved else None, "traffic": None,
+                     "bytes_per_iteration": bpi, "iterations": prof_it, "kernel_ms": prof_ms},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "history_newton": history,
+    }  # fmt: skip
+    # kernel launches in one timed step: per Newton iteration elements+condense+norms (3) + bsr+bj (2)
+    # + per solve the PCG launches and ~8 small refinement kernels per sweep
+    per_newton = 3 + 2
+    line["gpu_launches"] = int(sum(newton) * per_newton + a.steps * 0 + sum(sum(k) > 0 for k in krylov) * 0) + int(
+        prof_launch * (1 + 8) * a.steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(a, newton_per_step, krylov_per_step):
+    """Oracle (numpy restatement of the reference CPU path) on a bounded sample, scaled to one load step.
+
+    Sample: the element loop + CSR update of an element subset, and 30 Jacobi-CG iterations on
+    the full CSR system (scipy), scaled by the GPU run's Newton/Krylov counts per load step."""
+    import scipy.sparse as sp
+
+    from oracle.element import SmallStrainElements
+    from oracle.mesh import BoxMesh
+    from oracle.system import csr_slot_map, csr_update, element_dofs, vij_pattern
+
+    t_start = time.time()
+    nEl = a.nx * a.ny * a.nz
+    m = BoxMesh(a.nx, a.ny, a.nz, 0.1 * a.nx, 0.1 * a.ny, 0.1 * a.nz)
+    sub = min(nEl, 4000)
+    els = SmallStrainElements("C3D8", m.coords[m.elements[:sub]], "vonmises", PROPS)
+    rng = np.random.default_rng(0)
+    dU = rng.normal(0, 2e-4, (sub, 24))
+    t0 = time.perf_counter()
+    Ke, Pe = els.compute_yourself(dU, dU)
+    t_el = (time.perf_counter() - t0) * nEl / sub
+    ed = element_dofs(m.elements[:sub])
+    I, J = vij_pattern(ed)
+    indptr, indices, x = csr_slot_map(I, J, 3 * m.nNodes)
+    t0 = time.perf_counter()
+    csr_update(Ke.reshape(-1), x, len(indices))
+    t_csr = (time.perf_counter() - t0) * nEl / sub
+    # full-size SpMV-dominated CG iterations on a system with the full-size pattern
+    nn = 3 * m.nNodes
+    ed_all = element_dofs(m.elements)
+    Kfull = np.tile(Ke[0].reshape(-1), nEl)
+    Ia, Ja = vij_pattern(ed_all)
+    A = sp.csr_matrix((Kfull, (Ia, Ja)), shape=(nn, nn))
+    del Ia, Ja, Kfull
+    A = A + sp.identity(nn) * 1.0
+    b = np.ones(nn)
+    dinv = 1.0 / A.diagonal()
+    xk = np.zeros(nn)
+    r = b.copy()
+    z = dinv * r
+    p = z.copy()
+    rz = r @ z
+    n_it = 30
+    t0 = time.perf_counter()
+    for _ in range(n_it):
+        q = A @ p
+        al = rz / (p @ q)
+        xk += al * p
+        r -= al * q
+        z = dinv * r
+        rz2 = r @ z
+        p = z + (rz2 / rz) * p
+        rz = rz2
+    t_it = (time.perf_counter() - t0) / n_it
+    load_step = newton_per_step * (t_el + t_csr) + krylov_per_step * t_it
+    return {
+        "value": load_step,
+        "unit": "s",
+        "cores": 1,
+        "kind": "port",
+        "sample": f"element loop + CSR update of {sub} of {nEl} elements (scaled), {n_it} Jacobi-CG iterations on the "
+                  f"full {nn}-DOF CSR system; scaled by {newton_per_step:.1f} Newton and {krylov_per_step:.0f} Krylov "
+                  f"iterations per load step; wall {time.time() - t_start:.0f}s",
+        "element_loop_s": t_el,
+        "csr_update_s": t_csr,
+        "cg_iteration_s": t_it,
+    }  # fmt: skip
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t0 = time.time()
+    # the reference's CPU path timed through the oracle restatement (the reference itself is
+    # Python + Cython and does not travel to the GPU machine); Newton/Krylov counts of the
+    # 10x4x4 reference run scaled to the configuration by the GPU arm are not available here,
+    # so the counts of this configuration are taken as 5 Newton iterations and 2000 CG iterations
+    vals = []
+    for _ in range(max(1, a.steps)):
+        cb = cpu_baseline(a, newton_per_step=5.0, krylov_per_step=2000.0)
+        vals.append(cb["value"])
+    v = float(np.median(vals))
+    line = {
+        "impl": "reference",
+        "metric": "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s",
+        "value": v,
+        "unit": "s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": v * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": workload(a),
+        "cpu_baseline": dict(cb, value=v),
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.time() - t0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)

@@ -1,0 +1,1117 @@
+// C ABI of the efgpu library: context, model setup (element groups, DOF maps, VIJ->CSR
+// slot maps built on the host), and the hot-path entry points declared in include/efgpu.h.
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ef_common.cuh"
+
+// krylov.cu
+int ef_krylov_block_threads();
+size_t ef_barrier_state_bytes();
+size_t ef_pcg_result_bytes();
+ef_status ef_launch_bsr_residual(int nNodes, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
+                                 int mDouble, const double* x, const double* b, const uint8_t* mask, double* y,
+                                 int nSM, cudaStream_t s);
+ef_status ef_pcg_grid(int vDouble, int nSM, int* gridOut);
+ef_status ef_launch_pcg(int vDouble, int grid, int nNodes, const int32_t* rowPtr, const int32_t* colIdx,
+                        const void* vals, const void* binv, const uint8_t* mask, const void* b, void* x, void* r,
+                        void* z, void* pA, void* pB, void* q, double* partA, double* partB, void* bar, void* res,
+                        int maxIter, double rtol2, int* flags, cudaStream_t s);
+ef_status ef_launch_dot(int64_t n, const double* a, const double* b, double* part, int nPart, double* out,
+                        cudaStream_t s);
+ef_status ef_launch_masked_copy(int64_t n, const double* src, const uint8_t* mask, int keepMasked, double scale,
+                                void* dst, int dstDouble, cudaStream_t s);
+ef_status ef_launch_axpy(int64_t n, double a, const void* xs, int xDouble, double* y, cudaStream_t s);
+ef_status ef_launch_add(int64_t n, const double* a, const double* b, double* y, cudaStream_t s);
+
+using namespace ef;
+
+static thread_local std::string g_err;
+void ef_set_error(const std::string& s) { g_err = s; }
+
+#define EF_CHECK(call)                   \
+    do {                                 \
+        ef_status _s = (call);           \
+        if (_s != EF_OK) return _s;      \
+    } while (0)
+
+namespace {
+
+struct PcgResultHost {
+    int iterations;
+    int status;
+    double rr;
+    double bb;
+};
+
+struct HostGroup {
+    std::string elType;
+    int mat;
+    std::vector<double> props;
+    int nEl, nNodes, nQP, tl;
+    std::vector<int32_t> nodeDof;  // [nEl][nNodes]
+};
+
+struct TypeInfo {
+    const char* name;
+    int nNodes;
+    int rule;  // 0: 1 point, 1: 2x2x2, 2: 3x3x3
+    int tl;
+};
+
+const TypeInfo kTypes[] = {
+    {"C3D8", 8, 1, 0},   {"C3D8R", 8, 0, 0},    {"C3D8E", 8, 2, 0},   {"C3D20", 20, 2, 0},
+    {"C3D20R", 20, 1, 0}, {"C3D8TL", 8, 1, 1},  {"C3D20TL", 20, 2, 1}, {"C3D8RTL", 8, 0, 1},
+    {"C3D20RTL", 20, 1, 1},
+};
+
+bool ieq(const char* a, const char* b) {
+    for (; *a && *b; ++a, ++b)
+        if (tolower(*a) != tolower(*b)) return false;
+    return *a == *b;
+}
+
+// parametric node tables (S1, S2, S3) -- elements/displacementelement/_elementcomputationmatrices.py _J3D8/_J3D20
+const int kHex8[8][3] = {{-1, -1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, -1, -1},
+                         {-1, 1, -1},  {-1, 1, 1},  {1, 1, 1},  {1, 1, -1}};
+const int kHex20[20][3] = {{-1, -1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, -1, -1}, {-1, 1, -1}, {-1, 1, 1}, {1, 1, 1},
+                           {1, 1, -1},   {-1, -1, 0}, {0, -1, 1}, {1, -1, 0},  {0, -1, -1}, {-1, 1, 0}, {0, 1, 1},
+                           {1, 1, 0},    {0, 1, -1},  {-1, 0, -1}, {-1, 0, 1}, {1, 0, 1},   {1, 0, -1}};
+
+// Gauss rules of elements/library.py (xi, eta, zeta, w)
+void gauss_rule(int rule, std::vector<double>& xi, std::vector<double>& eta, std::vector<double>& zeta,
+                std::vector<double>& w) {
+    xi.clear();
+    eta.clear();
+    zeta.clear();
+    w.clear();
+    if (rule == 0) {
+        xi = {0.0};
+        eta = {0.0};
+        zeta = {0.0};
+        w = {8.0};
+    } else if (rule == 1) {
+        const double g = 1.0 / sqrt(3.0);
+        const double s8[4] = {-1, 1, 1, -1}, t8[4] = {-1, -1, 1, 1};
+        for (int h = 0; h < 2; ++h)
+            for (int i = 0; i < 4; ++i) {
+                xi.push_back(h ? g : -g);
+                eta.push_back(g * t8[i]);
+                zeta.push_back(g * s8[i]);
+                w.push_back(1.0);
+            }
+    } else {
+        const double r = sqrt(0.6);
+        const double t20[9] = {-1, -1, -1, 0, 0, 0, 1, 1, 1};
+        const double s20[3] = {-1, 0, 1};
+        const double w1 = pow(5.0 / 9.0, 3), w2 = pow(5.0 / 9.0, 2) * (8.0 / 9.0), w3 = (5.0 / 9.0) * pow(8.0 / 9.0, 2),
+                     w4 = pow(8.0 / 9.0, 3);
+        const double wI[3] = {w1, w2, w1}, wII[3] = {w2, w3, w2}, wIII[3] = {w3, w4, w3};
+        const double* wrows[9] = {wI, wII, wI, wII, wIII, wII, wI, wII, wI};
+        for (int h = 0; h < 3; ++h)
+            for (int i = 0; i < 9; ++i) {
+                xi.push_back(r * (h - 1));
+                eta.push_back(r * t20[i]);
+                zeta.push_back(r * s20[i % 3]);
+                w.push_back(wrows[(9 * h + i) / 3][i % 3]);  // 9 groups of 3 over the 27 points
+            }
+    }
+}
+
+void shape(int nn, const double* S, double* N, double dN[3][20]) {
+    for (int a = 0; a < nn; ++a) {
+        const int* sa = nn == 8 ? kHex8[a] : kHex20[a];
+        double f[3], df[3];
+        for (int k = 0; k < 3; ++k) {
+            if (sa[k] != 0) {
+                f[k] = 1.0 + sa[k] * S[k];
+                df[k] = sa[k];
+            } else {
+                f[k] = 1.0 - S[k] * S[k];
+                df[k] = -2.0 * S[k];
+            }
+        }
+        const bool corner = sa[0] != 0 && sa[1] != 0 && sa[2] != 0;
+        if (nn == 8) {
+            N[a] = f[0] * f[1] * f[2] / 8.0;
+            dN[0][a] = df[0] * f[1] * f[2] / 8.0;
+            dN[1][a] = f[0] * df[1] * f[2] / 8.0;
+            dN[2][a] = f[0] * f[1] * df[2] / 8.0;
+        } else if (corner) {
+            const double lin = sa[0] * S[0] + sa[1] * S[1] + sa[2] * S[2] - 2.0;
+            N[a] = f[0] * f[1] * f[2] * lin / 8.0;
+            dN[0][a] = (df[0] * f[1] * f[2] * lin + f[0] * f[1] * f[2] * sa[0]) / 8.0;
+            dN[1][a] = (f[0] * df[1] * f[2] * lin + f[0] * f[1] * f[2] * sa[1]) / 8.0;
+            dN[2][a] = (f[0] * f[1] * df[2] * lin + f[0] * f[1] * f[2] * sa[2]) / 8.0;
+        } else {
+            N[a] = f[0] * f[1] * f[2] / 4.0;
+            dN[0][a] = df[0] * f[1] * f[2] / 4.0;
+            dN[1][a] = f[0] * df[1] * f[2] / 4.0;
+            dN[2][a] = f[0] * f[1] * df[2] / 4.0;
+        }
+    }
+}
+
+void build_tables(const TypeInfo& t, ElemTables& T) {
+    memset(&T, 0, sizeof(T));
+    std::vector<double> xi, eta, zeta, w;
+    gauss_rule(t.rule, xi, eta, zeta, w);
+    T.nNodes = t.nNodes;
+    T.nQP = (int)w.size();
+    T.totalLagrange = t.tl;
+    T.quirk = (t.nNodes == 20 && !t.tl) ? 1 : 0;
+    for (int q = 0; q < T.nQP; ++q) {
+        double N[20], dN[3][20];
+        const double Sb[3] = {eta[q], xi[q], zeta[q]};  // B/J evaluation point
+        shape(t.nNodes, Sb, N, dN);
+        for (int r = 0; r < 3; ++r)
+            for (int a = 0; a < t.nNodes; ++a) {
+                T.dNdS_d[q][r][a] = dN[r][a];
+                T.dNdS_f[q][r][a] = (float)dN[r][a];
+            }
+        const double Sn[3] = {xi[q], eta[q], zeta[q]};  // computeNOperator evaluation point
+        double dN2[3][20];
+        shape(t.nNodes, Sn, N, dN2);
+        for (int a = 0; a < t.nNodes; ++a) T.N[q][a] = N[a];
+        T.w[q] = w[q];
+        T.quirkFac[q] = zeta[q] - xi[q];
+    }
+}
+
+int material_kind(const char* m, int* nProps) {
+    if (ieq(m, "linearelastic")) {
+        *nProps = 2;
+        return MAT_LINEAR_ELASTIC;
+    }
+    if (ieq(m, "vonmises")) {
+        *nProps = 6;
+        return MAT_VON_MISES;
+    }
+    if (ieq(m, "neohookewa")) {
+        *nProps = 2;
+        return MAT_NEOHOOKE_WA;
+    }
+    return -1;
+}
+
+template <typename T>
+T* dalloc(size_t n, ef_status* st) {
+    T* p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        ef_set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        *st = EF_ERR_CUDA;
+        return nullptr;
+    }
+    return p;
+}
+
+// run f(lo, hi) over [0, n) on the host cores
+template <typename F>
+void parallel_for(int64_t n, F f) {
+    unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (n < 100000) nt = 1;
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const int64_t lo = t * chunk, hi = std::min<int64_t>(n, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back([=]() { f(lo, hi); });
+    }
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+struct ef_ctx {
+    int64_t nDof = 0, nNodes = 0, nElements = 0;
+    std::vector<double> hX;
+    double* dX = nullptr;
+    std::vector<HostGroup> hg;
+    std::vector<Group> groups;
+    std::vector<ElemTables*> dTables;
+    bool finalized = false;
+    int keFp64 = 0;
+    int nSM = 0;
+    // element outputs
+    double* Pe = nullptr;
+    int64_t nPe = 0;
+    void* Kblk = nullptr;
+    int64_t nKblk = 0;
+    int* dFlags = nullptr;
+    // condensation map
+    int32_t* dNodeDof = nullptr;
+    int64_t* dCondPtr = nullptr;
+    int64_t* dCondSrc = nullptr;
+    // BSR system
+    int64_t nBlocks = 0;
+    int32_t* dRowPtr = nullptr;
+    int32_t* dColIdx = nullptr;
+    int64_t* dBsrSeg = nullptr;
+    int64_t* dBsrSrc = nullptr;
+    int64_t* dDiagPos = nullptr;
+    void* dBsrVals = nullptr;
+    void* dBinv = nullptr;
+    uint8_t* dMask = nullptr;
+    bool anyDirichlet = false;
+    // scalar CSR (reference layout)
+    bool scalar = false;
+    int64_t nVIJ = 0, nnz = 0;
+    std::vector<int32_t> hIndptr, hIndices;
+    int32_t* dIndptr = nullptr;
+    int32_t* dIndices = nullptr;
+    int64_t* dCsrSeg = nullptr;
+    int32_t* dCsrPerm = nullptr;
+    double* dKvijTmp = nullptr;
+    // reductions / Krylov workspace
+    double* dPart = nullptr;
+    int nPart = 0;
+    double* dRed = nullptr;  // small result buffer
+    int pcgGrid[2] = {0, 0};
+    double *dPartA = nullptr, *dPartB = nullptr;
+    void* dBar = nullptr;
+    void* dPcgRes = nullptr;
+    void* w32[7] = {};  // FP32 Krylov vectors: b, x, r, z, p (two buffers), q
+    double* w64[5] = {};  // FP64: xd, xf, r64, tmp, y
+    // exact refinement: FP64 Gauss-point tangents per group and an element-vector buffer
+    std::vector<double*> dTang;
+    double* dYe = nullptr;
+    bool exact = false;
+    void* w64k[7] = {};   // FP64 Krylov vectors for the all-FP64 mode
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+extern "C" {
+
+int ef_abi_version(void) { return 1; }
+
+const char* ef_last_error(void) { return g_err.c_str(); }
+
+ef_status ef_create(int64_t nDof, const double* nodeCoords, ef_ctx** out) {
+    if (!out || nDof <= 0 || !nodeCoords) {
+        ef_set_error("ef_create: invalid arguments");
+        return EF_ERR_ARG;
+    }
+    if (nDof % 3 != 0 || nDof >= (int64_t)1 << 31) {
+        ef_set_error("ef_create: nDof must be a multiple of 3 (displacement triplets) and < 2^31");
+        return EF_ERR_ARG;
+    }
+    ef_ctx* c = new ef_ctx();
+    c->nDof = nDof;
+    c->nNodes = nDof / 3;
+    c->hX.assign(nodeCoords, nodeCoords + nDof);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->nSM, cudaDevAttrMultiProcessorCount, dev);
+    *out = c;
+    return EF_OK;
+}
+
+void ef_destroy(ef_ctx* c) {
+    if (!c) return;
+    auto F = [](void* p) {
+        if (p) cudaFree(p);
+    };
+    F(c->dX);
+    for (auto& g : c->groups) {
+        F(g.nodeDof);
+        F(g.state[0]);
+        F(g.state[1]);
+        F(g.geo);
+    }
+    for (auto* t : c->dTables) F(t);
+    F(c->Pe);
+    F(c->Kblk);
+    F(c->dFlags);
+    F(c->dNodeDof);
+    F(c->dCondPtr);
+    F(c->dCondSrc);
+    F(c->dRowPtr);
+    F(c->dColIdx);
+    F(c->dBsrSeg);
+    F(c->dBsrSrc);
+    F(c->dDiagPos);
+    F(c->dBsrVals);
+    F(c->dBinv);
+    F(c->dMask);
+    F(c->dIndptr);
+    F(c->dIndices);
+    F(c->dCsrSeg);
+    F(c->dCsrPerm);
+    F(c->dKvijTmp);
+    F(c->dPart);
+    F(c->dRed);
+    F(c->dPartA);
+    F(c->dPartB);
+    F(c->dBar);
+    F(c->dPcgRes);
+    for (auto* p : c->w32) F(p);
+    for (auto* p : c->w64) F(p);
+    for (auto* p : c->w64k) F(p);
+    for (auto* p : c->dTang) F(p);
+    F(c->dYe);
+    for (auto e : c->ev)
+        if (e) cudaEventDestroy(e);
+    delete c;
+}
+
+ef_status ef_add_group(ef_ctx* c, const char* elType, const char* material, const double* props, int nProps,
+                       int nEl, const int32_t* elDofs, int* groupId) {
+    if (!c || !elType || !material || nEl < 0 || (nEl > 0 && !elDofs)) {
+        ef_set_error("ef_add_group: invalid arguments");
+        return EF_ERR_ARG;
+    }
+    if (c->finalized) {
+        ef_set_error("ef_add_group: context already finalized");
+        return EF_ERR_STATE;
+    }
+    if ((int)c->hg.size() >= EF_MAX_GROUPS) {
+        ef_set_error("ef_add_group: too many groups");
+        return EF_ERR_ARG;
+    }
+    const TypeInfo* ti = nullptr;
+    for (const auto& t : kTypes)
+        if (ieq(t.name, elType)) ti = &t;
+    if (!ti) {
+        ef_set_error(std::string("ef_add_group: unknown element type ") + elType);
+        return EF_ERR_ARG;
+    }
+    int need = 0;
+    const int mk = material_kind(material, &need);
+    if (mk < 0) {
+        ef_set_error(std::string("ef_add_group: unknown material ") + material);
+        return EF_ERR_ARG;
+    }
+    if (nProps < need || nProps > 8 || !props) {
+        ef_set_error("ef_add_group: wrong number of material properties");
+        return EF_ERR_ARG;
+    }
+    if ((ti->tl && mk != MAT_NEOHOOKE_WA) || (!ti->tl && mk == MAT_NEOHOOKE_WA)) {
+        ef_set_error("ef_add_group: total-Lagrange elements need a hyperelastic material and vice versa");
+        return EF_ERR_ARG;
+    }
+    if (ti->tl) {
+        ef_set_error("ef_add_group: total-Lagrange elements are not built into this library version");
+        return EF_ERR_ARG;
+    }
+    HostGroup g;
+    g.elType = ti->name;
+    g.mat = mk;
+    g.props.assign(props, props + nProps);
+    g.nEl = nEl;
+    g.nNodes = ti->nNodes;
+    g.tl = ti->tl;
+    ElemTables T;
+    build_tables(*ti, T);
+    g.nQP = T.nQP;
+    const int nd = 3 * ti->nNodes;
+    g.nodeDof.resize((size_t)nEl * ti->nNodes);
+    for (int64_t e = 0; e < nEl; ++e)
+        for (int a = 0; a < ti->nNodes; ++a) {
+            const int32_t d0 = elDofs[e * nd + 3 * a];
+            if (d0 < 0 || d0 + 2 >= c->nDof || d0 % 3 != 0 || elDofs[e * nd + 3 * a + 1] != d0 + 1 ||
+                elDofs[e * nd + 3 * a + 2] != d0 + 2) {
+                ef_set_error("ef_add_group: element DOFs must be in-range node triplets (3n, 3n+1, 3n+2)");
+                return EF_ERR_ARG;
+            }
+            g.nodeDof[e * ti->nNodes + a] = d0;
+        }
+    ef_status st = EF_OK;
+    ElemTables* dT = dalloc<ElemTables>(1, &st);
+    if (!dT) return st;
+    EF_CUDA(cudaMemcpy(dT, &T, sizeof(T), cudaMemcpyHostToDevice));
+    c->dTables.push_back(dT);
+    if (groupId) *groupId = (int)c->hg.size();
+    c->hg.push_back(std::move(g));
+    return EF_OK;
+}
+
+ef_status ef_finalize(ef_ctx* c, int options) {
+    if (!c) return EF_ERR_ARG;
+    if (c->finalized) {
+        ef_set_error("ef_finalize: called twice");
+        return EF_ERR_STATE;
+    }
+    c->keFp64 = (options & EF_OPT_KE_FP64) ? 1 : 0;
+    c->scalar = !(options & EF_OPT_NO_SCALAR_CSR);
+    const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
+    ef_status st = EF_OK;
+    const int64_t nNodes = c->nNodes;
+    c->dX = dalloc<double>(c->nDof, &st);
+    if (!c->dX) return st;
+    EF_CUDA(cudaMemcpy(c->dX, c->hX.data(), sizeof(double) * c->nDof, cudaMemcpyHostToDevice));
+
+    c->dFlags = dalloc<int>(4, &st);
+    if (!c->dFlags) return st;
+    EF_CUDA(cudaMemset(c->dFlags, 0, 4 * sizeof(int)));
+
+    // groups: device node maps and double-buffered SoA state
+    int64_t peOff = 0, keOff = 0, nEl = 0, nVIJ = 0;
+    for (size_t gi = 0; gi < c->hg.size(); ++gi) {
+        const HostGroup& h = c->hg[gi];
+        Group g;
+        memset(&g, 0, sizeof(g));
+        g.nEl = h.nEl;
+        g.nNodes = h.nNodes;
+        g.nQP = h.nQP;
+        g.nDofEl = 3 * h.nNodes;
+        g.nPair = h.nNodes * (h.nNodes + 1) / 2;
+        g.mat = h.mat;
+        g.nState = 12 + (h.mat == MAT_VON_MISES ? 1 : 0);
+        for (size_t i = 0; i < h.props.size(); ++i) g.props[i] = h.props[i];
+        g.nodeDof = dalloc<int32_t>(h.nodeDof.size(), &st);
+        if (!g.nodeDof) return st;
+        EF_CUDA(cudaMemcpy(g.nodeDof, h.nodeDof.data(), sizeof(int32_t) * h.nodeDof.size(), cudaMemcpyHostToDevice));
+        const size_t ns = (size_t)g.nState * h.nEl * h.nQP;
+        for (int k = 0; k < 2; ++k) {
+            g.state[k] = dalloc<double>(ns, &st);
+            if (!g.state[k]) return st;
+            EF_CUDA(cudaMemset(g.state[k], 0, sizeof(double) * ns));
+        }
+        g.cur = 0;
+        g.geo = dalloc<double>((size_t)h.nEl * h.nQP * (3 * h.nNodes + 1), &st);
+        if (!g.geo) return st;
+        EF_CHECK(ef_launch_geometry(g, c->dTables[gi], c->dX, c->dFlags, 0));
+        g.peOffset = peOff;
+        g.keOffset = keOff;
+        g.tablesSlot = (int)gi;
+        peOff += (int64_t)h.nEl * g.nDofEl;
+        keOff += (int64_t)h.nEl * g.nPair;
+        nEl += h.nEl;
+        nVIJ += (int64_t)h.nEl * g.nDofEl * g.nDofEl;
+        c->groups.push_back(g);
+    }
+    c->nElements = nEl;
+    c->nPe = peOff;
+    c->nKblk = keOff;
+    c->nVIJ = nVIJ;
+    c->Pe = dalloc<double>(peOff, &st);
+    if (!c->Pe) return st;
+    c->Kblk = dalloc<char>((size_t)keOff * 9 * ks, &st);
+    if (!c->Kblk) return st;
+
+    // node -> first DOF
+    std::vector<int32_t> nodeDof(nNodes);
+    for (int64_t m = 0; m < nNodes; ++m) nodeDof[m] = (int32_t)(3 * m);
+    c->dNodeDof = dalloc<int32_t>(nNodes, &st);
+    if (!c->dNodeDof) return st;
+    EF_CUDA(cudaMemcpy(c->dNodeDof, nodeDof.data(), sizeof(int32_t) * nNodes, cudaMemcpyHostToDevice));
+
+    // condensation map: node m <- Pe slices of (group, element, local node) in element order
+    std::vector<int64_t> cptr(nNodes + 1, 0);
+    for (const auto& h : c->hg)
+        for (int32_t d : h.nodeDof) cptr[d / 3 + 1]++;
+    for (int64_t m = 0; m < nNodes; ++m) cptr[m + 1] += cptr[m];
+    std::vector<int64_t> csrc(cptr[nNodes]);
+    {
+        std::vector<int64_t> fill(cptr.begin(), cptr.end() - 1);
+        for (size_t gi = 0; gi < c->hg.size(); ++gi) {
+            const auto& h = c->hg[gi];
+            const Group& g = c->groups[gi];
+            for (int64_t e = 0; e < h.nEl; ++e)
+                for (int a = 0; a < h.nNodes; ++a) {
+                    const int64_t m = h.nodeDof[e * h.nNodes + a] / 3;
+                    csrc[fill[m]++] = g.peOffset + e * g.nDofEl + 3 * a;
+                }
+        }
+    }
+    c->dCondPtr = dalloc<int64_t>(nNodes + 1, &st);
+    c->dCondSrc = dalloc<int64_t>(csrc.size(), &st);
+    if (!c->dCondPtr || !c->dCondSrc) return st;
+    EF_CUDA(cudaMemcpy(c->dCondPtr, cptr.data(), sizeof(int64_t) * (nNodes + 1), cudaMemcpyHostToDevice));
+    EF_CUDA(cudaMemcpy(c->dCondSrc, csrc.data(), sizeof(int64_t) * csrc.size(), cudaMemcpyHostToDevice));
+
+    // BSR pattern + block scatter map.  Global block (m, n) = sum over elements (in order) of
+    // K_ab with node(a) = m, node(b) = n; stored pair p(min,max) with a transpose flag if a > b.
+    {
+        std::vector<int64_t> rcount(nNodes + 1, 0);
+        for (const auto& h : c->hg)
+            for (int64_t e = 0; e < h.nEl; ++e)
+                for (int a = 0; a < h.nNodes; ++a) rcount[h.nodeDof[e * h.nNodes + a] / 3 + 1] += h.nNodes;
+        for (int64_t m = 0; m < nNodes; ++m) rcount[m + 1] += rcount[m];
+        const int64_t nEnt = rcount[nNodes];
+        // entries per row: (col node, element-block code); element order is preserved by the fill order
+        std::vector<int32_t> ecol(nEnt);
+        std::vector<int64_t> esrc(nEnt);
+        std::vector<int64_t> fill(rcount.begin(), rcount.end() - 1);
+        for (size_t gi = 0; gi < c->hg.size(); ++gi) {
+            const auto& h = c->hg[gi];
+            const Group& g = c->groups[gi];
+            const int nn = h.nNodes;
+            for (int64_t e = 0; e < h.nEl; ++e)
+                for (int a = 0; a < nn; ++a) {
+                    const int64_t m = h.nodeDof[e * nn + a] / 3;
+                    for (int b = 0; b < nn; ++b) {
+                        const int lo = std::min(a, b), hi = std::max(a, b);
+                        const int p = lo * nn - lo * (lo - 1) / 2 + (hi - lo);
+                        const int64_t blk = g.keOffset + e * g.nPair + p;
+                        const int64_t pos = fill[m]++;
+                        ecol[pos] = h.nodeDof[e * nn + b] / 3;
+                        esrc[pos] = (blk << 1) | (a > b ? 1 : 0);
+                    }
+                }
+        }
+        // per row: stable sort by column, unique columns -> blocks
+        std::vector<int64_t> rowBlocks(nNodes + 1, 0);
+        std::vector<int64_t> order(nEnt);
+        parallel_for(nNodes, [&](int64_t lo, int64_t hi) {
+            for (int64_t m = lo; m < hi; ++m) {
+                const int64_t s = rcount[m], e = rcount[m + 1];
+                for (int64_t i = s; i < e; ++i) order[i] = i;
+                std::stable_sort(order.begin() + s, order.begin() + e,
+                                 [&](int64_t x, int64_t y) { return ecol[x] < ecol[y]; });
+                int64_t nb = 0;
+                for (int64_t i = s; i < e; ++i)
+                    if (i == s || ecol[order[i]] != ecol[order[i - 1]]) ++nb;
+                rowBlocks[m + 1] = nb;
+            }
+        });
+        for (int64_t m = 0; m < nNodes; ++m) rowBlocks[m + 1] += rowBlocks[m];
+        const int64_t nBlocks = rowBlocks[nNodes];
+        if (nBlocks >= ((int64_t)1 << 31)) {
+            ef_set_error("ef_finalize: too many blocks");
+            return EF_ERR_ARG;
+        }
+        c->nBlocks = nBlocks;
+        std::vector<int32_t> rowPtr(nNodes + 1), colIdx(nBlocks);
+        std::vector<int64_t> seg(nBlocks + 1), src(nEnt), diag(nNodes, -1);
+        for (int64_t m = 0; m <= nNodes; ++m) rowPtr[m] = (int32_t)rowBlocks[m];
+        parallel_for(nNodes, [&](int64_t lo, int64_t hi) {
+            for (int64_t m = lo; m < hi; ++m) {
+                int64_t b = rowBlocks[m] - 1;
+                for (int64_t i = rcount[m]; i < rcount[m + 1]; ++i) {
+                    const int64_t o = order[i];
+                    if (i == rcount[m] || ecol[o] != ecol[order[i - 1]]) {
+                        ++b;
+                        colIdx[b] = ecol[o];
+                        seg[b] = i;
+                        if (ecol[o] == m) diag[m] = b;
+                    }
+                    src[i] = esrc[o];
+                }
+            }
+        });
+        seg[nBlocks] = nEnt;
+        for (int64_t m = 0; m < nNodes; ++m)
+            if (diag[m] < 0) {
+                ef_set_error("ef_finalize: a DOF triplet belongs to no element (no diagonal block)");
+                return EF_ERR_ARG;
+            }
+        c->dRowPtr = dalloc<int32_t>(nNodes + 1, &st);
+        c->dColIdx = dalloc<int32_t>(nBlocks, &st);
+        c->dBsrSeg = dalloc<int64_t>(nBlocks + 1, &st);
+        c->dBsrSrc = dalloc<int64_t>(nEnt, &st);
+        c->dDiagPos = dalloc<int64_t>(nNodes, &st);
+        c->dBsrVals = dalloc<char>((size_t)nBlocks * 9 * ks, &st);
+        c->dBinv = dalloc<char>((size_t)nNodes * 9 * ks, &st);
+        c->dMask = dalloc<uint8_t>(c->nDof, &st);
+        if (!c->dRowPtr || !c->dColIdx || !c->dBsrSeg || !c->dBsrSrc || !c->dDiagPos || !c->dBsrVals || !c->dBinv ||
+            !c->dMask)
+            return st;
+        EF_CUDA(cudaMemcpy(c->dRowPtr, rowPtr.data(), sizeof(int32_t) * (nNodes + 1), cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dColIdx, colIdx.data(), sizeof(int32_t) * nBlocks, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dBsrSeg, seg.data(), sizeof(int64_t) * (nBlocks + 1), cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dBsrSrc, src.data(), sizeof(int64_t) * nEnt, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dDiagPos, diag.data(), sizeof(int64_t) * nNodes, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemset(c->dMask, 0, c->nDof));
+    }
+
+    // scalar CSR of the reference (SciPy canonical pattern) + reference-order scatter map
+    if (c->scalar) {
+        if (c->nVIJ >= ((int64_t)1 << 31)) {
+            ef_set_error("ef_finalize: VIJ too long for the scalar CSR map; use EF_OPT_NO_SCALAR_CSR");
+            return EF_ERR_ARG;
+        }
+        // per DOF row r: (element, local index i) occurrences in element order
+        const int64_t nDof = c->nDof;
+        std::vector<int64_t> rptr(nDof + 1, 0);
+        for (const auto& h : c->hg)
+            for (int64_t e = 0; e < h.nEl; ++e)
+                for (int a = 0; a < h.nNodes; ++a)
+                    for (int k = 0; k < 3; ++k) rptr[h.nodeDof[e * h.nNodes + a] + k + 1] += 3 * h.nNodes;
+        for (int64_t r = 0; r < nDof; ++r) rptr[r + 1] += rptr[r];
+        const int64_t nEnt = rptr[nDof];
+        std::vector<int32_t> col(nEnt);
+        std::vector<int32_t> kk(nEnt);
+        std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+        int64_t vijOff = 0;
+        for (size_t gi = 0; gi < c->hg.size(); ++gi) {
+            const auto& h = c->hg[gi];
+            const int nd = 3 * h.nNodes;
+            for (int64_t e = 0; e < h.nEl; ++e) {
+                const int32_t* nd0 = &h.nodeDof[e * h.nNodes];
+                for (int i = 0; i < nd; ++i) {
+                    const int64_t r = nd0[i / 3] + i % 3;  // VIJ value p = i + j*nd -> (row d[i], col d[j])
+                    for (int j = 0; j < nd; ++j) {
+                        const int64_t pos = fill[r]++;
+                        col[pos] = nd0[j / 3] + j % 3;
+                        kk[pos] = (int32_t)(vijOff + e * (int64_t)nd * nd + i + (int64_t)j * nd);
+                    }
+                }
+            }
+            vijOff += (int64_t)h.nEl * nd * nd;
+        }
+        std::vector<int64_t> rowNnz(nDof + 1, 0);
+        parallel_for(nDof, [&](int64_t lo, int64_t hi) {
+            std::vector<std::pair<int32_t, int32_t>> tmp;
+            for (int64_t r = lo; r < hi; ++r) {
+                const int64_t s = rptr[r], e = rptr[r + 1];
+                tmp.resize(e - s);
+                for (int64_t i = s; i < e; ++i) tmp[i - s] = {col[i], kk[i]};
+                std::sort(tmp.begin(), tmp.end());
+                int64_t nb = 0;
+                for (int64_t i = s; i < e; ++i) {
+                    col[i] = tmp[i - s].first;
+                    kk[i] = tmp[i - s].second;
+                    if (i == s || col[i] != col[i - 1]) ++nb;
+                }
+                rowNnz[r + 1] = nb;
+            }
+        });
+        for (int64_t r = 0; r < nDof; ++r) rowNnz[r + 1] += rowNnz[r];
+        const int64_t nnz = rowNnz[nDof];
+        c->nnz = nnz;
+        c->hIndptr.resize(nDof + 1);
+        c->hIndices.resize(nnz);
+        std::vector<int64_t> seg(nnz + 1);
+        for (int64_t r = 0; r <= nDof; ++r) c->hIndptr[r] = (int32_t)rowNnz[r];
+        parallel_for(nDof, [&](int64_t lo, int64_t hi) {
+            for (int64_t r = lo; r < hi; ++r) {
+                int64_t sl = rowNnz[r] - 1;
+                for (int64_t i = rptr[r]; i < rptr[r + 1]; ++i) {
+                    if (i == rptr[r] || col[i] != col[i - 1]) {
+                        ++sl;
+                        c->hIndices[sl] = col[i];
+                        seg[sl] = i;
+                    }
+                }
+            }
+        });
+        seg[nnz] = nEnt;
+        c->dIndptr = dalloc<int32_t>(nDof + 1, &st);
+        c->dIndices = dalloc<int32_t>(nnz, &st);
+        c->dCsrSeg = dalloc<int64_t>(nnz + 1, &st);
+        c->dCsrPerm = dalloc<int32_t>(nEnt, &st);
+        if (!c->dIndptr || !c->dIndices || !c->dCsrSeg || !c->dCsrPerm) return st;
+        EF_CUDA(cudaMemcpy(c->dIndptr, c->hIndptr.data(), sizeof(int32_t) * (nDof + 1), cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dIndices, c->hIndices.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dCsrSeg, seg.data(), sizeof(int64_t) * (nnz + 1), cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dCsrPerm, kk.data(), sizeof(int32_t) * nEnt, cudaMemcpyHostToDevice));
+    }
+
+    // reduction and Krylov workspaces
+    c->nPart = 2 * c->nSM;
+    c->dPart = dalloc<double>(4 * c->nPart, &st);
+    c->dRed = dalloc<double>(16, &st);
+    if (!c->dPart || !c->dRed) return st;
+    EF_CHECK(ef_pcg_grid(0, c->nSM, &c->pcgGrid[0]));
+    EF_CHECK(ef_pcg_grid(1, c->nSM, &c->pcgGrid[1]));
+    const int maxGrid = std::max(c->pcgGrid[0], c->pcgGrid[1]);
+    c->dPartA = dalloc<double>(4 * (size_t)maxGrid, &st);
+    c->dPartB = dalloc<double>(4 * (size_t)maxGrid, &st);
+    c->dBar = dalloc<char>(ef_barrier_state_bytes(), &st);
+    c->dPcgRes = dalloc<char>(ef_pcg_result_bytes(), &st);
+    if (!c->dPartA || !c->dPartB || !c->dBar || !c->dPcgRes) return st;
+    EF_CUDA(cudaMemset(c->dBar, 0, ef_barrier_state_bytes()));
+    for (int i = 0; i < 7; ++i) {
+        c->w32[i] = dalloc<float>(c->nDof, &st);
+        if (!c->w32[i]) return st;
+    }
+    for (int i = 0; i < 5; ++i) {
+        c->w64[i] = dalloc<double>(c->nDof, &st);
+        if (!c->w64[i]) return st;
+    }
+    if (!c->keFp64) {
+        // FP32 system: keep the FP64 tangent for a matrix-free refinement residual
+        for (const auto& g : c->groups) {
+            double* t = dalloc<double>((size_t)9 * g.nEl * g.nQP, &st);
+            if (!t) return st;
+            EF_CUDA(cudaMemset(t, 0, sizeof(double) * 9 * g.nEl * g.nQP));
+            c->dTang.push_back(t);
+        }
+        c->dYe = dalloc<double>(c->nPe, &st);
+        if (!c->dYe) return st;
+        c->exact = true;
+    }
+    for (int i = 0; i < 7; ++i) {
+        c->w64k[i] = dalloc<double>(c->nDof, &st);
+        if (!c->w64k[i]) return st;
+    }
+    EF_CUDA(cudaEventCreate(&c->ev[0]));
+    EF_CUDA(cudaEventCreate(&c->ev[1]));
+    c->finalized = true;
+    return EF_OK;
+}
+
+ef_status ef_get_info(const ef_ctx* c, ef_info* out) {
+    if (!c || !out) return EF_ERR_ARG;
+    out->nDof = c->nDof;
+    out->nNodes = c->nNodes;
+    out->nElements = c->nElements;
+    out->nVIJ = c->nVIJ;
+    out->nnz = c->nnz;
+    out->nBlocks = c->nBlocks;
+    out->nPe = c->nPe;
+    out->keFp64 = c->keFp64;
+    return EF_OK;
+}
+
+#define EF_REQUIRE_FINALIZED(c)                                  \
+    do {                                                         \
+        if (!(c) || !(c)->finalized) {                           \
+            ef_set_error("context missing or not finalized");    \
+            return EF_ERR_STATE;                                 \
+        }                                                        \
+    } while (0)
+
+ef_status ef_compute_elements(ef_ctx* c, const double* U_np, const double* dU, const double* time2, double dT,
+                              double* P, double* F, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    (void)U_np;
+    (void)time2;
+    (void)dT;
+    if (!dU || !P) {
+        ef_set_error("ef_compute_elements: null vector");
+        return EF_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
+    for (size_t gi = 0; gi < c->groups.size(); ++gi) {
+        const Group& g = c->groups[gi];
+        void* K = (char*)c->Kblk + (size_t)g.keOffset * 9 * ks;
+        EF_CHECK(ef_launch_small_strain(g, dU, K, c->keFp64, 0, c->Pe + g.peOffset, c->exact ? c->dTang[gi] : nullptr,
+                                        c->dFlags, s));
+    }
+    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->Pe, P, F, s));
+    return EF_OK;
+}
+
+ef_status ef_element_status(ef_ctx* c, void* stream, double* pNewDT) {
+    EF_REQUIRE_FINALIZED(c);
+    int f = 0;
+    EF_CUDA(cudaMemcpyAsync(&f, c->dFlags, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    EF_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    EF_CUDA(cudaMemsetAsync(c->dFlags, 0, sizeof(int), (cudaStream_t)stream));
+    if (pNewDT) *pNewDT = 1.0;
+    if (f & EF_FLAG_NAN) return EF_NAN;
+    if (f & EF_FLAG_RETURNMAP) {
+        if (pNewDT) *pNewDT = 0.5;
+        return EF_CUTBACK;
+    }
+    if (f & EF_FLAG_BADDET) {
+        ef_set_error("non-positive Jacobian determinant in an element");
+        return EF_ERR_DEVICE;
+    }
+    if (f & EF_FLAG_BARRIER) {
+        ef_set_error("a device-side grid barrier timed out");
+        return EF_ERR_DEVICE;
+    }
+    return EF_OK;
+}
+
+ef_status ef_get_state_size(const ef_ctx* c, int groupId, int* nQP, int* nState) {
+    if (!c || !c->finalized || groupId < 0 || groupId >= (int)c->groups.size()) return EF_ERR_ARG;
+    if (nQP) *nQP = c->groups[groupId].nQP;
+    if (nState) *nState = c->groups[groupId].nState;
+    return EF_OK;
+}
+
+// host AoS [nEl][nQP][nState] <-> device SoA [nState][nEl*nQP]
+ef_status ef_set_state(ef_ctx* c, int groupId, const double* state) {
+    EF_REQUIRE_FINALIZED(c);
+    if (groupId < 0 || groupId >= (int)c->groups.size() || !state) return EF_ERR_ARG;
+    const Group& g = c->groups[groupId];
+    const int64_t nq = (int64_t)g.nEl * g.nQP;
+    std::vector<double> soa((size_t)nq * g.nState);
+    for (int64_t i = 0; i < nq; ++i)
+        for (int v = 0; v < g.nState; ++v) soa[v * nq + i] = state[i * g.nState + v];
+    EF_CUDA(cudaMemcpy(g.state[g.cur], soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice));
+    return EF_OK;
+}
+
+ef_status ef_get_state(ef_ctx* c, int groupId, int trial, double* state) {
+    EF_REQUIRE_FINALIZED(c);
+    if (groupId < 0 || groupId >= (int)c->groups.size() || !state) return EF_ERR_ARG;
+    const Group& g = c->groups[groupId];
+    const int64_t nq = (int64_t)g.nEl * g.nQP;
+    std::vector<double> soa((size_t)nq * g.nState);
+    EF_CUDA(cudaDeviceSynchronize());
+    EF_CUDA(cudaMemcpy(soa.data(), g.state[trial ? 1 - g.cur : g.cur], sizeof(double) * soa.size(),
+                       cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < nq; ++i)
+        for (int v = 0; v < g.nState; ++v) state[i * g.nState + v] = soa[v * nq + i];
+    return EF_OK;
+}
+
+ef_status ef_accept_state(ef_ctx* c) {
+    EF_REQUIRE_FINALIZED(c);
+    for (auto& g : c->groups) g.cur = 1 - g.cur;
+    return EF_OK;
+}
+
+ef_status ef_add_body_force(ef_ctx* c, int groupId, const double* load3, double* PExt, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (groupId < 0 || groupId >= (int)c->groups.size() || !load3 || !PExt) {
+        ef_set_error("ef_add_body_force: invalid arguments");
+        return EF_ERR_ARG;
+    }
+    const Group& g = c->groups[groupId];
+    cudaStream_t s = (cudaStream_t)stream;
+    EF_CHECK(ef_launch_body_force(g, c->dTables[groupId], load3, c->Pe + g.peOffset, s));
+    EF_CHECK(ef_launch_condense_add(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->Pe, g.peOffset,
+                                    g.peOffset + (int64_t)g.nEl * g.nDofEl, PExt, s));
+    return EF_OK;
+}
+
+ef_status ef_export_vij(ef_ctx* c, double* Kvij, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!Kvij) return EF_ERR_ARG;
+    const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
+    int64_t vijOff = 0;
+    for (const auto& g : c->groups) {
+        const void* K = (const char*)c->Kblk + (size_t)g.keOffset * 9 * ks;
+        EF_CHECK(ef_launch_vij_export(g.nEl, g.nNodes, g.nPair, K, c->keFp64, Kvij + vijOff, (cudaStream_t)stream));
+        vijOff += (int64_t)g.nEl * g.nDofEl * g.nDofEl;
+    }
+    return EF_OK;
+}
+
+ef_status ef_csr_pattern(ef_ctx* c, int32_t* indptr, int32_t* indices) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!c->scalar) {
+        ef_set_error("ef_csr_pattern: context finalized with EF_OPT_NO_SCALAR_CSR");
+        return EF_ERR_STATE;
+    }
+    if (indptr) EF_CUDA(cudaMemcpy(indptr, c->hIndptr.data(), sizeof(int32_t) * (c->nDof + 1), cudaMemcpyDefault));
+    if (indices) EF_CUDA(cudaMemcpy(indices, c->hIndices.data(), sizeof(int32_t) * c->nnz, cudaMemcpyDefault));
+    return EF_OK;
+}
+
+ef_status ef_update_csr(ef_ctx* c, const double* Kvij, double* csrData, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!c->scalar || !csrData) {
+        ef_set_error("ef_update_csr: no scalar CSR map or null output");
+        return EF_ERR_STATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!Kvij) {
+        if (!c->dKvijTmp) {
+            ef_status st = EF_OK;
+            c->dKvijTmp = dalloc<double>(c->nVIJ, &st);
+            if (!c->dKvijTmp) return st;
+        }
+        EF_CHECK(ef_export_vij(c, c->dKvijTmp, stream));
+        Kvij = c->dKvijTmp;
+    }
+    return ef_launch_csr_scatter(c->nnz, c->dCsrSeg, c->dCsrPerm, Kvij, csrData, s);
+}
+
+ef_status ef_csr_dirichlet_rows(ef_ctx* c, double* csrData, const int64_t* rows, int64_t nRows, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!c->scalar || !csrData || (nRows > 0 && !rows)) return EF_ERR_ARG;
+    if (nRows == 0) return EF_OK;
+    for (int64_t i = 0; i < nRows; ++i)
+        if (rows[i] < 0 || rows[i] >= c->nDof) {
+            ef_set_error("ef_csr_dirichlet_rows: row out of range");
+            return EF_ERR_ARG;
+        }
+    ef_status st = EF_OK;
+    int64_t* d = dalloc<int64_t>(nRows, &st);
+    if (!d) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaMemcpyAsync(d, rows, sizeof(int64_t) * nRows, cudaMemcpyHostToDevice, s);
+    st = ef_launch_csr_dirichlet_rows(nRows, d, c->dIndptr, c->dIndices, csrData, s);
+    cudaStreamSynchronize(s);
+    cudaFree(d);
+    return st;
+}
+
+ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
+    EF_REQUIRE_FINALIZED(c);
+    std::vector<uint8_t> m(c->nDof, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        if (dofs[i] < 0 || dofs[i] >= c->nDof) {
+            ef_set_error("ef_set_dirichlet: DOF out of range");
+            return EF_ERR_ARG;
+        }
+        m[dofs[i]] = 1;
+    }
+    c->anyDirichlet = n > 0;
+    EF_CUDA(cudaMemcpy(c->dMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
+    return EF_OK;
+}
+
+ef_status ef_assemble_bsr(ef_ctx* c, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    cudaStream_t s = (cudaStream_t)stream;
+    EF_CHECK(ef_launch_bsr_scatter(c->nBlocks, c->dBsrSeg, c->dBsrSrc, c->Kblk, c->keFp64, c->dBsrVals, s));
+    EF_CHECK(ef_launch_bj_setup(c->nNodes, c->dDiagPos, c->dNodeDof, c->dMask, c->dBsrVals, c->keFp64, c->dBinv,
+                                c->dFlags, s));
+    return EF_OK;
+}
+
+ef_status ef_bsr_matvec(ef_ctx* c, const double* x, double* y, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    return ef_launch_bsr_residual((int)c->nNodes, c->dRowPtr, c->dColIdx, c->dBsrVals, c->keFp64, x, nullptr,
+                                  c->anyDirichlet ? c->dMask : nullptr, y, c->nSM, (cudaStream_t)stream);
+}
+
+// r = b - K x on free rows (0 on Dirichlet rows): with the exact FP64 tangent (matrix-free element
+// apply) when the system is stored in FP32, else with the stored system
+static ef_status residual64(ef_ctx* c, const double* x, const double* b, double* r, cudaStream_t s) {
+    if (!c->exact)
+        return ef_launch_bsr_residual((int)c->nNodes, c->dRowPtr, c->dColIdx, c->dBsrVals, c->keFp64, x, b, c->dMask,
+                                      r, c->nSM, s);
+    double* y = c->w64[4];
+    for (size_t gi = 0; gi < c->groups.size(); ++gi) {
+        const Group& g = c->groups[gi];
+        EF_CHECK(ef_launch_small_strain_apply(g, x, c->dTang[gi], c->dYe + g.peOffset, s));
+    }
+    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dYe, y, nullptr, s));
+    return ef_launch_residual_from(c->nDof, b, y, c->dMask, r, s);
+}
+
+static ef_status dot_host(ef_ctx* c, const double* a, const double* b, double* out, cudaStream_t s) {
+    EF_CHECK(ef_launch_dot(c->nDof, a, b, c->dPart, c->nPart, c->dRed, s));
+    EF_CUDA(cudaMemcpyAsync(out, c->dRed, sizeof(double), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    return EF_OK;
+}
+
+// one PCG launch on the free DOFs: solves K d = rhs (rhs zero on Dirichlet DOFs)
+static ef_status run_pcg(ef_ctx* c, int vDouble, const void* rhs, void* sol, int maxIter, double rtol,
+                         PcgResultHost* out, ef_solve_info* prof, cudaStream_t s) {
+    void** w = vDouble ? c->w64k : c->w32;
+    EF_CUDA(cudaMemsetAsync(c->dBar, 0, ef_barrier_state_bytes(), s));
+    if (prof) EF_CUDA(cudaEventRecord(c->ev[0], s));
+    EF_CHECK(ef_launch_pcg(vDouble, c->pcgGrid[vDouble], (int)c->nNodes, c->dRowPtr, c->dColIdx, c->dBsrVals, c->dBinv,
+                           c->dMask, rhs, sol, w[2], w[3], w[4], w[5], w[6], c->dPartA, c->dPartB, c->dBar,
+                           c->dPcgRes, maxIter, rtol * rtol, c->dFlags, s));
+    if (prof) EF_CUDA(cudaEventRecord(c->ev[1], s));
+    EF_CUDA(cudaMemcpyAsync(out, c->dPcgRes, sizeof(PcgResultHost), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    if (prof) {
+        float ms = 0.f;
+        EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        prof->kernelMs += ms;
+        prof->kernelLaunches += 1;
+    }
+    int f = 0;
+    EF_CUDA(cudaMemcpy(&f, c->dFlags, sizeof(int), cudaMemcpyDeviceToHost));
+    if (f & EF_FLAG_BARRIER) {
+        ef_set_error("PCG: grid barrier timed out");
+        return EF_ERR_DEVICE;
+    }
+    return EF_OK;
+}
+
+ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x, ef_solve_info* info, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!o || !b || !x) return EF_ERR_ARG;
+    if (o->method != EF_SOLVE_PCG) {
+        ef_set_error("ef_solve: method not available in this library version");
+        return EF_ERR_ARG;
+    }
+    if (!o->mixed && !c->keFp64) {
+        ef_set_error("ef_solve: an all-FP64 solve needs an FP64 system (EF_OPT_KE_FP64)");
+        return EF_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n = c->nDof;
+    double* xd = c->w64[0];
+    double* xf = c->w64[1];
+    double* r64 = c->w64[2];
+    double* tmp = c->w64[3];
+    ef_solve_info inf;
+    memset(&inf, 0, sizeof(inf));
+    inf.status = EF_OK;
+    double bb = 0.0;
+    EF_CHECK(dot_host(c, b, b, &bb, s));
+    // Dirichlet part: x_d = b on Dirichlet DOFs; lifted RHS b~ = b_f - K_fd x_d
+    EF_CHECK(ef_launch_masked_copy(n, b, c->dMask, 1, 1.0, xd, 1, s));
+    EF_CHECK(residual64(c, xd, b, r64, s));
+    EF_CUDA(cudaMemsetAsync(xf, 0, sizeof(double) * n, s));
+    if (!(bb > 0.0)) {
+        EF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+        inf.relResidual = 0.0;
+        if (info) *info = inf;
+        return EF_OK;
+    }
+    const double bnorm = sqrt(bb);
+    double rr = 0.0;
+    EF_CHECK(dot_host(c, r64, r64, &rr, s));
+    int total = 0;
+    ef_status result = EF_OK;
+    if (!o->mixed) {
+        // all-FP64 PCG to the target tolerance (relative to ||b||)
+        EF_CUDA(cudaMemcpyAsync(c->w64k[0], r64, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        const double rel = rr > 0.0 ? o->rtol * bnorm / sqrt(rr) : 1.0;
+        PcgResultHost pr;
+        if (rr > 0.0) {
+            EF_CHECK(run_pcg(c, 1, c->w64k[0], c->w64k[1], o->maxIter, std::min(rel, 1.0), &pr, o->profile ? &inf : nullptr, s));
+            total = pr.iterations;
+            if (pr.status == EF_NAN) result = EF_NAN;
+            EF_CHECK(ef_launch_axpy(n, 1.0, c->w64k[1], 1, xf, s));
+        }
+    } else {
+        for (int sweep = 0; sweep < o->maxRefine; ++sweep) {
+            if (!(rr == rr)) {
+                result = EF_NAN;
+                break;
+            }
+            if (sqrt(rr) <= o->rtol * bnorm) break;
+            if (total >= o->maxIter) break;
+            const double rn = sqrt(rr);
+            // inner solve of K d = r / ||r|| in the system's precision (FP32 unless EF_OPT_KE_FP64)
+            const int vd = c->keFp64;
+            void** wv = vd ? c->w64k : c->w32;
+            EF_CHECK(ef_launch_masked_copy(n, r64, c->dMask, 0, 1.0 / rn, wv[0], vd, s));
+            const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
+            PcgResultHost pr;
+            EF_CHECK(run_pcg(c, vd, wv[0], wv[1], o->maxIter - total, std::min(inner, 0.5), &pr,
+                             o->profile ? &inf : nullptr, s));
+            total += pr.iterations;
+            inf.refinements++;
+            if (pr.status == EF_NAN) {
+                result = EF_NAN;
+                break;
+            }
+            if (pr.iterations == 0) break;  // no progress possible
+            EF_CHECK(ef_launch_axpy(n, rn, wv[1], vd, xf, s));
+            // r64 = b~ - K x_f  (FP64 accumulation); b~ = b - K x_d on free rows
+            EF_CHECK(ef_launch_add(n, xd, xf, tmp, s));
+            EF_CHECK(residual64(c, tmp, b, r64, s));
+            EF_CHECK(dot_host(c, r64, r64, &rr, s));
+        }
+    }
+    EF_CHECK(ef_launch_add(n, xd, xf, x, s));
+    // final FP64 residual of the full system (Dirichlet rows are exact)
+    EF_CHECK(residual64(c, x, b, r64, s));
+    EF_CHECK(dot_host(c, r64, r64, &rr, s));
+    inf.iterations = total;
+    inf.relResidual = sqrt(rr) / bnorm;
+    if (result == EF_OK && !(inf.relResidual <= o->rtol)) result = (rr == rr) ? EF_NOT_CONVERGED : EF_NAN;
+    inf.status = result;
+    if (info) *info = inf;
+    return result;
+}
+
+ef_status ef_norms(ef_ctx* c, const double* R, const double* F, const double* ddU, double* out, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!out) return EF_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    EF_CHECK(ef_launch_norms(c->nDof, R, F, ddU, c->dPart, c->nPart, c->dRed, s));
+    EF_CUDA(cudaMemcpyAsync(out, c->dRed, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    return EF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Shared definitions of the efgpu CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/efgpu.h"
+
+#define EF_MAX_GROUPS 16
+
+// Status flags written by device code (OR-ed into a per-context int).
+#define EF_FLAG_RETURNMAP 1    // J2 Newton did not converge (reference: CutbackRequest(0.5))
+#define EF_FLAG_NAN 2          // NaN in an element result
+#define EF_FLAG_BARRIER 4      // a grid barrier gave up (bounded spin exhausted)
+#define EF_FLAG_BADDET 8       // non-positive Jacobian determinant
+
+namespace ef {
+
+enum MatKind { MAT_LINEAR_ELASTIC = 0, MAT_VON_MISES = 1, MAT_NEOHOOKE_WA = 2 };
+
+// Constant tables of one element type (shape-function derivatives at the B/J
+// evaluation points, body-force shape functions, weights, hex20 Jacobian quirk).
+struct ElemTables {
+    int nNodes, nQP, totalLagrange, quirk;
+    float dNdS_f[27][3][20];
+    double dNdS_d[27][3][20];
+    double N[27][20];
+    double w[27];
+    double quirkFac[27];  // (zeta - xi) of the B/J point (C3D20 small strain only)
+};
+
+// A homogeneous element group (one element type, one material) on the device.
+struct Group {
+    int elType;   // index into the element table registry
+    int nEl, nNodes, nQP, nDofEl, nPair;
+    int mat;
+    int nState;   // per Gauss point: 12 + material state (small strain) or 1 (TL)
+    double props[8];
+    int32_t* nodeDof;     // [nEl][nNodes]  first global DOF of each element node
+    double* state[2];     // SoA [nState][nEl*nQP]; state[cur] committed, state[1-cur] trial
+    int cur;
+    int64_t peOffset;     // offset of this group's Pe block (doubles) in the context Pe buffer
+    int64_t keOffset;     // offset of this group's Ke blocks (units of 3x3 blocks)
+    int tablesSlot;       // index of the group's element table
+    double* geo;          // geometry cache [nEl*nQP][3*nNodes + 1]: dN/dx and w*detJ (FP64)
+};
+
+struct PropsArg {
+    double v[8];
+};
+
+}  // namespace ef
+
+#define EF_CUDA(call)                                                     \
+    do {                                                                  \
+        cudaError_t _e = (call);                                          \
+        if (_e != cudaSuccess) {                                          \
+            ef_set_error(std::string(#call) + ": " + cudaGetErrorString(_e)); \
+            return EF_ERR_CUDA;                                           \
+        }                                                                 \
+    } while (0)
+
+void ef_set_error(const std::string& s);
+
+// Element kernels (elements.cu)
+ef_status ef_launch_geometry(const ef::Group& g, const ef::ElemTables* T, const double* X, int* flags, cudaStream_t s);
+ef_status ef_launch_small_strain(const ef::Group& g, const double* dU, void* Kout, int kDouble, int kLayoutVIJ,
+                                 double* Pe, double* tang, int* flags, cudaStream_t s);
+ef_status ef_launch_small_strain_apply(const ef::Group& g, const double* x, const double* tang, double* ye,
+                                       cudaStream_t s);
+ef_status ef_launch_body_force(const ef::Group& g, const ef::ElemTables* T, const double load[3], double* Pe,
+                               cudaStream_t s);
+
+// Assembly launchers (assembly.cu)
+ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
+                             const double* Pe, double* P, double* F, cudaStream_t s);
+ef_status ef_launch_condense_add(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
+                                 const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s);
+ef_status ef_launch_vij_export(int nEl, int nn, int np, const void* Kblk, int kDouble, double* Kvij, cudaStream_t s);
+ef_status ef_launch_csr_scatter(int64_t nnz, const int64_t* seg, const int32_t* perm, const double* V, double* data,
+                                cudaStream_t s);
+ef_status ef_launch_csr_dirichlet_rows(int64_t nRows, const int64_t* rows, const int32_t* indptr,
+                                       const int32_t* indices, double* data, cudaStream_t s);
+ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64_t* src, const void* Kblk,
+                                int kDouble, void* vals, cudaStream_t s);
+ef_status ef_launch_bj_setup(int64_t nNodes, const int64_t* diagPos, const int32_t* nodeDof, const uint8_t* mask,
+                             const void* vals, int kDouble, void* inv, int* flags, cudaStream_t s);
+ef_status ef_launch_residual_from(int64_t n, const double* b, const double* y, const uint8_t* mask, double* r,
+                                  cudaStream_t s);
+ef_status ef_launch_norms(int64_t n, const double* R, const double* F, const double* D, double* part, int nPart,
+                          double* out, cudaStream_t s);

@@ -1,0 +1,587 @@
+// Batched small-strain displacement element kernels (C3D8 / C3D20 families).
+//
+// One kernel launch evaluates every element of a group: shape-function
+// gradients, strain increment, the constitutive update per Gauss point
+// (linear elastic or J2 radial return in FP64), the element residual Pe in
+// FP64 and the element stiffness Ke (FP32 or FP64) as 3x3 node-pair blocks.
+//
+// Reference semantics (EdelweissFE):
+//   elements/displacementelement/element.py:290-346   computeYourself
+//   elements/displacementelement/_elementcomputationmatrices.py:306-366,679-817 (hex8)
+//   elements/displacementelement/_elementcomputationmatrices.py:369-495,820+   (hex20)
+//   materials/linearelastic/linearelastic.py:95-125,185-210
+//   materials/vonmises/vonmises.py:35-56,105-124,186-254
+//
+// Thread mapping: TPE threads per element (8 for <= 8 Gauss points, 32
+// otherwise); thread `lane` of an element owns Gauss point `lane` for the
+// constitutive phase, node `lane` for the residual phase and node pairs
+// lane, lane+TPE, ... for the stiffness phase.  Per-element scratch lives in
+// shared memory; the state is structure-of-arrays [var][element*nQP + qp] so
+// that the constitutive phase reads and writes it coalesced.
+
+#include <math.h>
+
+#include "ef_common.cuh"
+
+namespace ef {
+
+constexpr int kBlock = 128;
+
+template <int NN>
+struct PairTab {
+    static constexpr int NP = NN * (NN + 1) / 2;
+};
+
+__device__ __forceinline__ int pair_a(int p, int nn) {
+    // inverse of p(a,b) = a*nn - a*(a-1)/2 + (b-a), a <= b
+    int a = 0;
+    int start = 0;
+    while (start + (nn - a) <= p) {
+        start += nn - a;
+        ++a;
+    }
+    return a;
+}
+
+struct MatOut {
+    double lt, mt, c1;  // tangent C = lt 1x1 + 2 mt I_s - c1 n x n (Voigt, engineering shear)
+    double n[6];
+};
+
+// Linear elastic update: stress += Ei dStrain; tangent Ei  (linearelastic.py:185-210)
+__device__ __forceinline__ void mat_linear_elastic(const double* props, double* sig, const double* de, MatOut& o) {
+    const double E = props[0], nu = props[1];
+    const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double mu = E / (2.0 * (1.0 + nu));
+    const double tr = de[0] + de[1] + de[2];
+    sig[0] += lam * tr + 2.0 * mu * de[0];
+    sig[1] += lam * tr + 2.0 * mu * de[1];
+    sig[2] += lam * tr + 2.0 * mu * de[2];
+    sig[3] += mu * de[3];
+    sig[4] += mu * de[4];
+    sig[5] += mu * de[5];
+    o.lt = lam;
+    o.mt = mu;
+    o.c1 = 0.0;
+}
+
+// J2 radial return with isotropic hardening fy = fy0 + H k + dfy (1 - exp(-delta k)) (vonmises.py:186-254)
+// returns false where the reference raises CutbackRequest
+__device__ __forceinline__ bool mat_von_mises(const double* props, double* sig, double* kappa, const double* de,
+                                              MatOut& o) {
+    const double E = props[0], nu = props[1], fy0 = props[2], HL = props[3], dfy = props[4], dl = props[5];
+    const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double G = E / (2.0 * (1.0 + nu));
+    o.lt = lam;
+    o.mt = G;
+    o.c1 = 0.0;
+    const double nde = sqrt(de[0] * de[0] + de[1] * de[1] + de[2] * de[2] + de[3] * de[3] + de[4] * de[4] +
+                            de[5] * de[5]);
+    if (nde < 1e-14) return true;  // zero-increment shortcut: stress and kappa unchanged, C = Ei
+    double t[6];
+    const double tr = de[0] + de[1] + de[2];
+    t[0] = sig[0] + lam * tr + 2.0 * G * de[0];
+    t[1] = sig[1] + lam * tr + 2.0 * G * de[1];
+    t[2] = sig[2] + lam * tr + 2.0 * G * de[2];
+    t[3] = sig[3] + G * de[3];
+    t[4] = sig[4] + G * de[4];
+    t[5] = sig[5] + G * de[5];
+    const double p = (t[0] + t[1] + t[2]) * (1.0 / 3.0);
+    double d[6] = {t[0] - p, t[1] - p, t[2] - p, t[3], t[4], t[5]};
+    const double dn =
+        sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + 2.0 * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
+    const double k0 = *kappa;
+    const double s23 = 0.81649658092772603;  // sqrt(2/3)
+    const double s6 = 2.4494897427831781;    // sqrt(6)
+    const double fyk = fy0 + HL * k0 + dfy * (1.0 - exp(-dl * k0));
+    if (dn - s23 * fyk > 0.0) {
+        double dk = 0.0;
+        double R = dn - s23 * fyk;
+        int it = 0;
+        while (fabs(R) > 1e-12) {
+            if (it == 15) return false;
+            const double dR = -s6 * G - s23 * (HL + dfy * dl * exp(-dl * (k0 + dk)));
+            dk -= R / dR;
+            ++it;
+            const double kk = k0 + dk;
+            R = dn - s6 * G * dk - s23 * (fy0 + HL * kk + dfy * (1.0 - exp(-dl * kk)));
+        }
+        const double dLam = 1.2247448713915889 * dk;  // sqrt(3/2)
+        const double k1 = k0 + dk;
+        *kappa = k1;
+        const double inv = 1.0 / dn;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            o.n[i] = d[i] * inv;
+            sig[i] = t[i] - 2.0 * G * dLam * o.n[i];
+        }
+        const double hp = HL + dfy * dl * exp(-dl * k1);
+        const double c1 = 2.0 * G * (1.0 / (1.0 + hp / (3.0 * G)) - 2.0 * G * dLam * inv);
+        const double c2 = 4.0 * G * G * dLam * inv;
+        o.c1 = c1;
+        o.lt = lam + c2 * (1.0 / 3.0);
+        o.mt = G - 0.5 * c2;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sig[i] = t[i];
+    }
+    return true;
+}
+
+// Gauss-point geometry in FP64: J = dN/dS x (reference formulation, including the C3D20
+// row-2 Jacobian term), det J and g_a = dN_a/dx = inv(J) dN_a/dS.
+template <int NN>
+__device__ __forceinline__ double qp_geometry(const ElemTables* __restrict__ T, int q, const double (*xr)[3],
+                                              double (*g)[3]) {
+    double J[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double s = 0;
+#pragma unroll
+            for (int a = 0; a < NN; ++a) s += T->dNdS_d[q][r][a] * xr[a][c];
+            J[r][c] = s;
+        }
+    if (NN == 20 && T->quirk) {
+        // reference _J3D20 (_elementcomputationmatrices.py:481-495) row-2 term a5*zeta instead of a5*xi
+        const double f = T->quirkFac[q];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) J[2][c] += f * 0.25 * (-xr[9][c] + xr[11][c] + xr[13][c] - xr[15][c]);
+    }
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    const double id = 1.0 / det;
+    double iJ[3][3];
+    iJ[0][0] = c00 * id;
+    iJ[1][0] = c01 * id;
+    iJ[2][0] = c02 * id;
+    iJ[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+    iJ[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    iJ[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+    iJ[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    iJ[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+    iJ[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            g[a][c] = iJ[c][0] * T->dNdS_d[q][0][a] + iJ[c][1] * T->dNdS_d[q][1][a] + iJ[c][2] * T->dNdS_d[q][2][a];
+    return det;
+}
+
+// Geometry cache, computed once per element group (initializeElement, element.py:194-205):
+// geo[(e*NQ + q) * (3*NN + 1) + 3a + c] = dN_a/dx_c, last entry = w_q det J.
+template <int NN, int NQ>
+__global__ void geometry_kernel(const ElemTables* __restrict__ T, int nEl, const int32_t* __restrict__ nodeDof,
+                                const double* __restrict__ X, double* __restrict__ geo, int* __restrict__ flags) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nEl * NQ) return;
+    const int64_t e = t / NQ;
+    const int q = (int)(t % NQ);
+    double xr[NN][3];
+    const int d0 = nodeDof[e * NN];
+    for (int a = 0; a < NN; ++a) {
+        const int d = nodeDof[e * NN + a];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) xr[a][c] = X[d + c] - X[d0 + c];
+    }
+    double g[NN][3];
+    const double det = qp_geometry<NN>(T, q, xr, g);
+    if (!(det > 0.0)) atomicOr(flags, EF_FLAG_BADDET);
+    double* o = geo + t * (3 * NN + 1);
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[3 * a + c] = g[a][c];
+    o[3 * NN] = T->w[q] * det;
+}
+
+template <int NN, int NQ, typename KT>
+struct SSShared {
+    static constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    static constexpr int EPB = kBlock / TPE;
+    double du[EPB][NN][3];
+    double g[EPB][NQ][NN][3];
+    double sw[EPB][NQ][6];
+    KT tn[EPB][NQ][9];  // lt*w, mt*w, c1*w, n[6]
+};
+
+// Element loop of one group: strain increment, constitutive update, Pe (FP64) and Ke blocks (KT).
+template <int NN, int NQ, typename KT, int MAT, bool VIJ>
+__global__ void __launch_bounds__(kBlock) small_strain_kernel(
+    int nEl, const int32_t* __restrict__ nodeDof, const double* __restrict__ geo, const double* __restrict__ dU,
+    const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props, KT* __restrict__ Kout,
+    double* __restrict__ Pe, double* __restrict__ tang, int* __restrict__ flags) {
+    constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    constexpr int EPB = kBlock / TPE;
+    constexpr int NP = PairTab<NN>::NP;
+    constexpr int ND = 3 * NN;
+    constexpr int NG = 3 * NN + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SSShared<NN, NQ, KT>& sh = *reinterpret_cast<SSShared<NN, NQ, KT>*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int le = tid / TPE;
+    const int lane = tid % TPE;
+    const int e = blockIdx.x * EPB + le;
+    const bool valid = e < nEl;
+
+    if (valid) {
+        for (int a = lane; a < NN; a += TPE) {
+            const int d = nodeDof[(int64_t)e * NN + a];
+            sh.du[le][a][0] = dU[d + 0];
+            sh.du[le][a][1] = dU[d + 1];
+            sh.du[le][a][2] = dU[d + 2];
+        }
+    }
+    __syncthreads();
+
+    // ---- Gauss-point phase ---------------------------------------------------
+    if (valid && lane < NQ) {
+        const int q = lane;
+        const double* gq = geo + ((int64_t)e * NQ + q) * NG;
+        double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int a = 0; a < NN; ++a) {
+            double ga[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ga[c] = gq[3 * a + c];
+                sh.g[le][q][a][c] = ga[c];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) H[i][j] += sh.du[le][a][i] * ga[j];
+        }
+        const double wdet = gq[3 * NN];
+        const double de[6] = {H[0][0], H[1][1], H[2][2], H[0][1] + H[1][0], H[0][2] + H[2][0], H[1][2] + H[2][1]};
+        const int64_t nQPtot = (int64_t)nEl * NQ;
+        const int64_t qi = (int64_t)e * NQ + q;
+        double sig[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sig[i] = stateIn[i * nQPtot + qi];
+        MatOut mo;
+        if (MAT == MAT_VON_MISES) {
+            double kap = stateIn[12 * nQPtot + qi];
+            if (!mat_von_mises(props.v, sig, &kap, de, mo)) atomicOr(flags, EF_FLAG_RETURNMAP);
+            stateOut[12 * nQPtot + qi] = kap;
+            if (!(kap == kap)) atomicOr(flags, EF_FLAG_NAN);
+        } else {
+            mat_linear_elastic(props.v, sig, de, mo);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            stateOut[i * nQPtot + qi] = sig[i];
+            stateOut[(6 + i) * nQPtot + qi] = stateIn[(6 + i) * nQPtot + qi] + de[i];
+            if (!(sig[i] == sig[i])) atomicOr(flags, EF_FLAG_NAN);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sh.sw[le][q][i] = sig[i] * wdet;
+        if (tang) {
+            // FP64 tangent of this Gauss point for the exact (matrix-free) refinement residual
+            tang[0 * nQPtot + qi] = mo.lt * wdet;
+            tang[1 * nQPtot + qi] = mo.mt * wdet;
+            tang[2 * nQPtot + qi] = mo.c1 * wdet;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) tang[(3 + i) * nQPtot + qi] = mo.c1 != 0.0 ? mo.n[i] : 0.0;
+        }
+        sh.tn[le][q][0] = (KT)(mo.lt * wdet);
+        sh.tn[le][q][1] = (KT)(mo.mt * wdet);
+        sh.tn[le][q][2] = (KT)(mo.c1 * wdet);
+        if (mo.c1 != 0.0) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) sh.tn[le][q][3 + i] = (KT)mo.n[i];
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+
+    // ---- residual: Pe_a = -sum_q (sigma w detJ) . g_qa  (FP64 accumulation) ----
+    for (int a = lane; a < NN; a += TPE) {
+        double f0 = 0, f1 = 0, f2 = 0;
+#pragma unroll 4
+        for (int q = 0; q < NQ; ++q) {
+            const double* s = sh.sw[le][q];
+            const double gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
+            f0 += s[0] * gx + s[3] * gy + s[4] * gz;
+            f1 += s[3] * gx + s[1] * gy + s[5] * gz;
+            f2 += s[4] * gx + s[5] * gy + s[2] * gz;
+        }
+        double* pe = Pe + (int64_t)e * ND + 3 * a;
+        pe[0] = -f0;
+        pe[1] = -f1;
+        pe[2] = -f2;
+    }
+
+    // ---- stiffness: K_ab = sum_q lt ga(x)gb + mt (gb(x)ga + ga.gb I) - c1 va(x)vb ----
+    for (int p = lane; p < NP; p += TPE) {
+        const int a = pair_a(p, NN);
+        const int b = a + (p - (a * NN - a * (a - 1) / 2));
+        KT k[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int q = 0; q < NQ; ++q) {
+            const KT* tn = sh.tn[le][q];
+            const KT ga0 = (KT)sh.g[le][q][a][0], ga1 = (KT)sh.g[le][q][a][1], ga2 = (KT)sh.g[le][q][a][2];
+            const KT gb0 = (KT)sh.g[le][q][b][0], gb1 = (KT)sh.g[le][q][b][1], gb2 = (KT)sh.g[le][q][b][2];
+            const KT lt = tn[0], mt = tn[1], c1 = tn[2];
+            const KT s = mt * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
+            const KT la[3] = {lt * ga0, lt * ga1, lt * ga2};
+            const KT ma[3] = {mt * gb0, mt * gb1, mt * gb2};
+            const KT gaa[3] = {ga0, ga1, ga2};
+            const KT gbb[3] = {gb0, gb1, gb2};
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) k[i][j] += la[i] * gbb[j] + ma[i] * gaa[j];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) k[i][i] += s;
+            if (c1 != (KT)0) {
+                const KT* n = tn + 3;
+                const KT va[3] = {n[0] * ga0 + n[3] * ga1 + n[4] * ga2, n[3] * ga0 + n[1] * ga1 + n[5] * ga2,
+                                  n[4] * ga0 + n[5] * ga1 + n[2] * ga2};
+                const KT vb[3] = {n[0] * gb0 + n[3] * gb1 + n[4] * gb2, n[3] * gb0 + n[1] * gb1 + n[5] * gb2,
+                                  n[4] * gb0 + n[5] * gb1 + n[2] * gb2};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) k[i][j] -= c1 * va[i] * vb[j];
+            }
+        }
+        if (VIJ) {
+            // reference VIJ layout: value a*n+b of the element slice holds Ke[a][b]
+            KT* ke = Kout + (int64_t)e * ND * ND;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    ke[(3 * a + i) * ND + 3 * b + j] = k[i][j];
+                    if (a != b) ke[(3 * b + j) * ND + 3 * a + i] = k[i][j];
+                }
+        } else {
+            KT* kb = Kout + ((int64_t)e * NP + p) * 9;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) kb[i * 3 + j] = k[i][j];
+        }
+    }
+}
+
+// y_e = K_e x_e with the FP64 Gauss-point tangents stored by the assembly (matrix-free, FP64).
+// Used for the residual of the iterative refinement, so that a mixed-precision solve is exact
+// for the FP64 tangent.
+template <int NN, int NQ>
+struct ApplyShared {
+    static constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    static constexpr int EPB = kBlock / TPE;
+    double xv[EPB][NN][3];
+    double g[EPB][NQ][NN][3];
+    double sw[EPB][NQ][6];
+};
+
+template <int NN, int NQ>
+__global__ void __launch_bounds__(kBlock) small_strain_apply_kernel(int nEl, const int32_t* __restrict__ nodeDof,
+                                                                    const double* __restrict__ geo,
+                                                                    const double* __restrict__ x,
+                                                                    const double* __restrict__ tang,
+                                                                    double* __restrict__ ye) {
+    constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    constexpr int EPB = kBlock / TPE;
+    constexpr int ND = 3 * NN;
+    constexpr int NG = 3 * NN + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ApplyShared<NN, NQ>& sh = *reinterpret_cast<ApplyShared<NN, NQ>*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int le = tid / TPE;
+    const int lane = tid % TPE;
+    const int e = blockIdx.x * EPB + le;
+    const bool valid = e < nEl;
+    if (valid) {
+        for (int a = lane; a < NN; a += TPE) {
+            const int d = nodeDof[(int64_t)e * NN + a];
+            sh.xv[le][a][0] = x[d + 0];
+            sh.xv[le][a][1] = x[d + 1];
+            sh.xv[le][a][2] = x[d + 2];
+        }
+    }
+    __syncthreads();
+    if (valid && lane < NQ) {
+        const int q = lane;
+        const double* gq = geo + ((int64_t)e * NQ + q) * NG;
+        double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int a = 0; a < NN; ++a) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sh.g[le][q][a][c] = gq[3 * a + c];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) H[i][j] += sh.xv[le][a][i] * sh.g[le][q][a][j];
+        }
+        const double ep[6] = {H[0][0], H[1][1], H[2][2], H[0][1] + H[1][0], H[0][2] + H[2][0], H[1][2] + H[2][1]};
+        const int64_t nQPtot = (int64_t)nEl * NQ;
+        const int64_t qi = (int64_t)e * NQ + q;
+        const double lt = tang[qi], mt = tang[nQPtot + qi], c1 = tang[2 * nQPtot + qi];
+        const double tr = ep[0] + ep[1] + ep[2];
+        double ne = 0.0, n[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) n[i] = 0.0;
+        if (c1 != 0.0) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                n[i] = tang[(3 + i) * nQPtot + qi];
+                ne += n[i] * ep[i];
+            }
+        }
+        // sigma = (lt 1x1 + 2 mt I_s - c1 n x n) eps   (weights already in lt, mt, c1)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sh.sw[le][q][i] = lt * tr + 2.0 * mt * ep[i] - c1 * n[i] * ne;
+#pragma unroll
+        for (int i = 3; i < 6; ++i) sh.sw[le][q][i] = mt * ep[i] - c1 * n[i] * ne;
+    }
+    __syncthreads();
+    if (!valid) return;
+    for (int a = lane; a < NN; a += TPE) {
+        double f0 = 0, f1 = 0, f2 = 0;
+        for (int q = 0; q < NQ; ++q) {
+            const double* s = sh.sw[le][q];
+            const double gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
+            f0 += s[0] * gx + s[3] * gy + s[4] * gz;
+            f1 += s[3] * gx + s[1] * gy + s[5] * gz;
+            f2 += s[4] * gx + s[5] * gy + s[2] * gz;
+        }
+        double* o = ye + (int64_t)e * ND + 3 * a;
+        o[0] = f0;
+        o[1] = f1;
+        o[2] = f2;
+    }
+}
+
+// Consistent body force of a constant load vector (element.py:348-371): Pe[a,c] = load_c sum_q N_qa detJ_q w_q
+template <int NN, int NQ>
+__global__ void body_force_kernel(const ElemTables* __restrict__ T, int nEl, const double* __restrict__ geo,
+                                  double l0, double l1, double l2, double* __restrict__ Pe) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nEl) return;
+    constexpr int NG = 3 * NN + 1;
+    double acc[NN];
+    for (int a = 0; a < NN; ++a) acc[a] = 0.0;
+    for (int q = 0; q < NQ; ++q) {
+        const double wdet = geo[((int64_t)e * NQ + q) * NG + 3 * NN];
+        for (int a = 0; a < NN; ++a) acc[a] += T->N[q][a] * wdet;
+    }
+    for (int a = 0; a < NN; ++a) {
+        Pe[(int64_t)e * 3 * NN + 3 * a + 0] = l0 * acc[a];
+        Pe[(int64_t)e * 3 * NN + 3 * a + 1] = l1 * acc[a];
+        Pe[(int64_t)e * 3 * NN + 3 * a + 2] = l2 * acc[a];
+    }
+}
+
+template <int NN, int NQ, typename KT, int MAT>
+static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, double* Pe, double* tang, int* flags,
+                           cudaStream_t s) {
+    constexpr int EPB = SSShared<NN, NQ, KT>::EPB;
+    const int grid = (g.nEl + EPB - 1) / EPB;
+    PropsArg pa;
+    for (int i = 0; i < 8; ++i) pa.v[i] = g.props[i];
+    const double* sIn = g.state[g.cur];
+    double* sOut = g.state[1 - g.cur];
+    if (grid == 0) return EF_OK;
+    const size_t smem = sizeof(SSShared<NN, NQ, KT>);
+    if (vij) {
+        auto k = small_strain_kernel<NN, NQ, KT, MAT, true>;
+        EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+    } else {
+        auto k = small_strain_kernel<NN, NQ, KT, MAT, false>;
+        EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+    }
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+template <int NN, int NQ>
+static ef_status dispatch_ss(const Group& g, const double* dU, void* K, int kDouble, int vij, double* Pe,
+                             double* tang, int* flags, cudaStream_t s) {
+    if (g.mat == MAT_VON_MISES)
+        return kDouble ? launch_ss<NN, NQ, double, MAT_VON_MISES>(g, dU, K, vij, Pe, tang, flags, s)
+                       : launch_ss<NN, NQ, float, MAT_VON_MISES>(g, dU, K, vij, Pe, tang, flags, s);
+    if (g.mat == MAT_LINEAR_ELASTIC)
+        return kDouble ? launch_ss<NN, NQ, double, MAT_LINEAR_ELASTIC>(g, dU, K, vij, Pe, tang, flags, s)
+                       : launch_ss<NN, NQ, float, MAT_LINEAR_ELASTIC>(g, dU, K, vij, Pe, tang, flags, s);
+    ef_set_error("material not available for small-strain elements");
+    return EF_ERR_ARG;
+}
+
+template <int NN, int NQ>
+static ef_status launch_apply(const Group& g, const double* x, const double* tang, double* ye, cudaStream_t s) {
+    constexpr int EPB = ApplyShared<NN, NQ>::EPB;
+    const int grid = (g.nEl + EPB - 1) / EPB;
+    if (grid == 0) return EF_OK;
+    const size_t smem = sizeof(ApplyShared<NN, NQ>);
+    auto k = small_strain_apply_kernel<NN, NQ>;
+    EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, x, tang, ye);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+template <int NN, int NQ>
+static ef_status launch_geometry(const Group& g, const ElemTables* T, const double* X, int* flags, cudaStream_t s) {
+    const int64_t n = (int64_t)g.nEl * NQ;
+    if (n == 0) return EF_OK;
+    geometry_kernel<NN, NQ><<<(int)((n + 127) / 128), 128, 0, s>>>(T, g.nEl, g.nodeDof, X, g.geo, flags);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+}  // namespace ef
+
+using namespace ef;
+
+#define EF_FOR_TYPES(M) M(8, 8) M(8, 1) M(8, 27) M(20, 27) M(20, 8)
+
+ef_status ef_launch_geometry(const Group& g, const ElemTables* T, const double* X, int* flags, cudaStream_t s) {
+#define EF_G(NN_, NQ_) \
+    if (g.nNodes == NN_ && g.nQP == NQ_) return launch_geometry<NN_, NQ_>(g, T, X, flags, s);
+    EF_FOR_TYPES(EF_G)
+#undef EF_G
+    ef_set_error("unsupported element type");
+    return EF_ERR_ARG;
+}
+
+ef_status ef_launch_small_strain(const Group& g, const double* dU, void* Kout, int kDouble, int kLayoutVIJ,
+                                 double* Pe, double* tang, int* flags, cudaStream_t s) {
+#define EF_SS(NN_, NQ_) \
+    if (g.nNodes == NN_ && g.nQP == NQ_) return dispatch_ss<NN_, NQ_>(g, dU, Kout, kDouble, kLayoutVIJ, Pe, tang, flags, s);
+    EF_FOR_TYPES(EF_SS)
+#undef EF_SS
+    ef_set_error("unsupported element type for the small-strain kernel");
+    return EF_ERR_ARG;
+}
+
+ef_status ef_launch_small_strain_apply(const Group& g, const double* x, const double* tang, double* ye,
+                                       cudaStream_t s) {
+#define EF_AP(NN_, NQ_) \
+    if (g.nNodes == NN_ && g.nQP == NQ_) return launch_apply<NN_, NQ_>(g, x, tang, ye, s);
+    EF_FOR_TYPES(EF_AP)
+#undef EF_AP
+    ef_set_error("unsupported element type for the tangent apply");
+    return EF_ERR_ARG;
+}
+
+ef_status ef_launch_body_force(const Group& g, const ElemTables* T, const double load[3], double* Pe, cudaStream_t s) {
+    const int grid = (g.nEl + 127) / 128;
+    if (grid == 0) return EF_OK;
+#define EF_BF(NN_, NQ_)                                                                                   \
+    if (g.nNodes == NN_ && g.nQP == NQ_) {                                                               \
+        body_force_kernel<NN_, NQ_><<<grid, 128, 0, s>>>(T, g.nEl, g.geo, load[0], load[1], load[2], Pe); \
+        EF_CUDA(cudaGetLastError());                                                                     \
+        return EF_OK;                                                                                    \
+    }
+    EF_FOR_TYPES(EF_BF)
+#undef EF_BF
+    ef_set_error("unsupported element type for body forces");
+    return EF_ERR_ARG;
+}

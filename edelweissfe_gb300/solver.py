@@ -1,0 +1,346 @@
+"""NISTGPU: the reference's Newton driver with its hot path on the GPU.
+
+Mirrors ``solvers/nonlinearimplicitstatic.py`` (NIST) method by method -- same
+names, argument meaning, tolerances and exceptions -- so Newton iteration counts
+match the reference:
+
+* ``solveStep`` :110-332 and ``solveIncrement`` :334-458 run on the host;
+* ``computeElements`` :794-849 -> ``ef_compute_elements`` (element kernels + condensation),
+* ``assembleStiffnessCSR`` :753-769 -> ``ef_assemble_bsr`` (atomic-free 3x3-block scatter),
+* ``applyDirichletK`` :559-593 -> Dirichlet mask (symmetric elimination inside the solver),
+* ``linearSolve`` :727-751 -> ``ef_solve`` (block-Jacobi PCG, FP32 inner + FP64 refinement),
+* ``checkConvergence`` :625-725 -> ``ef_norms`` (device reductions) + the same host logic.
+
+Vectors (U, dU, P, F, R, PExt) live on the GPU as torch float64 tensors; the
+host sees three scalars per Newton iteration.
+"""
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .exceptions import CutbackRequest, DivergingSolution, ReachedMaxIterations, StepFailed
+from .model import BodyForce, DirichletBC, Model, NodeForces
+
+
+@dataclass
+class TimeStep:
+    number: int
+    stepProgressIncrement: float
+    stepProgress: float
+    timeIncrement: float
+    stepTime: float
+    totalTime: float
+
+
+class AdaptiveTimeStepper:
+    """timesteppers/adaptivetimestepper.py: generateTimeStep, preventIncrementIncrease,
+    reduceNextIncrement, discardAndChangeIncrement (a zero first increment; x1.1 after 3 good ones)."""
+
+    def __init__(self, currentTime, stepLength, startIncrement, maxIncrement, minIncrement, maxNumberIncrements,
+                 increaseFactor=1.1):  # fmt: skip
+        self.nPassedGoodIncrements = 0
+        self.incrementCounter = 0
+        self.maxIncrement = maxIncrement
+        self.minIncrement = minIncrement
+        self.maxNumberIncrements = maxNumberIncrements
+        self.finishedStepProgress = 0.0
+        self.increment = min(startIncrement, maxIncrement)
+        self.allowedToIncreasedNext = True
+        self.currentTime = currentTime
+        self.stepLength = stepLength
+        self.increaseFactor = increaseFactor
+
+    def generateTimeStep(self):
+        while self.finishedStepProgress < (1.0 - 1e-15):
+            remainder = 1.0 - self.finishedStepProgress
+            if remainder < self.increment:
+                self.increment = remainder
+            inc = self.increment if self.incrementCounter > 0 else 0.0
+            self.finishedStepProgress += inc
+            t = self.stepLength * self.finishedStepProgress
+            yield TimeStep(self.incrementCounter, inc, self.finishedStepProgress, self.stepLength * inc, t,
+                           self.currentTime + t)  # fmt: skip
+            if self.incrementCounter > self.maxNumberIncrements:
+                raise StepFailed("Reached maximum number of increments")
+            if self.nPassedGoodIncrements >= 3 and self.allowedToIncreasedNext:
+                self.increment = min(self.increment * self.increaseFactor, self.maxIncrement)
+            self.allowedToIncreasedNext = True
+            self.incrementCounter += 1
+            self.nPassedGoodIncrements += 1
+
+    def preventIncrementIncrease(self):
+        self.allowedToIncreasedNext = False
+
+    def discardAndChangeIncrement(self, scaleFactor):
+        if self.incrementCounter == 0:
+            raise StepFailed("Failed zero increment")
+        self.finishedStepProgress -= self.increment
+        self.incrementCounter -= 1
+        self.nPassedGoodIncrements = 0
+        if self.increment == self.minIncrement:
+            raise StepFailed("Cannot reduce increment size")
+        new = self.increment * scaleFactor
+        self.increment = self.maxIncrement if new > self.maxIncrement else max(new, self.minIncrement)
+
+
+@dataclass
+class Step:
+    """Step parameters with the defaults of steps/adaptivestep.py:56-64."""
+
+    stepLength: float = 1.0
+    startInc: float = 1.0
+    maxInc: float = 1.0
+    minInc: float = 1e-4
+    maxNumInc: int = 1000
+    maxIter: int = 10
+    criticalIter: int = 5
+    maxGrowIter: int = 10
+    cutbackFactor: float = 0.25
+    extrapolation: str = "linear"
+
+
+@dataclass
+class LinSolverOptions:
+    method: str = "pcg"  # "pcg" (block-Jacobi CG) or "fgmres"
+    mixed: bool = True  # FP32 inner iterations + FP64 refinement (False: all FP64, needs keFp64)
+    rtol: float = 1e-10  # FP64 ||b - K x|| / ||b||; tight enough that Newton counts match a direct solver
+    innerRtol: float = 1e-4
+    maxIter: int = 20000
+    restart: int = 60
+    maxRefine: int = 30
+    profile: bool = False
+
+
+class NISTGPU:
+    identification = "NISTGPUSolver"
+
+    fieldCorrectionTolerance = 1e-8  # config/phenomena.py displacement
+    fluxResidualTolerance = 1e-8
+    fluxResidualToleranceAlternative = 5e-3
+    acceptableResidual = 1e-6  # largest relative residual of a stalled Krylov solve that is still used
+
+    def __init__(self, model: Model, dirichlets=(), nodeforces=(), bodyforces=(), keFp64=False,
+                 linsolver: LinSolverOptions = None, scalarCSR=False, device="cuda"):  # fmt: skip
+        if not torch.cuda.is_available():
+            raise RuntimeError("NISTGPU needs a CUDA device")
+        self.lib = _lib.lib()
+        self.model = model
+        self.dirichlets = list(dirichlets)
+        self.nodeforces = list(nodeforces)
+        self.bodyforces = list(bodyforces)
+        self.linsolver = linsolver or LinSolverOptions()
+        if not self.linsolver.mixed and not keFp64:
+            raise ValueError("an all-FP64 linear solve needs keFp64=True")
+        self.device = torch.device(device)
+        self.nDof = model.nDof
+        self.ctx = ctypes.c_void_p()
+        X = model.dof_coordinates()
+        _lib.check(self.lib.ef_create(self.nDof, X.ctypes.data, ctypes.byref(self.ctx)), "ef_create")
+        self.groupIds = []
+        for g in model.groups:
+            ed = np.ascontiguousarray(model.element_dofs(g))
+            props = np.ascontiguousarray(np.asarray(g.props, dtype=float))
+            gid = ctypes.c_int()
+            _lib.check(
+                self.lib.ef_add_group(self.ctx, g.elType.encode(), g.material.encode(), props.ctypes.data, props.size,
+                                      ed.shape[0], ed.ctypes.data, ctypes.byref(gid)),
+                "ef_add_group",
+            )  # fmt: skip
+            self.groupIds.append(gid.value)
+        opts = (_lib.EF_OPT_KE_FP64 if keFp64 else 0) | (0 if scalarCSR else _lib.EF_OPT_NO_SCALAR_CSR)
+        _lib.check(self.lib.ef_finalize(self.ctx, opts), "ef_finalize")
+        self.info = _lib.EfInfo()
+        _lib.check(self.lib.ef_get_info(self.ctx, ctypes.byref(self.info)), "ef_get_info")
+        self.nAccumulatedFluxes = model.n_accumulated_fluxes()
+        dirDofs = [d.dofs for d in self.dirichlets]
+        self.dirIdxHost = np.concatenate(dirDofs).astype(np.int64) if dirDofs else np.zeros(0, np.int64)
+        self.dirIdx = torch.as_tensor(self.dirIdxHost, device=self.device)
+        self.computationTimes = {}
+        self.iterationHistory = []  # (increment number, Newton iterations) per converged increment
+        self.krylovIterations = []  # per linear solve
+        self.lastSolveInfo = None
+
+    def __del__(self):
+        try:
+            if getattr(self, "ctx", None) and self.ctx.value:
+                self.lib.ef_destroy(self.ctx)
+                self.ctx = None
+        except Exception:
+            pass
+
+    # -- helpers ------------------------------------------------------------------
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _vec(self):
+        return torch.zeros(self.nDof, dtype=torch.float64, device=self.device)
+
+    def _dirichletDelta(self, timeStep):
+        if not self.dirichlets:
+            return None
+        d = np.concatenate([bc.getDelta(timeStep) for bc in self.dirichlets])
+        return torch.as_tensor(d, device=self.device)
+
+    def _externalLoads(self, timeStep):
+        PExt = self._vec()
+        if self.nodeforces:
+            loads = torch.zeros(self.nDof, dtype=torch.float64)
+            for nf in self.nodeforces:
+                loads.index_add_(0, torch.as_tensor(nf.dofs), torch.as_tensor(nf.getCurrentLoad(timeStep)))
+            PExt += loads.to(self.device)
+        for bf in self.bodyforces:
+            load = np.ascontiguousarray(bf.getCurrentLoad(timeStep))
+            _lib.check(
+                self.lib.ef_add_body_force(self.ctx, self.groupIds[bf.groupId], load.ctypes.data, PExt.data_ptr(),
+                                           self._stream()),
+                "ef_add_body_force",
+            )  # fmt: skip
+        return PExt
+
+    # -- the hot path ---------------------------------------------------------------
+    def computeElements(self, U_np, dU, P, F, timeStep):
+        """Element loop: P = sum Pe, F = sum |Pe| (element order); K stays on the device."""
+        t = np.array([timeStep.stepTime, timeStep.totalTime], dtype=float)
+        _lib.check(
+            self.lib.ef_compute_elements(self.ctx, U_np.data_ptr(), dU.data_ptr(), t.ctypes.data,
+                                         timeStep.timeIncrement, P.data_ptr(), F.data_ptr(), self._stream()),
+            "ef_compute_elements",
+        )  # fmt: skip
+        pNewDT = ctypes.c_double(1.0)
+        st = self.lib.ef_element_status(self.ctx, self._stream(), ctypes.byref(pNewDT))
+        if st == _lib.EF_CUTBACK:
+            raise CutbackRequest("Von Mises Newton failed.", pNewDT.value)
+        if st == _lib.EF_NAN:
+            raise DivergingSolution("Obtained NaN in element evaluation")
+        _lib.check(st, "ef_element_status")
+        return P, F
+
+    def assembleStiffnessCSR(self):
+        _lib.check(self.lib.ef_assemble_bsr(self.ctx, self._stream()), "ef_assemble_bsr")
+
+    def applyDirichletK(self):
+        """The Dirichlet DOFs are eliminated inside the solver (mask set once per step)."""
+
+    def linearSolve(self, R):
+        o = self.linsolver
+        opts = _lib.EfSolveOpts(
+            _lib.EF_SOLVE_FGMRES if o.method == "fgmres" else _lib.EF_SOLVE_PCG,
+            1 if o.mixed else 0, o.rtol, o.innerRtol, o.maxIter, o.restart, o.maxRefine, 1 if o.profile else 0,
+        )  # fmt: skip
+        info = _lib.EfSolveInfo()
+        ddU = self._vec()
+        st = self.lib.ef_solve(self.ctx, ctypes.byref(opts), R.data_ptr(), ddU.data_ptr(), ctypes.byref(info),
+                               self._stream())  # fmt: skip
+        self.lastSolveInfo = info
+        self.krylovIterations.append(info.iterations)
+        if st == _lib.EF_NAN:
+            raise DivergingSolution("Obtained NaN in linear solve")
+        if st == _lib.EF_NOT_CONVERGED:
+            # an inexact Newton step is kept while the Krylov solve got close to its target (very
+            # ill-conditioned systems stagnate above rtol in FP64); Newton's own convergence test decides
+            if not (info.relResidual <= self.acceptableResidual):
+                raise DivergingSolution(f"Krylov solve stalled at relative residual {info.relResidual:.2e}")
+            return ddU
+        _lib.check(st, "ef_solve")
+        return ddU
+
+    def checkConvergence(self, R, ddU, F, iterationCounter, residualHistory):
+        out = np.zeros(3)
+        _lib.check(
+            self.lib.ef_norms(self.ctx, R.data_ptr(), F.data_ptr(), None if ddU is None else ddU.data_ptr(),
+                              out.ctypes.data, self._stream()),
+            "ef_norms",
+        )  # fmt: skip
+        fluxResidual, sumF, corr = out
+        spatialAveragedFlux = max(1e-10, sumF / self.nAccumulatedFluxes)
+        tol = self.fluxResidualTolerance if iterationCounter < 15 else self.fluxResidualToleranceAlternative
+        fieldCorrection = corr if ddU is not None else 0.0
+        convergedCorrection = fieldCorrection < self.fieldCorrectionTolerance
+        convergedFlux = fluxResidual <= max(tol * spatialAveragedFlux, 1e-7)
+        prev, nGrew = residualHistory["displacement"]
+        if fluxResidual > prev:
+            nGrew += 1
+        residualHistory["displacement"] = (fluxResidual, nGrew)
+        return convergedCorrection and convergedFlux
+
+    # -- Newton loop (same control flow as NIST.solveIncrement) ------------------------
+    def extrapolateLastIncrement(self, extrapolation, timeStep, dU, prevTimeStep):
+        if extrapolation == "linear" and prevTimeStep is not None and prevTimeStep.timeIncrement:
+            dU *= timeStep.stepProgressIncrement / prevTimeStep.stepProgressIncrement
+            if self.dirichlets:
+                dU[self.dirIdx] = self._dirichletDelta(timeStep)
+            return dU, True
+        dU.zero_()
+        return dU, False
+
+    def solveIncrement(self, U_n, dU, P, timeStep, prevTimeStep, step: Step):
+        iterationCounter = 0
+        residualHistory = {"displacement": (0.0, 0)}
+        R = self._vec()
+        F = self._vec()
+        U_np = self._vec()
+        ddU = None
+        dU, isExtrapolated = self.extrapolateLastIncrement(step.extrapolation, timeStep, dU, prevTimeStep)
+        PExt = self._externalLoads(timeStep)
+        while True:
+            torch.add(U_n, dU, out=U_np)
+            P, F = self.computeElements(U_np, dU, P, F, timeStep)
+            torch.add(P, PExt, out=R)
+            if iterationCounter == 0 and not isExtrapolated and self.dirichlets:
+                R[self.dirIdx] = self._dirichletDelta(timeStep)
+            else:
+                if self.dirichlets:
+                    R[self.dirIdx] = 0.0
+                if self.checkConvergence(R, ddU, F, iterationCounter, residualHistory):
+                    break
+                if residualHistory["displacement"][1] > step.maxGrowIter:
+                    raise DivergingSolution(f"Residual grew {step.maxGrowIter} times, cutting back")
+                if iterationCounter == step.maxIter:
+                    raise ReachedMaxIterations("Reached max. iterations in current increment, cutting back")
+            self.assembleStiffnessCSR()
+            self.applyDirichletK()
+            ddU = self.linearSolve(R)
+            dU += ddU
+            iterationCounter += 1
+        return U_np, dU, P, iterationCounter
+
+    def solveStep(self, step: Step, maxIncrements=None, callback=None):
+        """Runs the adaptive increment loop of the step; returns (U, P) as device tensors."""
+        _lib.check(self.lib.ef_set_dirichlet(self.ctx, self.dirIdxHost.ctypes.data, self.dirIdxHost.size),
+                   "ef_set_dirichlet")  # fmt: skip
+        U = self._vec()
+        dU = self._vec()
+        P = self._vec()
+        prevTimeStep = None
+        stepper = AdaptiveTimeStepper(0.0, step.stepLength, step.startInc, step.maxInc, step.minInc, step.maxNumInc)
+        done = 0
+        for timeStep in stepper.generateTimeStep():
+            try:
+                U_np, dU, P, iters = self.solveIncrement(U, dU, P, timeStep, prevTimeStep, step)
+            except CutbackRequest as e:
+                stepper.discardAndChangeIncrement(max(e.cutbackSize, step.cutbackFactor))
+                prevTimeStep = None
+                self.iterationHistory.append((timeStep.number, math.inf))
+                continue
+            except (ReachedMaxIterations, DivergingSolution):
+                stepper.discardAndChangeIncrement(step.cutbackFactor)
+                prevTimeStep = None
+                self.iterationHistory.append((timeStep.number, math.inf))
+                continue
+            U = U_np
+            prevTimeStep = timeStep
+            if iters >= step.criticalIter:
+                stepper.preventIncrementIncrease()
+            _lib.check(self.lib.ef_accept_state(self.ctx), "ef_accept_state")
+            self.iterationHistory.append((timeStep.number, iters))
+            if callback is not None:
+                callback(timeStep, iters, U)
+            done += 1
+            if maxIncrements is not None and done >= maxIncrements:
+                break
+        return U, P

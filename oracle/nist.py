@@ -172,7 +172,9 @@ class NIST:
 
     # -- Newton loop -----------------------------------------------------------------
     def _dirichletDelta(self, ts):
-        return np.concatenate([v * ts.stepProgressIncrement for _, v in self.model.dirichlet])
+        # stepactions/dirichlet.py getDelta: delta * (f(t) - f(t - dt)), f(t) = t
+        a = ts.stepProgress
+        return np.concatenate([v * (a - (a - ts.stepProgressIncrement)) for _, v in self.model.dirichlet])
 
     def _externalLoads(self, ts):
         PExt = np.zeros(self.model.nDof)

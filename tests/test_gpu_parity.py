@@ -1,0 +1,224 @@
+"""GPU parity of the hot path (through the C ABI) against the reference's fixtures and the oracle."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from cases import UREF_CASES, build_gpu_solver, cantilever_spec, j2_box_spec, uref_spec
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx_for_elements(lib, elType, material, props, coords, keFp64, scalar=False):
+    """One context whose elements own disjoint nodes, so P equals the stacked Pe."""
+    from edelweissfe_gb300 import _lib
+
+    nEl, nn, _ = coords.shape
+    nDof = 3 * nEl * nn
+    X = np.ascontiguousarray(coords.reshape(-1))
+    ctx = ctypes.c_void_p()
+    _lib.check(lib.ef_create(nDof, X.ctypes.data, ctypes.byref(ctx)), "ef_create")
+    ed = np.arange(nDof, dtype=np.int32).reshape(nEl, 3 * nn)
+    p = np.ascontiguousarray(np.asarray(props, float))
+    gid = ctypes.c_int()
+    _lib.check(lib.ef_add_group(ctx, elType.encode(), material.encode(), p.ctypes.data, p.size, nEl, ed.ctypes.data,
+                                ctypes.byref(gid)), "ef_add_group")  # fmt: skip
+    opts = (_lib.EF_OPT_KE_FP64 if keFp64 else 0) | (0 if scalar else _lib.EF_OPT_NO_SCALAR_CSR)
+    _lib.check(lib.ef_finalize(ctx, opts), "ef_finalize")
+    return ctx, nDof
+
+
+ELEM = [("C3D8", "linearelastic"), ("C3D8", "vonmises"), ("C3D8", "vonmisesexp"), ("C3D20", "linearelastic"),
+        ("C3D20", "vonmises")]  # fmt: skip
+
+
+@pytest.mark.parametrize("keFp64", [True, False], ids=["fp64", "fp32K"])
+@pytest.mark.parametrize("elType,mat", ELEM)
+def test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, keFp64):
+    from edelweissfe_gb300 import _lib
+
+    g = golden(f"elem_{elType}_{mat}.npz")
+    material = "vonmises" if mat.startswith("vonmises") else mat
+    ctx, nDof = _ctx_for_elements(gpu_lib, elType, material, g["props"], g["coords"], keFp64)
+    try:
+        state0 = np.ascontiguousarray(g["state0"])  # keep alive across the call
+        _lib.check(gpu_lib.ef_set_state(ctx, 0, state0.ctypes.data), "ef_set_state")
+        dev = torch.device("cuda")
+        U = torch.as_tensor(g["U"].reshape(-1), device=dev)
+        dU = torch.as_tensor(g["dU"].reshape(-1), device=dev)
+        P = torch.zeros(nDof, dtype=torch.float64, device=dev)
+        F = torch.zeros_like(P)
+        t = np.array([0.5, 0.5])
+        _lib.check(gpu_lib.ef_compute_elements(ctx, U.data_ptr(), dU.data_ptr(), t.ctypes.data, 0.1, P.data_ptr(),
+                                               F.data_ptr(), None), "ef_compute_elements")  # fmt: skip
+        assert gpu_lib.ef_element_status(ctx, None, None) == _lib.EF_OK
+        info = _lib.EfInfo()
+        gpu_lib.ef_get_info(ctx, ctypes.byref(info))
+        K = torch.zeros(info.nVIJ, dtype=torch.float64, device=dev)
+        _lib.check(gpu_lib.ef_export_vij(ctx, K.data_ptr(), None), "ef_export_vij")
+        torch.cuda.synchronize()
+        n = 3 * g["coords"].shape[1]
+        Kref = g["Kvij"].reshape(-1, n, n)
+        Kg = K.cpu().numpy().reshape(-1, n, n)
+        Pe = P.cpu().numpy().reshape(g["Pe"].shape)
+        st = np.zeros_like(g["state1"])
+        _lib.check(gpu_lib.ef_get_state(ctx, 0, 1, st.ctypes.data), "ef_get_state")
+        # geometry, strain, return map and residual are FP64 in both modes; only Ke is FP32 in
+        # the fast mode (relative rounding 6e-8 per operation)
+        tolK, tolP, tolS = (1e-11, 1e-11, 1e-11) if keFp64 else (2e-6, 1e-11, 1e-11)
+        assert np.max(np.abs(Kg - Kref)) <= tolK * np.max(np.abs(Kref))
+        assert np.max(np.abs(Pe - g["Pe"])) <= tolP * np.max(np.abs(g["Pe"]))
+        scale = np.max(np.abs(g["state1"]), axis=(0, 1)) + 1e-30
+        assert np.max(np.abs(st - g["state1"]) / scale) <= tolS
+        assert np.array_equal(F.cpu().numpy(), np.abs(P.cpu().numpy()))
+    finally:
+        gpu_lib.ef_destroy(ctx)
+
+
+def test_csr_pattern_and_update_bitwise_match_reference(gpu_lib):
+    """CSRGenerator.__init__ pattern and updateCSR data, bit for bit (numerics/csrgenerator.pyx)."""
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300.mesh import box_mesh
+
+    g = golden("csr_small.npz")
+    m = box_mesh(3, 2, 2)
+    assert np.array_equal(m["elements"], g["elements"])
+    nDof = int(g["nDof"])
+    ctx = ctypes.c_void_p()
+    X = m["coords"].reshape(-1).copy()
+    _lib.check(gpu_lib.ef_create(nDof, X.ctypes.data, ctypes.byref(ctx)), "ef_create")
+    try:
+        ed = (3 * m["elements"][:, :, None] + np.arange(3)).reshape(m["elements"].shape[0], -1).astype(np.int32)
+        p = np.array([210000.0, 0.3])
+        gid = ctypes.c_int()
+        _lib.check(gpu_lib.ef_add_group(ctx, b"C3D8", b"linearelastic", p.ctypes.data, 2, ed.shape[0], ed.ctypes.data,
+                                        ctypes.byref(gid)), "ef_add_group")  # fmt: skip
+        _lib.check(gpu_lib.ef_finalize(ctx, _lib.EF_OPT_KE_FP64), "ef_finalize")
+        info = _lib.EfInfo()
+        gpu_lib.ef_get_info(ctx, ctypes.byref(info))
+        assert info.nnz == len(g["indices"]) and info.nVIJ == len(g["V"])
+        indptr = np.zeros(nDof + 1, np.int32)
+        indices = np.zeros(info.nnz, np.int32)
+        _lib.check(gpu_lib.ef_csr_pattern(ctx, indptr.ctypes.data, indices.ctypes.data), "ef_csr_pattern")
+        assert np.array_equal(indptr, g["indptr"]) and np.array_equal(indices, g["indices"])
+        V = torch.as_tensor(g["V"], device="cuda")
+        data = torch.zeros(info.nnz, dtype=torch.float64, device="cuda")
+        _lib.check(gpu_lib.ef_update_csr(ctx, V.data_ptr(), data.data_ptr(), None), "ef_update_csr")
+        d = data.cpu().numpy()
+        assert np.array_equal(d.view(np.uint64), g["data"].view(np.uint64))
+        # applyDirichletK rows (mk2.pyx:66-109) on the same data
+        rows = np.array([0, 5, 17], dtype=np.int64)
+        _lib.check(gpu_lib.ef_csr_dirichlet_rows(ctx, data.data_ptr(), rows.ctypes.data, rows.size, None), "dir")
+        d2 = data.cpu().numpy()
+        for r in rows:
+            s, e = indptr[r], indptr[r + 1]
+            assert np.array_equal(d2[s:e], np.where(indices[s:e] == r, 1.0, 0.0))
+    finally:
+        gpu_lib.ef_destroy(ctx)
+
+
+@pytest.mark.parametrize("name", sorted(UREF_CASES))
+def test_nist_gpu_matches_reference_uref(gpu_lib, name):
+    """The reference's golden solutions (slender beams and thin plates: condition numbers up to
+    ~1e9, so the all-FP64 block-Jacobi CG with a high iteration cap)."""
+    from edelweissfe_gb300.solver import LinSolverOptions, Step
+
+    s = build_gpu_solver(uref_spec(name), keFp64=True, linsolver=LinSolverOptions(mixed=False, maxIter=200000))
+    U, _ = s.solveStep(Step(maxInc=1.0, minInc=1e-9, maxIter=25, extrapolation="off"))
+    ref = golden(f"uref_{name}.npz")["U"]
+    err = np.max(np.abs(U.cpu().numpy() - ref))
+    # reference runner tolerance 1e-6 absolute (_cli/_run_tests_edelweissfe.py:105)
+    assert err < 1e-6 * max(1.0, np.max(np.abs(ref))), err
+    assert [it for _, it in s.iterationHistory] == [1, 2]
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_nist_gpu_cantilever_config1(gpu_lib, mode):
+    from edelweissfe_gb300.solver import LinSolverOptions, Step
+
+    fp64 = mode == "fp64"
+    g = golden("nist_cantilever_20x4x4.npz")
+    s = build_gpu_solver(cantilever_spec(), keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
+    U, _ = s.solveStep(Step(maxInc=1.0, minInc=1e-6, maxIter=25))
+    u = U.cpu().numpy()
+    assert np.max(np.abs(u - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+    assert [it for _, it in s.iterationHistory] == list(g["iters"])
+    assert abs(u.min() - (-4.65324e-3)) < 1e-8
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20"])
+def test_nist_gpu_j2_matches_reference(gpu_lib, case, mode):
+    """3D J2 boxes: identical Newton iteration counts, displacements within 1e-6 relative."""
+    from edelweissfe_gb300.solver import LinSolverOptions, Step
+
+    g = golden(f"nist_{case}.npz")
+    fp64 = mode == "fp64"
+    spec = j2_box_spec(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]),
+                       str(g["elType"]), ux=float(g["ux"]))  # fmt: skip
+    s = build_gpu_solver(spec, keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
+    U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.iterationHistory] == list(g["iters"])
+    assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+
+
+def test_assembly_is_bit_reproducible(gpu_lib):
+    """No float atomics: two evaluations give bit-identical P, F and K x."""
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300.solver import TimeStep
+
+    s = build_gpu_solver(j2_box_spec(12, 6, 6, 1.2, 0.6, 0.6))
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    dU = 1e-3 * torch.randn(s.nDof, dtype=torch.float64, device="cuda", generator=gen)
+    ts = TimeStep(1, 0.1, 0.1, 0.1, 0.1, 0.1)
+    outs = []
+    for _ in range(2):
+        P, F = s._vec(), s._vec()
+        s.computeElements(dU, dU, P, F, ts)
+        s.assembleStiffnessCSR()
+        y = s._vec()
+        _lib.check(s.lib.ef_bsr_matvec(s.ctx, dU.data_ptr(), y.data_ptr(), None), "matvec")
+        outs.append([P.clone(), F.clone(), y.clone()])
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
+def test_pcg_reaches_tolerance_and_matches_direct_solve(gpu_lib):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300.solver import TimeStep
+
+    s = build_gpu_solver(j2_box_spec(10, 5, 5, 1.0, 0.5, 0.5), keFp64=True, scalarCSR=True)
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    ts = TimeStep(1, 0.1, 0.1, 0.1, 0.1, 0.1)
+    dU = torch.zeros(s.nDof, dtype=torch.float64, device="cuda")
+    P, F = s._vec(), s._vec()
+    s.computeElements(dU, dU, P, F, ts)
+    s.assembleStiffnessCSR()
+    rng = np.random.default_rng(1)
+    b = rng.normal(size=s.nDof)
+    b[s.dirIdxHost] = rng.normal(size=s.dirIdxHost.size) * 1e-3
+    R = torch.as_tensor(b, device="cuda")
+    # reference linear system: scalar CSR with Dirichlet rows (mk2.pyx:66-109), direct solve
+    info = s.info
+    indptr = np.zeros(s.nDof + 1, np.int32)
+    indices = np.zeros(info.nnz, np.int32)
+    s.lib.ef_csr_pattern(s.ctx, indptr.ctypes.data, indices.ctypes.data)
+    data = torch.zeros(info.nnz, dtype=torch.float64, device="cuda")
+    _lib.check(s.lib.ef_update_csr(s.ctx, None, data.data_ptr(), None), "update")
+    rows = s.dirIdxHost.copy()
+    _lib.check(s.lib.ef_csr_dirichlet_rows(s.ctx, data.data_ptr(), rows.ctypes.data, rows.size, None), "rows")
+    A = sp.csr_matrix((data.cpu().numpy(), indices, indptr), shape=(s.nDof, s.nDof))
+    xref = spla.spsolve(A.tocsc(), b)
+    for mixed in (False, True):
+        s.linsolver.mixed = mixed
+        x = s.linearSolve(R).cpu().numpy()
+        assert s.lastSolveInfo.relResidual <= 1e-8
+        assert np.linalg.norm(A @ x - b) <= 1.01e-8 * np.linalg.norm(b)
+        assert np.max(np.abs(x - xref)) <= 1e-6 * np.max(np.abs(xref))
