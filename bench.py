@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one assembly and one capped PCG solve, for ncu captures of single kernels")
     return ap.parse_args()
 
 
@@ -429,9 +431,39 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(a):
+    """Short kernel sequence for ncu: geometry, one element pass, condensation, BSR scatter, block-Jacobi
+    setup and one PCG solve capped at 200 iterations on the full system."""
+    import torch
+
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300 import build as b
+    from edelweissfe_gb300.solver import LinSolverOptions, TimeStep
+
+    b.build()
+    s = build_solver(a, LinSolverOptions(rtol=1e-8, maxIter=200, maxRefine=1))
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    ts = TimeStep(1, 0.05, 0.05, 0.05, 0.05, 0.05)
+    dU = s._vec()
+    dU[s.dirIdx] = torch.as_tensor(np.concatenate([d.getDelta(ts) for d in s.dirichlets]), device=dU.device)
+    P, F = s._vec(), s._vec()
+    s.computeElements(dU, dU, P, F, ts)
+    s.assembleStiffnessCSR()
+    R = s._vec()
+    R[s.dirIdx] = dU[s.dirIdx]
+    try:
+        s.linearSolve(R)
+    except Exception:
+        pass
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": True, "krylov": s.krylovIterations, "nBlocks": s.info.nBlocks}))
+
+
 if __name__ == "__main__":
     args = parse()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
