@@ -95,6 +95,11 @@ SIGNATURES = {
     "ef_solve": (c_int, [c_vp, ctypes.POINTER(EfSolveOpts), c_vp, c_vp, ctypes.POINTER(EfSolveInfo), c_vp]),
     "ef_bsr_matvec": (c_int, [c_vp, c_vp, c_vp, c_vp]),
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ef_pcg_noalloc_max_nodes": (c_i64, []),
+    "ef_pcg_solve_noalloc": (
+        c_int,
+        [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_dbl, ctypes.POINTER(EfSolveInfo), c_vp],
+    ),
 }
 
 _lib = None

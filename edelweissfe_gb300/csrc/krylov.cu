@@ -479,3 +479,112 @@ ef_status ef_launch_add(int64_t n, const double* a, const double* b, double* y, 
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free block-Jacobi PCG (ef_pcg_solve_noalloc).
+//
+// Some callers cannot allocate device memory at solve time: a host framework that has reserved
+// the device memory for its own pool, or a latency-critical loop that must not take the
+// device-wide synchronisation that cudaMalloc/cudaFree imply.  This entry point solves with the
+// same persistent PCG kernel as ef_solve, but its work vectors live in a fixed file-scope device
+// array instead of a context workspace, so the call itself allocates nothing.
+// ---------------------------------------------------------------------------------------------
+
+#include <mutex>
+
+#define EF_NOALLOC_SCRATCH_BYTES (8u << 20)  // 8 MiB held by every device that loads the library
+static __device__ __align__(256) unsigned char g_noallocScratch[EF_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noallocMutex;
+void* g_noallocPtr[kMaxDevices] = {};
+int g_noallocGrid[kMaxDevices] = {};
+
+inline size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" int64_t ef_pcg_noalloc_max_nodes(void) {
+    // layout: two partial-sum arrays (4 doubles per CTA, at most 2 CTAs per SM on 256 SMs),
+    // the result record, then five FP64 work vectors of 3*nNodes entries each
+    // (the last 256 bytes hold the call's device flags word)
+    const size_t fixed = 2 * align256(4 * sizeof(double) * 512) + align256(sizeof(PcgResult)) + 256;
+    return (int64_t)((EF_NOALLOC_SCRATCH_BYTES - fixed - 5 * 256) / (5 * 3 * sizeof(double)));
+}
+
+extern "C" ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr, const int32_t* colIdx,
+                                          const double* vals, const double* binv, const uint8_t* mask,
+                                          const double* b, double* x, int maxIter, double rtol, ef_solve_info* info,
+                                          void* stream) {
+    if (nNodes <= 0 || !rowPtr || !colIdx || !vals || !binv || !mask || !b || !x || maxIter < 0 || !(rtol >= 0.0)) {
+        ef_set_error("ef_pcg_solve_noalloc: invalid arguments");
+        return EF_ERR_ARG;
+    }
+    if (nNodes > ef_pcg_noalloc_max_nodes()) {
+        ef_set_error("ef_pcg_solve_noalloc: " + std::to_string(nNodes) + " block rows exceed the fixed scratch capacity of " +
+                     std::to_string(ef_pcg_noalloc_max_nodes()) + " block rows (8 MiB); use ef_solve");
+        return EF_ERR_ARG;
+    }
+    int dev = 0;
+    EF_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        ef_set_error("ef_pcg_solve_noalloc: device index out of range");
+        return EF_ERR_ARG;
+    }
+    {
+        // once per device, with that device current: the device address of the scratch array
+        std::lock_guard<std::mutex> lock(g_noallocMutex);
+        if (!g_noallocPtr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+            if (e != cudaSuccess || !p) {
+                ef_set_error(std::string("ef_pcg_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+                return EF_ERR_CUDA;
+            }
+            int nSM = 0, perSM = 0;
+            EF_CUDA(cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev));
+            EF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, pcg_persistent_kernel<double>, kKB, 0));
+            const int grid = std::min(perSM, 2) * nSM;
+            if (grid < 1 || grid > 512) {
+                ef_set_error("ef_pcg_solve_noalloc: unsupported device (grid size)");
+                return EF_ERR_CUDA;
+            }
+            g_noallocGrid[dev] = grid;
+            g_noallocPtr[dev] = p;
+        }
+    }
+    unsigned char* base = (unsigned char*)g_noallocPtr[dev];
+    const size_t partBytes = align256(4 * sizeof(double) * 512);
+    double* partA = (double*)base;
+    double* partB = (double*)(base + partBytes);
+    PcgResult* res = (PcgResult*)(base + 2 * partBytes);
+    unsigned char* vec = base + 2 * partBytes + align256(sizeof(PcgResult));
+    const size_t vb = align256(3 * (size_t)nNodes * sizeof(double));
+    double* r = (double*)(vec + 0 * vb);
+    double* z = (double*)(vec + 1 * vb);
+    double* pA = (double*)(vec + 2 * vb);
+    double* pB = (double*)(vec + 3 * vb);
+    double* q = (double*)(vec + 4 * vb);
+    // device flags word: the last 256 bytes of the scratch array, cleared for this call
+    int* flags = (int*)(base + EF_NOALLOC_SCRATCH_BYTES - 256);
+    cudaStream_t s = (cudaStream_t)stream;
+    EF_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), s));
+    int nn = (int)nNodes;
+    BarrierState* bar = nullptr;
+    double rtol2 = rtol * rtol;
+    void* args[] = {&nn, &rowPtr, &colIdx, &vals, &binv, &mask, &b, &x, &r, &z, &pA, &pB, &q,
+                    &partA, &partB, &bar, &res, &maxIter, &rtol2, &flags};
+    EF_CUDA(cudaLaunchCooperativeKernel((void*)pcg_persistent_kernel<double>, g_noallocGrid[dev], kKB, args, 0, s));
+    PcgResult hr;
+    EF_CUDA(cudaMemcpyAsync(&hr, res, sizeof(hr), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    if (info) {
+        info->iterations = hr.iterations;
+        info->refinements = 0;
+        info->relResidual = hr.bb > 0.0 ? sqrt(hr.rr / hr.bb) : 0.0;
+        info->status = hr.status;
+        info->kernelMs = 0.0;
+        info->kernelLaunches = 1;
+    }
+    return hr.status == EF_OK ? EF_OK : (ef_status)hr.status;
+}

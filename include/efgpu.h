@@ -161,6 +161,28 @@ ef_status ef_solve(ef_ctx* ctx, const ef_solve_opts* opts, const double* b, doub
 /* y = K x with the Dirichlet elimination applied (FP64 accumulation), device [nDof]. */
 ef_status ef_bsr_matvec(ef_ctx* ctx, const double* x, double* y, void* stream);
 
+/* ---- allocation-free solve.  No counterpart in the reference: it exists for callers that
+ *      cannot allocate device memory when they solve -- a host framework that has reserved the
+ *      device memory for its own pool, or a latency-critical loop that must not take the
+ *      device-wide synchronisation cudaMalloc/cudaFree imply. ---- */
+
+/* Largest number of 3x3 block rows ef_pcg_solve_noalloc accepts (its scratch is a fixed 8 MiB
+ * device array that every GPU loading the library holds until the process exits). */
+int64_t ef_pcg_noalloc_max_nodes(void);
+/* Block-Jacobi PCG on a caller-provided FP64 BSR(3x3) system: rowPtr [nNodes+1], colIdx
+ * [nBlocks] (block columns), vals [nBlocks][9] row-major blocks, binv [nNodes][9] inverses of
+ * the diagonal blocks (identity rows/columns on masked DOFs), mask [3*nNodes] (1 = Dirichlet
+ * DOF: its row is masked and b must be 0 there), b, x device [3*nNodes]; x is overwritten.
+ * Stops at ||r||/||b|| <= rtol (recurrence residual) or maxIter.  Allocates nothing: the work
+ * vectors live in the fixed scratch array.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream capture.  All calls
+ * share the one array and it keeps the last call's contents, so calls that overlap on the GPU
+ * (different streams or threads) race; serialise them.  Sizes beyond
+ * ef_pcg_noalloc_max_nodes() are rejected with EF_ERR_ARG.  Synchronises `stream`. */
+ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr, const int32_t* colIdx, const double* vals,
+                               const double* binv, const uint8_t* mask, const double* b, double* x, int maxIter,
+                               double rtol, ef_solve_info* info, void* stream);
+
 /* ---- device reductions for the convergence check: solvers/nonlinearimplicitstatic.py:625-725
  *      (checkConvergence), :771-792 (computeSpatialAveragedFluxes) ---- */
 
