@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--method", default="pcg", choices=["pcg", "fgmres"])
     ap.add_argument("--profile", action="store_true",
                     help="one assembly and one capped PCG solve, for ncu captures of single kernels")
     return ap.parse_args()
@@ -157,7 +158,7 @@ def run_ours(a):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     t0 = time.time()
-    s = build_solver(a, LinSolverOptions(rtol=1e-8, profile=True))
+    s = build_solver(a, LinSolverOptions(method=a.method, rtol=1e-8, profile=True))
     setup_s = time.time() - t0
     info = s.info
     stream = torch.cuda.current_stream()
@@ -441,7 +442,8 @@ def run_profile(a):
     from edelweissfe_gb300.solver import LinSolverOptions, TimeStep
 
     b.build()
-    s = build_solver(a, LinSolverOptions(rtol=1e-8, maxIter=200, maxRefine=1))
+    s = build_solver(a, LinSolverOptions(method=a.method, rtol=1e-8, maxIter=200 if a.method == "pcg" else 60,
+                                         maxRefine=1))
     _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
     ts = TimeStep(1, 0.05, 0.05, 0.05, 0.05, 0.05)
     dU = s._vec()

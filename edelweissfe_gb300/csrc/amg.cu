@@ -1,0 +1,493 @@
+// Aggregation multigrid with rigid-body coarse spaces on the block system.
+//
+// Level 0 is the context's 3x3-block (displacement) system.  Every coarser node is an aggregate
+// of finer nodes and carries 6 DOFs: 3 translations and 3 rotations about the aggregate
+// centroid, so the coarse spaces contain the rigid-body modes that elasticity needs.  The
+// tentative prolongation of a finer node m with offset d = x_m - c_I from its aggregate
+// centroid is
+//   level 0 -> 1 (3 DOFs):  P_m = [ I | R(d) ]               (3 x 6)
+//   level l -> l+1 (6 DOFs): P_m = [ I R(d) ; 0 I ]          (6 x 6)
+// with R(d) = [e_x x d, e_y x d, e_z x d].  The Galerkin operators P^T A P are sums of
+// P_m^T A_mn P_n over the finer blocks, formed by an atomic-free segmented sum in FP64.
+// Smoothing is damped block Jacobi; the coarsest level is solved with a dense
+// pseudo-inverse (Gauss-Jordan, pivots below a relative threshold dropped).
+
+#include "ef_common.cuh"
+
+namespace ef {
+
+constexpr int BC = 6;  // DOFs of a coarse node
+
+// finer-node prolongation block, BF x 6
+template <int BF>
+__device__ __forceinline__ void pblock(const float* __restrict__ d, float P[BF][BC]) {
+    const float dx = d[0], dy = d[1], dz = d[2];
+#pragma unroll
+    for (int i = 0; i < BF; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) P[i][j] = 0.f;
+    P[0][0] = P[1][1] = P[2][2] = 1.f;
+    // rotation columns: e_x x d = (0,-dz,dy), e_y x d = (dz,0,-dx), e_z x d = (-dy,dx,0)
+    P[1][3] = -dz;
+    P[2][3] = dy;
+    P[0][4] = dz;
+    P[2][4] = -dx;
+    P[0][5] = -dy;
+    P[1][5] = dx;
+    if (BF == 6) {
+        P[3 % BF][3] = 1.f;
+        P[4 % BF][4] = 1.f;
+        P[5 % BF][5] = 1.f;
+    }
+}
+
+// coarse block S = sum over finer blocks f = (m, n) of P_m^T A_f P_n; on level 0 masked fine
+// rows/columns are left out; dead coarse DOFs get identity rows/columns
+template <int BF>
+__global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict__ seg, const int32_t* __restrict__ src,
+                                const int32_t* __restrict__ fineRowOfBlock, const int32_t* __restrict__ fineCol,
+                                const float* __restrict__ fineVals, const uint8_t* __restrict__ fineMask,
+                                const float* __restrict__ offs, const int32_t* __restrict__ coarseRowOfBlock,
+                                const int32_t* __restrict__ coarseCol, const uint8_t* __restrict__ coarseDead,
+                                float* __restrict__ coarseVals) {
+    const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (S >= nCoarseBlocks) return;
+    double acc[BC][BC];
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) acc[i][j] = 0.0;
+    for (int64_t t = seg[S]; t < seg[S + 1]; ++t) {
+        const int32_t f = src[t];
+        const int m = fineRowOfBlock[f], n = fineCol[f];
+        float A[BF][BF];
+        const float* v = fineVals + (int64_t)f * BF * BF;
+#pragma unroll
+        for (int i = 0; i < BF; ++i)
+#pragma unroll
+            for (int j = 0; j < BF; ++j) {
+                float a = v[i * BF + j];
+                if (fineMask && (fineMask[BF * m + i] || fineMask[BF * n + j])) a = 0.f;
+                A[i][j] = a;
+            }
+        float Pm[BF][BC], Pn[BF][BC];
+        pblock<BF>(offs + 3 * (int64_t)m, Pm);
+        pblock<BF>(offs + 3 * (int64_t)n, Pn);
+        float AP[BF][BC];
+#pragma unroll
+        for (int i = 0; i < BF; ++i)
+#pragma unroll
+            for (int j = 0; j < BC; ++j) {
+                float s = 0.f;
+#pragma unroll
+                for (int k = 0; k < BF; ++k) s += A[i][k] * Pn[k][j];
+                AP[i][j] = s;
+            }
+#pragma unroll
+        for (int i = 0; i < BC; ++i)
+#pragma unroll
+            for (int j = 0; j < BC; ++j) {
+                float s = 0.f;
+#pragma unroll
+                for (int k = 0; k < BF; ++k) s += Pm[k][i] * AP[k][j];
+                acc[i][j] += (double)s;
+            }
+    }
+    const int I = coarseRowOfBlock[S], J = coarseCol[S];
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            double a = acc[i][j];
+            if (coarseDead[BC * I + i] || coarseDead[BC * J + j]) a = (I == J && i == j) ? 1.0 : 0.0;
+            coarseVals[S * BC * BC + i * BC + j] = (float)a;
+        }
+}
+
+// inverse of each 6x6 diagonal block (pseudo-inverse: pivots below 1e-9 of the largest
+// diagonal entry are dropped), FP64 Gauss-Jordan in registers
+__global__ void bj6_setup_kernel(int nN, const int64_t* __restrict__ diagPos, const float* __restrict__ vals,
+                                 float* __restrict__ inv) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    double A[BC][2 * BC];
+    const float* D = vals + diagPos[m] * BC * BC;
+    double dmax = 0.0;
+#pragma unroll
+    for (int i = 0; i < BC; ++i) {
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            A[i][j] = (double)D[i * BC + j];
+            A[i][BC + j] = i == j ? 1.0 : 0.0;
+        }
+        dmax = fmax(dmax, fabs(A[i][i]));
+    }
+    bool drop[BC];
+#pragma unroll
+    for (int c = 0; c < BC; ++c) drop[c] = false;
+    for (int c = 0; c < BC; ++c) {
+        if (!(fabs(A[c][c]) > 1e-9 * dmax)) {
+            drop[c] = true;
+            continue;
+        }
+        const double p = 1.0 / A[c][c];
+        for (int j = 0; j < 2 * BC; ++j) A[c][j] *= p;
+        for (int r = 0; r < BC; ++r) {
+            if (r == c) continue;
+            const double f = A[r][c];
+            for (int j = 0; j < 2 * BC; ++j) A[r][j] -= f * A[c][j];
+        }
+    }
+    for (int i = 0; i < BC; ++i)
+        for (int j = 0; j < BC; ++j)
+            inv[(int64_t)m * BC * BC + i * BC + j] = (drop[i] || drop[j]) ? 0.f : (float)A[i][BC + j];
+}
+
+// x = omega * D^-1 r (+ x when accumulating); masked DOFs -> 0
+template <int BS>
+__global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega,
+                                const float* __restrict__ r, float* __restrict__ x, int accumulate) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    const float* B = binv + (int64_t)m * BS * BS;
+    float rv[BS];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) rv[i] = r[BS * m + i];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+        float z = 0.f;
+#pragma unroll
+        for (int j = 0; j < BS; ++j) z += B[i * BS + j] * rv[j];
+        z *= omega;
+        if (mask && mask[BS * m + i]) z = 0.f;
+        if (accumulate)
+            x[BS * m + i] += z;
+        else
+            x[BS * m + i] = z;
+    }
+}
+
+// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads
+template <int BS>
+__global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32_t* __restrict__ rowPtr,
+                                                              const int32_t* __restrict__ colIdx,
+                                                              const float* __restrict__ vals,
+                                                              const float* __restrict__ x, const float* __restrict__ r,
+                                                              const uint8_t* __restrict__ mask, float* __restrict__ t) {
+    const int lane = threadIdx.x & 7;
+    const int m0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int m = m0 < nN ? m0 : nN - 1;
+    float y[BS];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) y[i] = 0.f;
+    const int s = rowPtr[m], e = rowPtr[m + 1];
+    for (int base = s; base < e; base += 32) {
+        int cc[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = base + lane + 8 * j;
+            cc[j] = k < e ? BS * colIdx[k] : -1;
+        }
+        float xv[4][BS];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (cc[j] >= 0)
+#pragma unroll
+                for (int i = 0; i < BS; ++i) xv[j][i] = x[cc[j] + i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (cc[j] >= 0) {
+                const float* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
+#pragma unroll
+                for (int i = 0; i < BS; ++i) {
+                    float a = 0.f;
+#pragma unroll
+                    for (int k = 0; k < BS; ++k) a += v[i * BS + k] * xv[j][k];
+                    y[i] += a;
+                }
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < BS; ++i)
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
+    if (m0 < nN && lane < BS) {
+        const int d = BS * m + lane;
+        float yy = y[0];
+#pragma unroll
+        for (int i = 1; i < BS; ++i)
+            if (lane == i) yy = y[i];
+        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+    }
+}
+
+// t = r - A x for 6x6 blocks: one warp per block row, one block per lane (coarse rows have
+// at most a few dozen blocks), fixed shuffle tree
+__global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int32_t* __restrict__ rowPtr,
+                                                               const int32_t* __restrict__ colIdx,
+                                                               const float* __restrict__ vals,
+                                                               const float* __restrict__ x, const float* __restrict__ r,
+                                                               const uint8_t* __restrict__ mask, float* __restrict__ t) {
+    const int lane = threadIdx.x & 31;
+    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (m >= nN) return;
+    float y[BC];
+#pragma unroll
+    for (int i = 0; i < BC; ++i) y[i] = 0.f;
+    for (int k = rowPtr[m] + lane; k < rowPtr[m + 1]; k += 32) {
+        const int c = BC * colIdx[k];
+        const float* v = vals + (int64_t)k * BC * BC;
+        float xv[BC];
+#pragma unroll
+        for (int j = 0; j < BC; ++j) xv[j] = x[c + j];
+#pragma unroll
+        for (int i = 0; i < BC; ++i)
+#pragma unroll
+            for (int j = 0; j < BC; ++j) y[i] += v[i * BC + j] * xv[j];
+    }
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
+    if (lane < BC) {
+        float yy = y[0];
+#pragma unroll
+        for (int i = 1; i < BC; ++i)
+            if (lane == i) yy = y[i];
+        const int d = BC * m + lane;
+        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+    }
+}
+
+// rc[I] = sum over members m of aggregate I of P_m^T t[m]; one warp per aggregate, members
+// strided over the lanes and combined by a fixed shuffle tree
+template <int BF>
+__global__ void restrict_kernel(int nC, const int32_t* __restrict__ aggPtr, const int32_t* __restrict__ aggIdx,
+                                const float* __restrict__ offs, const float* __restrict__ t,
+                                const uint8_t* __restrict__ coarseDead, float* __restrict__ rc) {
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= nC) return;
+    float a[BC];
+#pragma unroll
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    for (int k = aggPtr[I] + lane; k < aggPtr[I + 1]; k += 32) {
+        const int m = aggIdx[k];
+        float P[BF][BC];
+        pblock<BF>(offs + 3 * (int64_t)m, P);
+#pragma unroll
+        for (int i = 0; i < BF; ++i) {
+            const float ti = t[BF * m + i];
+#pragma unroll
+            for (int j = 0; j < BC; ++j) a[j] += P[i][j] * ti;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < BC; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+    if (lane < BC) {
+        float v = a[0];
+#pragma unroll
+        for (int j = 1; j < BC; ++j)
+            if (lane == j) v = a[j];
+        rc[BC * I + lane] = coarseDead[BC * I + lane] ? 0.f : v;
+    }
+}
+
+// x[m] += P_m xc[agg(m)] on free finer DOFs
+template <int BF>
+__global__ void prolong_kernel(int nN, const int32_t* __restrict__ agg, const float* __restrict__ offs,
+                               const float* __restrict__ xc, const uint8_t* __restrict__ mask, float* __restrict__ x,
+                               float alpha) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    const int I = agg[m];
+    float P[BF][BC];
+    pblock<BF>(offs + 3 * (int64_t)m, P);
+    float c[BC];
+#pragma unroll
+    for (int j = 0; j < BC; ++j) c[j] = xc[BC * I + j];
+#pragma unroll
+    for (int i = 0; i < BF; ++i) {
+        if (mask && mask[BF * m + i]) continue;
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < BC; ++j) s += P[i][j] * c[j];
+        x[BF * m + i] += alpha * s;
+    }
+}
+
+// dense pseudo-inverse of the coarsest operator (n = 6 nN <= kMaxCoarsestDof), FP64 Gauss-Jordan
+// with partial pivoting in shared memory, one CTA; pivots below 1e-10 of the largest diagonal
+// entry mark a null direction whose rows/columns of the inverse are zero
+constexpr int kMaxCoarsestDof = 96;
+__global__ void coarsest_inverse_kernel(int nN, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
+                                        const float* __restrict__ vals, float* __restrict__ inv) {
+    extern __shared__ double smemA[];
+    const int n = BC * nN;
+    const int ld = 2 * n + 1;
+    auto A = [&](int r, int c) -> double& { return smemA[r * ld + c]; };
+    __shared__ int piv;
+    __shared__ double dmax;
+    __shared__ unsigned char drop[kMaxCoarsestDof];
+    for (int i = threadIdx.x; i < n * 2 * n; i += blockDim.x) {
+        const int r = i / (2 * n), c = i % (2 * n);
+        A(r, c) = (c >= n && c - n == r) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < nN; m += blockDim.x)
+        for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k) {
+            const int cn = colIdx[k];
+            for (int i = 0; i < BC; ++i)
+                for (int j = 0; j < BC; ++j) A(BC * m + i, BC * cn + j) = (double)vals[(int64_t)k * BC * BC + i * BC + j];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double d = 0.0;
+        for (int i = 0; i < n; ++i) d = fmax(d, fabs(A(i, i)));
+        dmax = d;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) drop[i] = 0;
+    __syncthreads();
+    for (int col = 0; col < n; ++col) {
+        if (threadIdx.x == 0) {
+            int p = col;
+            double best = fabs(A(col, col));
+            for (int r = col + 1; r < n; ++r)
+                if (fabs(A(r, col)) > best) {
+                    best = fabs(A(r, col));
+                    p = r;
+                }
+            piv = best > 1e-10 * dmax ? p : -1;
+            if (piv < 0) drop[col] = 1;
+        }
+        __syncthreads();
+        if (piv < 0) continue;
+        if (piv != col)
+            for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) {
+                const double tmp = A(col, c);
+                A(col, c) = A(piv, c);
+                A(piv, c) = tmp;
+            }
+        __syncthreads();
+        const double d = A(col, col);
+        __syncthreads();
+        for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) A(col, c) /= d;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * 2 * n; i += blockDim.x) {
+            const int r = i / (2 * n), c = i % (2 * n);
+            if (r != col && c != col) A(r, c) -= A(r, col) * A(col, c);
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < n; r += blockDim.x)
+            if (r != col) A(r, col) = 0.0;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+        const int r = i / n, c = i % n;
+        inv[i] = (drop[r] || drop[c]) ? 0.f : (float)A(r, n + c);
+    }
+}
+
+// x = Ainv r on the coarsest level (dense matvec), dead DOFs -> 0
+__global__ void coarsest_apply_kernel(int n, const float* __restrict__ inv, const float* __restrict__ r,
+                                      const uint8_t* __restrict__ dead, float* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int j = 0; j < n; ++j) s += inv[(int64_t)i * n + j] * r[j];
+    x[i] = dead[i] ? 0.f : s;
+}
+
+}  // namespace ef
+
+using namespace ef;
+
+static inline int nb_(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+int ef_amg_coarse_dofs() { return BC; }
+int ef_max_coarsest_nodes() { return kMaxCoarsestDof / BC; }
+
+ef_status ef_launch_galerkin(int bf, int64_t nCoarseBlocks, const int64_t* seg, const int32_t* src,
+                             const int32_t* fineRowOfBlock, const int32_t* fineCol, const float* fineVals,
+                             const uint8_t* fineMask, const float* offs, const int32_t* coarseRowOfBlock,
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals, cudaStream_t s) {
+    if (nCoarseBlocks == 0) return EF_OK;
+    if (bf == 3)
+        galerkin_kernel<3><<<nb_(nCoarseBlocks, 64), 64, 0, s>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
+                                                                 fineVals, fineMask, offs, coarseRowOfBlock, coarseCol,
+                                                                 coarseDead, coarseVals);
+    else
+        galerkin_kernel<6><<<nb_(nCoarseBlocks, 64), 64, 0, s>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
+                                                                 fineVals, fineMask, offs, coarseRowOfBlock, coarseCol,
+                                                                 coarseDead, coarseVals);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals, float* inv, cudaStream_t s) {
+    bj6_setup_kernel<<<nb_(nN, 64), 64, 0, s>>>(nN, diagPos, vals, inv);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
+                             float* x, int accumulate, cudaStream_t s) {
+    if (bs == 3)
+        bj_apply_kernel<3><<<nb_(nN, 256), 256, 0, s>>>(nN, binv, mask, omega, r, x, accumulate);
+    else
+        bj_apply_kernel<6><<<nb_(nN, 256), 256, 0, s>>>(nN, binv, mask, omega, r, x, accumulate);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s) {
+    if (bs == 3)
+        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, s>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+    else
+        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, s>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
+                             const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s) {
+    if (bf == 3)
+        restrict_kernel<3><<<nb_((int64_t)nC * 32, 256), 256, 0, s>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
+    else
+        restrict_kernel<6><<<nb_((int64_t)nC * 32, 256), 256, 0, s>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
+                            const uint8_t* mask, float* x, cudaStream_t s, float alpha) {
+    if (bf == 3)
+        prolong_kernel<3><<<nb_(nN, 256), 256, 0, s>>>(nN, agg, offs, xc, mask, x, alpha);
+    else
+        prolong_kernel<6><<<nb_(nN, 256), 256, 0, s>>>(nN, agg, offs, xc, mask, x, alpha);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                     float* inv, cudaStream_t s) {
+    if (BC * nN > kMaxCoarsestDof) {
+        ef_set_error("coarsest level too large for the dense solve");
+        return EF_ERR_ARG;
+    }
+    const size_t smem = sizeof(double) * BC * nN * (2 * BC * nN + 1);
+    EF_CUDA(cudaFuncSetAttribute(coarsest_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    coarsest_inverse_kernel<<<1, 256, smem, s>>>(nN, rowPtr, colIdx, vals, inv);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
+                                   cudaStream_t s) {
+    coarsest_apply_kernel<<<nb_(n, 64), 64, 0, s>>>(n, inv, r, dead, x);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}

@@ -31,6 +31,58 @@ ef_status ef_launch_masked_copy(int64_t n, const double* src, const uint8_t* mas
 ef_status ef_launch_axpy(int64_t n, double a, const void* xs, int xDouble, double* y, cudaStream_t s);
 ef_status ef_launch_add(int64_t n, const double* a, const double* b, double* y, cudaStream_t s);
 
+// amg.cu
+int ef_amg_coarse_dofs();
+int ef_max_coarsest_nodes();
+ef_status ef_launch_galerkin(int bf, int64_t nCoarseBlocks, const int64_t* seg, const int32_t* src,
+                             const int32_t* fineRowOfBlock, const int32_t* fineCol, const float* fineVals,
+                             const uint8_t* fineMask, const float* offs, const int32_t* coarseRowOfBlock,
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals, cudaStream_t s);
+ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals, float* inv, cudaStream_t s);
+ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
+                             float* x, int accumulate, cudaStream_t s);
+ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s);
+ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
+                             const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s);
+ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
+                            const uint8_t* mask, float* x, cudaStream_t s, float alpha);
+ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                     float* inv, cudaStream_t s);
+ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
+                                   cudaStream_t s);
+// mpnn.cu
+int ef_mpnn_nparam();
+int ef_mpnn_hidden();
+int ef_mpnn_layer_offset(int l);
+int ef_mpnn_out_offset();
+ef_status ef_mpnn_setup_kernels();
+ef_status ef_launch_edge_weights(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, float* a,
+                                 cudaStream_t s);
+ef_status ef_launch_gather_f32(int64_t n, const int64_t* idx, const float* src, float* dst, cudaStream_t s);
+ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* a, const float* P,
+                          const float* f, const float* base, const uint8_t* mask, float so, float* acts, float* z,
+                          cudaStream_t s);
+ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* aT, const float* P,
+                           const float* f, const float* acts, const float* z, const float* e, const uint8_t* mask,
+                           float scale, float so, float* grad, float* work, float* part, int nPart, cudaStream_t s);
+ef_status ef_mpnn_adam(int n, float* p, const float* g, float* m1, float* m2, float lr, float b1, float b2, float eps,
+                       int step, void* pb, float* pf, cudaStream_t s);
+ef_status ef_launch_features(int nN, const float* Mv, const float* v, const float* binv, float s0, float s1, float s2,
+                             float* f, cudaStream_t s);
+ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s);
+// fgmres.cu
+int ef_fgmres_max_basis();
+ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, const float* x,
+                             const uint8_t* mask, float* y, cudaStream_t s);
+ef_status ef_launch_multidot(int64_t n, int nv, const float* V, int64_t ldv, const float* w, double* part, int nPart,
+                             double* h, double* hAcc, float* invNorm, cudaStream_t s);
+ef_status ef_launch_multiaxpy(int64_t n, int nv, const float* V, int64_t ldv, const double* h, float* w,
+                              cudaStream_t s);
+ef_status ef_launch_scale(int64_t n, const float* w, const float* invNorm, float* v, cudaStream_t s);
+ef_status ef_launch_combine(int64_t n, int nv, const float* Z, int64_t ldz, const double* y, float* x, cudaStream_t s);
+ef_status ef_launch_sub(int64_t n, const float* b, const float* y, float* r, cudaStream_t s);
+
 using namespace ef;
 
 static thread_local std::string g_err;
@@ -231,6 +283,26 @@ void parallel_for(int64_t n, F f) {
 
 }  // namespace
 
+// one coarse level of the aggregation multigrid (level 0 is the context's own BSR system)
+struct AmgLevel {
+    int nN = 0;
+    int64_t nBlocks = 0;
+    int32_t *rowPtr = nullptr, *colIdx = nullptr, *rowOfBlock = nullptr;
+    int64_t* diagPos = nullptr;
+    float *vals = nullptr, *binv = nullptr;
+    uint8_t* dead = nullptr;                // coarse DOFs without a free fine DOF
+    int32_t *agg = nullptr;                 // finer node -> this level's node
+    float* offs = nullptr;                  // finer node position relative to its aggregate centroid [nFiner][3]
+    std::vector<float> hOffs;
+    std::vector<double> hCentroid;          // [nN][3]
+    int32_t *aggPtr = nullptr, *aggIdx = nullptr;  // members of each node of this level
+    int64_t* gseg = nullptr;                // Galerkin map: blocks of the finer level per block here
+    int32_t* gsrc = nullptr;
+    float *x = nullptr, *r = nullptr, *t = nullptr;  // V-cycle work vectors of this level
+    std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
+    std::vector<uint8_t> hDead;
+};
+
 struct ef_ctx {
     int64_t nDof = 0, nNodes = 0, nElements = 0;
     std::vector<double> hX;
@@ -287,6 +359,48 @@ struct ef_ctx {
     bool exact = false;
     void* w64k[7] = {};   // FP64 Krylov vectors for the all-FP64 mode
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // aggregation multigrid for the FGMRES preconditioner
+    std::vector<AmgLevel> amg;           // levels 1..L-1
+    float* amgCoarsestInv = nullptr;
+    int32_t* dRowOfBlock0 = nullptr;     // fine-level block -> block row
+    float *fineX = nullptr, *fineT = nullptr;  // level-0 V-cycle work vectors
+    bool amgStale = true;                // coarse values need a refresh (new system or mask)
+    std::vector<uint8_t> hMask;
+    std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
+    // V-cycle parameters: damping, smoothing sweeps per side, coarse over-correction, cycle type
+    float amgOmega = 0.65f;
+    int amgSweeps = 2;
+    float amgAlpha = 1.5f;
+    int amgCycle = 2;  // 1: V-cycle, 2: W-cycle below the finest level
+    // the whole preconditioner application captured once as a CUDA graph (fixed in/out buffers)
+    float *vcIn = nullptr, *vcOut = nullptr;
+    cudaStream_t capStream = nullptr;
+    cudaGraphExec_t vcGraph = nullptr;
+    // learned correction (message-passing network) on top of the V-cycle
+    struct NNSample {
+        float *f = nullptr, *base = nullptr, *e = nullptr, *a = nullptr, *aT = nullptr;
+        double e2 = 0.0;
+    };
+    bool nnInit = false, nnOn = false;
+    float *nnP = nullptr, *nnPf = nullptr, *nnM1 = nullptr, *nnM2 = nullptr, *nnG = nullptr;
+    void* nnPb = nullptr;
+    float *nnActs = nullptr, *nnF = nullptr, *nnWork = nullptr, *nnPart = nullptr, *nnZ = nullptr;
+    float *nnA = nullptr, *nnAT = nullptr, *nnRin = nullptr;
+    int64_t* nnTpos = nullptr;
+    float nnS[3] = {1.f, 1.f, 1.f};
+    float nnSo = 1.f;
+    bool nnScalesSet = false;
+    int nnStep = 0;
+    std::vector<NNSample> nnSamples;
+    cudaGraphExec_t nnGraph = nullptr;
+    float* vcOut2 = nullptr;
+    // FGMRES workspace
+    float* fgV = nullptr;                // [restart+1][nDof]
+    float* fgZ = nullptr;                // [restart][nDof]
+    float* fgW = nullptr;
+    double* fgPart = nullptr;
+    double* fgH = nullptr;               // device scratch: h (128) + second pass (128) + norm + y (128)
+    int fgRestart = 0;
 };
 
 extern "C" {
@@ -358,6 +472,44 @@ void ef_destroy(ef_ctx* c) {
     for (auto* p : c->w64k) F(p);
     for (auto* p : c->dTang) F(p);
     F(c->dYe);
+    for (auto& L : c->amg) {
+        F(L.rowPtr);
+        F(L.colIdx);
+        F(L.rowOfBlock);
+        F(L.diagPos);
+        F(L.vals);
+        F(L.binv);
+        F(L.dead);
+        F(L.agg);
+        F(L.offs);
+        F(L.aggPtr);
+        F(L.aggIdx);
+        F(L.gseg);
+        F(L.gsrc);
+        F(L.x);
+        F(L.r);
+        F(L.t);
+    }
+    F(c->amgCoarsestInv);
+    F(c->vcIn);
+    F(c->vcOut);
+    if (c->vcGraph) cudaGraphExecDestroy(c->vcGraph);
+    if (c->nnGraph) cudaGraphExecDestroy(c->nnGraph);
+    for (void* p : {(void*)c->nnP, (void*)c->nnPf, (void*)c->nnM1, (void*)c->nnM2, (void*)c->nnG, c->nnPb,
+                    (void*)c->nnActs, (void*)c->nnF, (void*)c->nnWork, (void*)c->nnPart, (void*)c->nnZ, (void*)c->nnA,
+                    (void*)c->nnAT, (void*)c->nnTpos, (void*)c->vcOut2, (void*)c->nnRin})
+        F(p);
+    for (auto& smp : c->nnSamples)
+        for (void* p : {(void*)smp.f, (void*)smp.base, (void*)smp.e, (void*)smp.a, (void*)smp.aT}) F(p);
+    if (c->capStream) cudaStreamDestroy(c->capStream);
+    F(c->dRowOfBlock0);
+    F(c->fineX);
+    F(c->fineT);
+    F(c->fgV);
+    F(c->fgZ);
+    F(c->fgW);
+    F(c->fgPart);
+    F(c->fgH);
     for (auto e : c->ev)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -622,6 +774,9 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         EF_CUDA(cudaMemcpy(c->dBsrSrc, src.data(), sizeof(int64_t) * nEnt, cudaMemcpyHostToDevice));
         EF_CUDA(cudaMemcpy(c->dDiagPos, diag.data(), sizeof(int64_t) * nNodes, cudaMemcpyHostToDevice));
         EF_CUDA(cudaMemset(c->dMask, 0, c->nDof));
+        c->hMask.assign(c->nDof, 0);
+        c->hRowPtr0 = rowPtr;
+        c->hColIdx0 = colIdx;
     }
 
     // scalar CSR of the reference (SciPy canonical pattern) + reference-order scatter map
@@ -946,6 +1101,8 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
     }
     c->anyDirichlet = n > 0;
     EF_CUDA(cudaMemcpy(c->dMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
+    c->hMask = std::move(m);
+    c->amgStale = true;
     return EF_OK;
 }
 
@@ -955,6 +1112,7 @@ ef_status ef_assemble_bsr(ef_ctx* c, void* stream) {
     EF_CHECK(ef_launch_bsr_scatter(c->nBlocks, c->dBsrSeg, c->dBsrSrc, c->Kblk, c->keFp64, c->dBsrVals, s));
     EF_CHECK(ef_launch_bj_setup(c->nNodes, c->dDiagPos, c->dNodeDof, c->dMask, c->dBsrVals, c->keFp64, c->dBinv,
                                 c->dFlags, s));
+    c->amgStale = true;
     return EF_OK;
 }
 
@@ -1013,11 +1171,481 @@ static ef_status run_pcg(ef_ctx* c, int vDouble, const void* rhs, void* sol, int
     return EF_OK;
 }
 
+
+}  // extern "C"
+
+// ---- aggregation multigrid (host setup, device refresh and V-cycle) -------------------------
+
+// greedy aggregation of a block graph: seeds take their whole (unaggregated) neighbourhood,
+// left-over nodes join a neighbouring seed aggregate, isolated ones form their own
+static int aggregate(int n, const std::vector<int32_t>& rowPtr, const std::vector<int32_t>& colIdx,
+                     std::vector<int32_t>& agg) {
+    agg.assign(n, -1);
+    int nAgg = 0;
+    for (int m = 0; m < n; ++m) {
+        if (agg[m] != -1) continue;
+        bool free = true;
+        for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k)
+            if (agg[colIdx[k]] != -1) {
+                free = false;
+                break;
+            }
+        if (!free) continue;
+        for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k) agg[colIdx[k]] = nAgg;
+        agg[m] = nAgg++;
+    }
+    std::vector<int32_t> first = agg;
+    for (int m = 0; m < n; ++m) {
+        if (agg[m] != -1) continue;
+        for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k)
+            if (first[colIdx[k]] != -1) {
+                agg[m] = first[colIdx[k]];
+                break;
+            }
+    }
+    for (int m = 0; m < n; ++m)
+        if (agg[m] == -1) agg[m] = nAgg++;
+    return nAgg;
+}
+
+template <typename T>
+static ef_status upload(T** dst, const std::vector<T>& v) {
+    ef_status st = EF_OK;
+    *dst = dalloc<T>(std::max<size_t>(1, v.size()), &st);
+    if (!*dst) return st;
+    if (!v.empty()) EF_CUDA(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return EF_OK;
+}
+
+static ef_status amg_build(ef_ctx* c) {
+    if (!c->amg.empty()) return EF_OK;
+    if (const char* e = getenv("EF_AMG_OMEGA")) c->amgOmega = (float)atof(e);
+    if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
+    if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
+    ef_status st = EF_OK;
+    const int n0 = (int)c->nNodes;
+    const int BCo = ef_amg_coarse_dofs();
+    // fine block -> block row
+    std::vector<int32_t> rob0(c->nBlocks);
+    for (int m = 0; m < n0; ++m)
+        for (int k = c->hRowPtr0[m]; k < c->hRowPtr0[m + 1]; ++k) rob0[k] = m;
+    EF_CHECK(upload(&c->dRowOfBlock0, rob0));
+    c->fineX = dalloc<float>(c->nDof, &st);
+    c->fineT = dalloc<float>(c->nDof, &st);
+    if (!c->fineX || !c->fineT) return st;
+    const std::vector<int32_t>* pRow = &c->hRowPtr0;
+    const std::vector<int32_t>* pCol = &c->hColIdx0;
+    std::vector<double> finePos(3 * (size_t)n0);
+    for (int m = 0; m < n0; ++m)
+        for (int k = 0; k < 3; ++k) finePos[3 * m + k] = c->hX[3 * m + k];
+    const std::vector<double>* pPos = &finePos;
+    int nFine = n0;
+    while (nFine > ef_max_coarsest_nodes()) {
+        AmgLevel L;
+        const int nC = aggregate(nFine, *pRow, *pCol, L.hAgg);
+        if (nC >= nFine) break;  // no coarsening progress
+        L.nN = nC;
+        // members of each coarse node (increasing finer index), centroids and offsets
+        L.hAggPtr.assign(nC + 1, 0);
+        for (int m = 0; m < nFine; ++m) L.hAggPtr[L.hAgg[m] + 1]++;
+        for (int I = 0; I < nC; ++I) L.hAggPtr[I + 1] += L.hAggPtr[I];
+        L.hAggIdx.resize(nFine);
+        {
+            std::vector<int32_t> fill(L.hAggPtr.begin(), L.hAggPtr.end() - 1);
+            for (int m = 0; m < nFine; ++m) L.hAggIdx[fill[L.hAgg[m]]++] = m;
+        }
+        L.hCentroid.assign(3 * (size_t)nC, 0.0);
+        for (int m = 0; m < nFine; ++m)
+            for (int k = 0; k < 3; ++k) L.hCentroid[3 * L.hAgg[m] + k] += (*pPos)[3 * m + k];
+        for (int I = 0; I < nC; ++I) {
+            const double cnt = (double)(L.hAggPtr[I + 1] - L.hAggPtr[I]);
+            for (int k = 0; k < 3; ++k) L.hCentroid[3 * I + k] /= cnt;
+        }
+        L.hOffs.resize(3 * (size_t)nFine);
+        for (int m = 0; m < nFine; ++m)
+            for (int k = 0; k < 3; ++k) L.hOffs[3 * m + k] = (float)((*pPos)[3 * m + k] - L.hCentroid[3 * L.hAgg[m] + k]);
+        // coarse pattern
+        std::vector<std::vector<int32_t>> cols(nC);
+        for (int m = 0; m < nFine; ++m)
+            for (int k = (*pRow)[m]; k < (*pRow)[m + 1]; ++k) cols[L.hAgg[m]].push_back(L.hAgg[(*pCol)[k]]);
+        L.hRowPtr.assign(nC + 1, 0);
+        for (int I = 0; I < nC; ++I) {
+            auto& v = cols[I];
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            L.hRowPtr[I + 1] = L.hRowPtr[I] + (int32_t)v.size();
+        }
+        L.nBlocks = L.hRowPtr[nC];
+        L.hColIdx.resize(L.nBlocks);
+        std::vector<int32_t> rob(L.nBlocks);
+        std::vector<int64_t> diag(nC, -1);
+        for (int I = 0; I < nC; ++I)
+            for (size_t j = 0; j < cols[I].size(); ++j) {
+                const int64_t k = L.hRowPtr[I] + (int64_t)j;
+                L.hColIdx[k] = cols[I][j];
+                rob[k] = I;
+                if (cols[I][j] == I) diag[I] = k;
+            }
+        // Galerkin map: finer blocks in increasing order, grouped by their coarse block
+        const int64_t nFineBlocks = (*pRow)[nFine];
+        std::vector<int64_t> gcount(L.nBlocks + 1, 0);
+        std::vector<int32_t> target(nFineBlocks);
+        for (int m = 0; m < nFine; ++m) {
+            const int I = L.hAgg[m];
+            for (int k = (*pRow)[m]; k < (*pRow)[m + 1]; ++k) {
+                const int J = L.hAgg[(*pCol)[k]];
+                const int32_t* b = L.hColIdx.data() + L.hRowPtr[I];
+                const int32_t* e = L.hColIdx.data() + L.hRowPtr[I + 1];
+                const int64_t S = L.hRowPtr[I] + (std::lower_bound(b, e, J) - b);
+                target[k] = (int32_t)S;
+                gcount[S + 1]++;
+            }
+        }
+        for (int64_t S = 0; S < L.nBlocks; ++S) gcount[S + 1] += gcount[S];
+        std::vector<int32_t> gsrc(nFineBlocks);
+        {
+            std::vector<int64_t> fill(gcount.begin(), gcount.end() - 1);
+            for (int64_t f = 0; f < nFineBlocks; ++f) gsrc[fill[target[f]]++] = (int32_t)f;
+        }
+        EF_CHECK(upload(&L.rowPtr, L.hRowPtr));
+        EF_CHECK(upload(&L.colIdx, L.hColIdx));
+        EF_CHECK(upload(&L.rowOfBlock, rob));
+        EF_CHECK(upload(&L.diagPos, diag));
+        EF_CHECK(upload(&L.agg, L.hAgg));
+        EF_CHECK(upload(&L.offs, L.hOffs));
+        EF_CHECK(upload(&L.aggPtr, L.hAggPtr));
+        EF_CHECK(upload(&L.aggIdx, L.hAggIdx));
+        EF_CHECK(upload(&L.gseg, gcount));
+        EF_CHECK(upload(&L.gsrc, gsrc));
+        L.vals = dalloc<float>((size_t)L.nBlocks * BCo * BCo, &st);
+        L.binv = dalloc<float>((size_t)nC * BCo * BCo, &st);
+        L.dead = dalloc<uint8_t>((size_t)BCo * nC, &st);
+        L.x = dalloc<float>((size_t)BCo * nC, &st);
+        L.r = dalloc<float>((size_t)BCo * nC, &st);
+        L.t = dalloc<float>((size_t)BCo * nC, &st);
+        if (!L.vals || !L.binv || !L.dead || !L.x || !L.r || !L.t) return st;
+        c->amg.push_back(std::move(L));
+        pRow = &c->amg.back().hRowPtr;
+        pCol = &c->amg.back().hColIdx;
+        pPos = &c->amg.back().hCentroid;
+        nFine = nC;
+    }
+    if (c->amg.empty() || c->amg.back().nN > ef_max_coarsest_nodes()) {
+        ef_set_error("multigrid: the block graph does not coarsen to a dense-solvable size");
+        return EF_ERR_ARG;
+    }
+    const int nc = BCo * c->amg.back().nN;
+    c->amgCoarsestInv = dalloc<float>((size_t)nc * nc, &st);
+    if (!c->amgCoarsestInv) return st;
+    c->vcIn = dalloc<float>(c->nDof, &st);
+    c->vcOut = dalloc<float>(c->nDof, &st);
+    if (!c->vcIn || !c->vcOut) return st;
+    c->amgStale = true;
+    return EF_OK;
+}
+
+static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s);
+
+// capture the preconditioner application (fixed device pointers; values may change later)
+static ef_status amg_capture(ef_ctx* c) {
+    if (c->vcGraph) return EF_OK;
+    EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
+    EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
+    const ef_status st = amg_vcycle(c, 0, c->vcIn, c->vcOut, c->capStream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->capStream, &g);
+    if (st != EF_OK) return st;
+    if (e != cudaSuccess) {
+        ef_set_error(std::string("V-cycle capture: ") + cudaGetErrorString(e));
+        return EF_ERR_CUDA;
+    }
+    EF_CUDA(cudaGraphInstantiate(&c->vcGraph, g, 0));
+    cudaGraphDestroy(g);
+    return EF_OK;
+}
+
+// A coarse DOF (translation or rotation of an aggregate) is dead when its prolongation column
+// vanishes on every live finer DOF (all members clamped, or a rotation about an axis through
+// all free members).
+static void amg_dead_mask(const AmgLevel& L, int bf, const uint8_t* fineDead, std::vector<uint8_t>& dead) {
+    const int BCo = ef_amg_coarse_dofs();
+    dead.assign((size_t)BCo * L.nN, 1);
+    for (int I = 0; I < L.nN; ++I) {
+        double colNorm[6] = {0, 0, 0, 0, 0, 0};
+        double scale = 0.0;
+        for (int k = L.hAggPtr[I]; k < L.hAggPtr[I + 1]; ++k) {
+            const int m = L.hAggIdx[k];
+            const double dx = L.hOffs[3 * m], dy = L.hOffs[3 * m + 1], dz = L.hOffs[3 * m + 2];
+            scale = std::max(scale, dx * dx + dy * dy + dz * dz);
+            // rows of P_m (bf x 6)
+            double P[6][6] = {};
+            P[0][0] = P[1][1] = P[2][2] = 1.0;
+            P[1][3] = -dz;
+            P[2][3] = dy;
+            P[0][4] = dz;
+            P[2][4] = -dx;
+            P[0][5] = -dy;
+            P[1][5] = dx;
+            if (bf == 6) P[3][3] = P[4][4] = P[5][5] = 1.0;
+            for (int i = 0; i < bf; ++i) {
+                if (fineDead[(size_t)bf * m + i]) continue;
+                for (int j = 0; j < 6; ++j) colNorm[j] += P[i][j] * P[i][j];
+            }
+        }
+        const double tol = 1e-12 * std::max(scale, 1e-300);
+        for (int j = 0; j < 3; ++j) dead[BCo * I + j] = colNorm[j] > 0.5 ? 0 : 1;
+        for (int j = 3; j < 6; ++j) dead[BCo * I + j] = colNorm[j] > tol && scale > 0.0 ? 0 : 1;
+    }
+}
+
+// dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses and
+// the coarsest inverse for the current fine system
+static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
+    if (!c->amgStale) return EF_OK;
+    const int BCo = ef_amg_coarse_dofs();
+    const uint8_t* fineDead = c->hMask.data();
+    for (size_t l = 0; l < c->amg.size(); ++l) {
+        AmgLevel& L = c->amg[l];
+        amg_dead_mask(L, l == 0 ? 3 : BCo, fineDead, L.hDead);
+        EF_CUDA(cudaMemcpyAsync(L.dead, L.hDead.data(), L.hDead.size(), cudaMemcpyHostToDevice, s));
+        fineDead = L.hDead.data();
+    }
+    for (size_t l = 0; l < c->amg.size(); ++l) {
+        AmgLevel& L = c->amg[l];
+        const bool fine = l == 0;
+        const int32_t* fRob = fine ? c->dRowOfBlock0 : c->amg[l - 1].rowOfBlock;
+        const int32_t* fCol = fine ? c->dColIdx : c->amg[l - 1].colIdx;
+        const float* fVals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
+        const uint8_t* fMask = fine ? c->dMask : c->amg[l - 1].dead;
+        EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
+                                    L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+        EF_CHECK(ef_launch_bj6_setup(L.nN, L.diagPos, L.vals, L.binv, s));
+    }
+    const AmgLevel& C = c->amg.back();
+    EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
+    if (c->nnInit) {
+        EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
+        EF_CHECK(ef_launch_gather_f32(c->nBlocks, c->nnTpos, c->nnA, c->nnAT, s));
+    }
+    c->amgStale = false;
+    return EF_OK;
+}
+
+// x = V-cycle(r) on level l (l = 0: the fine system); one damped block-Jacobi sweep before and
+// after the coarse correction, dense solve on the coarsest level
+static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s) {
+    const float omega = c->amgOmega;
+    const int nL = (int)c->amg.size();
+    const int BCo = ef_amg_coarse_dofs();
+    if (l == nL) {
+        const AmgLevel& C = c->amg.back();
+        return ef_launch_coarsest_apply(BCo * C.nN, c->amgCoarsestInv, r, C.dead, x, s);
+    }
+    const bool fine = l == 0;
+    const int bs = fine ? 3 : BCo;
+    const int nN = fine ? (int)c->nNodes : c->amg[l - 1].nN;
+    const int32_t* rowPtr = fine ? c->dRowPtr : c->amg[l - 1].rowPtr;
+    const int32_t* colIdx = fine ? c->dColIdx : c->amg[l - 1].colIdx;
+    const float* vals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
+    const float* binv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
+    const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
+    float* t = fine ? c->fineT : c->amg[l - 1].t;
+    AmgLevel& Cn = c->amg[l];
+    // pre-smoothing from zero
+    EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x, 0, s));
+    for (int k = 1; k < c->amgSweeps; ++k) {
+        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+    }
+    // coarse correction (repeated for a W-cycle below the finest level)
+    const int reps = (l > 0 && c->amgCycle > 1) ? c->amgCycle : 1;
+    for (int rep = 0; rep < reps; ++rep) {
+        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
+        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
+        EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, x, s, c->amgAlpha));
+    }
+    // post-smoothing
+    for (int k = 0; k < c->amgSweeps; ++k) {
+        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+    }
+    return EF_OK;
+}
+
+// preconditioner of FGMRES: z = V-cycle(v) (+ the learned correction when enabled)
+// learned correction: z = Mv + NN([Mv, v, D^-1 v]) with Mv in vcOut and v in vcIn, written to vcOut2
+static ef_status nn_apply(ef_ctx* c, cudaStream_t s) {
+    EF_CHECK(ef_launch_features((int)c->nNodes, c->vcOut, c->vcIn, (const float*)c->dBinv, c->nnS[0], c->nnS[1],
+                                c->nnS[2], c->nnF, s));
+    return ef_mpnn_forward((int)c->nNodes, c->dRowPtr, c->dColIdx, c->nnA, c->nnPf, c->nnF, c->vcOut, c->dMask,
+                           c->nnSo, c->nnActs, c->vcOut2, s);
+}
+
+static ef_status nn_capture(ef_ctx* c) {
+    if (c->nnGraph) return EF_OK;
+    EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
+    const ef_status st = nn_apply(c, c->capStream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->capStream, &g);
+    if (st != EF_OK) return st;
+    if (e != cudaSuccess) {
+        ef_set_error(std::string("network capture: ") + cudaGetErrorString(e));
+        return EF_ERR_CUDA;
+    }
+    EF_CUDA(cudaGraphInstantiate(&c->nnGraph, g, 0));
+    cudaGraphDestroy(g);
+    return EF_OK;
+}
+
+static ef_status fgmres_precond(ef_ctx* c, const float* v, float* z, cudaStream_t s) {
+    EF_CHECK(amg_capture(c));
+    EF_CUDA(cudaMemcpyAsync(c->vcIn, v, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+    EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
+    if (c->nnOn) {
+        EF_CHECK(nn_capture(c));
+        EF_CUDA(cudaGraphLaunch(c->nnGraph, s));
+        EF_CUDA(cudaMemcpyAsync(z, c->vcOut2, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+    } else {
+        EF_CUDA(cudaMemcpyAsync(z, c->vcOut, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+    }
+    return EF_OK;
+}
+
+// FGMRES(m) on the free DOFs for K x = b (FP32 vectors, FP64 reductions and Hessenberg);
+// x starts at 0; stops at ||b - K x|| <= rtol ||b|| (Arnoldi estimate) or maxIter
+static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, double rtol, int restart, int* iters,
+                            ef_solve_info* prof, cudaStream_t s) {
+    const int64_t n = c->nDof;
+    const int m = std::max(2, std::min(restart, ef_fgmres_max_basis() - 2));
+    ef_status st = EF_OK;
+    if (c->fgRestart < m) {
+        if (c->fgV) cudaFree(c->fgV);
+        if (c->fgZ) cudaFree(c->fgZ);
+        c->fgV = dalloc<float>((size_t)(m + 1) * n, &st);
+        c->fgZ = dalloc<float>((size_t)m * n, &st);
+        if (!c->fgV || !c->fgZ) return st;
+        c->fgRestart = m;
+    }
+    if (!c->fgW) {
+        c->fgW = dalloc<float>(n, &st);
+        c->fgPart = dalloc<double>((size_t)c->nPart * ef_fgmres_max_basis(), &st);
+        c->fgH = dalloc<double>(4 * (size_t)ef_fgmres_max_basis(), &st);
+        if (!c->fgW || !c->fgPart || !c->fgH) return st;
+    }
+    double* dh = c->fgH;                                // pass-1 coefficients (accumulated)
+    double* dh2 = c->fgH + ef_fgmres_max_basis();      // pass-2 coefficients
+    double* dnrm = c->fgH + 2 * ef_fgmres_max_basis(); // squared norm
+    double* dy = c->fgH + 3 * ef_fgmres_max_basis();   // solution coefficients
+    float* dinv = (float*)(c->fgH + 2 * ef_fgmres_max_basis() + 1);  // 1 / norm as float
+    float* V = c->fgV;
+    float* Z = c->fgZ;
+    float* w = c->fgW;
+    EF_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, s));
+    // r0 = b (x = 0)
+    EF_CUDA(cudaMemcpyAsync(w, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    double beta2 = 0.0;
+    EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
+    EF_CUDA(cudaMemcpyAsync(&beta2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    const double bnorm = sqrt(beta2);
+    *iters = 0;
+    if (!(bnorm > 0.0)) return EF_OK;
+    double beta = bnorm;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 2);
+    int total = 0;
+    bool converged = false;
+    while (total < maxIter && !converged) {
+        EF_CHECK(ef_launch_scale(n, w, dinv, V, s));  // v0 = r / ||r||
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && total < maxIter; ++j) {
+            if (prof) EF_CUDA(cudaEventRecord(c->ev[0], s));
+            EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, Z + (int64_t)j * n, s));
+            EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals,
+                                        Z + (int64_t)j * n, c->dMask, w, s));
+            // classical Gram-Schmidt, twice
+            EF_CUDA(cudaMemsetAsync(dh, 0, sizeof(double) * (j + 1), s));
+            EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
+            EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
+            EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
+            EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
+            EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
+            EF_CHECK(ef_launch_scale(n, w, dinv, V + (int64_t)(j + 1) * n, s));
+            if (prof) EF_CUDA(cudaEventRecord(c->ev[1], s));
+            EF_CUDA(cudaMemcpyAsync(hcol.data(), dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+            double hn2 = 0.0;
+            EF_CUDA(cudaMemcpyAsync(&hn2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+            EF_CUDA(cudaStreamSynchronize(s));
+            if (prof) {
+                float ms = 0.f;
+                EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+                prof->kernelMs += ms;
+                prof->kernelLaunches += 1;
+            }
+            ++total;
+            double* Hj = &H[(size_t)j * (m + 1)];  // column j
+            for (int i = 0; i <= j; ++i) Hj[i] = hcol[i];
+            Hj[j + 1] = sqrt(hn2);
+            for (int i = 0; i < j; ++i) {  // previous Givens rotations
+                const double t0 = cs[i] * Hj[i] + sn[i] * Hj[i + 1];
+                Hj[i + 1] = -sn[i] * Hj[i] + cs[i] * Hj[i + 1];
+                Hj[i] = t0;
+            }
+            const double den = hypot(Hj[j], Hj[j + 1]);
+            cs[j] = den > 0.0 ? Hj[j] / den : 1.0;
+            sn[j] = den > 0.0 ? Hj[j + 1] / den : 0.0;
+            Hj[j] = den;
+            Hj[j + 1] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            if (!(g[j + 1] == g[j + 1]) || !(den == den)) return EF_NAN;
+            if (fabs(g[j + 1]) <= rtol * bnorm || hn2 <= 0.0) {
+                converged = fabs(g[j + 1]) <= rtol * bnorm;
+                ++j;
+                break;
+            }
+        }
+        // y = R^-1 g, x += Z y
+        std::vector<double> y(j);
+        for (int i = j - 1; i >= 0; --i) {
+            double acc = g[i];
+            for (int k = i + 1; k < j; ++k) acc -= H[(size_t)k * (m + 1) + i] * y[k];
+            y[i] = acc / H[(size_t)i * (m + 1) + i];
+        }
+        EF_CUDA(cudaMemcpyAsync(dy, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        EF_CHECK(ef_launch_combine(n, j, Z, n, dy, x, s));
+        if (converged || total >= maxIter) break;
+        // restart: r = b - K x
+        EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, x, c->dMask,
+                                    c->fineT, s));
+        EF_CHECK(ef_launch_sub(n, b, c->fineT, w, s));
+        EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
+        EF_CUDA(cudaMemcpyAsync(&beta2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+        EF_CUDA(cudaStreamSynchronize(s));
+        beta = sqrt(beta2);
+        if (beta <= rtol * bnorm) {
+            converged = true;
+            break;
+        }
+    }
+    *iters = total;
+    return converged ? EF_OK : EF_NOT_CONVERGED;
+}
+
+extern "C" {
+
 ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x, ef_solve_info* info, void* stream) {
     EF_REQUIRE_FINALIZED(c);
     if (!o || !b || !x) return EF_ERR_ARG;
-    if (o->method != EF_SOLVE_PCG) {
-        ef_set_error("ef_solve: method not available in this library version");
+    if (o->method != EF_SOLVE_PCG && o->method != EF_SOLVE_FGMRES) {
+        ef_set_error("ef_solve: unknown method");
+        return EF_ERR_ARG;
+    }
+    if (o->method == EF_SOLVE_FGMRES && (c->keFp64 || !o->mixed)) {
+        ef_set_error("ef_solve: FGMRES runs as the FP32 inner solver of the mixed-precision refinement");
         return EF_ERR_ARG;
     }
     if (!o->mixed && !c->keFp64) {
@@ -1076,8 +1704,21 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             EF_CHECK(ef_launch_masked_copy(n, r64, c->dMask, 0, 1.0 / rn, wv[0], vd, s));
             const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
             PcgResultHost pr;
-            EF_CHECK(run_pcg(c, vd, wv[0], wv[1], o->maxIter - total, std::min(inner, 0.5), &pr,
-                             o->profile ? &inf : nullptr, s));
+            if (o->method == EF_SOLVE_FGMRES) {
+                EF_CHECK(amg_build(c));
+                EF_CHECK(amg_refresh(c, s));
+                int its = 0;
+                const ef_status fs = run_fgmres(c, (const float*)wv[0], (float*)wv[1], o->maxIter - total,
+                                                std::min(inner, 0.5), o->restart, &its, o->profile ? &inf : nullptr, s);
+                if (fs != EF_OK && fs != EF_NOT_CONVERGED && fs != EF_NAN) return fs;
+                pr.iterations = its;
+                pr.status = fs;
+                pr.rr = 0.0;
+                pr.bb = 0.0;
+            } else {
+                EF_CHECK(run_pcg(c, vd, wv[0], wv[1], o->maxIter - total, std::min(inner, 0.5), &pr,
+                                 o->profile ? &inf : nullptr, s));
+            }
             total += pr.iterations;
             inf.refinements++;
             if (pr.status == EF_NAN) {

@@ -111,7 +111,7 @@ class LinSolverOptions:
     rtol: float = 1e-10  # FP64 ||b - K x|| / ||b||; tight enough that Newton counts match a direct solver
     innerRtol: float = 1e-4
     maxIter: int = 20000
-    restart: int = 60
+    restart: int = 40
     maxRefine: int = 30
     profile: bool = False
 
