@@ -96,6 +96,21 @@ SIGNATURES = {
     "ef_bsr_matvec": (c_int, [c_vp, c_vp, c_vp, c_vp]),
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
+    "ef_mpnn_param_count": (c_int, []),
+    "ef_mpnn_init": (c_int, [c_vp, ctypes.c_uint64, c_int]),
+    "ef_mpnn_set_params": (c_int, [c_vp, c_vp, c_vp]),
+    "ef_mpnn_get_params": (c_int, [c_vp, c_vp, c_vp]),
+    "ef_mpnn_enable": (c_int, [c_vp, c_int]),
+    "ef_mpnn_collect": (c_int, [c_vp, c_int, c_int, c_int]),
+    "ef_mpnn_add_sample": (c_int, [c_vp, c_vp, c_vp, c_vp]),
+    "ef_mpnn_num_samples": (c_int, [c_vp, ctypes.POINTER(c_int)]),
+    "ef_mpnn_clear_samples": (c_int, [c_vp]),
+    "ef_mpnn_train": (c_int, [c_vp, c_int, ctypes.c_float, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl), c_vp]),
+    "ef_mpnn_eval": (
+        c_int,
+        [c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_float, ctypes.c_float, c_vp, c_vp,
+         ctypes.POINTER(c_dbl), c_vp],
+    ),
     "ef_pcg_solve_noalloc": (
         c_int,
         [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_dbl, ctypes.POINTER(EfSolveInfo), c_vp],

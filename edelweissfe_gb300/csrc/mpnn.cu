@@ -207,7 +207,7 @@ __global__ void output_backward_kernel(int nN, const float* __restrict__ z, cons
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int d = 3 * m + i;
-        const float g = (mask && mask[d]) ? 0.f : so * scale * (z[d] - e[d]);
+        const float g = (mask && mask[d]) ? 0.f : so * scale * (z[d] - (e ? e[d] : 0.f));
         if (c == 0) dout[d] = g;
         s += P[OFF_WOUT + i * H + c] * g;
     }
@@ -345,9 +345,91 @@ __global__ void adam_kernel(int n, float* __restrict__ p, const float* __restric
     pf[i] = __bfloat162float(q);
 }
 
+// BF16 inference copy and its FP32 view from the FP32 masters
+__global__ void refresh_kernel(int n, const float* __restrict__ p, __nv_bfloat16* __restrict__ pb,
+                               float* __restrict__ pf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const __nv_bfloat16 q = __float2bfloat16(p[i]);
+    pb[i] = q;
+    pf[i] = __bfloat162float(q);
+}
+
 __global__ void bf16_to_f32_kernel(int n, const __nv_bfloat16* __restrict__ pb, float* __restrict__ pf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) pf[i] = __bfloat162float(pb[i]);
+}
+
+// per-CTA partial sums in FP64 over the free DOFs: mode 1: (z - e)^2 (e may be null: z^2);
+// mode 0: z . e; mode 3: z^2 per 3-wide feature group of f ([n][9], no mask)
+__global__ void sumsq_partial_kernel(int64_t n, int groups, const float* __restrict__ z, const float* __restrict__ e,
+                                     const uint8_t* __restrict__ mask, double* __restrict__ part) {
+    __shared__ double red[8][3];
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (groups == 0) {
+            if (mask && mask[i]) continue;
+            acc[0] += (double)z[i] * (double)e[i];
+        } else if (groups == 3) {
+            const int g = (int)((i % FIN) / 3);
+            const double v = z[i];
+            acc[0] += g == 0 ? v * v : 0.0;
+            acc[1] += g == 1 ? v * v : 0.0;
+            acc[2] += g == 2 ? v * v : 0.0;
+        } else {
+            if (mask && mask[i]) continue;
+            const double d = (double)z[i] - (e ? (double)e[i] : 0.0);
+            acc[0] += d * d;
+        }
+    }
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+        double a = acc[g];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[wp][g] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+        part[(int64_t)blockIdx.x * 3 + threadIdx.x] = t;
+    }
+}
+
+__global__ void sumsq_final_kernel(int nPart, const double* __restrict__ part, double* __restrict__ out) {
+    const int g = threadIdx.x;
+    if (g >= 3) return;
+    double t = 0.0;
+    for (int c = 0; c < nPart; ++c) t += part[(int64_t)c * 3 + g];
+    out[g] = t;
+}
+
+__global__ void scale_inplace_kernel(int64_t n, float* __restrict__ x, float a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= a;
+}
+
+// fs[m][i] = s[i / 3] * f[m][i]
+__global__ void scale_features_kernel(int64_t n, const float* __restrict__ f, float s0, float s1, float s2,
+                                      float* __restrict__ fs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)((i % FIN) / 3);
+    fs[i] = f[i] * (g == 0 ? s0 : (g == 1 ? s1 : s2));
+}
+
+// z = Mv + alpha N on free DOFs (0 on masked), alpha = dots[0] / dots[3] (0 if dots[3] <= 0):
+// the step length along the network output that minimises |v - K z| given rho.KN and |KN|^2
+__global__ void alpha_combine_kernel(int64_t n, const float* __restrict__ Mv, const float* __restrict__ N,
+                                     const double* __restrict__ dots, const uint8_t* __restrict__ mask,
+                                     float* __restrict__ z) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double den = dots[3];
+    const float alpha = den > 0.0 ? (float)(dots[0] / den) : 0.f;
+    z[i] = (mask && mask[i]) ? 0.f : Mv[i] + alpha * N[i];
 }
 
 }  // namespace ef
@@ -405,7 +487,7 @@ ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, 
 }
 
 // backward pass for loss L = 0.5 * scale * sum_free (z - e)^2 (scale folds the 1/|e|^2 factor and 2);
-// grad [NPARAM] overwritten; work: 3 x nN x H floats; part: nPart x H*H floats
+// grad [NPARAM] overwritten; work: 4 x nN x H floats; part: nPart x H*H floats
 ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* aT, const float* P,
                            const float* f, const float* acts, const float* z, const float* e, const uint8_t* mask,
                            float scale, float so, float* grad, float* work, float* part, int nPart, cudaStream_t s) {
@@ -448,9 +530,9 @@ ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx,
 }
 
 ef_status ef_mpnn_adam(int n, float* p, const float* g, float* m1, float* m2, float lr, float b1, float b2, float eps,
-                       int step, __nv_bfloat16* pb, float* pf, cudaStream_t s) {
+                       int step, void* pb, float* pf, cudaStream_t s) {
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    adam_kernel<<<nbm(n, 256), 256, 0, s>>>(n, p, g, m1, m2, lr, b1, b2, eps, c1, c2, pb, pf);
+    adam_kernel<<<nbm(n, 256), 256, 0, s>>>(n, p, g, m1, m2, lr, b1, b2, eps, c1, c2, (__nv_bfloat16*)pb, pf);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -464,6 +546,43 @@ ef_status ef_launch_features(int nN, const float* Mv, const float* v, const floa
 
 ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s) {
     bf16_to_f32_kernel<<<nbm(n, 256), 256, 0, s>>>(n, (const __nv_bfloat16*)pb, pf);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// out[0..3) = the sums of sumsq_partial_kernel (mode `groups`); part holds nPart x 3 doubles;
+// deterministic
+ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
+                        int nPart, double* out, cudaStream_t s) {
+    sumsq_partial_kernel<<<nPart, 256, 0, s>>>(n, groups, z, e, mask, part);
+    sumsq_final_kernel<<<1, 32, 0, s>>>(nPart, part, out);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_mpnn_scale(int64_t n, float* x, float a, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    scale_inplace_kernel<<<nbm(n, 256), 256, 0, s>>>(n, x, a);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_mpnn_scale_features(int nN, const float* f, float s0, float s1, float s2, float* fs, cudaStream_t s) {
+    const int64_t n = (int64_t)nN * FIN;
+    scale_features_kernel<<<nbm(n, 256), 256, 0, s>>>(n, f, s0, s1, s2, fs);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_mpnn_refresh(int n, const float* p, void* pb, float* pf, cudaStream_t s) {
+    refresh_kernel<<<nbm(n, 256), 256, 0, s>>>(n, p, (__nv_bfloat16*)pb, pf);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, const double* dots, const uint8_t* mask,
+                                float* z, cudaStream_t s) {
+    alpha_combine_kernel<<<nbm(n, 256), 256, 0, s>>>(n, Mv, N, dots, mask, z);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -249,6 +249,56 @@ class NISTGPU:
         _lib.check(st, "ef_solve")
         return ddU
 
+    # ---- learned preconditioner correction (FGMRES only) ----------------------------------------
+
+    def initLearnedPreconditioner(self, seed=0, maxSamples=64):
+        """Allocates the message-passing correction applied after the multigrid cycle and sets
+        its initial weights (zero output layer: no correction until trained)."""
+        _lib.check(self.lib.ef_mpnn_init(self.ctx, seed, maxSamples), "ef_mpnn_init")
+
+    def collectTrainingPairs(self, every=25, maxPerSolve=10, kind="iterates"):
+        """Keep training pairs from the following FGMRES solves (every = 0: stop): "iterates"
+        (K e_k, e_k) with e_k the error of the k-th iterate, or "krylov" basis vectors (inputs
+        without a correction, for the residual-norm loss)."""
+        k = {"iterates": 0, "krylov": 1}[kind]
+        _lib.check(self.lib.ef_mpnn_collect(self.ctx, every, maxPerSolve, k), "ef_mpnn_collect")
+
+    def addTrainingPair(self, r, e):
+        """One pair of device FP64 vectors with K e = r on the free DOFs."""
+        _lib.check(self.lib.ef_mpnn_add_sample(self.ctx, r.data_ptr(), e.data_ptr(), self._stream()),
+                   "ef_mpnn_add_sample")  # fmt: skip
+
+    def numTrainingPairs(self):
+        n = ctypes.c_int()
+        _lib.check(self.lib.ef_mpnn_num_samples(self.ctx, ctypes.byref(n)), "ef_mpnn_num_samples")
+        return n.value
+
+    LOSS_NORMS = {"error": 0, "energy": 1, "residual": 2}
+
+    def trainLearnedPreconditioner(self, epochs=20, lr=1e-3, norm="energy"):
+        """Adam over the stored pairs; returns the mean relative loss of the first and the last
+        epoch (epochs = 0: evaluation only).  norm: "error" |z - e|^2, "energy" (z - e).K(z - e)
+        or "residual" |K(z - e)|^2, each relative to the same norm of e."""
+        first, last = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.ef_mpnn_train(self.ctx, epochs, lr, self.LOSS_NORMS[norm], ctypes.byref(first),
+                                          ctypes.byref(last), self._stream()), "ef_mpnn_train")  # fmt: skip
+        return first.value, last.value
+
+    def enableLearnedPreconditioner(self, on=True):
+        _lib.check(self.lib.ef_mpnn_enable(self.ctx, 1 if on else 0), "ef_mpnn_enable")
+
+    def learnedParameters(self):
+        p = np.zeros(self.lib.ef_mpnn_param_count(), np.float32)
+        sc = np.zeros(4, np.float32)
+        _lib.check(self.lib.ef_mpnn_get_params(self.ctx, p.ctypes.data, sc.ctypes.data), "ef_mpnn_get_params")
+        return p, sc
+
+    def setLearnedParameters(self, params=None, scales=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        sc = None if scales is None else np.ascontiguousarray(scales, np.float32)
+        _lib.check(self.lib.ef_mpnn_set_params(self.ctx, None if p is None else p.ctypes.data,
+                                               None if sc is None else sc.ctypes.data), "ef_mpnn_set_params")  # fmt: skip
+
     def checkConvergence(self, R, ddU, F, iterationCounter, residualHistory):
         out = np.zeros(3)
         _lib.check(

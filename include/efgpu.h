@@ -190,6 +190,55 @@ ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr, const int3
  * Deterministic; synchronises `stream`. */
 ef_status ef_norms(ef_ctx* ctx, const double* R, const double* F, const double* ddU, double* out, void* stream);
 
+/* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----
+ * The reference solves every Newton system with a direct or plain Krylov solver
+ * (solvers/nonlinearimplicitstatic.py:547-571, linearSolve; utils/linearsolve.py:35-77); this
+ * optional stage replaces nothing there.  With it enabled the FGMRES preconditioner becomes
+ * z = Mv + alpha N, N = NN([Mv, rho, D^-1 rho]), rho = v - K Mv: Mv the multigrid cycle, D the
+ * 3x3 diagonal blocks, NN a 3-layer message-passing network (hidden width 64, no biases, BF16
+ * weights, FP32 accumulation) on the node graph of the block system with edge weights
+ * |K_mn|_F / sum_n' |K_mn'|_F, and alpha = rho.KN / |KN|^2 (the step that minimises |v - K z|).
+ * It is trained with Adam on pairs (r, e), K e = r, taken from solves with the network disabled. */
+
+/* Number of network weights (W_in [64][9], 3 x (Ws [64][64], Wn [64][64]), W_out [3][64]). */
+int ef_mpnn_param_count(void);
+/* Allocates the network state (once) and (re)initialises the weights from `seed` (the output
+ * layer at zero, so the initial correction is zero); keeps up to maxSamples training pairs. */
+ef_status ef_mpnn_init(ef_ctx* ctx, uint64_t seed, int maxSamples);
+/* Host FP32 weights [ef_mpnn_param_count()] and scales [4] = {s_Mv, s_v, s_Dv, s_out}; either may
+ * be NULL.  Setting weights resets the Adam moments. */
+ef_status ef_mpnn_set_params(ef_ctx* ctx, const float* params, const float* scales);
+ef_status ef_mpnn_get_params(ef_ctx* ctx, float* params, float* scales);
+/* on != 0: FGMRES solves apply the network after the multigrid cycle. */
+ef_status ef_mpnn_enable(ef_ctx* ctx, int on);
+/* Training pairs from the following FGMRES solves, every `every` iterations and at most
+ * maxPerSolve per inner solve.  kind 0: the iterate x_k is kept (plus x_0 = 0) and, when the
+ * solve converges to x, (K (x - x_k), x - x_k) becomes a pair; kind 1: the Krylov basis vector
+ * v_k becomes an input without correction (usable by the residual-norm loss only).
+ * every = 0 switches collection off. */
+ef_status ef_mpnn_collect(ef_ctx* ctx, int every, int maxPerSolve, int kind);
+/* Adds one training pair from device FP64 vectors [nDof] with K e = r on the free DOFs. */
+ef_status ef_mpnn_add_sample(ef_ctx* ctx, const double* r, const double* e, void* stream);
+ef_status ef_mpnn_num_samples(const ef_ctx* ctx, int* n);
+ef_status ef_mpnn_clear_samples(ef_ctx* ctx);
+/* `epochs` passes of Adam (one pair per step, deterministic shuffle) at learning rate lr;
+ * epochs = 0 only evaluates.  Loss of a pair with d = z - e on the free DOFs, relative to the
+ * same norm of e: norm 0 |d|^2, norm 1 d.K d (energy), norm 2 |K d|^2 (residual), K the system
+ * the pair came from (up to 16 systems are kept; the pairs of the oldest are dropped first).
+ * lossFirst / lossLast (host, may be NULL) receive the mean over the pairs in the first and the
+ * last epoch.  Synchronises `stream`. */
+ef_status ef_mpnn_train(ef_ctx* ctx, int epochs, float lr, int norm, double* lossFirst, double* lossLast,
+                        void* stream);
+/* One forward and backward pass of the network on a caller's graph, all arrays on the HOST:
+ * rowPtr [nNodes+1], colIdx [nBlocks] (structurally symmetric, sorted rows), vals [nBlocks][9],
+ * params FP32 [ef_mpnn_param_count()], f [nNodes][9] features, base [3 nNodes] (may be NULL),
+ * e [3 nNodes] target, mask [3 nNodes] (may be NULL).  z = base + so * W_out h3 (0 on masked),
+ * loss = 0.5 * scale * sum_free (z - e)^2, grad = d loss / d params (may be NULL).  For
+ * verification against an independent implementation; synchronises `stream`. */
+ef_status ef_mpnn_eval(int nNodes, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                       const float* params, const float* f, const float* base, const float* e, const uint8_t* mask,
+                       float so, float scale, float* z, float* grad, double* loss, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,99 @@
+"""Learned preconditioner correction: the float64 oracle against finite differences (CPU), the
+CUDA forward/backward against the oracle, and the iteration gain of the trained network (GPU)."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import mpnn as om
+from oracle.mesh import BoxMesh
+
+
+def _graph(nX=4, nY=3, nZ=3):
+    m = BoxMesh(nX, nY, nZ)
+    return om.node_pattern(m.elements, m.nNodes)
+
+
+def test_oracle_edge_weights_are_row_normalised():
+    rowPtr, colIdx = _graph()
+    case = om.random_case(rowPtr, colIdx, seed=1)
+    a = om.edge_weights(rowPtr, colIdx, case["vals"])
+    rows = np.repeat(np.arange(len(rowPtr) - 1), np.diff(rowPtr))
+    assert np.all(a[colIdx == rows] == 0.0)
+    np.testing.assert_allclose(np.bincount(rows, weights=a), 1.0, rtol=1e-12)
+    # symmetric block magnitudes: a_mn * tot_m = a_nm * tot_n
+    assert np.all(a >= 0.0)
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rowPtr, colIdx = _graph(3, 2, 2)
+    c = om.random_case(rowPtr, colIdx, seed=2)
+    P = c["P"].astype(np.float64)
+    args = (rowPtr, colIdx, c["vals"])
+    rest = (c["f"], c["base"], c["e"], c["mask"], 0.7, 0.5)
+    _, loss, g = om.loss_and_grad(*args, P, *rest)
+    rng = np.random.default_rng(0)
+    # a few parameters of every block (input, each layer's Ws / Wn, output) and one random direction
+    idx = np.concatenate([rng.integers(lo, hi, 6) for lo, hi in [
+        (om.OFF_WIN, om.OFF_L0), (om.OFF_L0, om.OFF_L0 + om.H * om.H), (om.OFF_L0 + om.H * om.H, om.OFF_L0 + om.PER_LAYER),
+        (om.OFF_L0 + 2 * om.PER_LAYER, om.OFF_WOUT), (om.OFF_WOUT, om.NPARAM)]])  # fmt: skip
+    h = 1e-6
+    for i in idx:
+        Pp, Pm = P.copy(), P.copy()
+        Pp[i] += h
+        Pm[i] -= h
+        fd = (om.loss_and_grad(*args, Pp, *rest)[1] - om.loss_and_grad(*args, Pm, *rest)[1]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (i, fd, g[i])
+    d = rng.normal(size=P.size)
+    fd = (om.loss_and_grad(*args, P + h * d, *rest)[1] - om.loss_and_grad(*args, P - h * d, *rest)[1]) / (2 * h)
+    assert abs(fd - g @ d) <= 1e-6 * max(1.0, abs(g @ d))
+    assert loss > 0.0
+
+
+def test_oracle_network_is_positively_homogeneous():
+    rowPtr, colIdx = _graph()
+    c = om.random_case(rowPtr, colIdx, seed=3)
+    a = om.edge_weights(rowPtr, colIdx, c["vals"])
+    f, base = c["f"].astype(np.float64), c["base"].astype(np.float64)
+    z1, _ = om.forward(rowPtr, colIdx, a, c["P"], f, base, c["mask"], 1.0)
+    z2, _ = om.forward(rowPtr, colIdx, a, c["P"], 3.5 * f, 3.5 * base, c["mask"], 1.0)
+    np.testing.assert_allclose(z2, 3.5 * z1, rtol=1e-12, atol=1e-12)
+
+
+def _eval_gpu(lib, rowPtr, colIdx, c, so, scale, with_grad=True):
+    nN = len(rowPtr) - 1
+    z = np.zeros(3 * nN, np.float32)
+    g = np.zeros(om.NPARAM, np.float32)
+    loss = ctypes.c_double()
+    arrs = dict(r=np.ascontiguousarray(rowPtr, np.int32), c=np.ascontiguousarray(colIdx, np.int32),
+                v=np.ascontiguousarray(c["vals"], np.float32), p=np.ascontiguousarray(c["P"], np.float32),
+                f=np.ascontiguousarray(c["f"], np.float32), b=np.ascontiguousarray(c["base"], np.float32),
+                e=np.ascontiguousarray(c["e"], np.float32), m=np.ascontiguousarray(c["mask"], np.uint8))  # fmt: skip
+    st = lib.ef_mpnn_eval(nN, arrs["r"].ctypes.data, arrs["c"].ctypes.data, arrs["v"].ctypes.data,
+                          arrs["p"].ctypes.data, arrs["f"].ctypes.data, arrs["b"].ctypes.data, arrs["e"].ctypes.data,
+                          arrs["m"].ctypes.data, so, scale, z.ctypes.data, g.ctypes.data if with_grad else None,
+                          ctypes.byref(loss), None)  # fmt: skip
+    assert st == 0, lib.ef_last_error().decode()
+    return z, g, loss.value
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims", [(4, 3, 3), (12, 7, 5)])
+def test_gpu_network_forward_backward_match_oracle(gpu_lib, dims):
+    """FP32 CUDA forward/backward against the float64 oracle: z to 1e-5 and every gradient block
+    to 1e-4 of its largest entry (FP32 accumulation over the nodes)."""
+    rowPtr, colIdx = _graph(*dims)
+    c = om.random_case(rowPtr, colIdx, seed=7)
+    so, scale = 0.8, 1.0 / (3 * (len(rowPtr) - 1))
+    z, g, loss = _eval_gpu(gpu_lib, rowPtr, colIdx, c, so, scale)
+    zo, lo, go = om.loss_and_grad(rowPtr, colIdx, c["vals"], c["P"].astype(np.float64), c["f"], c["base"], c["e"],
+                                  c["mask"], so, scale)  # fmt: skip
+    assert np.max(np.abs(z - zo)) <= 1e-5 * np.max(np.abs(zo))
+    assert abs(loss - lo) <= 1e-5 * lo
+    blocks = [(om.OFF_WIN, om.OFF_L0)] + [
+        (om.OFF_L0 + l * om.PER_LAYER + k * om.H * om.H, om.OFF_L0 + l * om.PER_LAYER + (k + 1) * om.H * om.H)
+        for l in range(om.NL) for k in range(2)] + [(om.OFF_WOUT, om.NPARAM)]  # fmt: skip
+    for lo_, hi_ in blocks:
+        ref = go[lo_:hi_]
+        assert np.max(np.abs(g[lo_:hi_] - ref)) <= 1e-4 * np.max(np.abs(ref)), (lo_, hi_)
