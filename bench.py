@@ -6,12 +6,17 @@ assembly, Krylov solve, repeated until the reference's convergence test passes):
   x=10 face pulled to u_x = 0.02 over 20 increments (maxInc 0.05).  The load history is
   advanced (untimed) into the plastic regime; every timed step re-solves the same
   plastic increment from the same committed state (the trial state is not accepted).
-  Inputs are resident and larger than L2 (BSR system 159 MB FP32, state 266 MB).
+  Inputs are resident and larger than L2 (BSR system 159 MB FP32, element state 266 MB).
 
-value     : load-step seconds with the plain block-Jacobi PCG (FP32 inner, FP64 refinement)
-e2e       : the same through the public Python API with the step's inputs (U_n, dU) copied
-            from pinned host memory and the result (U, P) read back every step
-roofline  : the dominant kernel (persistent PCG), bytes per iteration / measured time
+value     : load-step seconds with FGMRES(40) preconditioned by the rigid-body aggregation
+            multigrid cycle plus the learned message-passing correction (trained on pairs from
+            the plain solves of the load history; a validation solve keeps it only if it makes
+            the step faster), FP32 inner iterations with FP64 refinement to 1e-8
+comparison: the same load step with block-Jacobi PCG (same system, same tolerance)
+e2e       : the same as value through the public Python API with the step's inputs (U_n, dU)
+            copied from pinned host memory and the results (U, P) read back every step
+roofline  : the fine-level FP32 BSR SpMV of FGMRES (the dominant kind of pass: every fine
+            smoothing residual and every Krylov product streams the same 159 MB of blocks)
 cpu_baseline: the numpy oracle (restatement of the reference's CPU path) on a bounded sample
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nx 100 --ny 40 --nz 40]
@@ -31,6 +36,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PROPS = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
+METRIC = "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s"
+# Newton and Krylov iterations of the timed increment (13) of the 100x40x40 model with
+# block-Jacobi PCG, measured on GB300; the CPU arms scale their per-iteration samples by them
+PCG_NEWTON_PER_STEP = 8
+PCG_KRYLOV_PER_STEP = 17028
 
 
 def parse():
@@ -44,9 +54,11 @@ def parse():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--method", default="pcg", choices=["pcg", "fgmres"])
+    ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
+    ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
+    ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")
     ap.add_argument("--profile", action="store_true",
-                    help="one assembly and one capped PCG solve, for ncu captures of single kernels")
+                    help="one assembly and one capped solve, for ncu captures of single kernels")
     return ap.parse_args()
 
 
@@ -120,6 +132,12 @@ def build_solver(a, linsolver):
     return NISTGPU(model, dirs, linsolver=linsolver)
 
 
+def spmv_bytes(info):
+    """Algorithmic DRAM bytes of one FP32 BSR(3x3) SpMV y = K x on the free DOFs."""
+    nb, nn, nd = info.nBlocks, info.nNodes, info.nDof
+    return nb * (9 * 4 + 4) + (nn + 1) * 4 + nd * 4 + nd * 4 + nd  # blocks + columns, row pointers, x, y, mask
+
+
 def pcg_bytes_per_iteration(info, fp32=True):
     """Algorithmic DRAM bytes of one PCG iteration on the BSR(3x3) system."""
     s = 4 if fp32 else 8
@@ -158,36 +176,67 @@ def run_ours(a):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     t0 = time.time()
-    s = build_solver(a, LinSolverOptions(method=a.method, rtol=1e-8, profile=True))
+    s = build_solver(a, LinSolverOptions(method="fgmres", rtol=1e-8))
     setup_s = time.time() - t0
     info = s.info
+    lib = s.lib
     stream = torch.cuda.current_stream()
     step = Step(maxInc=0.05, minInc=1e-6, maxIter=25)
-    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    _lib.check(lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    learned = not a.no_learned
+    if learned:
+        s.initLearnedPreconditioner(seed=0, maxSamples=64)
+        s.collectTrainingPairs(every=20, maxPerSolve=12, kind="iterates")
 
-    # advance the load history (untimed) up to the increment that the steps re-solve
-    U = s._vec()
-    dU = s._vec()
-    P = s._vec()
+    # advance the load history (untimed, FGMRES without the learned stage, collecting pairs) up to
+    # the increment that the steps re-solve
+    U, dU, P = s._vec(), s._vec(), s._vec()
     prev = None
     stepper = AdaptiveTimeStepper(0.0, 1.0, step.startInc, step.maxInc, step.minInc, step.maxNumInc)
-    history = []
-    target = None
+    history, target = [], None
+    t0 = time.time()
     for ts in stepper.generateTimeStep():
         if ts.number == a.increment:
             target = ts
             break
         U, dU, P, it = s.solveIncrement(U, dU, P, ts, prev, step)
-        _lib.check(s.lib.ef_accept_state(s.ctx), "accept")
+        _lib.check(lib.ef_accept_state(s.ctx), "accept")
         history.append(it)
         prev = ts
+    history_s = time.time() - t0
     U_n, dU_n = U.clone(), dU.clone()
 
     def one_step():
         s.krylovIterations.clear()
-        d = dU_n.clone()
-        _, _, _, it = s.solveIncrement(U_n, d, s._vec(), target, prev, step)
+        _, _, _, it = s.solveIncrement(U_n, dU_n.clone(), s._vec(), target, prev, step)
         return it
+
+    def timed(n):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        its = [one_step() for _ in range(n)]
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / n, its, sum(s.krylovIterations)
+
+    learned_info = None
+    if learned:
+        s.collectTrainingPairs(0, 0)
+        t0 = time.time()
+        lf, ll = s.trainLearnedPreconditioner(epochs=20, lr=3e-4, norm="energy")
+        torch.cuda.synchronize()
+        train_s = time.time() - t0
+        # validation on the timed increment (these solves are part of the warm-up)
+        s.enableLearnedPreconditioner(False)
+        off_s, _, off_k = timed(1)
+        s.enableLearnedPreconditioner(True)
+        timed(1)
+        on_s, _, on_k = timed(1)
+        keep = on_s < off_s
+        s.enableLearnedPreconditioner(keep)
+        learned_info = {"pairs": s.numTrainingPairs(), "epochs": 20, "loss": "energy", "loss_first": lf,
+                        "loss_last": ll, "train_s": train_s,
+                        "validation": {"on_s": on_s, "off_s": off_s, "on_krylov": on_k, "off_krylov": off_k},
+                        "enabled": keep}  # fmt: skip
 
     for _ in range(a.warmup):
         one_step()
@@ -198,67 +247,80 @@ def run_ours(a):
     clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    newton, krylov, kms, klaunch = [], [], 0.0, 0
+    newton, krylov = [], []
     torch.cuda.synchronize()
+    l0 = lib.ef_kernel_launches()
     e0.record(stream)
     for _ in range(a.steps):
-        s.linsolver.profile = True
         newton.append(one_step())
-        krylov.append(list(s.krylovIterations))
+        krylov.append(sum(s.krylovIterations))
     e1.record(stream)
     torch.cuda.synchronize()
+    launches = lib.ef_kernel_launches() - l0
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    # per-solve kernel timing (the persistent PCG launches) from the last timed step
-    prof_ms, prof_it, prof_launch = 0.0, 0, 0
-    for _ in range(1):
-        s.krylovIterations.clear()
-        d = dU_n.clone()
-        infos = []
-        orig = s.linearSolve
-
-        def wrapped(R):
-            x = orig(R)
-            infos.append((s.lastSolveInfo.kernelMs, s.lastSolveInfo.iterations, s.lastSolveInfo.kernelLaunches))
-            return x
-
-        s.linearSolve = wrapped
-        s.solveIncrement(U_n, d, s._vec(), target, prev, step)
-        s.linearSolve = orig
-        prof_ms = sum(i[0] for i in infos)
-        prof_it = sum(i[1] for i in infos)
-        prof_launch = sum(i[2] for i in infos)
-    t_step = ms / 1e3 / a.steps
+    t_step = e0.elapsed_time(e1) / 1e3 / a.steps
     if world > 1:
         t = torch.tensor([t_step], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_step = float(t.item())
 
+    def profiled_step():
+        infos = []
+        orig = s.linearSolve
+
+        def wrapped(R):
+            x = orig(R)
+            i = s.lastSolveInfo
+            infos.append((i.kernelMs, i.iterations, i.kernelLaunches, i.spmvMs, i.spmvLaunches))
+            return x
+
+        s.linsolver.profile = True
+        s.linearSolve = wrapped
+        try:
+            one_step()
+        finally:
+            s.linearSolve = orig
+            s.linsolver.profile = False
+        return [sum(x[i] for x in infos) for i in range(5)]
+
+    fg_kms, fg_it, _, sp_ms, sp_n = profiled_step()
+
+    # comparison arm: block-Jacobi PCG on the same load step
+    s.linsolver.method = "pcg"
+    if learned:
+        s.enableLearnedPreconditioner(False)
+    one_step()
+    pcg_s, pcg_newton, pcg_k = timed(max(1, a.pcg_steps))
+    pcg_kms, pcg_it, _, _, _ = profiled_step()
+    s.linsolver.method = "fgmres"
+    if learned_info and learned_info["enabled"]:
+        s.enableLearnedPreconditioner(True)
+
     # assembly timing: element kernel + condensation + BSR scatter on resident inputs
-    ts_ = target
-    t2 = np.array([ts_.stepTime, ts_.totalTime])
+    t2 = np.array([target.stepTime, target.totalTime])
     Pv, Fv = s._vec(), s._vec()
     times = {"elements": [], "assemble": []}
     for rep in range(6):
         ea, eb, ec = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         ea.record(stream)
-        _lib.check(s.lib.ef_compute_elements(s.ctx, U_n.data_ptr(), dU_n.data_ptr(), t2.ctypes.data, ts_.timeIncrement,
-                                             Pv.data_ptr(), Fv.data_ptr(), stream.cuda_stream), "ce")  # fmt: skip
+        _lib.check(lib.ef_compute_elements(s.ctx, U_n.data_ptr(), dU_n.data_ptr(), t2.ctypes.data,
+                                           target.timeIncrement, Pv.data_ptr(), Fv.data_ptr(), stream.cuda_stream),
+                   "ce")  # fmt: skip
         eb.record(stream)
-        _lib.check(s.lib.ef_assemble_bsr(s.ctx, stream.cuda_stream), "bsr")
+        _lib.check(lib.ef_assemble_bsr(s.ctx, stream.cuda_stream), "bsr")
         ec.record(stream)
         torch.cuda.synchronize()
         if rep >= 2:
             times["elements"].append(ea.elapsed_time(eb))
             times["assemble"].append(eb.elapsed_time(ec))
-    s.lib.ef_element_status(s.ctx, stream.cuda_stream, None)
+    lib.ef_element_status(s.ctx, stream.cuda_stream, None)
     nEl = a.nx * a.ny * a.nz
     b_elem, b_cond, b_scat = assembly_bytes(info, nEl)
     t_el = float(np.median(times["elements"])) * 1e-3
     t_as = float(np.median(times["assemble"])) * 1e-3
     asm_gbs = (b_elem + b_cond + b_scat) / (t_el + t_as) / 1e9
 
-    # e2e through the public API: host inputs -> device, solve, results -> host
+    # e2e through the public API: host inputs -> device, load step, results -> host
     hU = U_n.cpu().pin_memory()
     hdU = dU_n.cpu().pin_memory()
     outU = torch.empty(s.nDof, dtype=torch.float64).pin_memory()
@@ -279,14 +341,23 @@ def run_ours(a):
     e2e_s = f0.elapsed_time(f1) / 1e3 / e2e_steps
 
     peaks, peak_kind = measured_peaks()
-    bpi = pcg_bytes_per_iteration(info)
-    achieved = bpi * prof_it / (prof_ms * 1e-3) / 1e9 if prof_ms > 0 else None
+    sb = spmv_bytes(info)
+    sp_avg = sp_ms / sp_n if sp_n else None
+    achieved = sb / (sp_avg * 1e-3) / 1e9 if sp_avg else None
+    pcg_bpi = pcg_bytes_per_iteration(info)
+    pcg_gbs = pcg_bpi * pcg_it / (pcg_kms * 1e-3) / 1e9 if pcg_kms > 0 else None
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, newton_per_step=float(np.mean(newton)),
-                           krylov_per_step=float(np.mean([sum(k) for k in krylov])))  # fmt: skip
+        cpu = cpu_baseline(a, newton_per_step=PCG_NEWTON_PER_STEP, krylov_per_step=PCG_KRYLOV_PER_STEP, procs=1)
+    fg_k = float(np.mean(krylov))
+    if learned_info and learned_info["enabled"]:
+        stage = "learned correction kept"
+    elif learned_info:
+        stage = "learned correction trained, dropped by the validation solve"
+    else:
+        stage = "no learned correction"
     line = {
-        "metric": "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s",
+        "metric": METRIC,
         "value": t_step,
         "unit": "s",
         "n_gpus": world,
@@ -299,68 +370,94 @@ def run_ours(a):
         "dtype": "f64 residual/return map, f32 stiffness + Krylov inner, f64 refinement",
         "data": "synthetic (structured box mesh, seeded parameters)",
         "config": workload(a),
-        "solver": "block-Jacobi PCG (plain method)",
+        "solver": f"FGMRES(40) + rigid-body aggregation W-cycle ({stage})",
         "newton_iterations_per_step": newton,
-        "krylov_iterations_per_step": [sum(k) for k in krylov],
+        "krylov_iterations_per_step": krylov,
+        "comparison": {"jacobi_pcg_step_s": pcg_s, "speedup_vs_jacobi_pcg": pcg_s / t_step,
+                       "jacobi_pcg_krylov_per_step": pcg_k, "fgmres_krylov_per_step": fg_k,
+                       "krylov_ratio": pcg_k / fg_k if fg_k else None, "jacobi_pcg_newton": pcg_newton,
+                       "jacobi_pcg_kernel_GBps": pcg_gbs,
+                       "jacobi_pcg_frac_hbm": pcg_gbs / peaks["hbm_gbs"] if pcg_gbs else None},
+        "learned": learned_info,
         "assembly": {"elements_ms": t_el * 1e3, "bsr_scatter_ms": t_as * 1e3, "GBps": asm_gbs,
-                     "frac_hbm": asm_gbs / peaks["hbm_gbs"], "bytes": b_elem + b_cond + b_scat},
-        "dof_iterations_per_s": info.nDof * prof_it / (prof_ms * 1e-3) if prof_ms > 0 else None,
+                     "frac_hbm": asm_gbs / peaks["hbm_gbs"], "bytes": b_elem + b_cond + b_scat,
+                     "elements_per_s": nEl / (t_el + t_as)},
+        "fgmres_profile": {"iterations": fg_it, "kernel_ms": fg_kms,
+                           "ms_per_iteration": fg_kms / fg_it if fg_it else None},
+        "dof_iterations_per_s": info.nDof * fg_it / (fg_kms * 1e-3) if fg_kms > 0 else None,
         "setup_s": setup_s,
+        "history_s": history_s,
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.nDof, "d2h_bytes_per_step": 2 * 8 * s.nDof},
-        "gpu_launches": None,
-        "roofline": {"bound": "hbm", "kernel": "pcg_persistent_kernel<float>", "achieved": achieved,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "spmv_f32_kernel (fine-level BSR SpMV of FGMRES)", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"] if achieved else None, "traffic": None,
-                     "bytes_per_iteration": bpi, "iterations": prof_it, "kernel_ms": prof_ms},
+                     "bytes_per_launch": sb, "launches": sp_n, "avg_launch_ms": sp_avg},
         "clocks": clk,
         "cpu_baseline": cpu,
         "history_newton": history,
     }  # fmt: skip
-    # kernel launches in one timed step: per Newton iteration elements+condense+norms (3) + bsr+bj (2)
-    # + per solve the PCG launches and ~8 small refinement kernels per sweep
-    per_newton = 3 + 2
-    line["gpu_launches"] = int(sum(newton) * per_newton + a.steps * 0 + sum(sum(k) > 0 for k in krylov) * 0) + int(
-        prof_launch * (1 + 8) * a.steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(a, newton_per_step, krylov_per_step):
-    """Oracle (numpy restatement of the reference CPU path) on a bounded sample, scaled to one load step.
-
-    Sample: the element loop + CSR update of an element subset, and 30 Jacobi-CG iterations on
-    the full CSR system (scipy), scaled by the GPU run's Newton/Krylov counts per load step."""
-    import scipy.sparse as sp
-
+def _element_sample(args):
+    """Oracle element pass + CSR update over elements [lo, hi) of the box (one worker)."""
+    nx, ny, nz, lo, hi = args
     from oracle.element import SmallStrainElements
     from oracle.mesh import BoxMesh
     from oracle.system import csr_slot_map, csr_update, element_dofs, vij_pattern
 
+    m = BoxMesh(nx, ny, nz, 0.1 * nx, 0.1 * ny, 0.1 * nz)
+    els = SmallStrainElements("C3D8", m.coords[m.elements[lo:hi]], "vonmises", PROPS)
+    rng = np.random.default_rng(lo)
+    dU = rng.normal(0, 2e-4, (hi - lo, 24))
+    ed = element_dofs(m.elements[lo:hi])
+    I, J = vij_pattern(ed)
+    _, indices, x = csr_slot_map(I, J, 3 * m.nNodes)
+    t0 = time.perf_counter()
+    Ke, _ = els.compute_yourself(dU, dU)
+    t1 = time.perf_counter()
+    csr_update(Ke.reshape(-1), x, len(indices))
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1, Ke[0].reshape(-1)
+
+
+def cpu_baseline(a, newton_per_step, krylov_per_step, procs=1, sample=4000):
+    """Oracle (numpy restatement of the reference CPU path) on a bounded sample, scaled to one load step.
+
+    Sample: the element loop + CSR update of `sample` elements (split over `procs` spawned worker
+    processes, each timed over its own share; the sample's time is the slowest worker), and
+    Jacobi-CG iterations on the full-size CSR system (scipy, one thread), scaled by the Newton and
+    Krylov counts of one load step."""
+    import scipy.sparse as sp
+
+    from oracle.mesh import BoxMesh
+    from oracle.system import element_dofs, vij_pattern
+
     t_start = time.time()
     nEl = a.nx * a.ny * a.nz
-    m = BoxMesh(a.nx, a.ny, a.nz, 0.1 * a.nx, 0.1 * a.ny, 0.1 * a.nz)
-    sub = min(nEl, 4000)
-    els = SmallStrainElements("C3D8", m.coords[m.elements[:sub]], "vonmises", PROPS)
-    rng = np.random.default_rng(0)
-    dU = rng.normal(0, 2e-4, (sub, 24))
-    t0 = time.perf_counter()
-    Ke, Pe = els.compute_yourself(dU, dU)
-    t_el = (time.perf_counter() - t0) * nEl / sub
-    ed = element_dofs(m.elements[:sub])
-    I, J = vij_pattern(ed)
-    indptr, indices, x = csr_slot_map(I, J, 3 * m.nNodes)
-    t0 = time.perf_counter()
-    csr_update(Ke.reshape(-1), x, len(indices))
-    t_csr = (time.perf_counter() - t0) * nEl / sub
+    sub = min(nEl, sample)
+    chunks = np.linspace(0, sub, procs + 1).astype(int)
+    jobs = [(a.nx, a.ny, a.nz, int(chunks[i]), int(chunks[i + 1])) for i in range(procs)]
+    if procs > 1:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_element_sample, jobs)
+    else:
+        res = [_element_sample(jobs[0])]
+    t_el = max(r[0] for r in res) * nEl / sub
+    t_csr = max(r[1] for r in res) * nEl / sub
+    ke0 = res[0][2]
     # full-size SpMV-dominated CG iterations on a system with the full-size pattern
+    m = BoxMesh(a.nx, a.ny, a.nz, 0.1 * a.nx, 0.1 * a.ny, 0.1 * a.nz)
     nn = 3 * m.nNodes
-    ed_all = element_dofs(m.elements)
-    Kfull = np.tile(Ke[0].reshape(-1), nEl)
-    Ia, Ja = vij_pattern(ed_all)
-    A = sp.csr_matrix((Kfull, (Ia, Ja)), shape=(nn, nn))
-    del Ia, Ja, Kfull
+    Ia, Ja = vij_pattern(element_dofs(m.elements))
+    A = sp.csr_matrix((np.tile(ke0, nEl), (Ia, Ja)), shape=(nn, nn))
+    del Ia, Ja
     A = A + sp.identity(nn) * 1.0
     b = np.ones(nn)
     dinv = 1.0 / A.diagonal()
@@ -369,7 +466,7 @@ def cpu_baseline(a, newton_per_step, krylov_per_step):
     z = dinv * r
     p = z.copy()
     rz = r @ z
-    n_it = 30
+    n_it = 20
     t0 = time.perf_counter()
     for _ in range(n_it):
         q = A @ p
@@ -385,11 +482,12 @@ def cpu_baseline(a, newton_per_step, krylov_per_step):
     return {
         "value": load_step,
         "unit": "s",
-        "cores": 1,
+        "cores": procs,
         "kind": "port",
-        "sample": f"element loop + CSR update of {sub} of {nEl} elements (scaled), {n_it} Jacobi-CG iterations on the "
-                  f"full {nn}-DOF CSR system; scaled by {newton_per_step:.1f} Newton and {krylov_per_step:.0f} Krylov "
-                  f"iterations per load step; wall {time.time() - t_start:.0f}s",
+        "sample": f"element loop + CSR update of {sub} of {nEl} elements on {procs} process(es) (scaled), {n_it} "
+                  f"Jacobi-CG iterations on the full {nn}-DOF CSR system (scipy, 1 thread); scaled by "
+                  f"{newton_per_step:.0f} Newton and {krylov_per_step:.0f} Krylov iterations per load step; "
+                  f"wall {time.time() - t_start:.0f}s",
         "element_loop_s": t_el,
         "csr_update_s": t_csr,
         "cg_iteration_s": t_it,
@@ -397,34 +495,37 @@ def cpu_baseline(a, newton_per_step, krylov_per_step):
 
 
 def run_reference(a):
+    """The reference's CPU path for the workload, timed through the oracle restatement on the
+    host cores (the reference is Python + Cython and does not travel to the GPU machine)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     t0 = time.time()
-    # the reference's CPU path timed through the oracle restatement (the reference itself is
-    # Python + Cython and does not travel to the GPU machine); Newton/Krylov counts of the
-    # 10x4x4 reference run scaled to the configuration by the GPU arm are not available here,
-    # so the counts of this configuration are taken as 5 Newton iterations and 2000 CG iterations
+    procs = max(1, min(16, os.cpu_count() or 1))
     vals = []
     for _ in range(max(1, a.steps)):
-        cb = cpu_baseline(a, newton_per_step=5.0, krylov_per_step=2000.0)
+        cb = cpu_baseline(a, newton_per_step=PCG_NEWTON_PER_STEP, krylov_per_step=PCG_KRYLOV_PER_STEP, procs=procs,
+                          sample=2000 * procs)  # fmt: skip
         vals.append(cb["value"])
+        if time.time() - t0 > 150:  # keep the arm within a few minutes
+            break
     v = float(np.median(vals))
     line = {
         "impl": "reference",
-        "metric": "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s",
+        "metric": METRIC,
         "value": v,
         "unit": "s",
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": a.steps,
-        "warmup": a.warmup,
+        "steps": len(vals),
+        "warmup": 0,
         "ms_per_step": v * 1e3,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic",
+        "data": "synthetic (structured box mesh, seeded parameters)",
         "config": workload(a),
+        "solver": "element loop + serial CSR scatter + Jacobi-CG (the reference's linSolver slot), CPU",
         "cpu_baseline": dict(cb, value=v),
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.time() - t0,
@@ -434,7 +535,7 @@ def run_reference(a):
 
 def run_profile(a):
     """Short kernel sequence for ncu: geometry, one element pass, condensation, BSR scatter, block-Jacobi
-    setup and one PCG solve capped at 200 iterations on the full system."""
+    setup and one solve capped at 200 (PCG) or 60 (FGMRES) iterations on the full system."""
     import torch
 
     from edelweissfe_gb300 import _lib

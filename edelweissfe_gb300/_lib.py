@@ -67,6 +67,8 @@ class EfSolveInfo(ctypes.Structure):
         ("status", c_int),
         ("kernelMs", c_dbl),
         ("kernelLaunches", c_int),
+        ("spmvMs", c_dbl),
+        ("spmvLaunches", c_int),
     ]
 
 
@@ -96,6 +98,7 @@ SIGNATURES = {
     "ef_bsr_matvec": (c_int, [c_vp, c_vp, c_vp, c_vp]),
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
+    "ef_kernel_launches": (c_i64, []),
     "ef_mpnn_param_count": (c_int, []),
     "ef_mpnn_init": (c_int, [c_vp, ctypes.c_uint64, c_int]),
     "ef_mpnn_set_params": (c_int, [c_vp, c_vp, c_vp]),

@@ -415,11 +415,11 @@ ef_status ef_launch_galerkin(int bf, int64_t nCoarseBlocks, const int64_t* seg, 
                              const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals, cudaStream_t s) {
     if (nCoarseBlocks == 0) return EF_OK;
     if (bf == 3)
-        galerkin_kernel<3><<<nb_(nCoarseBlocks, 64), 64, 0, s>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
+        galerkin_kernel<3><<<nb_(nCoarseBlocks, 64), 64, 0, ef::counted(s)>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
                                                                  fineVals, fineMask, offs, coarseRowOfBlock, coarseCol,
                                                                  coarseDead, coarseVals);
     else
-        galerkin_kernel<6><<<nb_(nCoarseBlocks, 64), 64, 0, s>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
+        galerkin_kernel<6><<<nb_(nCoarseBlocks, 64), 64, 0, ef::counted(s)>>>(nCoarseBlocks, seg, src, fineRowOfBlock, fineCol,
                                                                  fineVals, fineMask, offs, coarseRowOfBlock, coarseCol,
                                                                  coarseDead, coarseVals);
     EF_CUDA(cudaGetLastError());
@@ -427,7 +427,7 @@ ef_status ef_launch_galerkin(int bf, int64_t nCoarseBlocks, const int64_t* seg, 
 }
 
 ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals, float* inv, cudaStream_t s) {
-    bj6_setup_kernel<<<nb_(nN, 64), 64, 0, s>>>(nN, diagPos, vals, inv);
+    bj6_setup_kernel<<<nb_(nN, 64), 64, 0, ef::counted(s)>>>(nN, diagPos, vals, inv);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -435,9 +435,9 @@ ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals,
 ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
                              float* x, int accumulate, cudaStream_t s) {
     if (bs == 3)
-        bj_apply_kernel<3><<<nb_(nN, 256), 256, 0, s>>>(nN, binv, mask, omega, r, x, accumulate);
+        bj_apply_kernel<3><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, omega, r, x, accumulate);
     else
-        bj_apply_kernel<6><<<nb_(nN, 256), 256, 0, s>>>(nN, binv, mask, omega, r, x, accumulate);
+        bj_apply_kernel<6><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, omega, r, x, accumulate);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -445,9 +445,9 @@ ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* m
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s) {
     if (bs == 3)
-        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, s>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
     else
-        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, s>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -455,9 +455,9 @@ ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const 
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
                              const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s) {
     if (bf == 3)
-        restrict_kernel<3><<<nb_((int64_t)nC * 32, 256), 256, 0, s>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
+        restrict_kernel<3><<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
     else
-        restrict_kernel<6><<<nb_((int64_t)nC * 32, 256), 256, 0, s>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
+        restrict_kernel<6><<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, aggPtr, aggIdx, offs, t, coarseDead, rc);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -465,9 +465,9 @@ ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_
 ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
                             const uint8_t* mask, float* x, cudaStream_t s, float alpha) {
     if (bf == 3)
-        prolong_kernel<3><<<nb_(nN, 256), 256, 0, s>>>(nN, agg, offs, xc, mask, x, alpha);
+        prolong_kernel<3><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, agg, offs, xc, mask, x, alpha);
     else
-        prolong_kernel<6><<<nb_(nN, 256), 256, 0, s>>>(nN, agg, offs, xc, mask, x, alpha);
+        prolong_kernel<6><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, agg, offs, xc, mask, x, alpha);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -480,14 +480,14 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
     }
     const size_t smem = sizeof(double) * BC * nN * (2 * BC * nN + 1);
     EF_CUDA(cudaFuncSetAttribute(coarsest_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    coarsest_inverse_kernel<<<1, 256, smem, s>>>(nN, rowPtr, colIdx, vals, inv);
+    coarsest_inverse_kernel<<<1, 256, smem, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, inv);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s) {
-    coarsest_apply_kernel<<<nb_(n, 64), 64, 0, s>>>(n, inv, r, dead, x);
+    coarsest_apply_kernel<<<nb_(n, 64), 64, 0, ef::counted(s)>>>(n, inv, r, dead, x);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -226,7 +226,7 @@ static inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
 ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
                              const double* Pe, double* P, double* F, cudaStream_t s) {
     if (nNodes == 0) return EF_OK;
-    condense_kernel<<<nblk(nNodes, 256), 256, 0, s>>>(nNodes, nodeDof, ptr, src, Pe, P, F);
+    condense_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, Pe, P, F);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -234,7 +234,7 @@ ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64
 ef_status ef_launch_condense_add(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
                                  const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s) {
     if (nNodes == 0) return EF_OK;
-    condense_add_kernel<<<nblk(nNodes, 256), 256, 0, s>>>(nNodes, nodeDof, ptr, src, Pe, lo, hi, V);
+    condense_add_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, Pe, lo, hi, V);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -243,9 +243,9 @@ ef_status ef_launch_vij_export(int nEl, int nn, int np, const void* Kblk, int kD
     const int64_t n = (int64_t)nEl * np;
     if (n == 0) return EF_OK;
     if (kDouble)
-        vij_export_kernel<double><<<nblk(n, 256), 256, 0, s>>>(nEl, nn, np, (const double*)Kblk, Kvij);
+        vij_export_kernel<double><<<nblk(n, 256), 256, 0, ef::counted(s)>>>(nEl, nn, np, (const double*)Kblk, Kvij);
     else
-        vij_export_kernel<float><<<nblk(n, 256), 256, 0, s>>>(nEl, nn, np, (const float*)Kblk, Kvij);
+        vij_export_kernel<float><<<nblk(n, 256), 256, 0, ef::counted(s)>>>(nEl, nn, np, (const float*)Kblk, Kvij);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -253,7 +253,7 @@ ef_status ef_launch_vij_export(int nEl, int nn, int np, const void* Kblk, int kD
 ef_status ef_launch_csr_scatter(int64_t nnz, const int64_t* seg, const int32_t* perm, const double* V, double* data,
                                 cudaStream_t s) {
     if (nnz == 0) return EF_OK;
-    csr_scatter_kernel<<<nblk(nnz, 256), 256, 0, s>>>(nnz, seg, perm, V, data);
+    csr_scatter_kernel<<<nblk(nnz, 256), 256, 0, ef::counted(s)>>>(nnz, seg, perm, V, data);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -261,7 +261,7 @@ ef_status ef_launch_csr_scatter(int64_t nnz, const int64_t* seg, const int32_t* 
 ef_status ef_launch_csr_dirichlet_rows(int64_t nRows, const int64_t* rows, const int32_t* indptr,
                                        const int32_t* indices, double* data, cudaStream_t s) {
     if (nRows == 0) return EF_OK;
-    csr_dirichlet_rows_kernel<<<nblk(nRows, 256), 256, 0, s>>>(nRows, rows, indptr, indices, data);
+    csr_dirichlet_rows_kernel<<<nblk(nRows, 256), 256, 0, ef::counted(s)>>>(nRows, rows, indptr, indices, data);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -270,10 +270,10 @@ ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64
                                 int kDouble, void* vals, cudaStream_t s) {
     if (nBlocks == 0) return EF_OK;
     if (kDouble)
-        bsr_scatter_kernel<double><<<nblk(nBlocks, 256), 256, 0, s>>>(nBlocks, seg, src, (const double*)Kblk,
+        bsr_scatter_kernel<double><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, (const double*)Kblk,
                                                                        (double*)vals);
     else
-        bsr_scatter_kernel<float><<<nblk(nBlocks, 256), 256, 0, s>>>(nBlocks, seg, src, (const float*)Kblk,
+        bsr_scatter_kernel<float><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, (const float*)Kblk,
                                                                       (float*)vals);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
@@ -283,10 +283,10 @@ ef_status ef_launch_bj_setup(int64_t nNodes, const int64_t* diagPos, const int32
                              const void* vals, int kDouble, void* inv, int* flags, cudaStream_t s) {
     if (nNodes == 0) return EF_OK;
     if (kDouble)
-        bj_setup_kernel<double><<<nblk(nNodes, 256), 256, 0, s>>>(nNodes, diagPos, nodeDof, mask,
+        bj_setup_kernel<double><<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, diagPos, nodeDof, mask,
                                                                    (const double*)vals, (double*)inv, flags);
     else
-        bj_setup_kernel<float><<<nblk(nNodes, 256), 256, 0, s>>>(nNodes, diagPos, nodeDof, mask, (const float*)vals,
+        bj_setup_kernel<float><<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, diagPos, nodeDof, mask, (const float*)vals,
                                                                   (float*)inv, flags);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
@@ -302,15 +302,15 @@ __global__ void residual_from_kernel(int64_t n, const double* __restrict__ b, co
 ef_status ef_launch_residual_from(int64_t n, const double* b, const double* y, const uint8_t* mask, double* r,
                                   cudaStream_t s) {
     if (n == 0) return EF_OK;
-    residual_from_kernel<<<nblk(n, 256), 256, 0, s>>>(n, b, y, mask, r);
+    residual_from_kernel<<<nblk(n, 256), 256, 0, ef::counted(s)>>>(n, b, y, mask, r);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_norms(int64_t n, const double* R, const double* F, const double* D, double* part, int nPart,
                           double* out, cudaStream_t s) {
-    norms_partial_kernel<<<nPart, 256, 0, s>>>(n, R, F, D, part);
-    norms_final_kernel<<<1, 32, 0, s>>>(nPart, part, out);
+    norms_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, R, F, D, part);
+    norms_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -13,6 +13,20 @@
 
 #include "ef_common.cuh"
 
+#include <atomic>
+
+// launch counter (see ef_common.cuh); launches issued during a stream capture are credited to the
+// graph being captured on this thread instead
+static std::atomic<long long> g_launchCount{0};
+static thread_local long long* t_captureCount = nullptr;
+void ef::note_launches(long long n) {
+    if (t_captureCount)
+        *t_captureCount += n;
+    else
+        g_launchCount.fetch_add(n, std::memory_order_relaxed);
+}
+long long ef::launches() { return g_launchCount.load(std::memory_order_relaxed); }
+
 // krylov.cu
 int ef_krylov_block_threads();
 size_t ef_barrier_state_bytes();
@@ -367,6 +381,7 @@ struct ef_ctx {
     bool exact = false;
     void* w64k[7] = {};   // FP64 Krylov vectors for the all-FP64 mode
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t evS[2] = {nullptr, nullptr};  // FGMRES SpMV timing
     // aggregation multigrid for the FGMRES preconditioner
     std::vector<AmgLevel> amg;           // levels 1..L-1
     float* amgCoarsestInv = nullptr;
@@ -384,6 +399,7 @@ struct ef_ctx {
     float *vcIn = nullptr, *vcOut = nullptr;
     cudaStream_t capStream = nullptr;
     cudaGraphExec_t vcGraph = nullptr;
+    long long vcGraphKernels = 0, nnGraphKernels = 0;
     // learned correction (message-passing network) on top of the V-cycle
     struct NNSystem {                       // a system the training pairs were taken from
         float *K = nullptr, *a = nullptr;   // BSR values, edge weights
@@ -431,7 +447,7 @@ struct ef_ctx {
 
 extern "C" {
 
-int ef_abi_version(void) { return 1; }
+int ef_abi_version(void) { return 2; }
 
 const char* ef_last_error(void) { return g_err.c_str(); }
 
@@ -547,6 +563,8 @@ void ef_destroy(ef_ctx* c) {
     F(c->fgPart);
     F(c->fgH);
     for (auto e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto e : c->evS)
         if (e) cudaEventDestroy(e);
     delete c;
 }
@@ -938,6 +956,8 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     }
     EF_CUDA(cudaEventCreate(&c->ev[0]));
     EF_CUDA(cudaEventCreate(&c->ev[1]));
+    EF_CUDA(cudaEventCreate(&c->evS[0]));
+    EF_CUDA(cudaEventCreate(&c->evS[1]));
     c->finalized = true;
     return EF_OK;
 }
@@ -1390,7 +1410,11 @@ static ef_status amg_capture(ef_ctx* c) {
     if (c->vcGraph) return EF_OK;
     EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
     EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
+    long long captured = 0;
+    t_captureCount = &captured;
     const ef_status st = amg_vcycle(c, 0, c->vcIn, c->vcOut, c->capStream);
+    t_captureCount = nullptr;
+    c->vcGraphKernels = captured;
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->capStream, &g);
     if (st != EF_OK) return st;
@@ -1536,7 +1560,11 @@ static ef_status nn_apply(ef_ctx* c, cudaStream_t s) {
 static ef_status nn_capture(ef_ctx* c) {
     if (c->nnGraph) return EF_OK;
     EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
+    long long captured = 0;
+    t_captureCount = &captured;
     const ef_status st = nn_apply(c, c->capStream);
+    t_captureCount = nullptr;
+    c->nnGraphKernels = captured;
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->capStream, &g);
     if (st != EF_OK) return st;
@@ -1552,9 +1580,11 @@ static ef_status nn_capture(ef_ctx* c) {
 static ef_status fgmres_precond(ef_ctx* c, const float* v, float* z, cudaStream_t s) {
     EF_CHECK(amg_capture(c));
     EF_CUDA(cudaMemcpyAsync(c->vcIn, v, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+    ef::note_launches(c->vcGraphKernels);
     EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
     if (c->nnOn) {
         EF_CHECK(nn_capture(c));
+        ef::note_launches(c->nnGraphKernels);
         EF_CUDA(cudaGraphLaunch(c->nnGraph, s));
         EF_CUDA(cudaMemcpyAsync(z, c->vcOut2, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
     } else {
@@ -1698,6 +1728,7 @@ static ef_status nn_add_sample(ef_ctx* c, const float* r, const float* e, cudaSt
     const float inv = (float)sqrt(inv2);
     EF_CHECK(amg_capture(c));
     EF_CUDA(cudaMemcpyAsync(c->vcIn, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    ef::note_launches(c->vcGraphKernels);
     EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
     EF_CHECK(ef_launch_spmv_f32((int)nN, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->vcOut, c->dMask,
                                 c->nnKd, s));
@@ -1896,8 +1927,10 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         for (; j < m && total < maxIter; ++j) {
             if (prof) EF_CUDA(cudaEventRecord(c->ev[0], s));
             EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, Z + (int64_t)j * n, s));
+            if (prof) EF_CUDA(cudaEventRecord(c->evS[0], s));
             EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals,
                                         Z + (int64_t)j * n, c->dMask, w, s));
+            if (prof) EF_CUDA(cudaEventRecord(c->evS[1], s));
             // classical Gram-Schmidt, twice
             EF_CUDA(cudaMemsetAsync(dh, 0, sizeof(double) * (j + 1), s));
             EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
@@ -1916,6 +1949,9 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
                 EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
                 prof->kernelMs += ms;
                 prof->kernelLaunches += 1;
+                EF_CUDA(cudaEventElapsedTime(&ms, c->evS[0], c->evS[1]));
+                prof->spmvMs += ms;
+                prof->spmvLaunches += 1;
             }
             ++total;
             double* Hj = &H[(size_t)j * (m + 1)];  // column j
@@ -2096,6 +2132,8 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     if (info) *info = inf;
     return result;
 }
+
+int64_t ef_kernel_launches(void) { return (int64_t)ef::launches(); }
 
 int ef_mpnn_param_count(void) { return ef_mpnn_nparam(); }
 

@@ -18,6 +18,15 @@
 
 namespace ef {
 
+// Running count of the kernels this library has put on the GPU (host side): every launch site
+// passes its stream through counted(); a CUDA-graph launch adds the kernels captured in it.
+void note_launches(long long n);
+long long launches();
+inline cudaStream_t counted(cudaStream_t s) {
+    note_launches(1);
+    return s;
+}
+
 enum MatKind { MAT_LINEAR_ELASTIC = 0, MAT_VON_MISES = 1, MAT_NEOHOOKE_WA = 2 };
 
 // Constant tables of one element type (shape-function derivatives at the B/J

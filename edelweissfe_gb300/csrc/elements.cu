@@ -491,11 +491,11 @@ static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, d
     if (vij) {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, true>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
     } else {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, false>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
     }
     EF_CUDA(cudaGetLastError());
     return EF_OK;
@@ -522,7 +522,7 @@ static ef_status launch_apply(const Group& g, const double* x, const double* tan
     const size_t smem = sizeof(ApplyShared<NN, NQ>);
     auto k = small_strain_apply_kernel<NN, NQ>;
     EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, kBlock, smem, s>>>(g.nEl, g.nodeDof, g.geo, x, tang, ye);
+    k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, x, tang, ye);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -531,7 +531,7 @@ template <int NN, int NQ>
 static ef_status launch_geometry(const Group& g, const ElemTables* T, const double* X, int* flags, cudaStream_t s) {
     const int64_t n = (int64_t)g.nEl * NQ;
     if (n == 0) return EF_OK;
-    geometry_kernel<NN, NQ><<<(int)((n + 127) / 128), 128, 0, s>>>(T, g.nEl, g.nodeDof, X, g.geo, flags);
+    geometry_kernel<NN, NQ><<<(int)((n + 127) / 128), 128, 0, ef::counted(s)>>>(T, g.nEl, g.nodeDof, X, g.geo, flags);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -576,7 +576,7 @@ ef_status ef_launch_body_force(const Group& g, const ElemTables* T, const double
     if (grid == 0) return EF_OK;
 #define EF_BF(NN_, NQ_)                                                                                   \
     if (g.nNodes == NN_ && g.nQP == NQ_) {                                                               \
-        body_force_kernel<NN_, NQ_><<<grid, 128, 0, s>>>(T, g.nEl, g.geo, load[0], load[1], load[2], Pe); \
+        body_force_kernel<NN_, NQ_><<<grid, 128, 0, ef::counted(s)>>>(T, g.nEl, g.geo, load[0], load[1], load[2], Pe); \
         EF_CUDA(cudaGetLastError());                                                                     \
         return EF_OK;                                                                                    \
     }

@@ -156,7 +156,7 @@ int ef_fgmres_max_basis() { return kMaxBasis; }
 
 ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, const float* x,
                              const uint8_t* mask, float* y, cudaStream_t s) {
-    spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, s>>>(nN, rowPtr, colIdx, vals, x, mask, y);
+    spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -164,34 +164,34 @@ ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colId
 // h[0..nv) = V^T w (deterministic); part: [nPart][kMaxBasis] doubles
 ef_status ef_launch_multidot(int64_t n, int nv, const float* V, int64_t ldv, const float* w, double* part, int nPart,
                              double* h, double* hAcc, float* invNorm, cudaStream_t s) {
-    multidot_partial_kernel<<<nPart, kFB, 0, s>>>(n, nv, V, ldv, w, part);
-    multidot_final_kernel<<<(nv + 7) / 8, 256, 0, s>>>(nPart, nv, part, h, hAcc, invNorm);
+    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, w, part);
+    multidot_final_kernel<<<(nv + 7) / 8, 256, 0, ef::counted(s)>>>(nPart, nv, part, h, hAcc, invNorm);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_multiaxpy(int64_t n, int nv, const float* V, int64_t ldv, const double* h, float* w,
                               cudaStream_t s) {
-    multiaxpy_kernel<<<nbf(n, 256), 256, 0, s>>>(n, nv, V, ldv, h, w);
+    multiaxpy_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, nv, V, ldv, h, w);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_scale(int64_t n, const float* w, const float* invNorm, float* v, cudaStream_t s) {
-    scale_kernel<<<nbf(n, 256), 256, 0, s>>>(n, w, invNorm, v);
+    scale_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, w, invNorm, v);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_combine(int64_t n, int nv, const float* Z, int64_t ldz, const double* y, float* x,
                             cudaStream_t s) {
-    combine_kernel<<<nbf(n, 256), 256, 0, s>>>(n, nv, Z, ldz, y, x);
+    combine_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, nv, Z, ldz, y, x);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_sub(int64_t n, const float* b, const float* y, float* r, cudaStream_t s) {
-    sub_kernel<<<nbf(n, 256), 256, 0, s>>>(n, b, y, r);
+    sub_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, b, y, r);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

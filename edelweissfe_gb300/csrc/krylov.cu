@@ -408,10 +408,10 @@ ef_status ef_launch_bsr_residual(int nNodes, const int32_t* rowPtr, const int32_
     const int cap = nSM * 8;
     if (grid > cap) grid = cap;
     if (mDouble)
-        bsr_residual_kernel<double, double, double><<<grid, kKB, 0, s>>>(nNodes, rowPtr, colIdx, (const double*)vals,
+        bsr_residual_kernel<double, double, double><<<grid, kKB, 0, ef::counted(s)>>>(nNodes, rowPtr, colIdx, (const double*)vals,
                                                                        x, b, mask, y);
     else
-        bsr_residual_kernel<float, double, double><<<grid, kKB, 0, s>>>(nNodes, rowPtr, colIdx, (const float*)vals, x,
+        bsr_residual_kernel<float, double, double><<<grid, kKB, 0, ef::counted(s)>>>(nNodes, rowPtr, colIdx, (const float*)vals, x,
                                                                       b, mask, y);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
@@ -437,6 +437,7 @@ ef_status ef_launch_pcg(int vDouble, int grid, int nNodes, const int32_t* rowPtr
                         int maxIter, double rtol2, int* flags, cudaStream_t s) {
     void* args[] = {&nNodes, &rowPtr, &colIdx, &vals, &binv, &mask, &b, &x, &r, &z, &pA, &pB, &q,
                     &partA, &partB, &bar, &res, &maxIter, &rtol2, &flags};
+    ef::note_launches(1);
     if (vDouble)
         EF_CUDA(cudaLaunchCooperativeKernel((void*)pcg_persistent_kernel<double>, grid, kKB, args, 0, s));
     else
@@ -446,8 +447,8 @@ ef_status ef_launch_pcg(int vDouble, int grid, int nNodes, const int32_t* rowPtr
 
 ef_status ef_launch_dot(int64_t n, const double* a, const double* b, double* part, int nPart, double* out,
                         cudaStream_t s) {
-    dot2_partial_kernel<<<nPart, kKB, 0, s>>>(n, a, b, part);
-    sum_final_kernel<<<1, 32, 0, s>>>(nPart, part, out);
+    dot2_partial_kernel<<<nPart, kKB, 0, ef::counted(s)>>>(n, a, b, part);
+    sum_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -456,9 +457,9 @@ ef_status ef_launch_masked_copy(int64_t n, const double* src, const uint8_t* mas
                                 void* dst, int dstDouble, cudaStream_t s) {
     if (n == 0) return EF_OK;
     if (dstDouble)
-        masked_copy_kernel<double><<<nb(n, 256), 256, 0, s>>>(n, src, mask, keepMasked, scale, (double*)dst);
+        masked_copy_kernel<double><<<nb(n, 256), 256, 0, ef::counted(s)>>>(n, src, mask, keepMasked, scale, (double*)dst);
     else
-        masked_copy_kernel<float><<<nb(n, 256), 256, 0, s>>>(n, src, mask, keepMasked, scale, (float*)dst);
+        masked_copy_kernel<float><<<nb(n, 256), 256, 0, ef::counted(s)>>>(n, src, mask, keepMasked, scale, (float*)dst);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -466,16 +467,16 @@ ef_status ef_launch_masked_copy(int64_t n, const double* src, const uint8_t* mas
 ef_status ef_launch_axpy(int64_t n, double a, const void* xs, int xDouble, double* y, cudaStream_t s) {
     if (n == 0) return EF_OK;
     if (xDouble)
-        axpy_kernel<double><<<nb(n, 256), 256, 0, s>>>(n, a, (const double*)xs, y);
+        axpy_kernel<double><<<nb(n, 256), 256, 0, ef::counted(s)>>>(n, a, (const double*)xs, y);
     else
-        axpy_kernel<float><<<nb(n, 256), 256, 0, s>>>(n, a, (const float*)xs, y);
+        axpy_kernel<float><<<nb(n, 256), 256, 0, ef::counted(s)>>>(n, a, (const float*)xs, y);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_add(int64_t n, const double* a, const double* b, double* y, cudaStream_t s) {
     if (n == 0) return EF_OK;
-    add_kernel<<<nb(n, 256), 256, 0, s>>>(n, a, b, y);
+    add_kernel<<<nb(n, 256), 256, 0, ef::counted(s)>>>(n, a, b, y);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -574,6 +575,7 @@ extern "C" ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr,
     double rtol2 = rtol * rtol;
     void* args[] = {&nn, &rowPtr, &colIdx, &vals, &binv, &mask, &b, &x, &r, &z, &pA, &pB, &q,
                     &partA, &partB, &bar, &res, &maxIter, &rtol2, &flags};
+    ef::note_launches(1);
     EF_CUDA(cudaLaunchCooperativeKernel((void*)pcg_persistent_kernel<double>, g_noallocGrid[dev], kKB, args, 0, s));
     PcgResult hr;
     EF_CUDA(cudaMemcpyAsync(&hr, res, sizeof(hr), cudaMemcpyDeviceToHost, s));

@@ -453,14 +453,14 @@ int ef_mpnn_out_offset() { return OFF_WOUT; }
 
 ef_status ef_launch_edge_weights(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, float* a,
                                  cudaStream_t s) {
-    edge_weight_kernel<<<nbm(nN, 128), 128, 0, s>>>(nN, rowPtr, colIdx, vals, a);
+    edge_weight_kernel<<<nbm(nN, 128), 128, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, a);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_gather_f32(int64_t n, const int64_t* idx, const float* src, float* dst, cudaStream_t s) {
     if (n == 0) return EF_OK;
-    gather_kernel<<<nbm(n, 256), 256, 0, s>>>(n, idx, src, dst);
+    gather_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, idx, src, dst);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -471,17 +471,17 @@ ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, 
                           cudaStream_t s) {
     const int64_t NH = (int64_t)nN * H;
     float* h0 = acts;
-    input_kernel<<<nbm(NH, 256), 256, 0, s>>>(nN, f, P, h0);
+    input_kernel<<<nbm(NH, 256), 256, 0, ef::counted(s)>>>(nN, f, P, h0);
     const float* hprev = h0;
     for (int l = 0; l < NL; ++l) {
         float* q = acts + NH * (1 + 3 * l);
         float* hl = q + NH;
         float* agg = hl + NH;
-        aggregate_kernel<<<nbm((int64_t)nN * 32, 256), 256, 0, s>>>(nN, rowPtr, colIdx, a, hprev, agg, 0);
-        dense_kernel<<<nbm(nN, TILE), 256, kDenseSmem, s>>>(nN, hprev, agg, P + OFF_L0 + l * PER_LAYER, q, hl);
+        aggregate_kernel<<<nbm((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, a, hprev, agg, 0);
+        dense_kernel<<<nbm(nN, TILE), 256, kDenseSmem, ef::counted(s)>>>(nN, hprev, agg, P + OFF_L0 + l * PER_LAYER, q, hl);
         hprev = hl;
     }
-    output_kernel<<<nbm((int64_t)nN * 3, 256), 256, 0, s>>>(nN, hprev, P, base, mask, so, z);
+    output_kernel<<<nbm((int64_t)nN * 3, 256), 256, 0, ef::counted(s)>>>(nN, hprev, P, base, mask, so, z);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -501,30 +501,30 @@ ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx,
     // output layer: dh3 and grad W_out = dout^T h3
     float* doutBuf = gn;  // reuse gn storage for dout (3 nN <= nN H)
     (void)dout;
-    output_backward_kernel<<<nbm(NH, 256), 256, 0, s>>>(nN, z, e, mask, scale, so, P, doutBuf, dh);
-    outer_partial_kernel<<<nPart, 256, 0, s>>>(nN, 3, H, doutBuf, h3, part);
-    partial_sum_kernel<<<nbm(3 * H, 256), 256, 0, s>>>(nPart, 3 * H, part, grad + OFF_WOUT);
+    output_backward_kernel<<<nbm(NH, 256), 256, 0, ef::counted(s)>>>(nN, z, e, mask, scale, so, P, doutBuf, dh);
+    outer_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(nN, 3, H, doutBuf, h3, part);
+    partial_sum_kernel<<<nbm(3 * H, 256), 256, 0, ef::counted(s)>>>(nPart, 3 * H, part, grad + OFF_WOUT);
     for (int l = NL - 1; l >= 0; --l) {
         const float* q = acts + NH * (1 + 3 * l);
         const float* agg = q + 2 * NH;
         const float* hprev = l == 0 ? h0 : acts + NH * (1 + 3 * (l - 1)) + NH;
         // du, gn, dhprev (written into dh in place is unsafe: use du as temp for dhprev afterwards)
         float* dhprev = work + 3 * NH;
-        dense_backward_kernel<<<nbm(nN, TILE), 256, kDenseBwdSmem, s>>>(nN, dh, q, P + OFF_L0 + l * PER_LAYER, du, gn,
+        dense_backward_kernel<<<nbm(nN, TILE), 256, kDenseBwdSmem, ef::counted(s)>>>(nN, dh, q, P + OFF_L0 + l * PER_LAYER, du, gn,
                                                                          dhprev);
         // grads Ws_l = du^T hprev, Wn_l = du^T agg
-        outer_partial_kernel<<<nPart, 256, 0, s>>>(nN, H, H, du, hprev, part);
-        partial_sum_kernel<<<nbm(H * H, 256), 256, 0, s>>>(nPart, H * H, part, grad + OFF_L0 + l * PER_LAYER);
-        outer_partial_kernel<<<nPart, 256, 0, s>>>(nN, H, H, du, agg, part);
-        partial_sum_kernel<<<nbm(H * H, 256), 256, 0, s>>>(nPart, H * H, part, grad + OFF_L0 + l * PER_LAYER + H * H);
+        outer_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(nN, H, H, du, hprev, part);
+        partial_sum_kernel<<<nbm(H * H, 256), 256, 0, ef::counted(s)>>>(nPart, H * H, part, grad + OFF_L0 + l * PER_LAYER);
+        outer_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(nN, H, H, du, agg, part);
+        partial_sum_kernel<<<nbm(H * H, 256), 256, 0, ef::counted(s)>>>(nPart, H * H, part, grad + OFF_L0 + l * PER_LAYER + H * H);
         // transpose aggregation: dhprev[m] += sum_k aT[(m,k)] gn[k]
-        aggregate_kernel<<<nbm((int64_t)nN * 32, 256), 256, 0, s>>>(nN, rowPtr, colIdx, aT, gn, dhprev, 1);
+        aggregate_kernel<<<nbm((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, aT, gn, dhprev, 1);
         EF_CUDA(cudaMemcpyAsync(dh, dhprev, sizeof(float) * NH, cudaMemcpyDeviceToDevice, s));
     }
     // input layer: grad W_in = (dh0 * relu'(h0))^T f
-    relu_mask_kernel<<<nbm(NH, 256), 256, 0, s>>>(NH, dh, h0, du);
-    outer_partial_kernel<<<nPart, 256, 0, s>>>(nN, H, FIN, du, f, part);
-    partial_sum_kernel<<<nbm(H * FIN, 256), 256, 0, s>>>(nPart, H * FIN, part, grad + OFF_WIN);
+    relu_mask_kernel<<<nbm(NH, 256), 256, 0, ef::counted(s)>>>(NH, dh, h0, du);
+    outer_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(nN, H, FIN, du, f, part);
+    partial_sum_kernel<<<nbm(H * FIN, 256), 256, 0, ef::counted(s)>>>(nPart, H * FIN, part, grad + OFF_WIN);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -532,20 +532,20 @@ ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx,
 ef_status ef_mpnn_adam(int n, float* p, const float* g, float* m1, float* m2, float lr, float b1, float b2, float eps,
                        int step, void* pb, float* pf, cudaStream_t s) {
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    adam_kernel<<<nbm(n, 256), 256, 0, s>>>(n, p, g, m1, m2, lr, b1, b2, eps, c1, c2, (__nv_bfloat16*)pb, pf);
+    adam_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, p, g, m1, m2, lr, b1, b2, eps, c1, c2, (__nv_bfloat16*)pb, pf);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_features(int nN, const float* Mv, const float* v, const float* binv, float s0, float s1, float s2,
                              float* f, cudaStream_t s) {
-    features_kernel<<<nbm(nN, 256), 256, 0, s>>>(nN, Mv, v, binv, s0, s1, s2, f);
+    features_kernel<<<nbm(nN, 256), 256, 0, ef::counted(s)>>>(nN, Mv, v, binv, s0, s1, s2, f);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s) {
-    bf16_to_f32_kernel<<<nbm(n, 256), 256, 0, s>>>(n, (const __nv_bfloat16*)pb, pf);
+    bf16_to_f32_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, (const __nv_bfloat16*)pb, pf);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -554,35 +554,35 @@ ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s) 
 // deterministic
 ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
                         int nPart, double* out, cudaStream_t s) {
-    sumsq_partial_kernel<<<nPart, 256, 0, s>>>(n, groups, z, e, mask, part);
-    sumsq_final_kernel<<<1, 32, 0, s>>>(nPart, part, out);
+    sumsq_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, groups, z, e, mask, part);
+    sumsq_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_mpnn_scale(int64_t n, float* x, float a, cudaStream_t s) {
     if (n == 0) return EF_OK;
-    scale_inplace_kernel<<<nbm(n, 256), 256, 0, s>>>(n, x, a);
+    scale_inplace_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, x, a);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_mpnn_scale_features(int nN, const float* f, float s0, float s1, float s2, float* fs, cudaStream_t s) {
     const int64_t n = (int64_t)nN * FIN;
-    scale_features_kernel<<<nbm(n, 256), 256, 0, s>>>(n, f, s0, s1, s2, fs);
+    scale_features_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, f, s0, s1, s2, fs);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_mpnn_refresh(int n, const float* p, void* pb, float* pf, cudaStream_t s) {
-    refresh_kernel<<<nbm(n, 256), 256, 0, s>>>(n, p, (__nv_bfloat16*)pb, pf);
+    refresh_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, p, (__nv_bfloat16*)pb, pf);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, const double* dots, const uint8_t* mask,
                                 float* z, cudaStream_t s) {
-    alpha_combine_kernel<<<nbm(n, 256), 256, 0, s>>>(n, Mv, N, dots, mask, z);
+    alpha_combine_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, Mv, N, dots, mask, z);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -45,7 +45,7 @@ typedef struct ef_ctx ef_ctx;
 
 /* solve methods */
 #define EF_SOLVE_PCG 0     /* block-Jacobi (3x3 nodal) preconditioned CG */
-#define EF_SOLVE_FGMRES 1  /* flexible GMRES(m), right preconditioned by block Jacobi */
+#define EF_SOLVE_FGMRES 1  /* flexible GMRES(m), right preconditioned by an aggregation multigrid cycle */
 
 typedef struct ef_info {
     int64_t nDof;
@@ -75,11 +75,16 @@ typedef struct ef_solve_info {
     double relResidual;  /* final ||b - A x|| / ||b|| computed in FP64 */
     int status;          /* ef_status of the solve */
     double kernelMs;     /* summed duration of the Krylov kernel launches (profile = 1) */
-    int kernelLaunches;  /* number of Krylov kernel launches timed */
+    int kernelLaunches;  /* number of Krylov kernel launches timed (PCG: solves; FGMRES: iterations) */
+    double spmvMs;       /* FGMRES: summed duration of its fine-level FP32 SpMV launches (profile = 1) */
+    int spmvLaunches;    /* number of those SpMV launches */
 } ef_solve_info;
 
 int ef_abi_version(void);
 const char* ef_last_error(void);
+/* Kernels this library has launched in this process so far (a CUDA-graph launch counts the
+ * kernels in the graph). */
+int64_t ef_kernel_launches(void);
 
 /* ---- model setup: numerics/dofmanager.py:153-218 (DofManager), :522-557 (VIJ pattern),
  *      elements/displacementelement/element.py:194-240 (initializeElement, setMaterial),
