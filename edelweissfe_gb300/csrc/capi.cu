@@ -240,7 +240,7 @@ void build_tables(const TypeInfo& t, ElemTables& T) {
     T.nNodes = t.nNodes;
     T.nQP = (int)w.size();
     T.totalLagrange = t.tl;
-    T.quirk = (t.nNodes == 20 && !t.tl) ? 1 : 0;
+    T.quirk = t.nNodes == 20 ? 1 : 0;  // both element families use _J3D20 with its row-2 term
     for (int q = 0; q < T.nQP; ++q) {
         double N[20], dN[3][20];
         const double Sb[3] = {eta[q], xi[q], zeta[q]};  // B/J evaluation point
@@ -604,10 +604,6 @@ ef_status ef_add_group(ef_ctx* c, const char* elType, const char* material, cons
         ef_set_error("ef_add_group: total-Lagrange elements need a hyperelastic material and vice versa");
         return EF_ERR_ARG;
     }
-    if (ti->tl) {
-        ef_set_error("ef_add_group: total-Lagrange elements are not built into this library version");
-        return EF_ERR_ARG;
-    }
     HostGroup g;
     g.elType = ti->name;
     g.mat = mk;
@@ -671,7 +667,8 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         g.nDofEl = 3 * h.nNodes;
         g.nPair = h.nNodes * (h.nNodes + 1) / 2;
         g.mat = h.mat;
-        g.nState = 12 + (h.mat == MAT_VON_MISES ? 1 : 0);
+        g.tl = h.tl;
+        g.nState = 12 + ((h.mat == MAT_VON_MISES || h.mat == MAT_NEOHOOKE_WA) ? 1 : 0);
         for (size_t i = 0; i < h.props.size(); ++i) g.props[i] = h.props[i];
         g.nodeDof = dalloc<int32_t>(h.nodeDof.size(), &st);
         if (!g.nodeDof) return st;
@@ -941,9 +938,10 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     if (!c->keFp64) {
         // FP32 system: keep the FP64 tangent for a matrix-free refinement residual
         for (const auto& g : c->groups) {
-            double* t = dalloc<double>((size_t)9 * g.nEl * g.nQP, &st);
+            const size_t nt = (size_t)(g.tl ? ef_tl_tangent_size() : 9) * g.nEl * g.nQP;
+            double* t = dalloc<double>(nt, &st);
             if (!t) return st;
-            EF_CUDA(cudaMemset(t, 0, sizeof(double) * 9 * g.nEl * g.nQP));
+            EF_CUDA(cudaMemset(t, 0, sizeof(double) * nt));
             c->dTang.push_back(t);
         }
         c->dYe = dalloc<double>(c->nPe, &st);
@@ -986,20 +984,27 @@ ef_status ef_get_info(const ef_ctx* c, ef_info* out) {
 ef_status ef_compute_elements(ef_ctx* c, const double* U_np, const double* dU, const double* time2, double dT,
                               double* P, double* F, void* stream) {
     EF_REQUIRE_FINALIZED(c);
-    (void)U_np;
     (void)time2;
     (void)dT;
     if (!dU || !P) {
         ef_set_error("ef_compute_elements: null vector");
         return EF_ERR_ARG;
     }
+    for (const auto& g : c->groups)
+        if (g.tl && !U_np) {
+            ef_set_error("ef_compute_elements: total-Lagrange elements need U_np");
+            return EF_ERR_ARG;
+        }
     cudaStream_t s = (cudaStream_t)stream;
     const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
     for (size_t gi = 0; gi < c->groups.size(); ++gi) {
         const Group& g = c->groups[gi];
         void* K = (char*)c->Kblk + (size_t)g.keOffset * 9 * ks;
-        EF_CHECK(ef_launch_small_strain(g, dU, K, c->keFp64, 0, c->Pe + g.peOffset, c->exact ? c->dTang[gi] : nullptr,
-                                        c->dFlags, s));
+        double* tang = c->exact ? c->dTang[gi] : nullptr;
+        if (g.tl)
+            EF_CHECK(ef_launch_total_lagrange(g, U_np, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
+        else
+            EF_CHECK(ef_launch_small_strain(g, dU, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
     }
     EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->Pe, P, F, s));
     return EF_OK;
@@ -1189,7 +1194,10 @@ static ef_status residual64(ef_ctx* c, const double* x, const double* b, double*
     double* y = c->w64[4];
     for (size_t gi = 0; gi < c->groups.size(); ++gi) {
         const Group& g = c->groups[gi];
-        EF_CHECK(ef_launch_small_strain_apply(g, x, c->dTang[gi], c->dYe + g.peOffset, s));
+        if (g.tl)
+            EF_CHECK(ef_launch_total_lagrange_apply(g, x, c->dTang[gi], c->dYe + g.peOffset, s));
+        else
+            EF_CHECK(ef_launch_small_strain_apply(g, x, c->dTang[gi], c->dYe + g.peOffset, s));
     }
     EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dYe, y, nullptr, s));
     return ef_launch_residual_from(c->nDof, b, y, c->dMask, r, s);

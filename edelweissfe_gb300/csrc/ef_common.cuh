@@ -45,7 +45,8 @@ struct Group {
     int elType;   // index into the element table registry
     int nEl, nNodes, nQP, nDofEl, nPair;
     int mat;
-    int nState;   // per Gauss point: 12 + material state (small strain) or 1 (TL)
+    int tl;       // 1: total-Lagrange (hyperelastic) element family
+    int nState;   // per Gauss point: 12 + material state (J2: kappa, NeoHookeWa: energy density)
     double props[8];
     int32_t* nodeDof;     // [nEl][nNodes]  first global DOF of each element node
     double* state[2];     // SoA [nState][nEl*nQP]; state[cur] committed, state[1-cur] trial
@@ -77,6 +78,11 @@ void ef_set_error(const std::string& s);
 ef_status ef_launch_geometry(const ef::Group& g, const ef::ElemTables* T, const double* X, int* flags, cudaStream_t s);
 ef_status ef_launch_small_strain(const ef::Group& g, const double* dU, void* Kout, int kDouble, int kLayoutVIJ,
                                  double* Pe, double* tang, int* flags, cudaStream_t s);
+ef_status ef_launch_total_lagrange(const ef::Group& g, const double* U, void* Kout, int kDouble, int kLayoutVIJ,
+                                   double* Pe, double* tang, int* flags, cudaStream_t s);
+ef_status ef_launch_total_lagrange_apply(const ef::Group& g, const double* x, const double* tang, double* ye,
+                                         cudaStream_t s);
+int ef_tl_tangent_size();
 ef_status ef_launch_small_strain_apply(const ef::Group& g, const double* x, const double* tang, double* ye,
                                        cudaStream_t s);
 ef_status ef_launch_body_force(const ef::Group& g, const ef::ElemTables* T, const double load[3], double* Pe,

@@ -12,6 +12,10 @@ shape-function conventions of
   at ``S = (eta[q], xi[q], zeta[q])`` of the library's Gauss arrays (row 0 of
   their ``h`` matrix depends on ``xi`` and ``zeta`` only, i.e. it is d/dS1 with
   S2 = xi, S3 = zeta).
+* The total-Lagrange element (``elements/displacementtlelement/_elementcomputationmatrices.py``)
+  uses the same conventions: ``_J3D8`` :592-652 / ``_J3D20`` :655+ (with the same row-2 term)
+  and ``computeNablaN`` :247-281 with ``_Ndiff3D`` :370-498 evaluated at ``(xi, eta, zeta)``,
+  whose row 0 is d/dS1 at S1 = eta -- the same point as the small-strain B operator.
 * ``computeNOperator`` :106-213 (used for body forces) evaluates the shape
   functions at ``S = (xi[q], eta[q], zeta[q])`` -- note the swapped first two
   coordinates relative to the B operator; this is reproduced as is.
@@ -170,6 +174,7 @@ def element_tables(elType: str):
         dNdS=shape_derivatives(nodes, S_b),
         N=shape_functions(nodes, S_n),
         totalLagrange=tl,
-        # per Gauss point: row-2 Jacobian quirk factor (zeta - xi) of the B/J evaluation point
-        jacobianQuirk=(zeta - xi) if (nodes.shape[0] == 20 and not tl) else None,
+        # per Gauss point: row-2 Jacobian quirk factor (zeta - xi) of the B/J evaluation point; the
+        # total-Lagrange family shares _J3D20 (displacementtlelement/_elementcomputationmatrices.py:655+)
+        jacobianQuirk=(zeta - xi) if nodes.shape[0] == 20 else None,
     )

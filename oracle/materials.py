@@ -129,3 +129,25 @@ MATERIALS = {
     "linearelastic": (linear_elastic, 0),
     "vonmises": (von_mises, 1),
 }
+
+
+def neo_hooke_wa(props, F):
+    """Kirchhoff stress, its derivative w.r.t. F and the energy density of the compressible
+    neo-Hookean W_a (materials/neohooke/neohookepencegouformulationa.py:107-141); props = [mu, K].
+
+    F [Q,3,3] -> tau [Q,3,3], dtau/dF [Q,3,3,3,3] (index order ijkl of the reference),
+    W [Q] = mu/2 (I1 - 3) + (K/2 - mu/3)(J - 1)^2 - mu ln J (the material's state variable)."""
+    mu, K = float(props[0]), float(props[1])
+    invF = np.linalg.inv(F)
+    B = F @ np.swapaxes(F, 1, 2)
+    J = np.linalg.det(F)
+    lamBar = (K - 2 / 3 * mu) * (J**2 - J) - mu
+    muBar = (K - 2 / 3 * mu) * (2 * J**2 - J)
+    I = np.eye(3)
+    tau = mu * B + lamBar[:, None, None] * I
+    D = mu * (np.einsum("ik,qjl->qijkl", I, F) + np.einsum("qil,jk->qijkl", F, I)) + muBar[
+        :, None, None, None, None
+    ] * np.einsum("ij,qlk->qijkl", I, invF)
+    I1 = np.trace(B, axis1=1, axis2=2)
+    W = mu / 2 * (I1 - 3) + (K / 2 - mu / 3) * (J - 1) ** 2 - mu * np.log(J)
+    return tau, D, W

@@ -33,6 +33,14 @@ def j2_box_spec(nX, nY, nZ, lX, lY, lZ, elType="C3D8", ux=None, props=J2_PROPS):
     )  # fmt: skip
 
 
+def tl_box_spec(nX, nY, nZ, lX, lY, lZ, elType, ux, props=(80.0, 200.0)):
+    """Total-Lagrange NeoHookeWa box: x = 0 face clamped, x = lX face displaced by ux."""
+    return dict(
+        nX=nX, nY=nY, nZ=nZ, lX=lX, lY=lY, lZ=lZ, elType=elType, material="neohookewa", props=list(props),
+        dirichlet=[("gen_left", {0: 0.0, 1: 0.0, 2: 0.0}), ("gen_right", {0: ux})], nodeforces=[], bodyforce=None,
+    )  # fmt: skip
+
+
 def uref_spec(name):
     nX, nY, nZ, lX, lY, lZ, elType, E, nu, dsets, nf, bf = UREF_CASES[name]
     return dict(

@@ -3,7 +3,8 @@
 Run in a container where the reference sources are available (default
 ``/root/reference``; override with ``EF_REFERENCE``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py        # all fixtures
+    python tests/golden/make_golden.py tl     # only the total-Lagrange ones
 
 What it does:
 
@@ -176,6 +177,47 @@ def element_fixture(elType, matName, props, nEl, seed, plastic=False):
     )
 
 
+def element_fixture_tl(elType, props, nEl, seed, scale=0.008):
+    """Ke, Pe and trial state of the reference's DisplacementTLElement with NeoHookeWa on random
+    distorted hexahedra under random total displacements of about `scale` (element size 0.1)."""
+    from edelweissfe.elements.displacementtlelement.element import DisplacementTLElement
+    from edelweissfe.materials.neohooke.neohookepencegouformulationa import NeoHookeanWaMaterial
+    from edelweissfe.points.node import Node
+
+    rng = np.random.default_rng(seed)
+    nNodes = 20 if "20" in elType else 8
+    coords = distorted_hex_coords(rng, nNodes, nEl)
+    nDof = 3 * nNodes
+    Ks, Ps, states0, states1, Us, dUs = [], [], [], [], [], []
+    for e in range(nEl):
+        el = DisplacementTLElement(elType, e + 1)
+        el.setNodes([Node(i + 1, coords[e, i]) for i in range(nNodes)])
+        el.initializeElement()
+        el.setMaterial(NeoHookeanWaMaterial(np.array(props, dtype=float)))
+        states0.append(el._stateVarsRef.copy())
+        U = rng.normal(0.0, scale, nDof)
+        dU = rng.normal(0.0, scale / 4, nDof)
+        K = np.zeros(nDof * nDof)
+        P = np.zeros(nDof)
+        el.computeYourself(K, P, U, dU, np.array([0.5, 0.5]), 0.1)
+        Ks.append(K.copy())
+        Ps.append(P.copy())
+        states1.append(np.array(el._stateVarsTemp))
+        Us.append(U)
+        dUs.append(dU)
+    np.savez_compressed(
+        os.path.join(HERE, f"elem_{elType}_neohookewa.npz"),
+        coords=coords,
+        props=np.array(props, dtype=float),
+        U=np.array(Us),
+        dU=np.array(dUs),
+        state0=np.array(states0),
+        Kvij=np.array(Ks),
+        Pe=np.array(Ps),
+        state1=np.array(states1),
+    )
+
+
 def csr_fixture(seed=3):
     from edelweissfe.numerics.csrgenerator import CSRGenerator
     from edelweissfe.numerics.dofmanager import VIJSystemMatrix
@@ -254,6 +296,27 @@ nodeforces, name=v4, nSet=gen_topRightBack, components='0, 0, -0.0625', field=di
 """
 
 
+BOX_TL_INP = """*material, name=neohookewa, id=mat, provider=edelweiss
+{mu}, {K}
+*job, name=job, domain=3d
+*solver, solver=NIST, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX ={nX}
+nY ={nY}
+nZ ={nZ}
+lX ={lX}
+lY ={lY}
+lZ ={lZ}
+elProvider =edelweiss
+elType ={elType}
+*section, name=section1, material=mat, type=solid
+all
+*step, solver=theSolver, maxInc={maxInc}, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0, 2=0.0, 3=0.0
+dirichlet, name=right, nSet=gen_right, field=displacement, 1={ux}
+"""
+
+
 def run_inp(text, scratch, name):
     from edelweissfe.drivers.inputfiledrivensimulation import finiteElementSimulation
     from edelweissfe.utils.inputfileparser import parseInputFile
@@ -297,10 +360,29 @@ def nist_fixtures(scratch):
         np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
 
 
+TL_CASES = {
+    "tl_box_6x3x3_c3d8tl": dict(nX=6, nY=3, nZ=3, lX=0.6, lY=0.3, lZ=0.3, elType="C3D8TL", maxInc=0.25, ux=-0.09),
+    "tl_box_3x2x2_c3d20tl": dict(nX=3, nY=2, nZ=2, lX=0.3, lY=0.2, lZ=0.2, elType="C3D20TL", maxInc=0.5, ux=-0.045),
+}
+
+
+def tl_fixtures(scratch):
+    """Total-Lagrange NeoHookeWa [80, 200] elements and boxes compressed by 15 % (x = 0 clamped)."""
+    element_fixture_tl("C3D8TL", [80.0, 200.0], 24, seed=11)
+    element_fixture_tl("C3D20TL", [80.0, 200.0], 8, seed=12)
+    for name, c in TL_CASES.items():
+        U, it = run_inp(BOX_TL_INP.format(mu=80.0, K=200.0, **c), scratch, name)
+        np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
+
+
 def main():
-    copy_uref()
     scratch = tempfile.mkdtemp(prefix="efref_")
     prepare_reference(scratch)
+    if sys.argv[1:] == ["tl"]:  # only the total-Lagrange fixtures
+        tl_fixtures(scratch)
+        shutil.rmtree(scratch, ignore_errors=True)
+        return
+    copy_uref()
     element_fixture("C3D8", "linearelastic", [210000.0, 0.3], 24, seed=1)
     element_fixture("C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], 48, seed=2, plastic=True)
     element_fixture("C3D8", "vonmisesexp", [210000.0, 0.3, 250.0, 1000.0, 80.0, 30.0], 16, seed=5, plastic=True)
@@ -308,6 +390,7 @@ def main():
     element_fixture("C3D20", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], 8, seed=6, plastic=True)
     csr_fixture()
     nist_fixtures(scratch)
+    tl_fixtures(scratch)
     shutil.rmtree(scratch, ignore_errors=True)
 
 

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from cases import UREF_CASES, build_gpu_solver, cantilever_spec, j2_box_spec, uref_spec
+from cases import UREF_CASES, build_gpu_solver, cantilever_spec, j2_box_spec, tl_box_spec, uref_spec
 from conftest import golden
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +32,7 @@ def _ctx_for_elements(lib, elType, material, props, coords, keFp64, scalar=False
 
 
 ELEM = [("C3D8", "linearelastic"), ("C3D8", "vonmises"), ("C3D8", "vonmisesexp"), ("C3D20", "linearelastic"),
-        ("C3D20", "vonmises")]  # fmt: skip
+        ("C3D20", "vonmises"), ("C3D8TL", "neohookewa"), ("C3D20TL", "neohookewa")]  # fmt: skip
 
 
 @pytest.mark.parametrize("keFp64", [True, False], ids=["fp64", "fp32K"])
@@ -159,6 +159,23 @@ def test_nist_gpu_j2_matches_reference(gpu_lib, case, mode):
     fp64 = mode == "fp64"
     spec = j2_box_spec(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]),
                        str(g["elType"]), ux=float(g["ux"]))  # fmt: skip
+    s = build_gpu_solver(spec, keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
+    U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.iterationHistory] == list(g["iters"])
+    assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl"])
+def test_nist_gpu_total_lagrange_matches_reference(gpu_lib, case, mode):
+    """Total-Lagrange NeoHookeWa boxes compressed by 15 %: identical Newton iteration counts,
+    displacements within 1e-6 relative."""
+    from edelweissfe_gb300.solver import LinSolverOptions, Step
+
+    g = golden(f"nist_{case}.npz")
+    fp64 = mode == "fp64"
+    spec = tl_box_spec(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]),
+                       str(g["elType"]), float(g["ux"]))  # fmt: skip
     s = build_gpu_solver(spec, keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.iterationHistory] == list(g["iters"])

@@ -4,14 +4,14 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from oracle.element import SmallStrainElements
+from oracle.element import SmallStrainElements, TLElements, make_elements
 from oracle.mesh import BoxMesh
 from oracle.nist import NIST, Model, Step
 from oracle.system import csr_slot_map, csr_update, element_dofs, vij_pattern
 
 
 def _box_model(mesh, elType, material, props, dir_sets, nodeforces=(), bodyforce=None, dir_values=None):
-    els = SmallStrainElements(elType, mesh.coords[mesh.elements], material, props)
+    els = make_elements(elType, mesh.coords[mesh.elements], material, props)
     ed = element_dofs(mesh.elements)
     dirs = []
     for s, comps in dir_sets:
@@ -104,6 +104,35 @@ def test_oracle_nist_j2_matches_reference(case):
         mesh, elType, "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0],
         [("gen_left", [0, 1, 2]), ("gen_right", [0])], dir_values={"gen_right": [float(g["ux"])]},
     )  # fmt: skip
+    s = NIST(model)
+    U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.history] == list(g["iters"])
+    assert np.max(np.abs(U - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
+
+
+@pytest.mark.parametrize("elType", ["C3D8TL", "C3D20TL"])
+def test_oracle_tl_element_matches_reference(elType):
+    g = golden(f"elem_{elType}_neohookewa.npz")
+    els = TLElements(elType, g["coords"], "neohookewa", g["props"])
+    els.stateRef[:] = g["state0"]
+    Ke, Pe = els.compute_yourself(g["U"], g["dU"])
+    n = els.nDof
+    Kref = g["Kvij"].reshape(-1, n, n)
+    assert np.max(np.abs(Ke - Kref)) <= 1e-12 * np.max(np.abs(Kref))
+    assert np.max(np.abs(Pe - g["Pe"])) <= 1e-12 * np.max(np.abs(g["Pe"]))
+    s1 = g["state1"]
+    scale = np.max(np.abs(s1), axis=(0, 1)) + 1e-30
+    assert np.max(np.abs(els.stateTemp - s1) / scale) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl"])
+def test_oracle_nist_tl_matches_reference(case):
+    g = golden(f"nist_{case}.npz")
+    elType = str(g["elType"])
+    mesh = BoxMesh(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]),
+                   nNodesPerElement=20 if "20" in elType else 8)  # fmt: skip
+    model = _box_model(mesh, elType, "neohookewa", [80.0, 200.0], [("gen_left", [0, 1, 2]), ("gen_right", [0])],
+                       dir_values={"gen_right": [float(g["ux"])]})  # fmt: skip
     s = NIST(model)
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.history] == list(g["iters"])
