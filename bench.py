@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")
+    ap.add_argument("--workload", default="box", choices=["box", "cubes"],
+                    help="box: the 160k-element J2 box (default); cubes: 1024 independent J2 cubes in one batch")
     ap.add_argument("--profile", action="store_true",
                     help="one assembly and one capped solve, for ncu captures of single kernels")
     return ap.parse_args()
@@ -403,6 +405,75 @@ def run_ours(a):
         torch.distributed.destroy_process_group()
 
 
+def run_cubes(a):
+    """1024 independent J2 hex8 cubes (edge n ~ U{4..16}, random sigma_y, H, nu per cube; base
+    clamped, top pulled by 1 % in 10 increments): one step = the whole load history of the batch."""
+    import torch
+
+    from edelweissfe_gb300 import build as b
+    from edelweissfe_gb300.batch import BatchNISTGPU, cube_batch_spec
+    from edelweissfe_gb300.solver import Step
+
+    b.build()
+    spec = cube_batch_spec(1024, 0)
+    step = Step(maxInc=0.1, minInc=1e-6, maxIter=25)
+    s = BatchNISTGPU(spec)
+    for _ in range(max(1, a.warmup)):
+        s.problemHistory.clear()
+        s.krylovPerProblem[:] = 0
+        s.solveStepBatch(step)
+    clocks = ClockSampler()
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = s.lib.ef_kernel_launches()
+    e0.record()
+    for _ in range(a.steps):
+        s.problemHistory.clear()
+        s.krylovPerProblem[:] = 0
+        s.solveStepBatch(step)
+    e1.record()
+    torch.cuda.synchronize()
+    launches = s.lib.ef_kernel_launches() - l0
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3 / a.steps
+    # batched-PCG roofline from one eager profiled run: bytes per problem-iteration = its blocks
+    # (72 B values + 4 B column) + row pointers + 10 vector passes of its DOFs
+    prof = BatchNISTGPU(spec, graph=False, tile=s.tile)
+    prof.profile = True
+    prof.solveStepBatch(step)
+    nodes = np.diff(prof.nodePtr)
+    info = prof.info
+    rowBlocks = info.nBlocks / info.nNodes
+    bytes_per_it = nodes * (rowBlocks * 76 + 4 + 3 * 8 * 10)
+    total_bytes = float((prof.krylovPerProblem * bytes_per_it).sum())
+    solve_s = sum(prof.solveMs) / 1e3
+    peaks, peak_kind = measured_peaks()
+    achieved = total_bytes / solve_s / 1e9
+    hist = np.array([it for _, it in s.problemHistory])
+    nEl = int(s.nElProb.sum())
+    line = {
+        "metric": "batched J2 cubes: load-history s (1024 cubes, 10 increments)",
+        "value": t, "unit": "s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (state, stiffness, PCG)", "data": "synthetic (seeded cube sizes and materials)",
+        "config": {"workload": "1024 J2 hex8 cubes, n ~ U{4..16}, sigma_y ~ U[150,350], H ~ U[200,2000], "
+                               "nu ~ U[0.2,0.4] (seed 0), base clamped, 1 % axial strain in 10 increments",
+                   "elements": nEl, "dofs": int(s.nDof)},
+        "newton_iterations_max_per_increment": hist.max(axis=1).tolist(),
+        "krylov_iterations_total": int(s.krylovPerProblem.sum()),
+        "tile": s.tile_shapes()[s.tile], "autotune_ms": s.tuning,
+        "elements_per_s": nEl * int(hist.max(axis=1).sum()) / t,
+        "dof_iterations_per_s": float((prof.krylovPerProblem * 3 * nodes).sum()) / solve_s,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "batched_pcg_kernel", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "solve_s": solve_s, "bytes": total_bytes},
+        "clocks": clk,
+    }  # fmt: skip
+    print(json.dumps(line), flush=True)
+
+
 def _element_sample(args):
     """Oracle element pass + CSR update over elements [lo, hi) of the box (one worker)."""
     nx, ny, nz, lo, hi = args
@@ -566,6 +637,8 @@ if __name__ == "__main__":
     args = parse()
     if args.profile:
         run_profile(args)
+    elif args.workload == "cubes" and args.impl == "ours":
+        run_cubes(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

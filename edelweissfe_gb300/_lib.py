@@ -99,6 +99,14 @@ SIGNATURES = {
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
     "ef_kernel_launches": (c_i64, []),
+    "ef_set_group_props": (c_int, [c_vp, c_int, c_vp, c_int, c_int, c_vp]),
+    "ef_batch_setup": (c_int, [c_vp, c_int, c_vp]),
+    "ef_batch_tile_count": (c_int, []),
+    "ef_batch_tile_info": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "ef_batch_set_tile": (c_int, [c_vp, c_int]),
+    "ef_batch_solve": (c_int, [c_vp, c_dbl, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ef_batch_autotune": (c_int, [c_vp, c_dbl, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.POINTER(c_int), c_vp]),
+    "ef_batch_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_mpnn_param_count": (c_int, []),
     "ef_mpnn_init": (c_int, [c_vp, ctypes.c_uint64, c_int]),
     "ef_mpnn_set_params": (c_int, [c_vp, c_vp, c_vp]),

@@ -93,6 +93,15 @@ ef_status ef_mpnn_scale(int64_t n, float* x, float a, cudaStream_t s);
 ef_status ef_mpnn_scale_features(int nN, const float* f, float s0, float s1, float s2, float* fs, cudaStream_t s);
 ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, const double* dots, const uint8_t* mask,
                                 float* z, cudaStream_t s);
+// batch.cu
+int ef_batch_num_tiles();
+void ef_batch_tile_shape(int tile, int* tpb, int* lpr);
+ef_status ef_launch_batched_pcg(int tile, int nSM, int nProb, const int32_t* nodePtr, const int32_t* order,
+                                const int32_t* rowPtr, const int32_t* colIdx, const double* vals, const double* binv,
+                                const uint8_t* mask, const double* b, double* x, double* r, double* z, double* p,
+                                double* q, int maxIter, double rtol2, int* iters, double* rel, cudaStream_t s);
+ef_status ef_launch_batch_norms(int nProb, const int32_t* nodePtr, const double* R, const double* F, const double* D,
+                                double* out, cudaStream_t s);
 // fgmres.cu
 int ef_fgmres_max_basis();
 ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, const float* x,
@@ -131,6 +140,8 @@ struct HostGroup {
     std::vector<double> props;
     int nEl, nNodes, nQP, tl;
     std::vector<int32_t> nodeDof;  // [nEl][nNodes]
+    std::vector<double> propsTable;  // optional per-element material rows [nRows][8]
+    std::vector<int32_t> elemRow;    // element -> row
 };
 
 struct TypeInfo {
@@ -436,6 +447,10 @@ struct ef_ctx {
     int nnSnapCount = 0;
     cudaGraphExec_t nnGraph = nullptr;
     float* vcOut2 = nullptr;
+    // batch of independent problems (contiguous node ranges), see ef_batch_setup
+    int batchN = 0;
+    int32_t *dBatchNodePtr = nullptr, *dBatchOrder = nullptr;
+    int batchTile = 1;  // index into the batched-PCG tile shapes
     // FGMRES workspace
     float* fgV = nullptr;                // [restart+1][nDof]
     float* fgZ = nullptr;                // [restart][nDof]
@@ -481,6 +496,8 @@ void ef_destroy(ef_ctx* c) {
         F(g.nodeDof);
         F(g.state[0]);
         F(g.state[1]);
+        F((void*)g.propsTable);
+        F((void*)g.elemRow);
         F(g.geo);
     }
     for (auto* t : c->dTables) F(t);
@@ -533,6 +550,8 @@ void ef_destroy(ef_ctx* c) {
         F(L.t);
     }
     F(c->amgCoarsestInv);
+    F(c->dBatchNodePtr);
+    F(c->dBatchOrder);
     F(c->vcIn);
     F(c->vcOut);
     if (c->vcGraph) cudaGraphExecDestroy(c->vcGraph);
@@ -636,6 +655,40 @@ ef_status ef_add_group(ef_ctx* c, const char* elType, const char* material, cons
     return EF_OK;
 }
 
+ef_status ef_set_group_props(ef_ctx* c, int groupId, const double* table, int nRows, int nProps,
+                             const int32_t* elemRow) {
+    if (!c) return EF_ERR_ARG;
+    if (c->finalized) {
+        ef_set_error("ef_set_group_props: context already finalized");
+        return EF_ERR_STATE;
+    }
+    if (groupId < 0 || groupId >= (int)c->hg.size() || !table || !elemRow || nRows <= 0 || nProps <= 0 ||
+        nProps > 8) {
+        ef_set_error("ef_set_group_props: bad arguments");
+        return EF_ERR_ARG;
+    }
+    HostGroup& h = c->hg[groupId];
+    int need = 0;
+    const char* names[3] = {"linearelastic", "vonmises", "neohookewa"};
+    material_kind(names[h.mat], &need);
+    if (nProps < need) {
+        ef_set_error("ef_set_group_props: too few material properties per row");
+        return EF_ERR_ARG;
+    }
+    h.propsTable.assign((size_t)nRows * 8, 0.0);
+    for (int r = 0; r < nRows; ++r)
+        for (int i = 0; i < nProps; ++i) h.propsTable[(size_t)r * 8 + i] = table[(size_t)r * nProps + i];
+    h.elemRow.assign(elemRow, elemRow + h.nEl);
+    for (int32_t r : h.elemRow)
+        if (r < 0 || r >= nRows) {
+            ef_set_error("ef_set_group_props: element row out of range");
+            h.propsTable.clear();
+            h.elemRow.clear();
+            return EF_ERR_ARG;
+        }
+    return EF_OK;
+}
+
 ef_status ef_finalize(ef_ctx* c, int options) {
     if (!c) return EF_ERR_ARG;
     if (c->finalized) {
@@ -680,6 +733,15 @@ ef_status ef_finalize(ef_ctx* c, int options) {
             EF_CUDA(cudaMemset(g.state[k], 0, sizeof(double) * ns));
         }
         g.cur = 0;
+        if (!h.propsTable.empty()) {
+            double* pt = dalloc<double>(h.propsTable.size(), &st);
+            int32_t* er = dalloc<int32_t>(h.elemRow.size(), &st);
+            if (!pt || !er) return st;
+            EF_CUDA(cudaMemcpy(pt, h.propsTable.data(), sizeof(double) * h.propsTable.size(), cudaMemcpyHostToDevice));
+            EF_CUDA(cudaMemcpy(er, h.elemRow.data(), sizeof(int32_t) * h.elemRow.size(), cudaMemcpyHostToDevice));
+            g.propsTable = pt;
+            g.elemRow = er;
+        }
         g.geo = dalloc<double>((size_t)h.nEl * h.nQP * (3 * h.nNodes + 1), &st);
         if (!g.geo) return st;
         EF_CHECK(ef_launch_geometry(g, c->dTables[gi], c->dX, c->dFlags, 0));
@@ -1069,7 +1131,11 @@ ef_status ef_get_state(ef_ctx* c, int groupId, int trial, double* state) {
 
 ef_status ef_accept_state(ef_ctx* c) {
     EF_REQUIRE_FINALIZED(c);
-    for (auto& g : c->groups) g.cur = 1 - g.cur;
+    // copy trial -> committed (acceptLastState copies stateTemp into stateRef); the buffers keep
+    // their roles, so launches captured in CUDA graphs stay valid across increments
+    for (auto& g : c->groups)
+        EF_CUDA(cudaMemcpy(g.state[g.cur], g.state[1 - g.cur], sizeof(double) * g.nState * g.nEl * g.nQP,
+                           cudaMemcpyDeviceToDevice));
     return EF_OK;
 }
 
@@ -2139,6 +2205,132 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     inf.status = result;
     if (info) *info = inf;
     return result;
+}
+
+ef_status ef_batch_setup(ef_ctx* c, int nProb, const int32_t* nodePtr) {
+    EF_REQUIRE_FINALIZED(c);
+    if (nProb <= 0 || !nodePtr || nodePtr[0] != 0 || nodePtr[nProb] != (int32_t)c->nNodes) {
+        ef_set_error("ef_batch_setup: node ranges must cover [0, nNodes)");
+        return EF_ERR_ARG;
+    }
+    for (int p = 0; p < nProb; ++p)
+        if (nodePtr[p + 1] < nodePtr[p]) {
+            ef_set_error("ef_batch_setup: node ranges must be increasing");
+            return EF_ERR_ARG;
+        }
+    if (!c->keFp64) {
+        ef_set_error("ef_batch_setup: the batched solve runs on the FP64 system (EF_OPT_KE_FP64)");
+        return EF_ERR_ARG;
+    }
+    // every block must couple nodes of one problem (block-diagonal system)
+    std::vector<int32_t> prob(c->nNodes);
+    for (int p = 0; p < nProb; ++p)
+        for (int32_t m = nodePtr[p]; m < nodePtr[p + 1]; ++m) prob[m] = p;
+    for (int64_t m = 0; m < c->nNodes; ++m)
+        for (int32_t k = c->hRowPtr0[m]; k < c->hRowPtr0[m + 1]; ++k)
+            if (prob[c->hColIdx0[k]] != prob[m]) {
+                ef_set_error("ef_batch_setup: a block couples two problems");
+                return EF_ERR_ARG;
+            }
+    std::vector<int32_t> order(nProb);
+    for (int p = 0; p < nProb; ++p) order[p] = p;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return nodePtr[a + 1] - nodePtr[a] > nodePtr[b + 1] - nodePtr[b];
+    });
+    if (c->dBatchNodePtr) cudaFree(c->dBatchNodePtr);
+    if (c->dBatchOrder) cudaFree(c->dBatchOrder);
+    ef_status st = EF_OK;
+    c->dBatchNodePtr = dalloc<int32_t>(nProb + 1, &st);
+    c->dBatchOrder = dalloc<int32_t>(nProb, &st);
+    if (st != EF_OK) return st;
+    EF_CUDA(cudaMemcpy(c->dBatchNodePtr, nodePtr, sizeof(int32_t) * (nProb + 1), cudaMemcpyHostToDevice));
+    EF_CUDA(cudaMemcpy(c->dBatchOrder, order.data(), sizeof(int32_t) * nProb, cudaMemcpyHostToDevice));
+    c->batchN = nProb;
+    return EF_OK;
+}
+
+ef_status ef_batch_set_tile(ef_ctx* c, int tile) {
+    EF_REQUIRE_FINALIZED(c);
+    if (tile < 0 || tile >= ef_batch_num_tiles()) {
+        ef_set_error("ef_batch_set_tile: unknown tile shape");
+        return EF_ERR_ARG;
+    }
+    c->batchTile = tile;
+    return EF_OK;
+}
+
+int ef_batch_tile_count(void) { return ef_batch_num_tiles(); }
+
+ef_status ef_batch_tile_info(int tile, int* threadsPerCta, int* lanesPerRow) {
+    if (tile < 0 || tile >= ef_batch_num_tiles() || !threadsPerCta || !lanesPerRow) return EF_ERR_ARG;
+    ef_batch_tile_shape(tile, threadsPerCta, lanesPerRow);
+    return EF_OK;
+}
+
+static ef_status batch_solve(ef_ctx* c, int tile, double rtol, int maxIter, const double* b, double* x, int* iters,
+                             double* relres, cudaStream_t s) {
+    const int64_t n = c->nDof;
+    double* xd = c->w64[0];
+    double* r64 = c->w64[2];
+    // Dirichlet DOFs take b; the free part solves K_ff x_f = b_f - K_fd x_d per problem
+    EF_CHECK(ef_launch_masked_copy(n, b, c->dMask, 1, 1.0, xd, 1, s));
+    EF_CHECK(residual64(c, xd, b, r64, s));
+    double* w[5];
+    for (int i = 0; i < 5; ++i) w[i] = (double*)c->w64k[1 + i];
+    EF_CHECK(ef_launch_batched_pcg(tile, c->nSM, c->batchN, c->dBatchNodePtr, c->dBatchOrder, c->dRowPtr, c->dColIdx,
+                                   (const double*)c->dBsrVals, (const double*)c->dBinv, c->dMask, r64, w[0], w[1],
+                                   w[2], w[3], w[4], maxIter, rtol * rtol, iters, relres, s));
+    return ef_launch_add(n, xd, w[0], x, s);
+}
+
+ef_status ef_batch_solve(ef_ctx* c, double rtol, int maxIter, const double* b, double* x, int* iters, double* relres,
+                         void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (c->batchN == 0) {
+        ef_set_error("ef_batch_solve: call ef_batch_setup first");
+        return EF_ERR_STATE;
+    }
+    if (!b || !x || !iters || !relres || !(rtol > 0.0) || maxIter < 0) return EF_ERR_ARG;
+    return batch_solve(c, c->batchTile, rtol, maxIter, b, x, iters, relres, (cudaStream_t)stream);
+}
+
+ef_status ef_batch_autotune(ef_ctx* c, double rtol, int maxIter, const double* b, double* x, int* iters,
+                            double* relres, void* stream, int* tileOut, float* msOut) {
+    EF_REQUIRE_FINALIZED(c);
+    if (c->batchN == 0) {
+        ef_set_error("ef_batch_autotune: call ef_batch_setup first");
+        return EF_ERR_STATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    float best = 1e30f;
+    int bestT = c->batchTile;
+    for (int t = 0; t < ef_batch_num_tiles(); ++t) {
+        EF_CHECK(batch_solve(c, t, rtol, maxIter, b, x, iters, relres, s));  // warm-up
+        EF_CUDA(cudaEventRecord(c->ev[0], s));
+        EF_CHECK(batch_solve(c, t, rtol, maxIter, b, x, iters, relres, s));
+        EF_CUDA(cudaEventRecord(c->ev[1], s));
+        EF_CUDA(cudaEventSynchronize(c->ev[1]));
+        float ms = 0.f;
+        EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        if (msOut) msOut[t] = ms;
+        if (ms < best) {
+            best = ms;
+            bestT = t;
+        }
+    }
+    c->batchTile = bestT;
+    if (tileOut) *tileOut = bestT;
+    return EF_OK;
+}
+
+ef_status ef_batch_norms(ef_ctx* c, const double* R, const double* F, const double* ddU, double* out, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (c->batchN == 0) {
+        ef_set_error("ef_batch_norms: call ef_batch_setup first");
+        return EF_ERR_STATE;
+    }
+    if (!R || !F || !out) return EF_ERR_ARG;
+    return ef_launch_batch_norms(c->batchN, c->dBatchNodePtr, R, F, ddU, out, (cudaStream_t)stream);
 }
 
 int64_t ef_kernel_launches(void) { return (int64_t)ef::launches(); }

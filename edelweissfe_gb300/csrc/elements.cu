@@ -211,7 +211,8 @@ struct SSShared {
 template <int NN, int NQ, typename KT, int MAT, bool VIJ>
 __global__ void __launch_bounds__(kBlock) small_strain_kernel(
     int nEl, const int32_t* __restrict__ nodeDof, const double* __restrict__ geo, const double* __restrict__ dU,
-    const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props, KT* __restrict__ Kout,
+    const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props,
+    const double* __restrict__ propsTable, const int32_t* __restrict__ elemRow, KT* __restrict__ Kout,
     double* __restrict__ Pe, double* __restrict__ tang, int* __restrict__ flags) {
     constexpr int TPE = (NQ <= 8) ? 8 : 32;
     constexpr int EPB = kBlock / TPE;
@@ -262,13 +263,14 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
 #pragma unroll
         for (int i = 0; i < 6; ++i) sig[i] = stateIn[i * nQPtot + qi];
         MatOut mo;
+        const double* pv = propsTable ? propsTable + 8 * (int64_t)elemRow[e] : props.v;
         if (MAT == MAT_VON_MISES) {
             double kap = stateIn[12 * nQPtot + qi];
-            if (!mat_von_mises(props.v, sig, &kap, de, mo)) atomicOr(flags, EF_FLAG_RETURNMAP);
+            if (!mat_von_mises(pv, sig, &kap, de, mo)) atomicOr(flags, EF_FLAG_RETURNMAP);
             stateOut[12 * nQPtot + qi] = kap;
             if (!(kap == kap)) atomicOr(flags, EF_FLAG_NAN);
         } else {
-            mat_linear_elastic(props.v, sig, de, mo);
+            mat_linear_elastic(pv, sig, de, mo);
         }
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
@@ -491,11 +493,13 @@ static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, d
     if (vij) {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, true>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
+                                                  (KT*)K, Pe, tang, flags);
     } else {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, false>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
+                                                  (KT*)K, Pe, tang, flags);
     }
     EF_CUDA(cudaGetLastError());
     return EF_OK;

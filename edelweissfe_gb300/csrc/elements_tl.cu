@@ -70,6 +70,8 @@ template <int NN, int NQ, typename KT, bool VIJ>
 __global__ void __launch_bounds__(kTLBlock) tl_kernel(int nEl, const int32_t* __restrict__ nodeDof,
                                                       const double* __restrict__ geo, const double* __restrict__ U,
                                                       double* __restrict__ stateOut, PropsArg props,
+                                                      const double* __restrict__ propsTable,
+                                                      const int32_t* __restrict__ elemRow,
                                                       KT* __restrict__ Kout, double* __restrict__ Pe,
                                                       double* __restrict__ tang, int* __restrict__ flags) {
     constexpr int TPE = (NQ <= 8) ? 8 : 32;
@@ -119,7 +121,8 @@ __global__ void __launch_bounds__(kTLBlock) tl_kernel(int nEl, const int32_t* __
             for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
         double Fi[3][3];
         const double J = inv3(F, Fi);
-        const double mu = props.v[0], Kb = props.v[1];
+        const double* pv = propsTable ? propsTable + 8 * (int64_t)elemRow[e] : props.v;
+        const double mu = pv[0], Kb = pv[1];
         const double kk = Kb - 2.0 / 3.0 * mu;
         const double lb = kk * (J * J - J) - mu;
         const double mb = kk * (2.0 * J * J - J);
@@ -336,11 +339,13 @@ static ef_status launch_tl(const Group& g, const double* U, void* K, int vij, do
     if (vij) {
         auto k = tl_kernel<NN, NQ, KT, true>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kTLBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, U, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kTLBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, U, sOut, pa, g.propsTable, g.elemRow,
+                                                    (KT*)K, Pe, tang, flags);
     } else {
         auto k = tl_kernel<NN, NQ, KT, false>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kTLBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, U, sOut, pa, (KT*)K, Pe, tang, flags);
+        k<<<grid, kTLBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, U, sOut, pa, g.propsTable, g.elemRow,
+                                                    (KT*)K, Pe, tang, flags);
     }
     EF_CUDA(cudaGetLastError());
     return EF_OK;

@@ -24,6 +24,8 @@ class ElementGroup:
     elements: np.ndarray  # [nEl, nNodes] node indices, element node order of the reference
     material: str
     props: np.ndarray
+    propsTable: np.ndarray = None  # optional per-element material rows [nRows, nProps]
+    elemRow: np.ndarray = None  # element -> row of propsTable
 
 
 class Model:
@@ -56,6 +58,18 @@ class DirichletBC:
         # findDirichletIndices (solvers/nonlinearimplicitstatic.py:1077-1084): node-major, selected components
         self.dofs = (3 * nodes[:, None] + np.asarray(comps)[None, :]).reshape(-1)
         self.delta = np.tile(np.array([float(components[c]) for c in comps]), nodes.size)
+
+    def getDelta(self, timeStep):
+        a = timeStep.stepProgress
+        return self.delta * (a - (a - timeStep.stepProgressIncrement))
+
+
+class DirichletDofs:
+    """Prescribed step totals on explicit DOFs (many node sets with different values at once)."""
+
+    def __init__(self, dofs, totals):
+        self.dofs = np.asarray(dofs, dtype=np.int64)
+        self.delta = np.asarray(totals, dtype=float)
 
     def getDelta(self, timeStep):
         a = timeStep.stepProgress

@@ -152,6 +152,11 @@ class NISTGPU:
                 "ef_add_group",
             )  # fmt: skip
             self.groupIds.append(gid.value)
+            if g.propsTable is not None:
+                tab = np.ascontiguousarray(np.asarray(g.propsTable, dtype=float))
+                rows = np.ascontiguousarray(np.asarray(g.elemRow, dtype=np.int32))
+                _lib.check(self.lib.ef_set_group_props(self.ctx, gid.value, tab.ctypes.data, tab.shape[0], tab.shape[1],
+                                                       rows.ctypes.data), "ef_set_group_props")  # fmt: skip
         opts = (_lib.EF_OPT_KE_FP64 if keFp64 else 0) | (0 if scalarCSR else _lib.EF_OPT_NO_SCALAR_CSR)
         _lib.check(self.lib.ef_finalize(self.ctx, opts), "ef_finalize")
         self.info = _lib.EfInfo()

@@ -128,7 +128,9 @@ ef_status ef_get_state_size(const ef_ctx* ctx, int groupId, int* nQP, int* nStat
 ef_status ef_set_state(ef_ctx* ctx, int groupId, const double* state);
 ef_status ef_get_state(ef_ctx* ctx, int groupId, int trial, double* state);
 
-/* elements/displacementelement/element.py:373-379 acceptLastState for all elements */
+/* elements/displacementelement/element.py:373-379 acceptLastState for all elements: the trial
+ * state is copied into the committed state (device-wide synchronous copy; the state buffers keep
+ * their addresses, so element launches captured in a CUDA graph remain valid). */
 ef_status ef_accept_state(ef_ctx* ctx);
 
 /* elements/displacementelement/element.py:348-371 computeBodyForce, added into PExt (device [nDof]) */
@@ -194,6 +196,40 @@ ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr, const int3
 /* out (host [3]) = { max_i |R_i|, sum_i |F_i|, max_i |ddU_i| } (ddU may be NULL -> 0).
  * Deterministic; synchronises `stream`. */
 ef_status ef_norms(ef_ctx* ctx, const double* R, const double* F, const double* ddU, double* out, void* stream);
+
+/* ---- batches of independent small problems ----
+ * The reference runs one model per job; a batch is many independent meshes held in one context
+ * (one element group may carry a material row per element), each with its own Newton checks.
+ * The per-problem solve replaces linearSolve (solvers/nonlinearimplicitstatic.py:727-751) and
+ * the per-problem norms the reductions of checkConvergence (:625-725). */
+
+/* Per-element material rows for group `groupId` (before ef_finalize): table host
+ * [nRows][nProps] (the material's property order), elemRow host [nEl] (row of each element). */
+ef_status ef_set_group_props(ef_ctx* ctx, int groupId, const double* table, int nRows, int nProps,
+                             const int32_t* elemRow);
+/* Declares the problems: problem p owns the nodes [nodePtr[p], nodePtr[p+1]) (host int32
+ * [nProb+1], covering all nodes); no 3x3 block may couple two problems.  Needs EF_OPT_KE_FP64. */
+ef_status ef_batch_setup(ef_ctx* ctx, int nProb, const int32_t* nodePtr);
+/* Tile shapes of the batched PCG: tile t in [0, ef_batch_tile_count()) runs threadsPerCta threads
+ * per problem with lanesPerRow lanes per 3x3 block row in the matrix products. */
+int ef_batch_tile_count(void);
+ef_status ef_batch_tile_info(int tile, int* threadsPerCta, int* lanesPerRow);
+ef_status ef_batch_set_tile(ef_ctx* ctx, int tile);
+/* Solves K x = b problem by problem in one persistent launch (block-Jacobi PCG, FP64): Dirichlet
+ * DOFs take b, each problem stops at |r| <= rtol |b_p| (its lifted right-hand side) or maxIter.
+ * b, x device FP64 [nDof]; iters (device int32 [nProb]) and relres (device FP64 [nProb]) receive
+ * each problem's iteration count and final relative residual (NaN on breakdown).  Does not
+ * synchronise `stream` (capturable into a CUDA graph). */
+ef_status ef_batch_solve(ef_ctx* ctx, double rtol, int maxIter, const double* b, double* x, int* iters,
+                         double* relres, void* stream);
+/* Times ef_batch_solve on (b, x) for every tile shape and keeps the fastest; tileOut (host)
+ * receives it, msOut (host [ef_batch_tile_count()], may be NULL) the times.  Synchronises `stream`. */
+ef_status ef_batch_autotune(ef_ctx* ctx, double rtol, int maxIter, const double* b, double* x, int* iters,
+                            double* relres, void* stream, int* tileOut, float* msOut);
+/* out (device FP64 [nProb][3]) = per problem {max |R|, sum |F|, max |ddU|} (ddU may be NULL).
+ * Does not synchronise `stream`. */
+ef_status ef_batch_norms(ef_ctx* ctx, const double* R, const double* F, const double* ddU, double* out,
+                         void* stream);
 
 /* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----
  * The reference solves every Newton system with a direct or plain Krylov solver
