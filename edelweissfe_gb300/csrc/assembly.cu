@@ -17,14 +17,20 @@ namespace ef {
 
 // P[d0+c] = sum_k Pe[src_k + c], F likewise with |.|; one thread per node (DOF triplet)
 __global__ void condense_kernel(int64_t nNodes, const int32_t* __restrict__ nodeDof, const int64_t* __restrict__ ptr,
-                                const int64_t* __restrict__ src, const double* __restrict__ Pe, double* __restrict__ P,
-                                double* __restrict__ F) {
+                                const int64_t* __restrict__ src, const float* __restrict__ w,
+                                const double* __restrict__ Pe, double* __restrict__ P, double* __restrict__ F) {
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nNodes) return;
     double p0 = 0.0, p1 = 0.0, p2 = 0.0, f0 = 0.0, f1 = 0.0, f2 = 0.0;
     for (int64_t k = ptr[m]; k < ptr[m + 1]; ++k) {
         const double* pe = Pe + src[k];
-        const double a = pe[0], b = pe[1], c = pe[2];
+        double a = pe[0], b = pe[1], c = pe[2];
+        if (w) {  // tied node: weighted share of the slave's element vectors
+            const double wk = w[k];
+            a *= wk;
+            b *= wk;
+            c *= wk;
+        }
         p0 += a;
         p1 += b;
         p2 += c;
@@ -46,7 +52,8 @@ __global__ void condense_kernel(int64_t nNodes, const int32_t* __restrict__ node
 // adds the condensed element vectors into V (V[d] += sum), used for body forces
 __global__ void condense_add_kernel(int64_t nNodes, const int32_t* __restrict__ nodeDof,
                                     const int64_t* __restrict__ ptr, const int64_t* __restrict__ src,
-                                    const double* __restrict__ Pe, int64_t lo, int64_t hi, double* __restrict__ V) {
+                                    const float* __restrict__ w, const double* __restrict__ Pe, int64_t lo, int64_t hi,
+                                    double* __restrict__ V) {
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nNodes) return;
     double p0 = 0.0, p1 = 0.0, p2 = 0.0;
@@ -55,9 +62,10 @@ __global__ void condense_add_kernel(int64_t nNodes, const int32_t* __restrict__ 
         const int64_t s = src[k];
         if (s < lo || s >= hi) continue;
         const double* pe = Pe + s;
-        p0 += pe[0];
-        p1 += pe[1];
-        p2 += pe[2];
+        const double wk = w ? (double)w[k] : 1.0;
+        p0 += wk * pe[0];
+        p1 += wk * pe[1];
+        p2 += wk * pe[2];
         any = true;
     }
     if (!any) return;
@@ -114,7 +122,7 @@ __global__ void csr_dirichlet_rows_kernel(int64_t nRows, const int64_t* __restri
 // (global element-block index << 1) | transpose
 template <typename KT>
 __global__ void bsr_scatter_kernel(int64_t nBlocks, const int64_t* __restrict__ seg, const int64_t* __restrict__ src,
-                                   const KT* __restrict__ Kblk, KT* __restrict__ vals) {
+                                   const float* __restrict__ w, const KT* __restrict__ Kblk, KT* __restrict__ vals) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nBlocks) return;
     KT acc[9];
@@ -123,9 +131,10 @@ __global__ void bsr_scatter_kernel(int64_t nBlocks, const int64_t* __restrict__ 
     for (int64_t t = seg[s]; t < seg[s + 1]; ++t) {
         const int64_t c = src[t];
         const KT* kb = Kblk + (c >> 1) * 9;
+        const KT wt = w ? (KT)w[t] : (KT)1;  // tie weight (products of 1/2), exact in either type
         KT v[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i) v[i] = kb[i];
+        for (int i = 0; i < 9; ++i) v[i] = wt * kb[i];
         if (c & 1) {
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -217,6 +226,16 @@ __global__ void norms_final_kernel(int nPart, const double* __restrict__ part, d
     out[2] = c;
 }
 
+// x[slave] = (x[a] + x[b]) / 2 per component (tied nodes)
+__global__ void tie_fill_kernel(int64_t n, const int32_t* __restrict__ slave, const int32_t* __restrict__ ma,
+                                const int32_t* __restrict__ mb, double* __restrict__ x) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    const int64_t k = t / 3;
+    const int c = (int)(t % 3);
+    x[3 * (int64_t)slave[k] + c] = 0.5 * (x[3 * (int64_t)ma[k] + c] + x[3 * (int64_t)mb[k] + c]);
+}
+
 }  // namespace ef
 
 using namespace ef;
@@ -224,17 +243,17 @@ using namespace ef;
 static inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
 ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
-                             const double* Pe, double* P, double* F, cudaStream_t s) {
+                             const float* w, const double* Pe, double* P, double* F, cudaStream_t s) {
     if (nNodes == 0) return EF_OK;
-    condense_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, Pe, P, F);
+    condense_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, w, Pe, P, F);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_condense_add(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
-                                 const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s) {
+                                 const float* w, const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s) {
     if (nNodes == 0) return EF_OK;
-    condense_add_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, Pe, lo, hi, V);
+    condense_add_kernel<<<nblk(nNodes, 256), 256, 0, ef::counted(s)>>>(nNodes, nodeDof, ptr, src, w, Pe, lo, hi, V);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -266,15 +285,15 @@ ef_status ef_launch_csr_dirichlet_rows(int64_t nRows, const int64_t* rows, const
     return EF_OK;
 }
 
-ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64_t* src, const void* Kblk,
-                                int kDouble, void* vals, cudaStream_t s) {
+ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64_t* src, const float* w,
+                                const void* Kblk, int kDouble, void* vals, cudaStream_t s) {
     if (nBlocks == 0) return EF_OK;
     if (kDouble)
-        bsr_scatter_kernel<double><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, (const double*)Kblk,
-                                                                       (double*)vals);
+        bsr_scatter_kernel<double><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, w,
+                                                                                   (const double*)Kblk, (double*)vals);
     else
-        bsr_scatter_kernel<float><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, (const float*)Kblk,
-                                                                      (float*)vals);
+        bsr_scatter_kernel<float><<<nblk(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, seg, src, w,
+                                                                                  (const float*)Kblk, (float*)vals);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -311,6 +330,14 @@ ef_status ef_launch_norms(int64_t n, const double* R, const double* F, const dou
                           double* out, cudaStream_t s) {
     norms_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, R, F, D, part);
     norms_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_tie_fill(int64_t n, const int32_t* slave, const int32_t* ma, const int32_t* mb, double* x,
+                             cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    tie_fill_kernel<<<nblk(3 * n, 256), 256, 0, ef::counted(s)>>>(n, slave, ma, mb, x);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

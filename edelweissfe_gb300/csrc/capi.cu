@@ -352,6 +352,11 @@ struct ef_ctx {
     void* Kblk = nullptr;
     int64_t nKblk = 0;
     int* dFlags = nullptr;
+    // node ties u_s = (u_a + u_b) / 2 (eliminated: K^ = T^T K T, P^ = T^T P, x_s filled after solves)
+    std::vector<int32_t> hTieS, hTieA, hTieB;
+    int32_t *dTieS = nullptr, *dTieA = nullptr, *dTieB = nullptr;
+    float *dCondW = nullptr, *dBsrW = nullptr;  // tie weights of the condensation / BSR sources (null: 1)
+    double* dTieTmp = nullptr;
     // condensation map
     int32_t* dNodeDof = nullptr;
     int64_t* dCondPtr = nullptr;
@@ -410,6 +415,11 @@ struct ef_ctx {
     float *vcIn = nullptr, *vcOut = nullptr;
     cudaStream_t capStream = nullptr;
     cudaGraphExec_t vcGraph = nullptr;
+    // captured element pass (several groups): the vectors it was captured for and its kernels
+    bool elemGraphs = true;
+    const void* egKey[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t egExec = nullptr;
+    long long egKernels = 0;
     long long vcGraphKernels = 0, nnGraphKernels = 0;
     // learned correction (message-passing network) on top of the V-cycle
     struct NNSystem {                       // a system the training pairs were taken from
@@ -507,6 +517,12 @@ void ef_destroy(ef_ctx* c) {
     F(c->dNodeDof);
     F(c->dCondPtr);
     F(c->dCondSrc);
+    F(c->dCondW);
+    F(c->dBsrW);
+    F(c->dTieS);
+    F(c->dTieA);
+    F(c->dTieB);
+    F(c->dTieTmp);
     F(c->dRowPtr);
     F(c->dColIdx);
     F(c->dBsrSeg);
@@ -555,6 +571,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->vcIn);
     F(c->vcOut);
     if (c->vcGraph) cudaGraphExecDestroy(c->vcGraph);
+    if (c->egExec) cudaGraphExecDestroy(c->egExec);
     if (c->nnGraph) cudaGraphExecDestroy(c->nnGraph);
     for (void* p : {(void*)c->nnP, (void*)c->nnPf, (void*)c->nnM1, (void*)c->nnM2, (void*)c->nnG, c->nnPb,
                     (void*)c->nnActs, (void*)c->nnF, (void*)c->nnWork, (void*)c->nnPart, (void*)c->nnA,
@@ -655,6 +672,34 @@ ef_status ef_add_group(ef_ctx* c, const char* elType, const char* material, cons
     return EF_OK;
 }
 
+ef_status ef_set_ties(ef_ctx* c, const int64_t* slave, const int64_t* masterA, const int64_t* masterB, int64_t n) {
+    if (!c) return EF_ERR_ARG;
+    if (c->finalized) {
+        ef_set_error("ef_set_ties: context already finalized");
+        return EF_ERR_STATE;
+    }
+    if (n < 0 || (n > 0 && (!slave || !masterA || !masterB))) return EF_ERR_ARG;
+    const int64_t nN = c->nNodes;
+    std::vector<uint8_t> isSlave(nN, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t s_ = slave[i], a = masterA[i], b = masterB[i];
+        if (s_ < 0 || s_ >= nN || a < 0 || a >= nN || b < 0 || b >= nN || s_ == a || s_ == b || isSlave[s_]) {
+            ef_set_error("ef_set_ties: node out of range, self-tied or tied twice");
+            return EF_ERR_ARG;
+        }
+        isSlave[s_] = 1;
+    }
+    for (int64_t i = 0; i < n; ++i)
+        if (isSlave[masterA[i]] || isSlave[masterB[i]]) {
+            ef_set_error("ef_set_ties: a master node is itself tied");
+            return EF_ERR_ARG;
+        }
+    c->hTieS.assign(slave, slave + n);
+    c->hTieA.assign(masterA, masterA + n);
+    c->hTieB.assign(masterB, masterB + n);
+    return EF_OK;
+}
+
 ef_status ef_set_group_props(ef_ctx* c, int groupId, const double* table, int nRows, int nProps,
                              const int32_t* elemRow) {
     if (!c) return EF_ERR_ARG;
@@ -696,7 +741,8 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         return EF_ERR_STATE;
     }
     c->keFp64 = (options & EF_OPT_KE_FP64) ? 1 : 0;
-    c->scalar = !(options & EF_OPT_NO_SCALAR_CSR);
+    c->scalar = !(options & EF_OPT_NO_SCALAR_CSR) && c->hTieS.empty();  // the reference CSR has no ties
+    if (const char* e = getenv("EF_ELEM_GRAPH")) c->elemGraphs = atoi(e) != 0;
     const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
     ef_status st = EF_OK;
     const int64_t nNodes = c->nNodes;
@@ -770,12 +816,48 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     if (!c->dNodeDof) return st;
     EF_CUDA(cudaMemcpy(c->dNodeDof, nodeDof.data(), sizeof(int32_t) * nNodes, cudaMemcpyHostToDevice));
 
+    // ties: every node maps to target nodes with weights (itself with 1; a tied node to its two
+    // masters with 1/2 each)
+    const bool ties = !c->hTieS.empty();
+    std::vector<int32_t> tieOf(nNodes, -1);
+    for (size_t i = 0; i < c->hTieS.size(); ++i) tieOf[c->hTieS[i]] = (int32_t)i;
+    auto targets = [&](int64_t m, int64_t* t, float* w) -> int {
+        const int32_t k = tieOf[m];
+        if (k < 0) {
+            t[0] = m;
+            w[0] = 1.f;
+            return 1;
+        }
+        t[0] = c->hTieA[k];
+        t[1] = c->hTieB[k];
+        w[0] = w[1] = 0.5f;
+        return 2;
+    };
+    if (ties) {
+        const int64_t nt = (int64_t)c->hTieS.size();
+        c->dTieS = dalloc<int32_t>(nt, &st);
+        c->dTieA = dalloc<int32_t>(nt, &st);
+        c->dTieB = dalloc<int32_t>(nt, &st);
+        c->dTieTmp = dalloc<double>(c->nDof, &st);
+        if (st != EF_OK) return st;
+        EF_CUDA(cudaMemcpy(c->dTieS, c->hTieS.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dTieA, c->hTieA.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dTieB, c->hTieB.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice));
+    }
+
     // condensation map: node m <- Pe slices of (group, element, local node) in element order
+    // (with ties: the slices of the nodes tied to m, weighted; a tied node itself gets none)
     std::vector<int64_t> cptr(nNodes + 1, 0);
     for (const auto& h : c->hg)
-        for (int32_t d : h.nodeDof) cptr[d / 3 + 1]++;
+        for (int32_t d : h.nodeDof) {
+            int64_t t[2];
+            float w[2];
+            const int nt = targets(d / 3, t, w);
+            for (int i = 0; i < nt; ++i) cptr[t[i] + 1]++;
+        }
     for (int64_t m = 0; m < nNodes; ++m) cptr[m + 1] += cptr[m];
     std::vector<int64_t> csrc(cptr[nNodes]);
+    std::vector<float> cw(ties ? cptr[nNodes] : 0);
     {
         std::vector<int64_t> fill(cptr.begin(), cptr.end() - 1);
         for (size_t gi = 0; gi < c->hg.size(); ++gi) {
@@ -783,8 +865,14 @@ ef_status ef_finalize(ef_ctx* c, int options) {
             const Group& g = c->groups[gi];
             for (int64_t e = 0; e < h.nEl; ++e)
                 for (int a = 0; a < h.nNodes; ++a) {
-                    const int64_t m = h.nodeDof[e * h.nNodes + a] / 3;
-                    csrc[fill[m]++] = g.peOffset + e * g.nDofEl + 3 * a;
+                    int64_t t[2];
+                    float w[2];
+                    const int nt = targets(h.nodeDof[e * h.nNodes + a] / 3, t, w);
+                    for (int i = 0; i < nt; ++i) {
+                        const int64_t pos = fill[t[i]]++;
+                        csrc[pos] = g.peOffset + e * g.nDofEl + 3 * a;
+                        if (ties) cw[pos] = w[i];
+                    }
                 }
         }
     }
@@ -793,19 +881,35 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     if (!c->dCondPtr || !c->dCondSrc) return st;
     EF_CUDA(cudaMemcpy(c->dCondPtr, cptr.data(), sizeof(int64_t) * (nNodes + 1), cudaMemcpyHostToDevice));
     EF_CUDA(cudaMemcpy(c->dCondSrc, csrc.data(), sizeof(int64_t) * csrc.size(), cudaMemcpyHostToDevice));
+    if (ties) {
+        c->dCondW = dalloc<float>(cw.size(), &st);
+        if (!c->dCondW) return st;
+        EF_CUDA(cudaMemcpy(c->dCondW, cw.data(), sizeof(float) * cw.size(), cudaMemcpyHostToDevice));
+    }
 
     // BSR pattern + block scatter map.  Global block (m, n) = sum over elements (in order) of
     // K_ab with node(a) = m, node(b) = n; stored pair p(min,max) with a transpose flag if a > b.
     {
         std::vector<int64_t> rcount(nNodes + 1, 0);
         for (const auto& h : c->hg)
-            for (int64_t e = 0; e < h.nEl; ++e)
-                for (int a = 0; a < h.nNodes; ++a) rcount[h.nodeDof[e * h.nNodes + a] / 3 + 1] += h.nNodes;
+            for (int64_t e = 0; e < h.nEl; ++e) {
+                int nb = 0;  // element nodes counted with their targets
+                for (int b = 0; b < h.nNodes; ++b) nb += tieOf[h.nodeDof[e * h.nNodes + b] / 3] < 0 ? 1 : 2;
+                for (int a = 0; a < h.nNodes; ++a) {
+                    int64_t t[2];
+                    float w[2];
+                    const int nt = targets(h.nodeDof[e * h.nNodes + a] / 3, t, w);
+                    for (int i = 0; i < nt; ++i) rcount[t[i] + 1] += nb;
+                }
+            }
+        for (int64_t m = 0; m < nNodes; ++m)
+            if (tieOf[m] >= 0) rcount[m + 1] += 1;  // the tied node's own (empty) diagonal block
         for (int64_t m = 0; m < nNodes; ++m) rcount[m + 1] += rcount[m];
         const int64_t nEnt = rcount[nNodes];
         // entries per row: (col node, element-block code); element order is preserved by the fill order
         std::vector<int32_t> ecol(nEnt);
         std::vector<int64_t> esrc(nEnt);
+        std::vector<float> ew(ties ? nEnt : 0);
         std::vector<int64_t> fill(rcount.begin(), rcount.end() - 1);
         for (size_t gi = 0; gi < c->hg.size(); ++gi) {
             const auto& h = c->hg[gi];
@@ -813,17 +917,30 @@ ef_status ef_finalize(ef_ctx* c, int options) {
             const int nn = h.nNodes;
             for (int64_t e = 0; e < h.nEl; ++e)
                 for (int a = 0; a < nn; ++a) {
-                    const int64_t m = h.nodeDof[e * nn + a] / 3;
-                    for (int b = 0; b < nn; ++b) {
-                        const int lo = std::min(a, b), hi = std::max(a, b);
-                        const int p = lo * nn - lo * (lo - 1) / 2 + (hi - lo);
-                        const int64_t blk = g.keOffset + e * g.nPair + p;
-                        const int64_t pos = fill[m]++;
-                        ecol[pos] = h.nodeDof[e * nn + b] / 3;
-                        esrc[pos] = (blk << 1) | (a > b ? 1 : 0);
-                    }
+                    int64_t ta[2], tb[2];
+                    float wa[2], wb[2];
+                    const int na = targets(h.nodeDof[e * nn + a] / 3, ta, wa);
+                    for (int ia = 0; ia < na; ++ia)
+                        for (int b = 0; b < nn; ++b) {
+                            const int nb = targets(h.nodeDof[e * nn + b] / 3, tb, wb);
+                            const int lo = std::min(a, b), hi = std::max(a, b);
+                            const int p = lo * nn - lo * (lo - 1) / 2 + (hi - lo);
+                            const int64_t blk = g.keOffset + e * g.nPair + p;
+                            for (int ib = 0; ib < nb; ++ib) {
+                                const int64_t pos = fill[ta[ia]]++;
+                                ecol[pos] = (int32_t)tb[ib];
+                                esrc[pos] = (blk << 1) | (a > b ? 1 : 0);
+                                if (ties) ew[pos] = wa[ia] * wb[ib];
+                            }
+                        }
                 }
         }
+        for (int64_t m = 0; m < nNodes; ++m)
+            if (tieOf[m] >= 0) {  // marker of the tied node's diagonal block: no source
+                const int64_t pos = fill[m]++;
+                ecol[pos] = (int32_t)m;
+                esrc[pos] = -1;
+            }
         // per row: stable sort by column, unique columns -> blocks
         std::vector<int64_t> rowBlocks(nNodes + 1, 0);
         std::vector<int64_t> order(nEnt);
@@ -848,6 +965,7 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         c->nBlocks = nBlocks;
         std::vector<int32_t> rowPtr(nNodes + 1), colIdx(nBlocks);
         std::vector<int64_t> seg(nBlocks + 1), src(nEnt), diag(nNodes, -1);
+        std::vector<float> sw(ties ? nEnt : 0);
         for (int64_t m = 0; m <= nNodes; ++m) rowPtr[m] = (int32_t)rowBlocks[m];
         parallel_for(nNodes, [&](int64_t lo, int64_t hi) {
             for (int64_t m = lo; m < hi; ++m) {
@@ -861,10 +979,32 @@ ef_status ef_finalize(ef_ctx* c, int options) {
                         if (ecol[o] == m) diag[m] = b;
                     }
                     src[i] = esrc[o];
+                    if (ties) sw[i] = ew[o];
                 }
             }
         });
         seg[nBlocks] = nEnt;
+        if (ties) {
+            // drop the markers of tied nodes' diagonal blocks (those blocks have no source: zero)
+            std::vector<int64_t> seg2(nBlocks + 1);
+            std::vector<int64_t> src2;
+            std::vector<float> sw2;
+            src2.reserve(nEnt);
+            sw2.reserve(nEnt);
+            for (int64_t b = 0; b < nBlocks; ++b) {
+                seg2[b] = (int64_t)src2.size();
+                for (int64_t i = seg[b]; i < seg[b + 1]; ++i)
+                    if (src[i] >= 0) {
+                        src2.push_back(src[i]);
+                        sw2.push_back(sw[i]);
+                    }
+            }
+            seg2[nBlocks] = (int64_t)src2.size();
+            seg.swap(seg2);
+            src.swap(src2);
+            sw.swap(sw2);
+        }
+        const int64_t nSrc = (int64_t)src.size();
         for (int64_t m = 0; m < nNodes; ++m)
             if (diag[m] < 0) {
                 ef_set_error("ef_finalize: a DOF triplet belongs to no element (no diagonal block)");
@@ -873,7 +1013,7 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         c->dRowPtr = dalloc<int32_t>(nNodes + 1, &st);
         c->dColIdx = dalloc<int32_t>(nBlocks, &st);
         c->dBsrSeg = dalloc<int64_t>(nBlocks + 1, &st);
-        c->dBsrSrc = dalloc<int64_t>(nEnt, &st);
+        c->dBsrSrc = dalloc<int64_t>(nSrc, &st);
         c->dDiagPos = dalloc<int64_t>(nNodes, &st);
         c->dBsrVals = dalloc<char>((size_t)nBlocks * 9 * ks, &st);
         c->dBinv = dalloc<char>((size_t)nNodes * 9 * ks, &st);
@@ -884,10 +1024,17 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         EF_CUDA(cudaMemcpy(c->dRowPtr, rowPtr.data(), sizeof(int32_t) * (nNodes + 1), cudaMemcpyHostToDevice));
         EF_CUDA(cudaMemcpy(c->dColIdx, colIdx.data(), sizeof(int32_t) * nBlocks, cudaMemcpyHostToDevice));
         EF_CUDA(cudaMemcpy(c->dBsrSeg, seg.data(), sizeof(int64_t) * (nBlocks + 1), cudaMemcpyHostToDevice));
-        EF_CUDA(cudaMemcpy(c->dBsrSrc, src.data(), sizeof(int64_t) * nEnt, cudaMemcpyHostToDevice));
+        EF_CUDA(cudaMemcpy(c->dBsrSrc, src.data(), sizeof(int64_t) * nSrc, cudaMemcpyHostToDevice));
+        if (ties) {
+            c->dBsrW = dalloc<float>(nSrc, &st);
+            if (!c->dBsrW) return st;
+            EF_CUDA(cudaMemcpy(c->dBsrW, sw.data(), sizeof(float) * nSrc, cudaMemcpyHostToDevice));
+        }
         EF_CUDA(cudaMemcpy(c->dDiagPos, diag.data(), sizeof(int64_t) * nNodes, cudaMemcpyHostToDevice));
-        EF_CUDA(cudaMemset(c->dMask, 0, c->nDof));
         c->hMask.assign(c->nDof, 0);
+        for (int32_t sN : c->hTieS)
+            for (int k = 0; k < 3; ++k) c->hMask[3 * (int64_t)sN + k] = 1;  // tied DOFs are eliminated
+        EF_CUDA(cudaMemcpy(c->dMask, c->hMask.data(), c->nDof, cudaMemcpyHostToDevice));
         c->hRowPtr0 = rowPtr;
         c->hColIdx0 = colIdx;
     }
@@ -1043,6 +1190,28 @@ ef_status ef_get_info(const ef_ctx* c, ef_info* out) {
         }                                                        \
     } while (0)
 
+}  // extern "C"
+
+// one element pass: every group's kernel, then the condensation into P and F
+static ef_status element_step(ef_ctx* c, const double* U_np, const double* dU, double* P, double* F, cudaStream_t s) {
+    const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
+    for (size_t gi = 0; gi < c->groups.size(); ++gi) {
+        const Group& g = c->groups[gi];
+        void* K = (char*)c->Kblk + (size_t)g.keOffset * 9 * ks;
+        double* tang = c->exact ? c->dTang[gi] : nullptr;
+        if (g.tl)
+            EF_CHECK(ef_launch_total_lagrange(g, U_np, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
+        else
+            EF_CHECK(ef_launch_small_strain(g, dU, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
+    }
+    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dCondW, c->Pe, P, F, s));
+    return EF_OK;
+}
+
+extern "C" {
+
+// With several element groups (element types), the pass is captured as one CUDA graph the second
+// time it runs on the same vectors and replayed from then on.
 ef_status ef_compute_elements(ef_ctx* c, const double* U_np, const double* dU, const double* time2, double dT,
                               double* P, double* F, void* stream) {
     EF_REQUIRE_FINALIZED(c);
@@ -1058,17 +1227,38 @@ ef_status ef_compute_elements(ef_ctx* c, const double* U_np, const double* dU, c
             return EF_ERR_ARG;
         }
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
-    for (size_t gi = 0; gi < c->groups.size(); ++gi) {
-        const Group& g = c->groups[gi];
-        void* K = (char*)c->Kblk + (size_t)g.keOffset * 9 * ks;
-        double* tang = c->exact ? c->dTang[gi] : nullptr;
-        if (g.tl)
-            EF_CHECK(ef_launch_total_lagrange(g, U_np, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
-        else
-            EF_CHECK(ef_launch_small_strain(g, dU, K, c->keFp64, 0, c->Pe + g.peOffset, tang, c->dFlags, s));
+    if (c->groups.size() < 2 || !c->elemGraphs) return element_step(c, U_np, dU, P, F, s);
+    const void* key[4] = {U_np, dU, P, F};
+    const bool same = memcmp(key, c->egKey, sizeof(key)) == 0;
+    if (same && c->egExec) {
+        ef::note_launches(c->egKernels);
+        EF_CUDA(cudaGraphLaunch(c->egExec, s));
+        return EF_OK;
     }
-    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->Pe, P, F, s));
+    if (!same) {  // new vectors: run eagerly and remember them
+        if (c->egExec) cudaGraphExecDestroy(c->egExec);
+        c->egExec = nullptr;
+        memcpy(c->egKey, key, sizeof(key));
+        return element_step(c, U_np, dU, P, F, s);
+    }
+    if (!c->capStream) EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
+    EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
+    long long captured = 0;
+    t_captureCount = &captured;
+    const ef_status st = element_step(c, U_np, dU, P, F, c->capStream);
+    t_captureCount = nullptr;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->capStream, &g);
+    if (st != EF_OK) return st;
+    if (e != cudaSuccess) {
+        ef_set_error(std::string("element-pass capture: ") + cudaGetErrorString(e));
+        return EF_ERR_CUDA;
+    }
+    EF_CUDA(cudaGraphInstantiate(&c->egExec, g, 0));
+    cudaGraphDestroy(g);
+    c->egKernels = captured;
+    ef::note_launches(c->egKernels);
+    EF_CUDA(cudaGraphLaunch(c->egExec, s));
     return EF_OK;
 }
 
@@ -1148,7 +1338,7 @@ ef_status ef_add_body_force(ef_ctx* c, int groupId, const double* load3, double*
     const Group& g = c->groups[groupId];
     cudaStream_t s = (cudaStream_t)stream;
     EF_CHECK(ef_launch_body_force(g, c->dTables[groupId], load3, c->Pe + g.peOffset, s));
-    EF_CHECK(ef_launch_condense_add(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->Pe, g.peOffset,
+    EF_CHECK(ef_launch_condense_add(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dCondW, c->Pe, g.peOffset,
                                     g.peOffset + (int64_t)g.nEl * g.nDofEl, PExt, s));
     return EF_OK;
 }
@@ -1226,7 +1416,9 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
         }
         m[dofs[i]] = 1;
     }
-    c->anyDirichlet = n > 0;
+    for (int32_t sN : c->hTieS)
+        for (int k = 0; k < 3; ++k) m[3 * (int64_t)sN + k] = 1;
+    c->anyDirichlet = n > 0 || !c->hTieS.empty();
     EF_CUDA(cudaMemcpy(c->dMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
     c->hMask = std::move(m);
     c->amgStale = true;
@@ -1237,7 +1429,7 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
 ef_status ef_assemble_bsr(ef_ctx* c, void* stream) {
     EF_REQUIRE_FINALIZED(c);
     cudaStream_t s = (cudaStream_t)stream;
-    EF_CHECK(ef_launch_bsr_scatter(c->nBlocks, c->dBsrSeg, c->dBsrSrc, c->Kblk, c->keFp64, c->dBsrVals, s));
+    EF_CHECK(ef_launch_bsr_scatter(c->nBlocks, c->dBsrSeg, c->dBsrSrc, c->dBsrW, c->Kblk, c->keFp64, c->dBsrVals, s));
     EF_CHECK(ef_launch_bj_setup(c->nNodes, c->dDiagPos, c->dNodeDof, c->dMask, c->dBsrVals, c->keFp64, c->dBinv,
                                 c->dFlags, s));
     c->amgStale = true;
@@ -1258,6 +1450,11 @@ static ef_status residual64(ef_ctx* c, const double* x, const double* b, double*
         return ef_launch_bsr_residual((int)c->nNodes, c->dRowPtr, c->dColIdx, c->dBsrVals, c->keFp64, x, b, c->dMask,
                                       r, c->nSM, s);
     double* y = c->w64[4];
+    if (c->dTieS) {  // the element apply needs the tied DOFs filled from their masters
+        EF_CUDA(cudaMemcpyAsync(c->dTieTmp, x, sizeof(double) * c->nDof, cudaMemcpyDeviceToDevice, s));
+        EF_CHECK(ef_launch_tie_fill((int64_t)c->hTieS.size(), c->dTieS, c->dTieA, c->dTieB, c->dTieTmp, s));
+        x = c->dTieTmp;
+    }
     for (size_t gi = 0; gi < c->groups.size(); ++gi) {
         const Group& g = c->groups[gi];
         if (g.tl)
@@ -1265,7 +1462,7 @@ static ef_status residual64(ef_ctx* c, const double* x, const double* b, double*
         else
             EF_CHECK(ef_launch_small_strain_apply(g, x, c->dTang[gi], c->dYe + g.peOffset, s));
     }
-    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dYe, y, nullptr, s));
+    EF_CHECK(ef_launch_condense(c->nNodes, c->dNodeDof, c->dCondPtr, c->dCondSrc, c->dCondW, c->dYe, y, nullptr, s));
     return ef_launch_residual_from(c->nDof, b, y, c->dMask, r, s);
 }
 
@@ -2196,6 +2393,7 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
         }
     }
     EF_CHECK(ef_launch_add(n, xd, xf, x, s));
+    if (c->dTieS) EF_CHECK(ef_launch_tie_fill((int64_t)c->hTieS.size(), c->dTieS, c->dTieA, c->dTieB, x, s));
     // final FP64 residual of the full system (Dirichlet rows are exact)
     EF_CHECK(residual64(c, x, b, r64, s));
     EF_CHECK(dot_host(c, r64, r64, &rr, s));

@@ -92,16 +92,18 @@ ef_status ef_launch_body_force(const ef::Group& g, const ef::ElemTables* T, cons
 
 // Assembly launchers (assembly.cu)
 ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
-                             const double* Pe, double* P, double* F, cudaStream_t s);
+                             const float* w, const double* Pe, double* P, double* F, cudaStream_t s);
 ef_status ef_launch_condense_add(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
-                                 const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s);
+                                 const float* w, const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s);
 ef_status ef_launch_vij_export(int nEl, int nn, int np, const void* Kblk, int kDouble, double* Kvij, cudaStream_t s);
 ef_status ef_launch_csr_scatter(int64_t nnz, const int64_t* seg, const int32_t* perm, const double* V, double* data,
                                 cudaStream_t s);
 ef_status ef_launch_csr_dirichlet_rows(int64_t nRows, const int64_t* rows, const int32_t* indptr,
                                        const int32_t* indices, double* data, cudaStream_t s);
-ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64_t* src, const void* Kblk,
-                                int kDouble, void* vals, cudaStream_t s);
+ef_status ef_launch_tie_fill(int64_t n, const int32_t* slave, const int32_t* ma, const int32_t* mb, double* x,
+                             cudaStream_t s);
+ef_status ef_launch_bsr_scatter(int64_t nBlocks, const int64_t* seg, const int64_t* src, const float* w,
+                                const void* Kblk, int kDouble, void* vals, cudaStream_t s);
 ef_status ef_launch_bj_setup(int64_t nNodes, const int64_t* diagPos, const int32_t* nodeDof, const uint8_t* mask,
                              const void* vals, int kDouble, void* inv, int* flags, cudaStream_t s);
 ef_status ef_launch_residual_from(int64_t n, const double* b, const double* y, const uint8_t* mask, double* r,

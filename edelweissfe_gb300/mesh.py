@@ -55,3 +55,54 @@ def box_mesh(nX, nY, nZ, lX=1.0, lY=1.0, lZ=1.0, x0=0.0, y0=0.0, z0=0.0, nNodesP
     sets = {f"{name}_{k}": sel(v) for k, v in faces.items()}
     sets[f"{name}_all"] = np.arange(coords.shape[0])
     return dict(coords=coords, elements=elements, nodeSets=sets)
+
+
+def tied_box_mesh(nXq, nXl, nY, nZ, lXq, lXl, lY=1.0, lZ=1.0, name="gen"):
+    """A box of two structured halves: x in [0, lXq] meshed with nXq x nY x nZ 20-node hexahedra,
+    x in [lXq, lXq + lXl] with nXl x nY x nZ 8-node hexahedra.  The 8-node half's nodes on the
+    interface are the 20-node half's corner nodes there; the 20-node half's mid-side nodes on the
+    interface are tied to the two corner nodes of their edge (u_mid = (u_a + u_b) / 2), which
+    makes the interface conforming.  The reference has no generator and no constraint for this
+    (its box generator makes one element type, constraints/ only equates DOFs).
+
+    Returns dict(coords, elements20, elements8, nodeSets (left = x = 0, right = x = lXq + lXl,
+    all), ties = (slave, masterA, masterB) node index arrays)."""
+    q = box_mesh(nXq, nY, nZ, lXq, lY, lZ, nNodesPerElement=20, name=name)
+    lin = box_mesh(nXl, nY, nZ, lXl, lY, lZ, x0=lXq, nNodesPerElement=8, name=name)
+    dy, dz = lY / nY, lZ / nZ
+    nq = q["coords"].shape[0]
+
+    def half_index(c):
+        return np.rint(c[:, 1] / (dy / 2)).astype(np.int64), np.rint(c[:, 2] / (dz / 2)).astype(np.int64)
+
+    face_q = np.asarray(q["nodeSets"][f"{name}_right"])
+    iy, iz = half_index(q["coords"][face_q])
+    key_q = {(a, b): n for a, b, n in zip(iy.tolist(), iz.tolist(), face_q.tolist())}
+    # renumber the 8-node half: interface nodes -> the matching 20-node corner nodes
+    face_l = np.asarray(lin["nodeSets"][f"{name}_left"])
+    ly, lz = half_index(lin["coords"][face_l])
+    new_of = np.full(lin["coords"].shape[0], -1, dtype=np.int64)
+    new_of[face_l] = [key_q[(a, b)] for a, b in zip(ly.tolist(), lz.tolist())]
+    rest = np.flatnonzero(new_of < 0)
+    new_of[rest] = nq + np.arange(rest.size)
+    coords = np.concatenate([q["coords"], lin["coords"][rest]])
+    # ties: interface mid-side nodes (exactly one odd half-index) -> their edge's corner nodes
+    slave, ma, mb = [], [], []
+    for (a, b), n in key_q.items():
+        if a % 2 == 1:
+            slave.append(n)
+            ma.append(key_q[(a - 1, b)])
+            mb.append(key_q[(a + 1, b)])
+        elif b % 2 == 1:
+            slave.append(n)
+            ma.append(key_q[(a, b - 1)])
+            mb.append(key_q[(a, b + 1)])
+    order = np.argsort(slave)
+    sets = {f"{name}_left": np.asarray(q["nodeSets"][f"{name}_left"]),
+            f"{name}_right": new_of[np.asarray(lin["nodeSets"][f"{name}_right"])],
+            f"{name}_all": np.arange(coords.shape[0])}  # fmt: skip
+    for side in ("top", "bottom", "front", "back"):
+        s = np.union1d(q["nodeSets"][f"{name}_{side}"], new_of[np.asarray(lin["nodeSets"][f"{name}_{side}"])])
+        sets[f"{name}_{side}"] = s
+    return dict(coords=coords, elements20=q["elements"], elements8=new_of[lin["elements"]], nodeSets=sets,
+                ties=(np.asarray(slave)[order], np.asarray(ma)[order], np.asarray(mb)[order]))  # fmt: skip

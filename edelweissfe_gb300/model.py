@@ -29,12 +29,14 @@ class ElementGroup:
 
 
 class Model:
-    def __init__(self, coords: np.ndarray, groups, nodeSets=None):
+    def __init__(self, coords: np.ndarray, groups, nodeSets=None, ties=None):
         self.coords = np.asarray(coords, dtype=float)
         self.nNodes = self.coords.shape[0]
         self.nDof = 3 * self.nNodes
         self.groups = list(groups)
         self.nodeSets = dict(nodeSets or {})
+        # node ties u_s = (u_a + u_b) / 2: (slave, masterA, masterB) node index arrays, or None
+        self.ties = ties
 
     def element_dofs(self, g: ElementGroup) -> np.ndarray:
         e = np.asarray(g.elements, dtype=np.int64)

@@ -157,6 +157,10 @@ class NISTGPU:
                 rows = np.ascontiguousarray(np.asarray(g.elemRow, dtype=np.int32))
                 _lib.check(self.lib.ef_set_group_props(self.ctx, gid.value, tab.ctypes.data, tab.shape[0], tab.shape[1],
                                                        rows.ctypes.data), "ef_set_group_props")  # fmt: skip
+        if model.ties is not None and len(model.ties[0]):
+            ts, ta, tb = (np.ascontiguousarray(np.asarray(v, dtype=np.int64)) for v in model.ties)
+            _lib.check(self.lib.ef_set_ties(self.ctx, ts.ctypes.data, ta.ctypes.data, tb.ctypes.data, ts.size),
+                       "ef_set_ties")  # fmt: skip
         opts = (_lib.EF_OPT_KE_FP64 if keFp64 else 0) | (0 if scalarCSR else _lib.EF_OPT_NO_SCALAR_CSR)
         _lib.check(self.lib.ef_finalize(self.ctx, opts), "ef_finalize")
         self.info = _lib.EfInfo()

@@ -203,6 +203,14 @@ ef_status ef_norms(ef_ctx* ctx, const double* R, const double* F, const double* 
  * The per-problem solve replaces linearSolve (solvers/nonlinearimplicitstatic.py:727-751) and
  * the per-problem norms the reductions of checkConvergence (:625-725). */
 
+/* Node ties u_slave = (u_masterA + u_masterB) / 2 for all three components (host int64 [n] node
+ * indices, before ef_finalize), e.g. the mid-side nodes of 20-node faces on an interface with
+ * 8-node elements.  The reference has no such constraint (constraints/ only equates DOFs); the
+ * tied DOFs are eliminated: the assembled system is T^T K T, P and F are condensed with T^T, the
+ * tied DOFs are masked in the solves and filled from their masters in every solution.  Turns off
+ * the scalar reference CSR. */
+ef_status ef_set_ties(ef_ctx* ctx, const int64_t* slave, const int64_t* masterA, const int64_t* masterB, int64_t n);
+
 /* Per-element material rows for group `groupId` (before ef_finalize): table host
  * [nRows][nProps] (the material's property order), elemRow host [nEl] (row of each element). */
 ef_status ef_set_group_props(ef_ctx* ctx, int groupId, const double* table, int nRows, int nProps,

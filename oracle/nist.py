@@ -20,6 +20,7 @@ Follows ``solvers/nonlinearimplicitstatic.py``:
 from dataclasses import dataclass, field
 
 import numpy as np
+import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from .materials import ReturnMapFailed
@@ -120,6 +121,25 @@ class Model:
     dirichlet: list = field(default_factory=list)  # of (dof indices, prescribed total value per dof)
     nodeforces: list = field(default_factory=list)  # of (dof indices, load per dof)
     bodyforces: list = field(default_factory=list)  # of (group index, load vector (3,))
+    # node ties u_s = (u_a + u_b) / 2 (all components) as (slave, masterA, masterB) node arrays; the
+    # reference has no such constraint, the oracle eliminates the slaves: K^ = T^T K T, R^ = T^T R,
+    # F^ = T^T F, ddU = T ddU^ (slave rows of K^ are identity rows with zero right-hand side)
+    ties: tuple = None
+
+
+def tie_matrix(nDof, ties):
+    """T [nDof, nDof]: identity except slave DOF rows (1/2 at both masters, 0 on the diagonal)."""
+    s, a, b = (np.asarray(v, dtype=np.int64) for v in ties)
+    rows, cols, vals = [], [], []
+    slaveDof = (3 * s[:, None] + np.arange(3)).ravel()
+    keep = np.setdiff1d(np.arange(nDof), slaveDof)
+    rows.append(keep), cols.append(keep), vals.append(np.ones(keep.size))
+    for m in (a, b):
+        rows.append(slaveDof)
+        cols.append((3 * m[:, None] + np.arange(3)).ravel())
+        vals.append(np.full(slaveDof.size, 0.5))
+    T = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(nDof, nDof))
+    return T, slaveDof
 
 
 def spsolve_direct(A, b):
@@ -143,6 +163,10 @@ class NIST:
         self.dirIdx = np.concatenate([d for d, _ in model.dirichlet]) if model.dirichlet else np.array([], dtype=np.int64)
         self.history = []  # (increment number, iterations) of converged increments
         self.iterationLog = []  # per Newton iteration (flux residual, correction)
+        self.T = None
+        if model.ties is not None and len(model.ties[0]):
+            self.T, self.slaveDof = tie_matrix(model.nDof, model.ties)
+            self.Tt = self.T.T.tocsr()
 
     # -- the four hot-path methods -------------------------------------------------
     def computeElements(self, U_np, dU):
@@ -156,16 +180,28 @@ class NIST:
             p, f = condense(Pe, elDofs, nDof)
             P += p
             F += f
+        if self.T is not None:
+            P, F = self.Tt @ P, self.Tt @ F
         return P, np.concatenate(Vs), F
 
     def assembleStiffnessCSR(self, V):
         return csr_update(V, self.x, len(self.indices))
 
     def applyDirichletK(self, data):
-        return dirichlet_rows(self.indptr, self.indices, data, self.dirIdx)
+        if self.T is None:
+            return dirichlet_rows(self.indptr, self.indices, data, self.dirIdx)
+        n = self.model.nDof
+        A = sp.csr_matrix((data, self.indices, self.indptr), shape=(n, n))
+        A = (self.Tt @ A @ self.T).tocsr()
+        A = (A + sp.csr_matrix((np.ones(self.slaveDof.size), (self.slaveDof, self.slaveDof)), shape=(n, n))).tocsr()
+        A.sum_duplicates()
+        A.sort_indices()
+        return dirichlet_rows(A.indptr, A.indices, A.data, self.dirIdx)
 
     def linearSolve(self, A, b):
         ddU = self.linsolve(A, b)
+        if self.T is not None:
+            ddU = self.T @ ddU
         if np.isnan(ddU).any():
             raise DivergingSolution("Obtained NaN in linear solve")
         return ddU

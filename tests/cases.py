@@ -69,3 +69,41 @@ def build_gpu_solver(spec, **kw):
     nfs = [NodeForces(m["nodeSets"][s], v) for s, v in spec["nodeforces"]]
     bfs = [BodyForce(0, spec["bodyforce"])] if spec.get("bodyforce") is not None else []
     return NISTGPU(model, dirs, nfs, bfs, **kw)
+
+
+def tied_tl_spec(nXq, nXl, nY, nZ, h=0.1, compression=0.15, props=(80.0, 200.0)):
+    """Hex20 (C3D20TL) | hex8 (C3D8TL) NeoHookeWa box with the tied interface, x = 0 face clamped,
+    x = L face displaced by -compression * L."""
+    from edelweissfe_gb300.mesh import tied_box_mesh
+
+    m = tied_box_mesh(nXq, nXl, nY, nZ, nXq * h, nXl * h, nY * h, nZ * h)
+    return dict(mesh=m, props=list(props), ux=-compression * (nXq + nXl) * h)
+
+
+def build_gpu_tied(spec, **kw):
+    from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model
+    from edelweissfe_gb300.solver import NISTGPU
+
+    m = spec["mesh"]
+    p = np.array(spec["props"])
+    model = Model(m["coords"], [ElementGroup("C3D20TL", m["elements20"], "neohookewa", p),
+                                ElementGroup("C3D8TL", m["elements8"], "neohookewa", p)], ties=m["ties"])  # fmt: skip
+    dirs = [DirichletBC(m["nodeSets"]["gen_left"], {0: 0.0, 1: 0.0, 2: 0.0}),
+            DirichletBC(m["nodeSets"]["gen_right"], {0: spec["ux"]})]  # fmt: skip
+    return NISTGPU(model, dirs, **kw)
+
+
+def oracle_tied(spec):
+    from oracle.element import TLElements
+    from oracle.nist import Model as OModel
+    from oracle.system import element_dofs
+
+    m = spec["mesh"]
+    c = m["coords"]
+    gq = TLElements("C3D20TL", c[m["elements20"]], "neohookewa", spec["props"])
+    gl = TLElements("C3D8TL", c[m["elements8"]], "neohookewa", spec["props"])
+    left, right = m["nodeSets"]["gen_left"], m["nodeSets"]["gen_right"]
+    dirs = [((3 * left[:, None] + np.arange(3)).ravel(), np.zeros(3 * left.size)),
+            (3 * right, np.full(right.size, spec["ux"]))]  # fmt: skip
+    return OModel(3 * c.shape[0], [(gq, element_dofs(m["elements20"])), (gl, element_dofs(m["elements8"]))], dirs,
+                  ties=m["ties"])  # fmt: skip

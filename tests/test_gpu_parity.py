@@ -286,3 +286,26 @@ def test_nist_gpu_fgmres_matches_reference_iteration_counts(gpu_lib):
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.iterationHistory] == list(g["iters"])
     assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_nist_gpu_tied_hex20_hex8_total_lagrange_matches_oracle(gpu_lib, mode):
+    """Hex20 | hex8 NeoHookeWa box with the tied interface compressed by 15 % in 4 increments:
+    identical Newton iteration counts and displacements within 1e-6 of the oracle (which
+    eliminates the ties the same way, K^ = T^T K T)."""
+    from cases import build_gpu_tied, oracle_tied, tied_tl_spec
+    from edelweissfe_gb300.solver import LinSolverOptions, Step
+    from oracle.nist import NIST
+    from oracle.nist import Step as OStep
+
+    spec = tied_tl_spec(2, 2, 2, 2)
+    o = NIST(oracle_tied(spec))
+    Uo, _ = o.solveStep(OStep(maxInc=0.25, minInc=1e-6, maxIter=25))
+    fp64 = mode == "fp64"
+    s = build_gpu_tied(spec, keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
+    U, _ = s.solveStep(Step(maxInc=0.25, minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.iterationHistory] == [it for _, it in o.history]
+    assert np.max(np.abs(U.cpu().numpy() - Uo)) <= 1e-6 * np.max(np.abs(Uo))
+    sl, a, b = spec["mesh"]["ties"]
+    u = U.cpu().numpy().reshape(-1, 3)
+    assert np.max(np.abs(u[sl] - 0.5 * (u[a] + u[b]))) <= 1e-14 * np.max(np.abs(u))

@@ -137,3 +137,33 @@ def test_oracle_nist_tl_matches_reference(case):
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.history] == list(g["iters"])
     assert np.max(np.abs(U - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
+
+
+def _tied_model(m, matQ, matL, propsQ, propsL, elQ, elL, dirs):
+    from oracle.element import make_elements
+
+    c = m["coords"]
+    gq = make_elements(elQ, c[m["elements20"]], matQ, propsQ)
+    gl = make_elements(elL, c[m["elements8"]], matL, propsL)
+    return Model(3 * c.shape[0], [(gq, element_dofs(m["elements20"])), (gl, element_dofs(m["elements8"]))], dirs,
+                 ties=m["ties"])  # fmt: skip
+
+
+def test_oracle_tied_interface_passes_the_patch_test():
+    """Hex20 | hex8 box with the tied interface under uniaxial stress (symmetry planes, end
+    displacement): the linear exact field u = eps (x, -nu y, -nu z) is reproduced."""
+    from edelweissfe_gb300.mesh import tied_box_mesh
+
+    m = tied_box_mesh(2, 3, 2, 2, 0.4, 0.6, 0.3, 0.3)
+    s = m["nodeSets"]
+    c = m["coords"]
+    eps, nu = 1e-3, 0.3
+    y0 = np.flatnonzero(np.abs(c[:, 1]) < 1e-12)
+    z0 = np.flatnonzero(np.abs(c[:, 2]) < 1e-12)
+    dirs = [(3 * s["gen_left"], np.zeros(s["gen_left"].size)), (3 * s["gen_right"], np.full(s["gen_right"].size, eps)),
+            (3 * y0 + 1, np.zeros(y0.size)), (3 * z0 + 2, np.zeros(z0.size))]  # fmt: skip
+    model = _tied_model(m, "linearelastic", "linearelastic", [210000.0, nu], [210000.0, nu], "C3D20", "C3D8", dirs)
+    U, _ = NIST(model).solveStep(Step(maxInc=1.0, minInc=1e-6, maxIter=25, extrapolation="off"))
+    u = U.reshape(-1, 3)
+    exact = eps / 1.0 * np.stack([c[:, 0], -nu * c[:, 1], -nu * c[:, 2]], axis=1)
+    assert np.max(np.abs(u - exact)) <= 1e-9 * eps
