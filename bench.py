@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")
-    ap.add_argument("--workload", default="box", choices=["box", "cubes"],
-                    help="box: the 160k-element J2 box (default); cubes: 1024 independent J2 cubes in one batch")
+    ap.add_argument("--workload", default="box", choices=["box", "cubes", "tied"],
+                    help="box: the 160k-element J2 box (default); cubes: 1024 independent J2 cubes in one batch; "
+                         "tied: 60x30x30 NeoHookeWa box, hex20 | hex8 halves with a tied interface")
     ap.add_argument("--profile", action="store_true",
                     help="one assembly and one capped solve, for ncu captures of single kernels")
     return ap.parse_args()
@@ -474,6 +475,74 @@ def run_cubes(a):
     print(json.dumps(line), flush=True)
 
 
+def run_tied(a):
+    """60x30x30 box (h = 1/30): x < 30 C3D20TL, x >= 30 C3D8TL, NeoHookeWa [80, 200], tied
+    interface, x = 0 clamped, x = 60 face compressed to 30 % over 40 increments.  A step is one
+    load increment (all Newton iterations, state accepted); warm-up increments run first."""
+    import torch
+
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300 import build as b
+    from edelweissfe_gb300.mesh import tied_box_mesh
+    from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, LinSolverOptions, NISTGPU, Step
+
+    b.build()
+    h = 1.0 / 30.0
+    m = tied_box_mesh(30, 30, 30, 30, 30 * h, 30 * h, 30 * h, 30 * h)
+    p = np.array([80.0, 200.0])
+    model = Model(m["coords"], [ElementGroup("C3D20TL", m["elements20"], "neohookewa", p),
+                                ElementGroup("C3D8TL", m["elements8"], "neohookewa", p)], ties=m["ties"])  # fmt: skip
+    dirs = [DirichletBC(m["nodeSets"]["gen_left"], {0: 0.0, 1: 0.0, 2: 0.0}),
+            DirichletBC(m["nodeSets"]["gen_right"], {0: -0.3 * 60 * h})]  # fmt: skip
+    s = NISTGPU(model, dirs, linsolver=LinSolverOptions(method="fgmres", rtol=1e-8))
+    step = Step(maxInc=1.0 / 40, minInc=1e-6, maxIter=25)
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    U, dU, P = s._vec(), s._vec(), s._vec()
+    prev = None
+    stepper = AdaptiveTimeStepper(0.0, 1.0, step.startInc, step.maxInc, step.minInc, step.maxNumInc)
+    gen = stepper.generateTimeStep()
+
+    def increment():
+        nonlocal U, dU, P, prev
+        ts = next(gen)
+        s.krylovIterations.clear()
+        Unp, dU, P, it = s.solveIncrement(U, dU, P, ts, prev, step)
+        _lib.check(s.lib.ef_accept_state(s.ctx), "accept")
+        U, prev = Unp, ts
+        return it, sum(s.krylovIterations)
+
+    for _ in range(max(3, a.warmup)):
+        increment()
+    clocks = ClockSampler()
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = s.lib.ef_kernel_launches()
+    e0.record()
+    its = [increment() for _ in range(a.steps)]
+    e1.record()
+    torch.cuda.synchronize()
+    launches = s.lib.ef_kernel_launches() - l0
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3 / a.steps
+    peaks, peak_kind = measured_peaks()
+    line = {
+        "metric": "tied hex20|hex8 NeoHookeWa box: load-increment s",
+        "value": t, "unit": "s", "n_gpus": 1, "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": t * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 kinematics/stress/residual, f32 stiffness + Krylov inner, f64 refinement",
+        "data": "synthetic (structured mesh)",
+        "config": {"workload": "60x30x30 box, 27000 C3D20TL (27 Gauss points) | 27000 C3D8TL, NeoHookeWa [80, 200], "
+                               "tied interface, 30 % compression in 40 increments", "dofs": int(s.nDof),
+                   "ties": int(len(m["ties"][0]))},
+        "newton_krylov_per_step": its,
+        "solver": "FGMRES(40) + rigid-body aggregation W-cycle",
+        "gpu_launches": int(launches), "clocks": clk, "peak_kind": peak_kind,
+    }  # fmt: skip
+    print(json.dumps(line), flush=True)
+
+
 def _element_sample(args):
     """Oracle element pass + CSR update over elements [lo, hi) of the box (one worker)."""
     nx, ny, nz, lo, hi = args
@@ -639,6 +708,8 @@ if __name__ == "__main__":
         run_profile(args)
     elif args.workload == "cubes" and args.impl == "ours":
         run_cubes(args)
+    elif args.workload == "tied" and args.impl == "ours":
+        run_tied(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

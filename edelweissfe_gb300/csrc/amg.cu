@@ -400,6 +400,19 @@ __global__ void coarsest_apply_kernel(int n, const float* __restrict__ inv, cons
     x[i] = dead[i] ? 0.f : s;
 }
 
+// deterministic pseudo-random start vector in [-0.5, 0.5) (integer hash of the index)
+__global__ void fill_hash_kernel(int64_t n, float* __restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t h = (uint32_t)i * 2654435761u + 0x9e3779b9u;
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    x[i] = (float)h * (1.0f / 4294967296.0f) - 0.5f;
+}
+
 }  // namespace ef
 
 using namespace ef;
@@ -488,6 +501,13 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s) {
     coarsest_apply_kernel<<<nb_(n, 64), 64, 0, ef::counted(s)>>>(n, inv, r, dead, x);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    fill_hash_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, x);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -64,6 +64,7 @@ ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* off
                             const uint8_t* mask, float* x, cudaStream_t s, float alpha);
 ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                      float* inv, cudaStream_t s);
+ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s);
 // mpnn.cu
@@ -407,7 +408,10 @@ struct ef_ctx {
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
     // V-cycle parameters: damping, smoothing sweeps per side, coarse over-correction, cycle type
-    float amgOmega = 0.65f;
+    float amgOmega = 0.65f;                 // upper bound of the smoothing damping
+    std::vector<float> levelOmega;          // per smoothed level: amgOmega, or 4 / (3 lambda_max(D^-1 A)) when smaller
+    float* amgPow[2] = {nullptr, nullptr};  // power-iteration vectors (fine size)
+    float* amgZero = nullptr;
     int amgSweeps = 2;
     float amgAlpha = 1.5f;
     int amgCycle = 2;  // 1: V-cycle, 2: W-cycle below the finest level
@@ -566,6 +570,9 @@ void ef_destroy(ef_ctx* c) {
         F(L.t);
     }
     F(c->amgCoarsestInv);
+    F(c->amgPow[0]);
+    F(c->amgPow[1]);
+    F(c->amgZero);
     F(c->dBatchNodePtr);
     F(c->dBatchOrder);
     F(c->vcIn);
@@ -1506,11 +1513,18 @@ static ef_status run_pcg(ef_ctx* c, int vDouble, const void* rhs, void* sol, int
 // ---- aggregation multigrid (host setup, device refresh and V-cycle) -------------------------
 
 // greedy aggregation of a block graph: seeds take their whole (unaggregated) neighbourhood,
-// left-over nodes join a neighbouring seed aggregate, isolated ones form their own
+// left-over nodes join a neighbouring seed aggregate; nodes coupled to nothing but themselves
+// (tied nodes, whose DOFs are eliminated) all share one aggregate, so they coarsen away
 static int aggregate(int n, const std::vector<int32_t>& rowPtr, const std::vector<int32_t>& colIdx,
                      std::vector<int32_t>& agg) {
     agg.assign(n, -1);
     int nAgg = 0;
+    int iso = -1;
+    for (int m = 0; m < n; ++m)
+        if (rowPtr[m + 1] - rowPtr[m] <= 1) {
+            if (iso < 0) iso = nAgg++;
+            agg[m] = iso;
+        }
     for (int m = 0; m < n; ++m) {
         if (agg[m] != -1) continue;
         bool free = true;
@@ -1732,6 +1746,75 @@ static void amg_dead_mask(const AmgLevel& L, int bf, const uint8_t* fineDead, st
     }
 }
 
+// Damping of the block-Jacobi smoother on every smoothed level.  lambda, the largest eigenvalue of
+// D^-1 A, is estimated by 12 power iterations from a fixed pseudo-random vector; damped Jacobi
+// smoothing is stable for omega lambda < 2.  Where amgOmega lambda exceeds 1.6 (quadratic
+// elements raise lambda well above its hex8 value of about 2) the level uses 4 / (3 lambda),
+// quantised to 1/64 so that small changes keep the captured cycle; any change re-captures it.
+static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
+    ef_status st = EF_OK;
+    if (!c->amgPow[0]) {
+        c->amgPow[0] = dalloc<float>(c->nDof, &st);
+        c->amgPow[1] = dalloc<float>(c->nDof, &st);
+        c->amgZero = dalloc<float>(c->nDof, &st);
+        if (st != EF_OK) return st;
+        EF_CUDA(cudaMemset(c->amgZero, 0, sizeof(float) * c->nDof));
+    }
+    if (!c->nnRed) {  // reduction scratch shared with the learned correction
+        c->nnPartN = 2 * c->nSM;
+        c->nnRed = dalloc<double>(3 * (size_t)c->nnPartN + 8, &st);
+        if (!c->nnRed) return st;
+    }
+    const int nL = (int)c->amg.size();
+    const int BCo = ef_amg_coarse_dofs();
+    std::vector<float> om(nL);
+    double* out = c->nnRed + 3 * c->nnPartN;
+    for (int l = 0; l < nL; ++l) {
+        const bool fine = l == 0;
+        const int bs = fine ? 3 : BCo;
+        const int nN = fine ? (int)c->nNodes : c->amg[l - 1].nN;
+        const int32_t* rowPtr = fine ? c->dRowPtr : c->amg[l - 1].rowPtr;
+        const int32_t* colIdx = fine ? c->dColIdx : c->amg[l - 1].colIdx;
+        const float* vals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
+        const float* binv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
+        const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
+        const int64_t n = (int64_t)bs * nN;
+        float* a = c->amgPow[0];
+        float* b = c->amgPow[1];
+        EF_CHECK(ef_launch_fill_hash(n, a, s));
+        double prev = 0.0, lam = 0.0;
+        for (int it = 0; it < 13; ++it) {
+            EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, out, s));
+            double nn2 = 0.0;
+            EF_CUDA(cudaMemcpyAsync(&nn2, out, sizeof(double), cudaMemcpyDeviceToHost, s));
+            EF_CUDA(cudaStreamSynchronize(s));
+            const double nrm = sqrt(nn2);
+            if (it > 0) lam = nrm / prev;
+            if (!(nrm > 0.0)) break;
+            EF_CHECK(ef_mpnn_scale(n, a, (float)(1.0 / nrm), s));
+            prev = 1.0;
+            EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, a, c->amgZero, mask, b, s));  // -A a
+            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
+        }
+        float w = c->amgOmega;
+        if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.6)  // beyond 80 % of the stability limit 2
+            w = std::max(1.f, std::round((float)(4.0 / (3.0 * lam)) * 64.f)) / 64.f;
+        om[l] = w;
+    }
+    if (om != c->levelOmega) {
+        c->levelOmega = om;
+        if (c->vcGraph) {
+            cudaGraphExecDestroy(c->vcGraph);
+            c->vcGraph = nullptr;
+        }
+        if (c->nnGraph) {
+            cudaGraphExecDestroy(c->nnGraph);
+            c->nnGraph = nullptr;
+        }
+    }
+    return EF_OK;
+}
+
 // dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses and
 // the coarsest inverse for the current fine system
 static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
@@ -1757,6 +1840,7 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     }
     const AmgLevel& C = c->amg.back();
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
+    EF_CHECK(amg_damping(c, s));
     if (c->nnInit) {
         EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
         EF_CHECK(ef_launch_gather_f32(c->nBlocks, c->nnTpos, c->nnA, c->nnAT, s));
@@ -1768,7 +1852,7 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
 // x = V-cycle(r) on level l (l = 0: the fine system); one damped block-Jacobi sweep before and
 // after the coarse correction, dense solve on the coarsest level
 static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s) {
-    const float omega = c->amgOmega;
+    const float omega = l < (int)c->levelOmega.size() ? c->levelOmega[l] : c->amgOmega;
     const int nL = (int)c->amg.size();
     const int BCo = ef_amg_coarse_dofs();
     if (l == nL) {
@@ -2561,7 +2645,7 @@ ef_status ef_mpnn_init(ef_ctx* c, uint64_t seed, int maxSamples) {
         c->nnA = dalloc<float>(c->nBlocks, &st);
         c->nnAT = dalloc<float>(c->nBlocks, &st);
         c->nnTpos = dalloc<int64_t>(c->nBlocks, &st);
-        c->nnRed = dalloc<double>(3 * (size_t)c->nnPartN + 8, &st);
+        if (!c->nnRed) c->nnRed = dalloc<double>(3 * (size_t)c->nnPartN + 8, &st);
         c->vcOut2 = dalloc<float>(c->nDof, &st);
         c->nnD = dalloc<float>(c->nDof, &st);
         c->nnKd = dalloc<float>(c->nDof, &st);
