@@ -472,6 +472,9 @@ struct ef_ctx {
     double* fgPart = nullptr;
     double* fgH = nullptr;               // device scratch: h (128) + second pass (128) + norm + y (128)
     int fgRestart = 0;
+    double* fgPin = nullptr;                   // pinned host copies of two columns' coefficients
+    cudaEvent_t fgDone[2] = {nullptr, nullptr};
+    cudaEvent_t fgEv[2][4] = {};               // per column slot: iteration start/end, SpMV start/end
 };
 
 extern "C" {
@@ -600,6 +603,12 @@ void ef_destroy(ef_ctx* c) {
     F(c->dRowOfBlock0);
     F(c->fineX);
     F(c->fineT);
+    if (c->fgPin) cudaFreeHost(c->fgPin);
+    for (int k = 0; k < 2; ++k) {
+        if (c->fgDone[k]) cudaEventDestroy(c->fgDone[k]);
+        for (int e = 0; e < 4; ++e)
+            if (c->fgEv[k][e]) cudaEventDestroy(c->fgEv[k][e]);
+    }
     F(c->fgV);
     F(c->fgZ);
     F(c->fgW);
@@ -1748,7 +1757,7 @@ static void amg_dead_mask(const AmgLevel& L, int bf, const uint8_t* fineDead, st
 
 // Damping of the block-Jacobi smoother on every smoothed level.  lambda, the largest eigenvalue of
 // D^-1 A, is estimated by 12 power iterations from a fixed pseudo-random vector; damped Jacobi
-// smoothing is stable for omega lambda < 2.  Where amgOmega lambda exceeds 1.6 (quadratic
+// smoothing is stable for omega lambda < 2.  Where amgOmega lambda exceeds 1.85 (quadratic
 // elements raise lambda well above its hex8 value of about 2) the level uses 4 / (3 lambda),
 // quantised to 1/64 so that small changes keep the captured cycle; any change re-captures it.
 static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
@@ -1797,7 +1806,7 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
             EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
         }
         float w = c->amgOmega;
-        if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.6)  // beyond 80 % of the stability limit 2
+        if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.85)  // close to the stability limit 2
             w = std::max(1.f, std::round((float)(4.0 / (3.0 * lam)) * 64.f)) / 64.f;
         om[l] = w;
     }
@@ -2271,7 +2280,41 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CHECK(nn_snapshot_buffer(c, &p));
         EF_CUDA(cudaMemsetAsync(p, 0, sizeof(float) * n, s));
     }
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 2);
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
+    // The GPU work of column j+1 is enqueued before the host waits for column j's coefficients
+    // (Givens rotations and the convergence test run on the host), so the GPU never idles on the
+    // host; a converged cycle computes at most one column it does not use.
+    const int ldh = ef_fgmres_max_basis() + 2;
+    if (!c->fgPin) {
+        EF_CUDA(cudaMallocHost(&c->fgPin, sizeof(double) * 2 * ldh));
+        for (int k = 0; k < 2; ++k) {
+            EF_CUDA(cudaEventCreateWithFlags(&c->fgDone[k], cudaEventDisableTiming));
+            for (int e = 0; e < 4; ++e) EF_CUDA(cudaEventCreate(&c->fgEv[k][e]));
+        }
+    }
+    auto enqueue_column = [&](int j) -> ef_status {
+        const int sl = j & 1;
+        if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][0], s));
+        EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, Z + (int64_t)j * n, s));
+        if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][2], s));
+        EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals,
+                                    Z + (int64_t)j * n, c->dMask, w, s));
+        if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][3], s));
+        // classical Gram-Schmidt, twice
+        EF_CUDA(cudaMemsetAsync(dh, 0, sizeof(double) * (j + 1), s));
+        EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
+        EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
+        EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
+        EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
+        EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
+        EF_CHECK(ef_launch_scale(n, w, dinv, V + (int64_t)(j + 1) * n, s));
+        if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][1], s));
+        double* hp = c->fgPin + sl * ldh;
+        EF_CUDA(cudaMemcpyAsync(hp, dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+        EF_CUDA(cudaMemcpyAsync(hp + ldh - 1, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+        EF_CUDA(cudaEventRecord(c->fgDone[sl], s));
+        return EF_OK;
+    };
     int total = 0;
     bool converged = false;
     while (total < maxIter && !converged) {
@@ -2279,32 +2322,19 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
+        EF_CHECK(enqueue_column(0));
         for (; j < m && total < maxIter; ++j) {
-            if (prof) EF_CUDA(cudaEventRecord(c->ev[0], s));
-            EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, Z + (int64_t)j * n, s));
-            if (prof) EF_CUDA(cudaEventRecord(c->evS[0], s));
-            EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals,
-                                        Z + (int64_t)j * n, c->dMask, w, s));
-            if (prof) EF_CUDA(cudaEventRecord(c->evS[1], s));
-            // classical Gram-Schmidt, twice
-            EF_CUDA(cudaMemsetAsync(dh, 0, sizeof(double) * (j + 1), s));
-            EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
-            EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
-            EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
-            EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
-            EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
-            EF_CHECK(ef_launch_scale(n, w, dinv, V + (int64_t)(j + 1) * n, s));
-            if (prof) EF_CUDA(cudaEventRecord(c->ev[1], s));
-            EF_CUDA(cudaMemcpyAsync(hcol.data(), dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
-            double hn2 = 0.0;
-            EF_CUDA(cudaMemcpyAsync(&hn2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
-            EF_CUDA(cudaStreamSynchronize(s));
+            if (j + 1 < m && total + 1 < maxIter) EF_CHECK(enqueue_column(j + 1));
+            const int sl = j & 1;
+            EF_CUDA(cudaEventSynchronize(c->fgDone[sl]));
+            const double* hcol = c->fgPin + sl * ldh;
+            const double hn2 = hcol[ldh - 1];
             if (prof) {
                 float ms = 0.f;
-                EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+                EF_CUDA(cudaEventElapsedTime(&ms, c->fgEv[sl][0], c->fgEv[sl][1]));
                 prof->kernelMs += ms;
                 prof->kernelLaunches += 1;
-                EF_CUDA(cudaEventElapsedTime(&ms, c->evS[0], c->evS[1]));
+                EF_CUDA(cudaEventElapsedTime(&ms, c->fgEv[sl][2], c->fgEv[sl][3]));
                 prof->spmvMs += ms;
                 prof->spmvLaunches += 1;
             }
@@ -2324,7 +2354,10 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
             Hj[j + 1] = 0.0;
             g[j + 1] = -sn[j] * g[j];
             g[j] = cs[j] * g[j];
-            if (!(g[j + 1] == g[j + 1]) || !(den == den)) return EF_NAN;
+            if (!(g[j + 1] == g[j + 1]) || !(den == den)) {
+                EF_CUDA(cudaStreamSynchronize(s));
+                return EF_NAN;
+            }
             if (krylovSamples && total % c->nnEvery == 0 && nKrylov < c->nnMaxPerSolve) {
                 EF_CHECK(nn_add_sample(c, V + (int64_t)j * n, nullptr, s));
                 ++nKrylov;
