@@ -62,6 +62,8 @@ def parse():
                          "tied: 60x30x30 NeoHookeWa box, hex20 | hex8 halves with a tied interface")
     ap.add_argument("--profile", action="store_true",
                     help="one assembly and one capped solve, for ncu captures of single kernels")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="with --profile: FGMRES with the learned correction enabled (untrained weights), 5 iterations")
     return ap.parse_args()
 
 
@@ -683,9 +685,16 @@ def run_profile(a):
     from edelweissfe_gb300.solver import LinSolverOptions, TimeStep
 
     b.build()
-    s = build_solver(a, LinSolverOptions(method=a.method, rtol=1e-8, maxIter=200 if a.method == "pcg" else 60,
-                                         maxRefine=1))
+    learned = a.profile_learned and a.method == "fgmres"
+    cap = 5 if learned else (200 if a.method == "pcg" else 60)
+    s = build_solver(a, LinSolverOptions(method=a.method, rtol=1e-8, maxIter=cap, maxRefine=1))
     _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    if learned:
+        s.initLearnedPreconditioner(seed=0, maxSamples=0)
+        p, sc = s.learnedParameters()
+        p[-3 * 64:] = np.random.default_rng(0).normal(scale=0.05, size=3 * 64)  # non-zero output layer
+        s.setLearnedParameters(p, sc)
+        s.enableLearnedPreconditioner(True)
     ts = TimeStep(1, 0.05, 0.05, 0.05, 0.05, 0.05)
     dU = s._vec()
     dU[s.dirIdx] = torch.as_tensor(np.concatenate([d.getDelta(ts) for d in s.dirichlets]), device=dU.device)

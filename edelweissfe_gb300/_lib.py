@@ -101,6 +101,7 @@ SIGNATURES = {
     "ef_kernel_launches": (c_i64, []),
     "ef_set_group_props": (c_int, [c_vp, c_int, c_vp, c_int, c_int, c_vp]),
     "ef_set_ties": (c_int, [c_vp, c_vp, c_vp, c_vp, c_i64]),
+    "ef_mpnn_dense_eval": (c_int, [c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_batch_setup": (c_int, [c_vp, c_int, c_vp]),
     "ef_batch_tile_count": (c_int, []),
     "ef_batch_tile_info": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),

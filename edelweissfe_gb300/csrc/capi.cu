@@ -78,7 +78,7 @@ ef_status ef_launch_edge_weights(int nN, const int32_t* rowPtr, const int32_t* c
 ef_status ef_launch_gather_f32(int64_t n, const int64_t* idx, const float* src, float* dst, cudaStream_t s);
 ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* a, const float* P,
                           const float* f, const float* base, const uint8_t* mask, float so, float* acts, float* z,
-                          cudaStream_t s);
+                          int tc, int* flags, cudaStream_t s);
 ef_status ef_mpnn_backward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* aT, const float* P,
                            const float* f, const float* acts, const float* z, const float* e, const uint8_t* mask,
                            float scale, float so, float* grad, float* work, float* part, int nPart, cudaStream_t s);
@@ -91,6 +91,8 @@ ef_status ef_mpnn_refresh(int n, const float* p, void* pb, float* pf, cudaStream
 ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
                         int nPart, double* out, cudaStream_t s);
 ef_status ef_mpnn_scale(int64_t n, float* x, float a, cudaStream_t s);
+ef_status ef_mpnn_dense_eval_host(int tc, int nN, const float* h, const float* agg, const float* W, float* q,
+                                  float* hout, int* flagsOut, cudaStream_t s);
 ef_status ef_mpnn_scale_features(int nN, const float* f, float s0, float s1, float s2, float* fs, cudaStream_t s);
 ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, const double* dots, const uint8_t* mask,
                                 float* z, cudaStream_t s);
@@ -437,6 +439,7 @@ struct ef_ctx {
         double ee = 0.0, er = 0.0, rr = 0.0;                              // e.e, e.r, r.r
     };
     bool nnInit = false, nnOn = false;
+    int nnTensorCores = 1;                  // dense layers on tcgen05 (0: FP32 CUDA cores)
     float *nnP = nullptr, *nnPf = nullptr, *nnM1 = nullptr, *nnM2 = nullptr, *nnG = nullptr;  // FP32 masters, BF16 view,
     void* nnPb = nullptr;                                                                   // Adam moments, gradient;
     float *nnActs = nullptr, *nnF = nullptr, *nnWork = nullptr, *nnPart = nullptr;          // BF16 inference copy
@@ -759,6 +762,7 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     c->keFp64 = (options & EF_OPT_KE_FP64) ? 1 : 0;
     c->scalar = !(options & EF_OPT_NO_SCALAR_CSR) && c->hTieS.empty();  // the reference CSR has no ties
     if (const char* e = getenv("EF_ELEM_GRAPH")) c->elemGraphs = atoi(e) != 0;
+    if (const char* e = getenv("EF_MPNN_TC")) c->nnTensorCores = atoi(e) != 0;
     const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
     ef_status st = EF_OK;
     const int64_t nNodes = c->nNodes;
@@ -1914,7 +1918,7 @@ static ef_status nn_apply(ef_ctx* c, cudaStream_t s) {
     EF_CHECK(ef_launch_features(nN, c->vcOut, c->nnRho, (const float*)c->dBinv, c->nnS[0], c->nnS[1], c->nnS[2],
                                 c->nnF, s));
     EF_CHECK(ef_mpnn_forward(nN, c->dRowPtr, c->dColIdx, c->nnA, c->nnPf, c->nnF, nullptr, c->dMask, c->nnSo,
-                             c->nnActs, c->nnN, s));
+                             c->nnActs, c->nnN, c->nnTensorCores, c->dFlags, s));
     EF_CHECK(ef_launch_spmv_f32(nN, c->dRowPtr, c->dColIdx, K, c->nnN, c->dMask, c->nnKN, s));
     EF_CHECK(ef_mpnn_sumsq(n, 0, c->nnRho, c->nnKN, c->dMask, c->nnRed, c->nnPartN, out, s));
     EF_CHECK(ef_mpnn_sumsq(n, 1, c->nnKN, nullptr, c->dMask, c->nnRed, c->nnPartN, out + 3, s));
@@ -2184,7 +2188,7 @@ static ef_status nn_train(ef_ctx* c, int epochs, float lr, int norm, double* los
             const ef_ctx::NNSystem& Y = c->nnSystems[S.sys];
             EF_CHECK(ef_mpnn_scale_features((int)nN, S.f, c->nnS[0], c->nnS[1], c->nnS[2], c->nnF, s));
             EF_CHECK(ef_mpnn_forward((int)nN, c->dRowPtr, c->dColIdx, Y.a, c->nnPf, c->nnF, S.base, c->dMask, c->nnSo,
-                                     c->nnActs, c->vcOut2, s));
+                                     c->nnActs, c->vcOut2, c->nnTensorCores, c->dFlags, s));
             // rho = dL/dz up to the factor scale: d, K d or K (K z - r), d = z - e
             const float* rho = c->nnD;
             double ref = S.ee;
@@ -2648,6 +2652,12 @@ ef_status ef_batch_norms(ef_ctx* c, const double* R, const double* F, const doub
     return ef_launch_batch_norms(c->batchN, c->dBatchNodePtr, R, F, ddU, out, (cudaStream_t)stream);
 }
 
+ef_status ef_mpnn_dense_eval(int tensorCores, int nNodes, const float* h, const float* agg, const float* W,
+                             float* q, float* hout, int* flags, void* stream) {
+    if (nNodes <= 0 || !h || !agg || !W || !q || !hout || !flags) return EF_ERR_ARG;
+    return ef_mpnn_dense_eval_host(tensorCores ? 1 : 0, nNodes, h, agg, W, q, hout, flags, (cudaStream_t)stream);
+}
+
 int64_t ef_kernel_launches(void) { return (int64_t)ef::launches(); }
 
 int ef_mpnn_param_count(void) { return ef_mpnn_nparam(); }
@@ -2890,7 +2900,7 @@ ef_status ef_mpnn_eval(int nNodes, const int32_t* rowPtr, const int32_t* colIdx,
     if (dM) EV_CUDA(cudaMemcpyAsync(dM, mask, n, cudaMemcpyHostToDevice, s));
     EV_CHECK(ef_launch_edge_weights((int)nN, dR, dC, dV, dA, s));
     EV_CHECK(ef_launch_gather_f32(nb, dT, dA, dAT, s));
-    EV_CHECK(ef_mpnn_forward((int)nN, dR, dC, dA, dP, dF, dB, dM, so, acts, dZ, s));
+    EV_CHECK(ef_mpnn_forward((int)nN, dR, dC, dA, dP, dF, dB, dM, so, acts, dZ, 0, nullptr, s));
     EV_CHECK(ef_mpnn_sumsq(n, 1, dZ, dE, dM, red, nPart, red + 3 * nPart, s));
     if (grad)
         EV_CHECK(ef_mpnn_backward((int)nN, dR, dC, dAT, dP, dF, acts, dZ, dE, dM, scale, so, dG, work, part, nPart, s));

@@ -178,6 +178,148 @@ __global__ void __launch_bounds__(256) dense_kernel(int nN, const float* __restr
     }
 }
 
+// ---- dense layer on the 5th-generation tensor cores ----------------------------------------------
+// One CTA (4 warps) per tile of 128 nodes: X = [h | agg] (128 x 128) and W = [Ws | Wn] (64 x 128)
+// are converted to BF16 into shared memory in the no-swizzle K-major layout of 8 x 16-byte core
+// matrices, one thread issues 8 tcgen05.mma (M = 128, N = 64, K = 16, FP32 accumulate) into a
+// 64-column TMEM accumulator, completion is signalled through an mbarrier (bounded wait), and
+// each warp reads its 32 accumulator rows with tcgen05.ld for the epilogue q = relu(D),
+// hout = h + q (h in FP32).
+constexpr int TC_M = 128;                      // nodes per tile
+constexpr int TC_K = 2 * H;                    // [h | agg]
+constexpr int TC_A_BYTES = TC_M * TC_K * 2;    // 32 KB
+constexpr int TC_B_BYTES = H * TC_K * 2;       // 16 KB
+constexpr int TC_SMEM = TC_A_BYTES + TC_B_BYTES + 64;
+constexpr long long TC_WAIT_LIMIT = 1ll << 22;       // mbarrier polls before giving up
+constexpr long long TC_CLOCK_LIMIT = 2000000000ll;   // SM clocks before giving up (about 1 s)
+
+// byte offset of element (row r, column k) in a no-swizzle K-major tile of K = 128 columns:
+// core matrix (r / 8, k / 8) of 128 bytes, rows of 16 bytes inside
+__device__ __forceinline__ uint32_t tc_offset(int r, int k) {
+    return (uint32_t)((((r >> 3) * (TC_K / 8) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
+// shared-memory matrix descriptor: start address, leading (K) and stride (8-row) byte offsets,
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+__global__ void __launch_bounds__(128) dense_tc_kernel(int nN, const float* __restrict__ h,
+                                                       const float* __restrict__ agg, const float* __restrict__ Wl,
+                                                       float* __restrict__ q, float* __restrict__ hout,
+                                                       int* __restrict__ flags) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    unsigned char* sA = tsm;
+    unsigned char* sB = tsm + TC_A_BYTES;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + TC_A_BYTES + TC_B_BYTES);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + TC_A_BYTES + TC_B_BYTES + 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_M;
+    // operands -> BF16 in the core-matrix layout
+    for (int i = tid; i < TC_M * TC_K; i += 128) {
+        const int r = i / TC_K, k = i % TC_K;
+        const int m = m0 + r;
+        float v = 0.f;
+        if (m < nN) v = k < H ? h[(int64_t)m * H + k] : agg[(int64_t)m * H + (k - H)];
+        *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(r, k)) = __float2bfloat16(v);
+    }
+    for (int i = tid; i < H * TC_K; i += 128) {
+        const int c = i / TC_K, k = i % TC_K;
+        const float v = k < H ? Wl[c * H + k] : Wl[H * H + c * H + (k - H)];
+        *reinterpret_cast<__nv_bfloat16*>(sB + tc_offset(c, k)) = __float2bfloat16(v);
+    }
+    const uint32_t mbarAddr = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbarAddr));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        const uint32_t slotAddr = (uint32_t)__cvta_generic_to_shared(tslot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(slotAddr));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic stores -> async proxy
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t aBase = (uint32_t)__cvta_generic_to_shared(sA);
+        const uint32_t bBase = (uint32_t)__cvta_generic_to_shared(sB);
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(H >> 3) << 17) |
+                               ((uint32_t)(TC_M >> 4) << 24);  // F32 accum, BF16 A/B, K-major, N = 64, M = 128
+#pragma unroll
+        for (int ks = 0; ks < TC_K / 16; ++ks) {
+            const uint64_t ad = tc_desc(aBase + ks * 256, 128, (TC_K / 8) * 128);
+            const uint64_t bd = tc_desc(bBase + ks * 256, 128, (TC_K / 8) * 128);
+            const uint32_t acc = ks > 0 ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbarAddr)
+                     : "memory");
+    }
+    // bounded wait for the accumulator (phase 0): a poll count and a clock limit of about a second
+    long long polls = 0;
+    const long long t0 = clock64();
+    uint32_t done = 0;
+    while (!done) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(mbarAddr)
+            : "memory");
+        if (!done && (++polls > TC_WAIT_LIMIT || clock64() - t0 > TC_CLOCK_LIMIT)) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (done) {
+        // warp w owns accumulator rows (TMEM lanes) 32w .. 32w + 31; 64 FP32 columns each
+        uint32_t r[64];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,"
+            "%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, "
+            "[%64];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]),
+              "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]),
+              "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]),
+              "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]),
+              "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int m = m0 + warp * 32 + lane;
+        if (m < nN) {
+            const float* hr = h + (int64_t)m * H;
+            float* qo = q + (int64_t)m * H;
+            float* ho = hout + (int64_t)m * H;
+#pragma unroll
+            for (int c = 0; c < H; ++c) {
+                const float qq = fmaxf(__uint_as_float(r[c]), 0.f);
+                qo[c] = qq;
+                ho[c] = hr[c] + qq;
+            }
+        }
+    } else if (tid == 0) {
+        atomicOr(flags, EF_FLAG_BARRIER);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
 // z = base + so * W_out h3 on free DOFs (0 on masked); base may be null
 __global__ void output_kernel(int nN, const float* __restrict__ h3, const float* __restrict__ P,
                               const float* __restrict__ base, const uint8_t* __restrict__ mask, float so,
@@ -442,6 +584,7 @@ static const size_t kDenseBwdSmem = sizeof(float) * (2 * H + TILE) * (H + 1);
 
 ef_status ef_mpnn_setup_kernels() {
     EF_CUDA(cudaFuncSetAttribute(dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseSmem));
+    EF_CUDA(cudaFuncSetAttribute(dense_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     EF_CUDA(cudaFuncSetAttribute(dense_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseBwdSmem));
     return EF_OK;
 }
@@ -466,9 +609,13 @@ ef_status ef_launch_gather_f32(int64_t n, const int64_t* idx, const float* src, 
 }
 
 // forward pass; acts = [h0 | q1 h1 agg1 | q2 h2 agg2 | q3 h3 agg3] (each nN x H floats)
+ef_status ef_mpnn_dense(int tc, int nN, const float* h, const float* agg, const float* Wl, float* q, float* hout,
+                        int* flags, cudaStream_t s);
+
+// tc != 0: dense layers on the tensor cores (flags receives a tile's timeout), else FP32 CUDA cores
 ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* a, const float* P,
                           const float* f, const float* base, const uint8_t* mask, float so, float* acts, float* z,
-                          cudaStream_t s) {
+                          int tc, int* flags, cudaStream_t s) {
     const int64_t NH = (int64_t)nN * H;
     float* h0 = acts;
     input_kernel<<<nbm(NH, 256), 256, 0, ef::counted(s)>>>(nN, f, P, h0);
@@ -478,7 +625,8 @@ ef_status ef_mpnn_forward(int nN, const int32_t* rowPtr, const int32_t* colIdx, 
         float* hl = q + NH;
         float* agg = hl + NH;
         aggregate_kernel<<<nbm((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, a, hprev, agg, 0);
-        dense_kernel<<<nbm(nN, TILE), 256, kDenseSmem, ef::counted(s)>>>(nN, hprev, agg, P + OFF_L0 + l * PER_LAYER, q, hl);
+        const ef_status st = ef_mpnn_dense(tc, nN, hprev, agg, P + OFF_L0 + l * PER_LAYER, q, hl, flags, s);
+        if (st != EF_OK) return st;
         hprev = hl;
     }
     output_kernel<<<nbm((int64_t)nN * 3, 256), 256, 0, ef::counted(s)>>>(nN, hprev, P, base, mask, so, z);
@@ -585,4 +733,57 @@ ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, cons
     alpha_combine_kernel<<<nbm(n, 256), 256, 0, ef::counted(s)>>>(n, Mv, N, dots, mask, z);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
+}
+
+// one dense layer, q = relu(Ws h + Wn agg), hout = h + q, on the tensor cores (tc != 0) or the
+// FP32 CUDA cores; flags receives EF_FLAG_BARRIER if a tensor-core tile gave up waiting
+ef_status ef_mpnn_dense(int tc, int nN, const float* h, const float* agg, const float* Wl, float* q, float* hout,
+                        int* flags, cudaStream_t s) {
+    if (nN == 0) return EF_OK;
+    if (tc)
+        dense_tc_kernel<<<nbm(nN, TC_M), 128, TC_SMEM, ef::counted(s)>>>(nN, h, agg, Wl, q, hout, flags);
+    else
+        dense_kernel<<<nbm(nN, TILE), 256, kDenseSmem, ef::counted(s)>>>(nN, h, agg, Wl, q, hout);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// host-array check entry: one dense layer on the tensor cores (tc = 1) or the CUDA cores (tc = 0)
+ef_status ef_mpnn_dense_eval_host(int tc, int nN, const float* h, const float* agg, const float* W, float* q,
+                                  float* hout, int* flagsOut, cudaStream_t s) {
+    const ef_status su = ef_mpnn_setup_kernels();
+    if (su != EF_OK) return su;
+    const size_t nh = (size_t)nN * H;
+    float *dh = nullptr, *da = nullptr, *dw = nullptr, *dq = nullptr, *dho = nullptr;
+    int* df = nullptr;
+    auto fin = [&](ef_status r) {
+        cudaFree(dh);
+        cudaFree(da);
+        cudaFree(dw);
+        cudaFree(dq);
+        cudaFree(dho);
+        cudaFree(df);
+        return r;
+    };
+    if (cudaMalloc(&dh, nh * 4) != cudaSuccess || cudaMalloc(&da, nh * 4) != cudaSuccess ||
+        cudaMalloc(&dw, 2 * H * H * 4) != cudaSuccess || cudaMalloc(&dq, nh * 4) != cudaSuccess ||
+        cudaMalloc(&dho, nh * 4) != cudaSuccess || cudaMalloc(&df, 4) != cudaSuccess) {
+        ef_set_error("ef_mpnn_dense_eval: cudaMalloc failed");
+        return fin(EF_ERR_CUDA);
+    }
+    if (cudaMemcpyAsync(dh, h, nh * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(da, agg, nh * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(dw, W, 2 * H * H * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(df, 0, 4, s) != cudaSuccess)
+        return fin(EF_ERR_CUDA);
+    const ef_status st = ef_mpnn_dense(tc, nN, dh, da, dw, dq, dho, df, s);
+    if (st != EF_OK) return fin(st);
+    if (cudaMemcpyAsync(q, dq, nh * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(hout, dho, nh * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(flagsOut, df, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        ef_set_error("ef_mpnn_dense_eval: copy back failed");
+        return fin(EF_ERR_CUDA);
+    }
+    return fin(EF_OK);
 }

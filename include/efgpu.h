@@ -288,6 +288,14 @@ ef_status ef_mpnn_eval(int nNodes, const int32_t* rowPtr, const int32_t* colIdx,
                        const float* params, const float* f, const float* base, const float* e, const uint8_t* mask,
                        float so, float scale, float* z, float* grad, double* loss, void* stream);
 
+/* One dense layer of the network, q = relu(Ws h + Wn agg), hout = h + q, on HOST arrays h, agg
+ * [nNodes][64], W [2][64][64] (Ws then Wn, row = output channel), q, hout [nNodes][64]: on the
+ * tensor cores (tcgen05, BF16 operands, FP32 accumulation; tensorCores != 0) or the FP32 CUDA
+ * cores.  flags (host) receives the kernel's status bits (EF_FLAG_BARRIER 4: a tile gave up
+ * waiting for its accumulator).  For verification; synchronises `stream`. */
+ef_status ef_mpnn_dense_eval(int tensorCores, int nNodes, const float* h, const float* agg, const float* W,
+                             float* q, float* hout, int* flags, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

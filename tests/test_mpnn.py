@@ -97,3 +97,36 @@ def test_gpu_network_forward_backward_match_oracle(gpu_lib, dims):
     for lo_, hi_ in blocks:
         ref = go[lo_:hi_]
         assert np.max(np.abs(g[lo_:hi_] - ref)) <= 1e-4 * np.max(np.abs(ref)), (lo_, hi_)
+
+
+def _bf16_round(a):
+    """Round float32 values to the nearest BF16 (ties to even), returned as float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nN", [128, 1000])
+def test_gpu_dense_layer_tensor_cores_match_cuda_cores(gpu_lib, nN):
+    """q = relu(Ws h + Wn agg) on the tensor cores (tcgen05, BF16 operands, FP32 accumulation)
+    against the FP32 CUDA-core kernel: within the BF16 rounding of h and agg (1e-2 of max |q|),
+    residual output hout = h + q likewise, and no tile gave up waiting."""
+    rng = np.random.default_rng(5)
+    h = rng.normal(size=(nN, om.H)).astype(np.float32)
+    agg = rng.normal(size=(nN, om.H)).astype(np.float32)
+    W = _bf16_round(rng.normal(scale=0.1, size=(2, om.H, om.H)).astype(np.float32))
+    out = {}
+    for tc in (0, 1):
+        q = np.zeros((nN, om.H), np.float32)
+        ho = np.zeros((nN, om.H), np.float32)
+        fl = ctypes.c_int()
+        st = gpu_lib.ef_mpnn_dense_eval(tc, nN, h.ctypes.data, agg.ctypes.data, W.ctypes.data, q.ctypes.data,
+                                        ho.ctypes.data, ctypes.byref(fl), None)  # fmt: skip
+        assert st == 0, gpu_lib.ef_last_error().decode()
+        assert fl.value == 0
+        out[tc] = (q, ho)
+    qr = np.maximum(h.astype(np.float64) @ W[0].T.astype(np.float64) + agg @ W[1].T.astype(np.float64), 0.0)
+    assert np.max(np.abs(out[0][0] - qr)) <= 1e-5 * np.max(np.abs(qr))
+    assert np.max(np.abs(out[1][0] - out[0][0])) <= 1e-2 * np.max(np.abs(out[0][0]))
+    assert np.max(np.abs(out[1][1] - out[0][1])) <= 1e-2 * np.max(np.abs(out[0][1]))
