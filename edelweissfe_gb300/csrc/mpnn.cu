@@ -221,18 +221,28 @@ __global__ void __launch_bounds__(128) dense_tc_kernel(int nN, const float* __re
     uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + TC_A_BYTES + TC_B_BYTES + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * TC_M;
-    // operands -> BF16 in the core-matrix layout
-    for (int i = tid; i < TC_M * TC_K; i += 128) {
-        const int r = i / TC_K, k = i % TC_K;
+    // operands -> BF16 in the core-matrix layout, one 16-byte core-matrix row (8 values) per step
+    for (int i = tid; i < TC_M * (TC_K / 8); i += 128) {
+        const int r = i / (TC_K / 8), k8 = i % (TC_K / 8);
         const int m = m0 + r;
-        float v = 0.f;
-        if (m < nN) v = k < H ? h[(int64_t)m * H + k] : agg[(int64_t)m * H + (k - H)];
-        *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(r, k)) = __float2bfloat16(v);
+        float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+        if (m < nN) {
+            const float* src = k8 < H / 8 ? h + (int64_t)m * H + 8 * k8 : agg + (int64_t)m * H + 8 * (k8 - H / 8);
+            v0 = *reinterpret_cast<const float4*>(src);
+            v1 = *reinterpret_cast<const float4*>(src + 4);
+        }
+        __nv_bfloat162 b[4] = {__floats2bfloat162_rn(v0.x, v0.y), __floats2bfloat162_rn(v0.z, v0.w),
+                               __floats2bfloat162_rn(v1.x, v1.y), __floats2bfloat162_rn(v1.z, v1.w)};
+        *reinterpret_cast<uint4*>(sA + tc_offset(r, 8 * k8)) = *reinterpret_cast<uint4*>(b);
     }
-    for (int i = tid; i < H * TC_K; i += 128) {
-        const int c = i / TC_K, k = i % TC_K;
-        const float v = k < H ? Wl[c * H + k] : Wl[H * H + c * H + (k - H)];
-        *reinterpret_cast<__nv_bfloat16*>(sB + tc_offset(c, k)) = __float2bfloat16(v);
+    for (int i = tid; i < H * (TC_K / 8); i += 128) {
+        const int c = i / (TC_K / 8), k8 = i % (TC_K / 8);
+        const float* src = k8 < H / 8 ? Wl + c * H + 8 * k8 : Wl + H * H + c * H + 8 * (k8 - H / 8);
+        const float4 v0 = *reinterpret_cast<const float4*>(src);
+        const float4 v1 = *reinterpret_cast<const float4*>(src + 4);
+        __nv_bfloat162 b[4] = {__floats2bfloat162_rn(v0.x, v0.y), __floats2bfloat162_rn(v0.z, v0.w),
+                               __floats2bfloat162_rn(v1.x, v1.y), __floats2bfloat162_rn(v1.z, v1.w)};
+        *reinterpret_cast<uint4*>(sB + tc_offset(c, 8 * k8)) = *reinterpret_cast<uint4*>(b);
     }
     const uint32_t mbarAddr = (uint32_t)__cvta_generic_to_shared(mbar);
     if (tid == 0) {
@@ -279,6 +289,7 @@ __global__ void __launch_bounds__(128) dense_tc_kernel(int nN, const float* __re
             : "memory");
         if (!done && (++polls > TC_WAIT_LIMIT || clock64() - t0 > TC_CLOCK_LIMIT)) break;
     }
+    done = __syncthreads_and(done);  // the whole CTA reads the accumulator, or none of it
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (done) {
         // warp w owns accumulator rows (TMEM lanes) 32w .. 32w + 31; 64 FP32 columns each
@@ -300,23 +311,29 @@ __global__ void __launch_bounds__(128) dense_tc_kernel(int nN, const float* __re
               "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int m = m0 + warp * 32 + lane;
-        if (m < nN) {
-            const float* hr = h + (int64_t)m * H;
-            float* qo = q + (int64_t)m * H;
-            float* ho = hout + (int64_t)m * H;
+        // stage relu(D) row by row through shared memory (the operand tiles are no longer read once
+        // the MMAs completed; 128 x 65 words), padded by one word per row against bank conflicts,
+        // then write q and hout coalesced
+        float* sD = reinterpret_cast<float*>(sA);
+        const int row = warp * 32 + lane;
 #pragma unroll
-            for (int c = 0; c < H; ++c) {
-                const float qq = fmaxf(__uint_as_float(r[c]), 0.f);
-                qo[c] = qq;
-                ho[c] = hr[c] + qq;
-            }
+        for (int c = 0; c < H; ++c) sD[row * (H + 1) + c] = fmaxf(__uint_as_float(r[c]), 0.f);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (done) {
+        const float* sD = reinterpret_cast<const float*>(sA);
+        for (int i = tid; i < TC_M * H; i += 128) {
+            const int rr = i / H, c = i % H;
+            const int m = m0 + rr;
+            if (m >= nN) continue;
+            const float qq = sD[rr * (H + 1) + c];
+            q[(int64_t)m * H + c] = qq;
+            hout[(int64_t)m * H + c] = h[(int64_t)m * H + c] + qq;
         }
     } else if (tid == 0) {
         atomicOr(flags, EF_FLAG_BARRIER);
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
