@@ -12,6 +12,8 @@
 // Smoothing is damped block Jacobi; the coarsest level is solved with a dense
 // pseudo-inverse (Gauss-Jordan, pivots below a relative threshold dropped).
 
+#include <cuda_bf16.h>
+
 #include "ef_common.cuh"
 
 namespace ef {
@@ -167,11 +169,15 @@ __global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const ui
     }
 }
 
-// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads
-template <int BS>
+__device__ __forceinline__ float ld_val(const float* p) { return *p; }
+__device__ __forceinline__ float ld_val(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads; the block
+// values in FP32 or (fine-level smoothing) as a BF16 copy
+template <int BS, typename VT = float>
 __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32_t* __restrict__ rowPtr,
                                                               const int32_t* __restrict__ colIdx,
-                                                              const float* __restrict__ vals,
+                                                              const VT* __restrict__ vals,
                                                               const float* __restrict__ x, const float* __restrict__ r,
                                                               const uint8_t* __restrict__ mask, float* __restrict__ t) {
     const int lane = threadIdx.x & 7;
@@ -197,12 +203,12 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (cc[j] >= 0) {
-                const float* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
+                const VT* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
 #pragma unroll
                 for (int i = 0; i < BS; ++i) {
                     float a = 0.f;
 #pragma unroll
-                    for (int k = 0; k < BS; ++k) a += v[i * BS + k] * xv[j][k];
+                    for (int k = 0; k < BS; ++k) a += ld_val(v + i * BS + k) * xv[j][k];
                     y[i] += a;
                 }
             }
@@ -413,6 +419,11 @@ __global__ void fill_hash_kernel(int64_t n, float* __restrict__ x) {
     x[i] = (float)h * (1.0f / 4294967296.0f) - 0.5f;
 }
 
+__global__ void to_bf16_kernel(int64_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = __float2bfloat16(src[i]);
+}
+
 }  // namespace ef
 
 using namespace ef;
@@ -508,6 +519,23 @@ ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, cons
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s) {
     if (n == 0) return EF_OK;
     fill_hash_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, x);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    to_bf16_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, src, (__nv_bfloat16*)dst);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// fine-level (3x3 blocks) residual t = r - A x with the BF16 copy of the block values
+ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
+                                        const float* x, const float* r, const uint8_t* mask, float* t,
+                                        cudaStream_t s) {
+    level_residual_kernel<3, __nv_bfloat16><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(
+        nN, rowPtr, colIdx, (const __nv_bfloat16*)vals, x, r, mask, t);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

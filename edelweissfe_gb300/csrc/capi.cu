@@ -65,6 +65,10 @@ ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* off
 ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                      float* inv, cudaStream_t s);
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
+ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
+ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
+                                        const float* x, const float* r, const uint8_t* mask, float* t,
+                                        cudaStream_t s);
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s);
 // mpnn.cu
@@ -414,6 +418,8 @@ struct ef_ctx {
     std::vector<float> levelOmega;          // per smoothed level: amgOmega, or 4 / (3 lambda_max(D^-1 A)) when smaller
     float* amgPow[2] = {nullptr, nullptr};  // power-iteration vectors (fine size)
     float* amgZero = nullptr;
+    bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
+    void* dBsrValsH = nullptr;
     int amgSweeps = 2;
     float amgAlpha = 1.5f;
     int amgCycle = 2;  // 1: V-cycle, 2: W-cycle below the finest level
@@ -579,6 +585,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->amgPow[0]);
     F(c->amgPow[1]);
     F(c->amgZero);
+    F(c->dBsrValsH);
     F(c->dBatchNodePtr);
     F(c->dBatchOrder);
     F(c->vcIn);
@@ -1579,6 +1586,7 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;
     const int BCo = ef_amg_coarse_dofs();
@@ -1590,6 +1598,10 @@ static ef_status amg_build(ef_ctx* c) {
     c->fineX = dalloc<float>(c->nDof, &st);
     c->fineT = dalloc<float>(c->nDof, &st);
     if (!c->fineX || !c->fineT) return st;
+    if (c->amgBf16) {
+        c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9, &st);
+        if (!c->dBsrValsH) return st;
+    }
     const std::vector<int32_t>* pRow = &c->hRowPtr0;
     const std::vector<int32_t>* pCol = &c->hColIdx0;
     std::vector<double> finePos(3 * (size_t)n0);
@@ -1853,6 +1865,8 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     }
     const AmgLevel& C = c->amg.back();
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
+    if (c->dBsrValsH)
+        EF_CHECK(ef_launch_to_bf16((int64_t)c->nBlocks * 9, (const float*)c->dBsrVals, c->dBsrValsH, s));
     EF_CHECK(amg_damping(c, s));
     if (c->nnInit) {
         EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
@@ -1882,23 +1896,28 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
     float* t = fine ? c->fineT : c->amg[l - 1].t;
     AmgLevel& Cn = c->amg[l];
+    auto residual = [&]() -> ef_status {
+        if (fine && c->dBsrValsH)
+            return ef_launch_level_residual_bf16(nN, rowPtr, colIdx, c->dBsrValsH, x, r, mask, t, s);
+        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s);
+    };
     // pre-smoothing from zero
     EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x, 0, s));
     for (int k = 1; k < c->amgSweeps; ++k) {
-        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(residual());
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
     }
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = (l > 0 && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
-        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(residual());
         EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
         EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, x, s, c->amgAlpha));
     }
     // post-smoothing
     for (int k = 0; k < c->amgSweeps; ++k) {
-        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s));
+        EF_CHECK(residual());
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
     }
     return EF_OK;
