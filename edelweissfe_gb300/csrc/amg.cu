@@ -424,6 +424,31 @@ __global__ void to_bf16_kernel(int64_t n, const float* __restrict__ src, __nv_bf
     if (i < n) dst[i] = __float2bfloat16(src[i]);
 }
 
+// one Chebyshev smoothing step on D^-1 A: d = a d + b D^-1 t (a = 0: d = b D^-1 t), x += d
+// (x = d when `first`); masked DOFs -> 0
+template <int BS>
+__global__ void cheb_step_kernel(int nN, const float* __restrict__ binv, const uint8_t* __restrict__ mask, float a,
+                                 float b, const float* __restrict__ t, float* __restrict__ d, float* __restrict__ x,
+                                 int first) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    const float* B = binv + (int64_t)m * BS * BS;
+    float tv[BS];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) tv[i] = t[BS * m + i];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+        float z = 0.f;
+#pragma unroll
+        for (int j = 0; j < BS; ++j) z += B[i * BS + j] * tv[j];
+        const int k = BS * m + i;
+        float dn = (a != 0.f ? a * d[k] : 0.f) + b * z;
+        if (mask && mask[k]) dn = 0.f;
+        d[k] = dn;
+        x[k] = first ? dn : x[k] + dn;
+    }
+}
+
 }  // namespace ef
 
 using namespace ef;
@@ -536,6 +561,16 @@ ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int
                                         cudaStream_t s) {
     level_residual_kernel<3, __nv_bfloat16><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(
         nN, rowPtr, colIdx, (const __nv_bfloat16*)vals, x, r, mask, t);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* mask, float a, float b, const float* t,
+                              float* d, float* x, int first, cudaStream_t s) {
+    if (bs == 3)
+        cheb_step_kernel<3><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, a, b, t, d, x, first);
+    else
+        cheb_step_kernel<6><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, a, b, t, d, x, first);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

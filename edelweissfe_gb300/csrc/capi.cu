@@ -65,6 +65,8 @@ ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* off
 ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                      float* inv, cudaStream_t s);
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
+ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* mask, float a, float b, const float* t,
+                              float* d, float* x, int first, cudaStream_t s);
 ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
 ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
                                         const float* x, const float* r, const uint8_t* mask, float* t,
@@ -419,6 +421,9 @@ struct ef_ctx {
     float* amgPow[2] = {nullptr, nullptr};  // power-iteration vectors (fine size)
     float* amgZero = nullptr;
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
+    bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
+    std::vector<float> levelLam;            // per smoothed level: estimated lambda_max(D^-1 A), quantised
+    std::vector<float*> chebD;              // per smoothed level: Chebyshev direction vector
     void* dBsrValsH = nullptr;
     int amgSweeps = 2;
     float amgAlpha = 1.5f;
@@ -586,6 +591,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->amgPow[1]);
     F(c->amgZero);
     F(c->dBsrValsH);
+    for (float* p : c->chebD) F(p);
     F(c->dBatchNodePtr);
     F(c->dBatchOrder);
     F(c->vcIn);
@@ -1587,6 +1593,7 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
+    if (const char* e = getenv("EF_AMG_SMOOTHER")) c->amgCheb = strcmp(e, "cheb") == 0;
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;
     const int BCo = ef_amg_coarse_dofs();
@@ -1699,6 +1706,12 @@ static ef_status amg_build(ef_ctx* c) {
         pPos = &c->amg.back().hCentroid;
         nFine = nC;
     }
+    c->chebD.assign(c->amg.size(), nullptr);  // Chebyshev directions of the smoothed levels
+    for (size_t l = 0; l < c->amg.size(); ++l) {
+        const size_t nl = l == 0 ? (size_t)c->nDof : (size_t)BCo * c->amg[l - 1].nN;
+        c->chebD[l] = dalloc<float>(nl, &st);
+        if (!c->chebD[l]) return st;
+    }
     if (c->amg.empty() || c->amg.back().nN > ef_max_coarsest_nodes()) {
         ef_set_error("multigrid: the block graph does not coarsen to a dense-solvable size");
         return EF_ERR_ARG;
@@ -1792,7 +1805,7 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
     }
     const int nL = (int)c->amg.size();
     const int BCo = ef_amg_coarse_dofs();
-    std::vector<float> om(nL);
+    std::vector<float> om(nL), lamq(nL);
     double* out = c->nnRed + 3 * c->nnPartN;
     for (int l = 0; l < nL; ++l) {
         const bool fine = l == 0;
@@ -1825,9 +1838,12 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
         if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.85)  // close to the stability limit 2
             w = std::max(1.f, std::round((float)(4.0 / (3.0 * lam)) * 64.f)) / 64.f;
         om[l] = w;
+        // lambda on a grid of 2^(1/16) steps for the Chebyshev bounds (stable captured cycles)
+        lamq[l] = lam > 0.0 && lam == lam ? (float)exp2(std::ceil(16.0 * log2(lam)) / 16.0) : 2.f;
     }
-    if (om != c->levelOmega) {
+    if (om != c->levelOmega || (c->amgCheb && lamq != c->levelLam)) {
         c->levelOmega = om;
+        c->levelLam = lamq;
         if (c->vcGraph) {
             cudaGraphExecDestroy(c->vcGraph);
             c->vcGraph = nullptr;
@@ -1901,11 +1917,37 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
             return ef_launch_level_residual_bf16(nN, rowPtr, colIdx, c->dBsrValsH, x, r, mask, t, s);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s);
     };
+    // Chebyshev smoothing of degree amgSweeps on [lmax / 30, 1.1 lmax] of D^-1 A; from zero the
+    // first residual is r itself
+    auto chebyshev = [&](bool fromZero) -> ef_status {
+        const double up = 1.1 * (l < (int)c->levelLam.size() ? c->levelLam[l] : 2.0), lo = up / 30.0;
+        const double theta = 0.5 * (up + lo), delta = 0.5 * (up - lo), sigma = theta / delta;
+        double rhoOld = 1.0 / sigma;
+        float* d = c->chebD[l];
+        if (fromZero) {
+            EF_CHECK(ef_launch_cheb_step(bs, nN, binv, mask, 0.f, (float)(1.0 / theta), r, d, x, 1, s));
+        } else {
+            EF_CHECK(residual());
+            EF_CHECK(ef_launch_cheb_step(bs, nN, binv, mask, 0.f, (float)(1.0 / theta), t, d, x, 0, s));
+        }
+        for (int k = 1; k < c->amgSweeps; ++k) {
+            const double rho = 1.0 / (2.0 * sigma - rhoOld);
+            EF_CHECK(residual());
+            EF_CHECK(ef_launch_cheb_step(bs, nN, binv, mask, (float)(rho * rhoOld), (float)(2.0 * rho / delta), t, d,
+                                         x, 0, s));
+            rhoOld = rho;
+        }
+        return EF_OK;
+    };
     // pre-smoothing from zero
-    EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x, 0, s));
-    for (int k = 1; k < c->amgSweeps; ++k) {
-        EF_CHECK(residual());
-        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+    if (c->amgCheb) {
+        EF_CHECK(chebyshev(true));
+    } else {
+        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x, 0, s));
+        for (int k = 1; k < c->amgSweeps; ++k) {
+            EF_CHECK(residual());
+            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+        }
     }
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = (l > 0 && c->amgCycle > 1) ? c->amgCycle : 1;
@@ -1916,9 +1958,13 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
         EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, x, s, c->amgAlpha));
     }
     // post-smoothing
-    for (int k = 0; k < c->amgSweeps; ++k) {
-        EF_CHECK(residual());
-        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+    if (c->amgCheb) {
+        EF_CHECK(chebyshev(false));
+    } else {
+        for (int k = 0; k < c->amgSweeps; ++k) {
+            EF_CHECK(residual());
+            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+        }
     }
     return EF_OK;
 }
