@@ -146,7 +146,7 @@ def load(path: str = LIB_PATH):
         return _lib
     if not os.path.exists(path):
         raise ImportError(f"libefgpu.so not built ({path} missing); run edelweissfe_gb300.build.build()")
-    lib = ctypes.CDLL(path)
+    lib = ctypes.CDLL(path, mode=os.RTLD_NOW)  # every symbol resolved at load: a missing one fails here
     for name, (res, args) in SIGNATURES.items():
         f = getattr(lib, name)
         f.restype = res

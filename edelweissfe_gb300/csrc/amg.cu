@@ -169,15 +169,11 @@ __global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const ui
     }
 }
 
-__device__ __forceinline__ float ld_val(const float* p) { return *p; }
-__device__ __forceinline__ float ld_val(const __nv_bfloat16* p) { return __bfloat162float(*p); }
-
-// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads; the block
-// values in FP32 or (fine-level smoothing) as a BF16 copy
-template <int BS, typename VT = float>
+// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads
+template <int BS>
 __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32_t* __restrict__ rowPtr,
                                                               const int32_t* __restrict__ colIdx,
-                                                              const VT* __restrict__ vals,
+                                                              const float* __restrict__ vals,
                                                               const float* __restrict__ x, const float* __restrict__ r,
                                                               const uint8_t* __restrict__ mask, float* __restrict__ t) {
     const int lane = threadIdx.x & 7;
@@ -203,12 +199,12 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (cc[j] >= 0) {
-                const VT* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
+                const float* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
 #pragma unroll
                 for (int i = 0; i < BS; ++i) {
                     float a = 0.f;
 #pragma unroll
-                    for (int k = 0; k < BS; ++k) a += ld_val(v + i * BS + k) * xv[j][k];
+                    for (int k = 0; k < BS; ++k) a += v[i * BS + k] * xv[j][k];
                     y[i] += a;
                 }
             }
@@ -419,11 +415,6 @@ __global__ void fill_hash_kernel(int64_t n, float* __restrict__ x) {
     x[i] = (float)h * (1.0f / 4294967296.0f) - 0.5f;
 }
 
-__global__ void to_bf16_kernel(int64_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = __float2bfloat16(src[i]);
-}
-
 // one Chebyshev smoothing step on D^-1 A: d = a d + b D^-1 t (a = 0: d = b D^-1 t), x += d
 // (x = d when `first`); masked DOFs -> 0
 template <int BS>
@@ -447,6 +438,71 @@ __global__ void cheb_step_kernel(int nN, const float* __restrict__ binv, const u
         d[k] = dn;
         x[k] = first ? dn : x[k] + dn;
     }
+}
+
+// fine-level residual t = r - A x from a split BF16 copy of the 3x3 blocks: values 0..7 of block
+// k in one 16-byte word, value 8 in a separate array (two loads per block instead of nine)
+__global__ void __launch_bounds__(256) level_residual3_bf16_kernel(int nN, const int32_t* __restrict__ rowPtr,
+                                                                    const int32_t* __restrict__ colIdx,
+                                                                    const uint4* __restrict__ v8,
+                                                                    const __nv_bfloat16* __restrict__ v1,
+                                                                    const float* __restrict__ x,
+                                                                    const float* __restrict__ r,
+                                                                    const uint8_t* __restrict__ mask,
+                                                                    float* __restrict__ t) {
+    const int lane = threadIdx.x & 7;
+    const int m0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int m = m0 < nN ? m0 : nN - 1;
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    const int s = rowPtr[m], e = rowPtr[m + 1];
+    for (int base = s; base < e; base += 32) {
+        int cc[4];
+        uint4 q[4];
+        float w8[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = base + lane + 8 * j;
+            cc[j] = k < e ? 3 * colIdx[k] : -1;
+            if (cc[j] >= 0) {
+                q[j] = v8[k];
+                w8[j] = __bfloat162float(v1[k]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (cc[j] >= 0) {
+                const float x0 = x[cc[j]], x1 = x[cc[j] + 1], x2 = x[cc[j] + 2];
+                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q[j]);
+                const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
+                const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
+                y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
+                y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
+                y2 += a67.x * x0 + a67.y * x1 + w8[j] * x2;
+            }
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+    }
+    if (m0 < nN && lane < 3) {
+        const int d = 3 * m + lane;
+        const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
+        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+    }
+}
+
+// split BF16 copy of 3x3 blocks for level_residual3_bf16_kernel
+__global__ void to_bf16_split_kernel(int64_t nb, const float* __restrict__ src, uint4* __restrict__ v8,
+                                     __nv_bfloat16* __restrict__ v1) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    const float* a = src + k * 9;
+    __nv_bfloat162 h[4] = {__floats2bfloat162_rn(a[0], a[1]), __floats2bfloat162_rn(a[2], a[3]),
+                           __floats2bfloat162_rn(a[4], a[5]), __floats2bfloat162_rn(a[6], a[7])};
+    v8[k] = *reinterpret_cast<uint4*>(h);
+    v1[k] = __float2bfloat16(a[8]);
 }
 
 }  // namespace ef
@@ -548,19 +604,24 @@ ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s) {
     return EF_OK;
 }
 
-ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s) {
-    if (n == 0) return EF_OK;
-    to_bf16_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, src, (__nv_bfloat16*)dst);
+// fine-level (3x3 blocks) residual t = r - A x with the split BF16 copy of the block values
+// (vals: nBlocks uint4 words followed by nBlocks BF16 values)
+ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
+                                        const void* vals, const float* x, const float* r, const uint8_t* mask,
+                                        float* t, cudaStream_t s) {
+    const uint4* v8 = (const uint4*)vals;
+    const __nv_bfloat16* v1 = (const __nv_bfloat16*)(v8 + nBlocks);
+    level_residual3_bf16_kernel<<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, v8, v1, x,
+                                                                                     r, mask, t);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
-// fine-level (3x3 blocks) residual t = r - A x with the BF16 copy of the block values
-ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
-                                        const float* x, const float* r, const uint8_t* mask, float* t,
-                                        cudaStream_t s) {
-    level_residual_kernel<3, __nv_bfloat16><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(
-        nN, rowPtr, colIdx, (const __nv_bfloat16*)vals, x, r, mask, t);
+ef_status ef_launch_to_bf16_split(int64_t nBlocks, const float* src, void* dst, cudaStream_t s) {
+    if (nBlocks == 0) return EF_OK;
+    uint4* v8 = (uint4*)dst;
+    to_bf16_split_kernel<<<nb_(nBlocks, 256), 256, 0, ef::counted(s)>>>(nBlocks, src, v8,
+                                                                        (__nv_bfloat16*)(v8 + nBlocks));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

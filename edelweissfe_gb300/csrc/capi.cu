@@ -67,10 +67,10 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
 ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* mask, float a, float b, const float* t,
                               float* d, float* x, int first, cudaStream_t s);
-ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
-ef_status ef_launch_level_residual_bf16(int nN, const int32_t* rowPtr, const int32_t* colIdx, const void* vals,
-                                        const float* x, const float* r, const uint8_t* mask, float* t,
-                                        cudaStream_t s);
+ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
+                                        const void* vals, const float* x, const float* r, const uint8_t* mask,
+                                        float* t, cudaStream_t s);
+ef_status ef_launch_to_bf16_split(int64_t nBlocks, const float* src, void* dst, cudaStream_t s);
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s);
 // mpnn.cu
@@ -1606,7 +1606,7 @@ static ef_status amg_build(ef_ctx* c) {
     c->fineT = dalloc<float>(c->nDof, &st);
     if (!c->fineX || !c->fineT) return st;
     if (c->amgBf16) {
-        c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9, &st);
+        c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9, &st);  // 16-byte words + 1 value per block
         if (!c->dBsrValsH) return st;
     }
     const std::vector<int32_t>* pRow = &c->hRowPtr0;
@@ -1882,7 +1882,7 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     const AmgLevel& C = c->amg.back();
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
     if (c->dBsrValsH)
-        EF_CHECK(ef_launch_to_bf16((int64_t)c->nBlocks * 9, (const float*)c->dBsrVals, c->dBsrValsH, s));
+        EF_CHECK(ef_launch_to_bf16_split(c->nBlocks, (const float*)c->dBsrVals, c->dBsrValsH, s));
     EF_CHECK(amg_damping(c, s));
     if (c->nnInit) {
         EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
@@ -1914,7 +1914,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     AmgLevel& Cn = c->amg[l];
     auto residual = [&]() -> ef_status {
         if (fine && c->dBsrValsH)
-            return ef_launch_level_residual_bf16(nN, rowPtr, colIdx, c->dBsrValsH, x, r, mask, t, s);
+            return ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, x, r, mask, t, s);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s);
     };
     // Chebyshev smoothing of degree amgSweeps on [lmax / 30, 1.1 lmax] of D^-1 A; from zero the
