@@ -157,7 +157,8 @@ def assembly_bytes(info, nEl, fp32=True):
     """Algorithmic DRAM bytes of one assembly (element kernel + condensation + BSR scatter)."""
     s = 4 if fp32 else 8
     nQP = 8
-    elem = nEl * (8 * 4 + nQP * 13 * 8 * 2 + 36 * 9 * s + 24 * 8) + info.nDof * 8 * 2  # node ids, state r/w, Ke, Pe, X+dU
+    # node ids, state r/w, Ke blocks, Pe, geometry cache (dN/dx and w detJ per Gauss point, FP64), dU
+    elem = nEl * (8 * 4 + nQP * 13 * 8 * 2 + 36 * 9 * s + 24 * 8 + nQP * 25 * 8) + info.nDof * 8
     cond = nEl * 24 * 8 + nEl * 8 * 8 + info.nDof * 8 * 2  # Pe read, map, P and F write
     scatter = nEl * 36 * 9 * s + nEl * 64 * 8 + info.nBlocks * (9 * s + 8)  # Ke read, map, BSR write
     return elem, cond, scatter

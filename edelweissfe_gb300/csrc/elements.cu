@@ -93,18 +93,20 @@ __device__ __forceinline__ bool mat_von_mises(const double* props, double* sig, 
     const double k0 = *kappa;
     const double s23 = 0.81649658092772603;  // sqrt(2/3)
     const double s6 = 2.4494897427831781;    // sqrt(6)
-    const double fyk = fy0 + HL * k0 + dfy * (1.0 - exp(-dl * k0));
+    // with dfy = 0 the exponential terms are exact zeros: skipped (FP64 exp is expensive here)
+    const bool expo = dfy != 0.0;
+    const double fyk = fy0 + HL * k0 + (expo ? dfy * (1.0 - exp(-dl * k0)) : 0.0);
     if (dn - s23 * fyk > 0.0) {
         double dk = 0.0;
         double R = dn - s23 * fyk;
         int it = 0;
         while (fabs(R) > 1e-12) {
             if (it == 15) return false;
-            const double dR = -s6 * G - s23 * (HL + dfy * dl * exp(-dl * (k0 + dk)));
+            const double dR = -s6 * G - s23 * (HL + (expo ? dfy * dl * exp(-dl * (k0 + dk)) : 0.0));
             dk -= R / dR;
             ++it;
             const double kk = k0 + dk;
-            R = dn - s6 * G * dk - s23 * (fy0 + HL * kk + dfy * (1.0 - exp(-dl * kk)));
+            R = dn - s6 * G * dk - s23 * (fy0 + HL * kk + (expo ? dfy * (1.0 - exp(-dl * kk)) : 0.0));
         }
         const double dLam = 1.2247448713915889 * dk;  // sqrt(3/2)
         const double k1 = k0 + dk;
@@ -115,7 +117,7 @@ __device__ __forceinline__ bool mat_von_mises(const double* props, double* sig, 
             o.n[i] = d[i] * inv;
             sig[i] = t[i] - 2.0 * G * dLam * o.n[i];
         }
-        const double hp = HL + dfy * dl * exp(-dl * k1);
+        const double hp = HL + (expo ? dfy * dl * exp(-dl * k1) : 0.0);
         const double c1 = 2.0 * G * (1.0 / (1.0 + hp / (3.0 * G)) - 2.0 * G * dLam * inv);
         const double c2 = 4.0 * G * G * dLam * inv;
         o.c1 = c1;
@@ -203,6 +205,7 @@ struct SSShared {
     static constexpr int EPB = kBlock / TPE;
     double du[EPB][NN][3];
     double g[EPB][NQ][NN][3];
+    KT gk[EPB][NQ][NN][3];  // g in the stiffness precision, converted once per Gauss point and node
     double sw[EPB][NQ][6];
     KT tn[EPB][NQ][9];  // lt*w, mt*w, c1*w, n[6]
 };
@@ -249,6 +252,7 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
             for (int c = 0; c < 3; ++c) {
                 ga[c] = gq[3 * a + c];
                 sh.g[le][q][a][c] = ga[c];
+                sh.gk[le][q][a][c] = (KT)ga[c];
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -323,8 +327,8 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
         KT k[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int q = 0; q < NQ; ++q) {
             const KT* tn = sh.tn[le][q];
-            const KT ga0 = (KT)sh.g[le][q][a][0], ga1 = (KT)sh.g[le][q][a][1], ga2 = (KT)sh.g[le][q][a][2];
-            const KT gb0 = (KT)sh.g[le][q][b][0], gb1 = (KT)sh.g[le][q][b][1], gb2 = (KT)sh.g[le][q][b][2];
+            const KT ga0 = sh.gk[le][q][a][0], ga1 = sh.gk[le][q][a][1], ga2 = sh.gk[le][q][a][2];
+            const KT gb0 = sh.gk[le][q][b][0], gb1 = sh.gk[le][q][b][1], gb2 = sh.gk[le][q][b][2];
             const KT lt = tn[0], mt = tn[1], c1 = tn[2];
             const KT s = mt * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
             const KT la[3] = {lt * ga0, lt * ga1, lt * ga2};
