@@ -277,7 +277,8 @@ def run_ours(a):
         def wrapped(R):
             x = orig(R)
             i = s.lastSolveInfo
-            infos.append((i.kernelMs, i.iterations, i.kernelLaunches, i.spmvMs, i.spmvLaunches))
+            infos.append((i.kernelMs, i.iterations, i.kernelLaunches, i.spmvMs, i.spmvLaunches, i.precondMs,
+                          i.orthoMs, i.reorths))
             return x
 
         s.linsolver.profile = True
@@ -287,9 +288,9 @@ def run_ours(a):
         finally:
             s.linearSolve = orig
             s.linsolver.profile = False
-        return [sum(x[i] for x in infos) for i in range(5)]
+        return [sum(x[i] for x in infos) for i in range(8)]
 
-    fg_kms, fg_it, _, sp_ms, sp_n = profiled_step()
+    fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth = profiled_step()
 
     # comparison arm: block-Jacobi PCG on the same load step
     s.linsolver.method = "pcg"
@@ -297,7 +298,7 @@ def run_ours(a):
         s.enableLearnedPreconditioner(False)
     one_step()
     pcg_s, pcg_newton, pcg_k = timed(max(1, a.pcg_steps))
-    pcg_kms, pcg_it, _, _, _ = profiled_step()
+    pcg_kms, pcg_it = profiled_step()[:2]
     s.linsolver.method = "fgmres"
     if learned_info and learned_info["enabled"]:
         s.enableLearnedPreconditioner(True)
@@ -389,7 +390,11 @@ def run_ours(a):
                      "frac_hbm": asm_gbs / peaks["hbm_gbs"], "bytes": b_elem + b_cond + b_scat,
                      "elements_per_s": nEl / (t_el + t_as)},
         "fgmres_profile": {"iterations": fg_it, "kernel_ms": fg_kms,
-                           "ms_per_iteration": fg_kms / fg_it if fg_it else None},
+                           "ms_per_iteration": fg_kms / fg_it if fg_it else None,
+                           "precond_ms_per_iteration": pre_ms / fg_it if fg_it else None,
+                           "spmv_ms_per_iteration": sp_ms / fg_it if fg_it else None,
+                           "ortho_ms_per_iteration": orth_ms / fg_it if fg_it else None,
+                           "reorthogonalised_columns": int(n_reorth)},
         "dof_iterations_per_s": info.nDof * fg_it / (fg_kms * 1e-3) if fg_kms > 0 else None,
         "setup_s": setup_s,
         "history_s": history_s,

@@ -69,6 +69,9 @@ class EfSolveInfo(ctypes.Structure):
         ("kernelLaunches", c_int),
         ("spmvMs", c_dbl),
         ("spmvLaunches", c_int),
+        ("precondMs", c_dbl),
+        ("orthoMs", c_dbl),
+        ("reorths", c_int),
     ]
 
 

@@ -20,6 +20,21 @@ namespace ef {
 
 constexpr int BC = 6;  // DOFs of a coarse node
 
+// Vector loads/stores of the multigrid phases: plain, or through L2 only (CG) in the cluster
+// kernel, whose CTAs read vectors that other CTAs of the cluster wrote in the same launch.
+template <bool CG>
+__device__ __forceinline__ float ldv(const float* p) {
+    if (CG) return __ldcg(p);
+    return *p;
+}
+template <bool CG>
+__device__ __forceinline__ void stv(float* p, float v) {
+    if (CG)
+        __stcg(p, v);
+    else
+        *p = v;
+}
+
 // finer-node prolongation block, BF x 6
 template <int BF>
 __device__ __forceinline__ void pblock(const float* __restrict__ d, float P[BF][BC]) {
@@ -146,15 +161,13 @@ __global__ void bj6_setup_kernel(int nN, const int64_t* __restrict__ diagPos, co
 }
 
 // x = omega * D^-1 r (+ x when accumulating); masked DOFs -> 0
-template <int BS>
-__global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega,
-                                const float* __restrict__ r, float* __restrict__ x, int accumulate) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nN) return;
+template <int BS, bool CG>
+__device__ __forceinline__ void bj_row(int m, const float* __restrict__ binv, const uint8_t* __restrict__ mask,
+                                       float omega, const float* r, float* x, int accumulate) {
     const float* B = binv + (int64_t)m * BS * BS;
     float rv[BS];
 #pragma unroll
-    for (int i = 0; i < BS; ++i) rv[i] = r[BS * m + i];
+    for (int i = 0; i < BS; ++i) rv[i] = ldv<CG>(r + BS * m + i);
 #pragma unroll
     for (int i = 0; i < BS; ++i) {
         float z = 0.f;
@@ -163,19 +176,48 @@ __global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const ui
         z *= omega;
         if (mask && mask[BS * m + i]) z = 0.f;
         if (accumulate)
-            x[BS * m + i] += z;
+            stv<CG>(x + BS * m + i, ldv<CG>(x + BS * m + i) + z);
         else
-            x[BS * m + i] = z;
+            stv<CG>(x + BS * m + i, z);
     }
 }
 
-// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads
+template <int BS>
+__global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega,
+                                const float* __restrict__ r, float* __restrict__ x, int accumulate) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    bj_row<BS, false>(m, binv, mask, omega, r, x, accumulate);
+}
+
+// One damped block-Jacobi sweep finished for block row m from y = (A x)_m, held by every lane:
+// lane i < BS writes xout_i = x_i + omega (D_m^-1 (r - A x)_m)_i (masked entries of the
+// residual count as zero, masked entries of x stay).  xout must not alias x.
+template <int BS, bool CG = false>
+__device__ __forceinline__ void smooth_row(int m, int lane, const float* y, const float* x, const float* r,
+                                           const uint8_t* __restrict__ mask, const float* __restrict__ binv,
+                                           float omega, float* xout) {
+    float tv[BS];
+#pragma unroll
+    for (int j = 0; j < BS; ++j) tv[j] = (mask && mask[BS * m + j]) ? 0.f : ldv<CG>(r + BS * m + j) - y[j];
+    const float* B = binv + (int64_t)m * BS * BS + lane * BS;
+    float z = 0.f;
+#pragma unroll
+    for (int j = 0; j < BS; ++j) z += B[j] * tv[j];
+    const int d = BS * m + lane;
+    const float xd = ldv<CG>(x + d);
+    stv<CG>(xout + d, (mask && mask[d]) ? xd : xd + omega * z);
+}
+
+// t = r - A x on one level (masked rows -> 0); 8 lanes per block row, batched loads.  With
+// binv set it runs a whole smoothing sweep instead: t receives x + omega D^-1 (r - A x).
 template <int BS>
 __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32_t* __restrict__ rowPtr,
                                                               const int32_t* __restrict__ colIdx,
                                                               const float* __restrict__ vals,
                                                               const float* __restrict__ x, const float* __restrict__ r,
-                                                              const uint8_t* __restrict__ mask, float* __restrict__ t) {
+                                                              const uint8_t* __restrict__ mask, float* __restrict__ t,
+                                                              const float* __restrict__ binv, float omega) {
     const int lane = threadIdx.x & 7;
     const int m0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
     const int m = m0 < nN ? m0 : nN - 1;
@@ -185,26 +227,30 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
     const int s = rowPtr[m], e = rowPtr[m + 1];
     for (int base = s; base < e; base += 32) {
         int cc[4];
+        float v[4][BS * BS];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int k = base + lane + 8 * j;
-            cc[j] = k < e ? BS * colIdx[k] : -1;
+            if (k < e) {
+                cc[j] = BS * colIdx[k];
+                const float* src = vals + (int64_t)k * BS * BS;
+#pragma unroll
+                for (int q = 0; q < BS * BS; ++q) v[j][q] = src[q];
+            } else {
+                cc[j] = -1;
+            }
         }
-        float xv[4][BS];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (cc[j] >= 0)
-#pragma unroll
-                for (int i = 0; i < BS; ++i) xv[j][i] = x[cc[j] + i];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (cc[j] >= 0) {
-                const float* v = vals + (int64_t)(base + lane + 8 * j) * BS * BS;
+                float xv[BS];
+#pragma unroll
+                for (int i = 0; i < BS; ++i) xv[i] = x[cc[j] + i];
 #pragma unroll
                 for (int i = 0; i < BS; ++i) {
                     float a = 0.f;
 #pragma unroll
-                    for (int k = 0; k < BS; ++k) a += v[i * BS + k] * xv[j][k];
+                    for (int k = 0; k < BS; ++k) a += v[j][i * BS + k] * xv[k];
                     y[i] += a;
                 }
             }
@@ -214,62 +260,80 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
     if (m0 < nN && lane < BS) {
-        const int d = BS * m + lane;
-        float yy = y[0];
+        if (binv) {
+            smooth_row<BS>(m, lane, y, x, r, mask, binv, omega, t);
+        } else {
+            const int d = BS * m + lane;
+            float yy = y[0];
 #pragma unroll
-        for (int i = 1; i < BS; ++i)
-            if (lane == i) yy = y[i];
-        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+            for (int i = 1; i < BS; ++i)
+                if (lane == i) yy = y[i];
+            t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+        }
     }
 }
 
-// t = r - A x for 6x6 blocks: one warp per block row, one block per lane (coarse rows have
-// at most a few dozen blocks), fixed shuffle tree
+// t = r - A x for 6x6 blocks, one warp per block row: lane 6g + i (g < 5, i < 6) takes row i of
+// the blocks g, g + 5, g + 10, ... of the row (three 8-byte loads of the block row, so that the
+// warp reads five consecutive blocks per step), the five slots of each i are combined by a
+// fixed shuffle sequence.  With binv set: one smoothing sweep, t = x + omega D^-1 (r - A x).
+template <bool CG>
+__device__ __forceinline__ float2 ldv2(const float* p) {
+    if (CG) return __ldcg(reinterpret_cast<const float2*>(p));
+    return *reinterpret_cast<const float2*>(p);
+}
+template <bool CG>
+__device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __restrict__ rowPtr,
+                                           const int32_t* __restrict__ colIdx, const float* __restrict__ vals,
+                                           const float* x, const float* r, const uint8_t* __restrict__ mask, float* t,
+                                           const float* __restrict__ binv, float omega) {
+    const int g = lane / BC, ri = lane - BC * g;
+    float acc = 0.f;
+    if (g < 5) {
+        const int e = rowPtr[m + 1];
+        for (int k = rowPtr[m] + g; k < e; k += 5) {
+            const int c = BC * colIdx[k];
+            const float2* v = reinterpret_cast<const float2*>(vals + (int64_t)k * BC * BC + BC * ri);
+            const float2 a0 = v[0], a1 = v[1], a2 = v[2];
+            const float2 x0 = ldv2<CG>(x + c), x1 = ldv2<CG>(x + c + 2), x2 = ldv2<CG>(x + c + 4);
+            acc += a0.x * x0.x + a0.y * x0.y + a1.x * x1.x + a1.y * x1.y + a2.x * x2.x + a2.y * x2.y;
+        }
+    }
+    // lanes i < 6: acc(i) + acc(i + 6) + acc(i + 12) + acc(i + 18) + acc(i + 24)
+    const float s1 = acc + __shfl_down_sync(0xffffffffu, acc, 6);
+    const float s2 = s1 + __shfl_down_sync(0xffffffffu, s1, 12);
+    const float yi = s2 + __shfl_down_sync(0xffffffffu, acc, 24);
+    float y[BC];
+#pragma unroll
+    for (int i = 0; i < BC; ++i) y[i] = __shfl_sync(0xffffffffu, yi, i);
+    if (lane < BC) {
+        if (binv) {
+            smooth_row<BC, CG>(m, lane, y, x, r, mask, binv, omega, t);
+        } else {
+            const int d = BC * m + lane;
+            stv<CG>(t + d, (mask && mask[d]) ? 0.f : ldv<CG>(r + d) - yi);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int32_t* __restrict__ rowPtr,
                                                                const int32_t* __restrict__ colIdx,
                                                                const float* __restrict__ vals,
                                                                const float* __restrict__ x, const float* __restrict__ r,
-                                                               const uint8_t* __restrict__ mask, float* __restrict__ t) {
+                                                               const uint8_t* __restrict__ mask, float* __restrict__ t,
+                                                               const float* __restrict__ binv, float omega) {
     const int lane = threadIdx.x & 31;
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (m >= nN) return;
-    float y[BC];
-#pragma unroll
-    for (int i = 0; i < BC; ++i) y[i] = 0.f;
-    for (int k = rowPtr[m] + lane; k < rowPtr[m + 1]; k += 32) {
-        const int c = BC * colIdx[k];
-        const float* v = vals + (int64_t)k * BC * BC;
-        float xv[BC];
-#pragma unroll
-        for (int j = 0; j < BC; ++j) xv[j] = x[c + j];
-#pragma unroll
-        for (int i = 0; i < BC; ++i)
-#pragma unroll
-            for (int j = 0; j < BC; ++j) y[i] += v[i * BC + j] * xv[j];
-    }
-#pragma unroll
-    for (int i = 0; i < BC; ++i)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
-    if (lane < BC) {
-        float yy = y[0];
-#pragma unroll
-        for (int i = 1; i < BC; ++i)
-            if (lane == i) yy = y[i];
-        const int d = BC * m + lane;
-        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
-    }
+    resid6_row<false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega);
 }
 
 // rc[I] = sum over members m of aggregate I of P_m^T t[m]; one warp per aggregate, members
 // strided over the lanes and combined by a fixed shuffle tree
-template <int BF>
-__global__ void restrict_kernel(int nC, const int32_t* __restrict__ aggPtr, const int32_t* __restrict__ aggIdx,
-                                const float* __restrict__ offs, const float* __restrict__ t,
-                                const uint8_t* __restrict__ coarseDead, float* __restrict__ rc) {
-    const int lane = threadIdx.x & 31;
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (I >= nC) return;
+template <int BF, bool CG>
+__device__ __forceinline__ void restrict_row(int I, int lane, const int32_t* __restrict__ aggPtr,
+                                             const int32_t* __restrict__ aggIdx, const float* __restrict__ offs,
+                                             const float* t, const uint8_t* __restrict__ coarseDead, float* rc) {
     float a[BC];
 #pragma unroll
     for (int j = 0; j < BC; ++j) a[j] = 0.f;
@@ -279,7 +343,7 @@ __global__ void restrict_kernel(int nC, const int32_t* __restrict__ aggPtr, cons
         pblock<BF>(offs + 3 * (int64_t)m, P);
 #pragma unroll
         for (int i = 0; i < BF; ++i) {
-            const float ti = t[BF * m + i];
+            const float ti = ldv<CG>(t + BF * m + i);
 #pragma unroll
             for (int j = 0; j < BC; ++j) a[j] += P[i][j] * ti;
         }
@@ -293,31 +357,47 @@ __global__ void restrict_kernel(int nC, const int32_t* __restrict__ aggPtr, cons
 #pragma unroll
         for (int j = 1; j < BC; ++j)
             if (lane == j) v = a[j];
-        rc[BC * I + lane] = coarseDead[BC * I + lane] ? 0.f : v;
+        stv<CG>(rc + BC * I + lane, coarseDead[BC * I + lane] ? 0.f : v);
     }
 }
 
-// x[m] += P_m xc[agg(m)] on free finer DOFs
 template <int BF>
-__global__ void prolong_kernel(int nN, const int32_t* __restrict__ agg, const float* __restrict__ offs,
-                               const float* __restrict__ xc, const uint8_t* __restrict__ mask, float* __restrict__ x,
-                               float alpha) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nN) return;
+__global__ void restrict_kernel(int nC, const int32_t* __restrict__ aggPtr, const int32_t* __restrict__ aggIdx,
+                                const float* __restrict__ offs, const float* __restrict__ t,
+                                const uint8_t* __restrict__ coarseDead, float* __restrict__ rc) {
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= nC) return;
+    restrict_row<BF, false>(I, lane, aggPtr, aggIdx, offs, t, coarseDead, rc);
+}
+
+// x[m] += P_m xc[agg(m)] on free finer DOFs
+template <int BF, bool CG>
+__device__ __forceinline__ void prolong_row(int m, const int32_t* __restrict__ agg, const float* __restrict__ offs,
+                                            const float* xc, const uint8_t* __restrict__ mask, float* x, float alpha) {
     const int I = agg[m];
     float P[BF][BC];
     pblock<BF>(offs + 3 * (int64_t)m, P);
     float c[BC];
 #pragma unroll
-    for (int j = 0; j < BC; ++j) c[j] = xc[BC * I + j];
+    for (int j = 0; j < BC; ++j) c[j] = ldv<CG>(xc + BC * I + j);
 #pragma unroll
     for (int i = 0; i < BF; ++i) {
         if (mask && mask[BF * m + i]) continue;
         float s = 0.f;
 #pragma unroll
         for (int j = 0; j < BC; ++j) s += P[i][j] * c[j];
-        x[BF * m + i] += alpha * s;
+        stv<CG>(x + BF * m + i, ldv<CG>(x + BF * m + i) + alpha * s);
     }
+}
+
+template <int BF>
+__global__ void prolong_kernel(int nN, const int32_t* __restrict__ agg, const float* __restrict__ offs,
+                               const float* __restrict__ xc, const uint8_t* __restrict__ mask, float* __restrict__ x,
+                               float alpha) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nN) return;
+    prolong_row<BF, false>(m, agg, offs, xc, mask, x, alpha);
 }
 
 // dense pseudo-inverse of the coarsest operator (n = 6 nN <= kMaxCoarsestDof), FP64 Gauss-Jordan
@@ -393,13 +473,72 @@ __global__ void coarsest_inverse_kernel(int nN, const int32_t* __restrict__ rowP
 }
 
 // x = Ainv r on the coarsest level (dense matvec), dead DOFs -> 0
+// x = inv r on the coarsest level (dead DOFs -> 0), one warp per row (coalesced row of inv,
+// fixed shuffle tree)
+template <bool CG>
+__device__ __forceinline__ void coarsest_row(int i, int lane, int n, const float* __restrict__ inv, const float* r,
+                                             const uint8_t* __restrict__ dead, float* x) {
+    float s = 0.f;
+    for (int j = lane; j < n; j += 32) s += inv[(int64_t)i * n + j] * ldv<CG>(r + j);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) stv<CG>(x + i, dead[i] ? 0.f : s);
+}
+
 __global__ void coarsest_apply_kernel(int n, const float* __restrict__ inv, const float* __restrict__ r,
                                       const uint8_t* __restrict__ dead, float* __restrict__ x) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n) return;
-    float s = 0.f;
-    for (int j = 0; j < n; ++j) s += inv[(int64_t)i * n + j] * r[j];
-    x[i] = dead[i] ? 0.f : s;
+    coarsest_row<false>(i, threadIdx.x & 31, n, inv, r, dead, x);
+}
+
+// The multigrid cycle below a level as one launch: one cluster of kCoarseCtas CTAs runs the
+// phases of a host-built program in order, with a cluster barrier (release/acquire at cluster
+// scope, after a device-scope fence) between phases.  Vectors written in the launch are read
+// and written through L2 only.  Every thread runs every phase loop and every barrier, so the
+// barrier count is uniform over the cluster.
+constexpr int kCoarseCtas = 8;
+constexpr int kCoarseThreads = 1024;
+__global__ void __cluster_dims__(kCoarseCtas, 1, 1) __launch_bounds__(kCoarseThreads, 1)
+    coarse_cycle_kernel(const CoarseOp* __restrict__ ops, int nOps) {
+    const int tid = blockIdx.x * kCoarseThreads + threadIdx.x;
+    const int nThreads = kCoarseCtas * kCoarseThreads;
+    const int lane = threadIdx.x & 31;
+    const int gw = tid >> 5;
+    const int nWarps = nThreads >> 5;
+    for (int o = 0; o < nOps; ++o) {
+        const CoarseOp op = ops[o];
+        switch (op.type) {
+            case COP_BJ:
+                for (int m = tid; m < op.n; m += nThreads) bj_row<BC, true>(m, op.f1, op.mask, op.omega, op.in, op.out, 0);
+                break;
+            case COP_SWEEP:
+                for (int m = gw; m < op.n; m += nWarps)
+                    resid6_row<true>(m, lane, op.p0, op.p1, op.f0, op.in, op.rhs, op.mask, op.out, op.f1, op.omega);
+                break;
+            case COP_RESID:
+                for (int m = gw; m < op.n; m += nWarps)
+                    resid6_row<true>(m, lane, op.p0, op.p1, op.f0, op.in, op.rhs, op.mask, op.out, nullptr, 0.f);
+                break;
+            case COP_RESTRICT:
+                for (int I = gw; I < op.n; I += nWarps)
+                    restrict_row<BC, true>(I, lane, op.p0, op.p1, op.f0, op.in, op.mask, op.out);
+                break;
+            case COP_PROLONG:
+                for (int m = tid; m < op.n; m += nThreads)
+                    prolong_row<BC, true>(m, op.p0, op.f0, op.in, op.mask, op.out, op.omega);
+                break;
+            case COP_COARSEST:
+                for (int i = gw; i < op.n; i += nWarps) coarsest_row<true>(i, lane, op.n, op.f0, op.in, op.mask, op.out);
+                break;
+            default:
+                break;
+        }
+        __threadfence();
+        __syncwarp();
+        asm volatile("barrier.cluster.arrive.release;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
+    }
 }
 
 // deterministic pseudo-random start vector in [-0.5, 0.5) (integer hash of the index)
@@ -449,7 +588,8 @@ __global__ void __launch_bounds__(256) level_residual3_bf16_kernel(int nN, const
                                                                     const float* __restrict__ x,
                                                                     const float* __restrict__ r,
                                                                     const uint8_t* __restrict__ mask,
-                                                                    float* __restrict__ t) {
+                                                                    float* __restrict__ t,
+                                                                    const float* __restrict__ binv, float omega) {
     const int lane = threadIdx.x & 7;
     const int m0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
     const int m = m0 < nN ? m0 : nN - 1;
@@ -459,13 +599,17 @@ __global__ void __launch_bounds__(256) level_residual3_bf16_kernel(int nN, const
         int cc[4];
         uint4 q[4];
         float w8[4];
+        // the block words are loaded beside the column indices (predicated on the row bounds,
+        // not on the loaded index), so only the x gathers wait for colIdx
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int k = base + lane + 8 * j;
-            cc[j] = k < e ? 3 * colIdx[k] : -1;
-            if (cc[j] >= 0) {
+            if (k < e) {
+                cc[j] = 3 * colIdx[k];
                 q[j] = v8[k];
                 w8[j] = __bfloat162float(v1[k]);
+            } else {
+                cc[j] = -1;
             }
         }
 #pragma unroll
@@ -487,9 +631,14 @@ __global__ void __launch_bounds__(256) level_residual3_bf16_kernel(int nN, const
         y2 += __shfl_xor_sync(0xffffffffu, y2, o);
     }
     if (m0 < nN && lane < 3) {
-        const int d = 3 * m + lane;
-        const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
-        t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+        if (binv) {
+            const float yv[3] = {y0, y1, y2};
+            smooth_row<3>(m, lane, yv, x, r, mask, binv, omega, t);
+        } else {
+            const int d = 3 * m + lane;
+            const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
+            t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+        }
     }
 }
 
@@ -547,12 +696,16 @@ ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* m
     return EF_OK;
 }
 
+// binv == nullptr: t = r - A x; otherwise one smoothing sweep t = x + omega D^-1 (r - A x)
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
-                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s) {
+                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
+                                   const float* binv, float omega) {
     if (bs == 3)
-        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r,
+                                                                                        mask, t, binv, omega);
     else
-        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r, mask, t);
+        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r,
+                                                                                       mask, t, binv, omega);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -592,7 +745,15 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
 
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s) {
-    coarsest_apply_kernel<<<nb_(n, 64), 64, 0, ef::counted(s)>>>(n, inv, r, dead, x);
+    coarsest_apply_kernel<<<nb_((int64_t)n * 32, 256), 256, 0, ef::counted(s)>>>(n, inv, r, dead, x);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+int ef_coarse_cycle_threads() { return kCoarseCtas * kCoarseThreads; }
+
+ef_status ef_launch_coarse_cycle(const ef::CoarseOp* ops, int nOps, cudaStream_t s) {
+    coarse_cycle_kernel<<<kCoarseCtas, kCoarseThreads, 0, ef::counted(s)>>>(ops, nOps);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -608,11 +769,11 @@ ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s) {
 // (vals: nBlocks uint4 words followed by nBlocks BF16 values)
 ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
                                         const void* vals, const float* x, const float* r, const uint8_t* mask,
-                                        float* t, cudaStream_t s) {
+                                        float* t, cudaStream_t s, const float* binv, float omega) {
     const uint4* v8 = (const uint4*)vals;
     const __nv_bfloat16* v1 = (const __nv_bfloat16*)(v8 + nBlocks);
     level_residual3_bf16_kernel<<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, v8, v1, x,
-                                                                                     r, mask, t);
+                                                                                     r, mask, t, binv, omega);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -57,7 +57,8 @@ ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals,
 ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
                              float* x, int accumulate, cudaStream_t s);
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
-                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s);
+                                   const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
+                                   const float* binv = nullptr, float omega = 0.f);
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
                              const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s);
 ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
@@ -69,8 +70,9 @@ ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* 
                               float* d, float* x, int first, cudaStream_t s);
 ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
                                         const void* vals, const float* x, const float* r, const uint8_t* mask,
-                                        float* t, cudaStream_t s);
+                                        float* t, cudaStream_t s, const float* binv = nullptr, float omega = 0.f);
 ef_status ef_launch_to_bf16_split(int64_t nBlocks, const float* src, void* dst, cudaStream_t s);
+ef_status ef_launch_coarse_cycle(const ef::CoarseOp* ops, int nOps, cudaStream_t s);
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s);
 // mpnn.cu
@@ -115,11 +117,13 @@ ef_status ef_launch_batch_norms(int nProb, const int32_t* nodePtr, const double*
 int ef_fgmres_max_basis();
 ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, const float* x,
                              const uint8_t* mask, float* y, cudaStream_t s);
-ef_status ef_launch_multidot(int64_t n, int nv, const float* V, int64_t ldv, const float* w, double* part, int nPart,
-                             double* h, double* hAcc, float* invNorm, cudaStream_t s);
-ef_status ef_launch_multiaxpy(int64_t n, int nv, const float* V, int64_t ldv, const double* h, float* w,
-                              cudaStream_t s);
-ef_status ef_launch_scale(int64_t n, const float* w, const float* invNorm, float* v, cudaStream_t s);
+ef_status ef_launch_spmv_f32_copy(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                  const float* x, const uint8_t* mask, float* y, float* xcopy, cudaStream_t s);
+ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double* part, double* partN, int nPart,
+                               double* hG, double* hTmp, double* hAcc, double eta2, float* w2, double* hostOut,
+                               int slotNorm, cudaStream_t s);
+ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
+                                    int slotNorm, cudaStream_t s);
 ef_status ef_launch_combine(int64_t n, int nv, const float* Z, int64_t ldz, const double* y, float* x, cudaStream_t s);
 ef_status ef_launch_sub(int64_t n, const float* b, const float* y, float* r, cudaStream_t s);
 
@@ -341,6 +345,7 @@ struct AmgLevel {
     int64_t* gseg = nullptr;                // Galerkin map: blocks of the finer level per block here
     int32_t* gsrc = nullptr;
     float *x = nullptr, *r = nullptr, *t = nullptr;  // V-cycle work vectors of this level
+    float* x2 = nullptr;                             // second smoothing iterate (sweeps alternate)
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
 };
@@ -422,6 +427,11 @@ struct ef_ctx {
     float* amgZero = nullptr;
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
+    bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
+    int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel
+    ef::CoarseOp* dCoarseOps = nullptr;     // its phase program (device)
+    int nCoarseOps = 0, nCoarseOpsCap = 0;
+    float* clusterCur = nullptr;            // level clusterLevel's iterate that the program updates
     std::vector<float> levelLam;            // per smoothed level: estimated lambda_max(D^-1 A), quantised
     std::vector<float*> chebD;              // per smoothed level: Chebyshev direction vector
     void* dBsrValsH = nullptr;
@@ -484,7 +494,12 @@ struct ef_ctx {
     float* fgZ = nullptr;                // [restart][nDof]
     float* fgW = nullptr;
     double* fgPart = nullptr;
-    double* fgH = nullptr;               // device scratch: h (128) + second pass (128) + norm + y (128)
+    double* fgH = nullptr;               // device scratch: [hG | hTmp | hAcc | y], 128 each
+    double* fgPartN = nullptr;           // per-CTA parts of |w|^2
+    int fgNPart = 0;                     // CTAs of the orthogonalisation kernels
+    double* fgPinDev = nullptr;          // device address of fgPin
+    bool vcInStale = true;               // vcIn does not hold the next basis vector
+    double fgEta2 = 0.0;                 // DGKS threshold squared (EF_FGMRES_ETA; 0: one pass)
     int fgRestart = 0;
     double* fgPin = nullptr;                   // pinned host copies of two columns' coefficients
     cudaEvent_t fgDone[2] = {nullptr, nullptr};
@@ -493,7 +508,7 @@ struct ef_ctx {
 
 extern "C" {
 
-int ef_abi_version(void) { return 2; }
+int ef_abi_version(void) { return 3; }
 
 const char* ef_last_error(void) { return g_err.c_str(); }
 
@@ -583,6 +598,7 @@ void ef_destroy(ef_ctx* c) {
         F(L.gseg);
         F(L.gsrc);
         F(L.x);
+        F(L.x2);
         F(L.r);
         F(L.t);
     }
@@ -597,6 +613,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->vcIn);
     F(c->vcOut);
     if (c->vcGraph) cudaGraphExecDestroy(c->vcGraph);
+    if (c->dCoarseOps) cudaFree(c->dCoarseOps);
     if (c->egExec) cudaGraphExecDestroy(c->egExec);
     if (c->nnGraph) cudaGraphExecDestroy(c->nnGraph);
     for (void* p : {(void*)c->nnP, (void*)c->nnPf, (void*)c->nnM1, (void*)c->nnM2, (void*)c->nnG, c->nnPb,
@@ -630,6 +647,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->fgW);
     F(c->fgPart);
     F(c->fgH);
+    F(c->fgPartN);
     for (auto e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto e : c->evS)
@@ -1594,6 +1612,7 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
     if (const char* e = getenv("EF_AMG_SMOOTHER")) c->amgCheb = strcmp(e, "cheb") == 0;
+    if (const char* e = getenv("EF_AMG_CLUSTER")) c->amgCluster = atoi(e) != 0;
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;
     const int BCo = ef_amg_coarse_dofs();
@@ -1699,7 +1718,8 @@ static ef_status amg_build(ef_ctx* c) {
         L.x = dalloc<float>((size_t)BCo * nC, &st);
         L.r = dalloc<float>((size_t)BCo * nC, &st);
         L.t = dalloc<float>((size_t)BCo * nC, &st);
-        if (!L.vals || !L.binv || !L.dead || !L.x || !L.r || !L.t) return st;
+        L.x2 = dalloc<float>((size_t)BCo * nC, &st);
+        if (!L.vals || !L.binv || !L.dead || !L.x || !L.r || !L.t || !L.x2) return st;
         c->amg.push_back(std::move(L));
         pRow = &c->amg.back().hRowPtr;
         pCol = &c->amg.back().hColIdx;
@@ -1729,9 +1749,159 @@ static ef_status amg_build(ef_ctx* c) {
 static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s);
 
 // capture the preconditioner application (fixed device pointers; values may change later)
+// Phase program of the cycle at level l >= 1 (6-DOF nodes) from right-hand side r into x: the
+// same operations, order and buffers as amg_vcycle's block-Jacobi path.
+static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std::vector<ef::CoarseOp>& ops) {
+    const int nL = (int)c->amg.size();
+    const int BCo = ef_amg_coarse_dofs();
+    auto op = [](int type, int n) {
+        ef::CoarseOp o{};
+        o.type = type;
+        o.n = n;
+        return o;
+    };
+    if (l == nL) {
+        const AmgLevel& C = c->amg.back();
+        ef::CoarseOp o = op(ef::COP_COARSEST, BCo * C.nN);
+        o.f0 = c->amgCoarsestInv;
+        o.in = r;
+        o.mask = C.dead;
+        o.out = x;
+        ops.push_back(o);
+        return;
+    }
+    const AmgLevel& L = c->amg[l - 1];
+    const AmgLevel& Cn = c->amg[l];
+    const float omega = l < (int)c->levelOmega.size() ? c->levelOmega[l] : c->amgOmega;
+    auto sweep = [&](const float* xin, float* xout) {
+        ef::CoarseOp o = op(ef::COP_SWEEP, L.nN);
+        o.p0 = L.rowPtr;
+        o.p1 = L.colIdx;
+        o.f0 = L.vals;
+        o.f1 = L.binv;
+        o.mask = L.dead;
+        o.in = xin;
+        o.rhs = r;
+        o.out = xout;
+        o.omega = omega;
+        ops.push_back(o);
+    };
+    float* x2 = L.x2;
+    float* cur = ((2 * c->amgSweeps - 1) & 1) ? x2 : x;
+    {
+        ef::CoarseOp o = op(ef::COP_BJ, L.nN);
+        o.f1 = L.binv;
+        o.mask = L.dead;
+        o.in = r;
+        o.out = cur;
+        o.omega = omega;
+        ops.push_back(o);
+    }
+    for (int k = 1; k < c->amgSweeps; ++k) {
+        float* nxt = cur == x ? x2 : x;
+        sweep(cur, nxt);
+        cur = nxt;
+    }
+    const int reps = c->amgCycle > 1 ? c->amgCycle : 1;
+    for (int rep = 0; rep < reps; ++rep) {
+        ef::CoarseOp o = op(ef::COP_RESID, L.nN);
+        o.p0 = L.rowPtr;
+        o.p1 = L.colIdx;
+        o.f0 = L.vals;
+        o.mask = L.dead;
+        o.in = cur;
+        o.rhs = r;
+        o.out = L.t;
+        ops.push_back(o);
+        ef::CoarseOp rs = op(ef::COP_RESTRICT, Cn.nN);
+        rs.p0 = Cn.aggPtr;
+        rs.p1 = Cn.aggIdx;
+        rs.f0 = Cn.offs;
+        rs.mask = Cn.dead;
+        rs.in = L.t;
+        rs.out = Cn.r;
+        ops.push_back(rs);
+        amg_cycle_ops(c, l + 1, Cn.r, Cn.x, ops);
+        ef::CoarseOp pr = op(ef::COP_PROLONG, L.nN);
+        pr.p0 = Cn.agg;
+        pr.f0 = Cn.offs;
+        pr.mask = L.dead;
+        pr.in = Cn.x;
+        pr.out = cur;
+        pr.omega = c->amgAlpha;
+        ops.push_back(pr);
+    }
+    for (int k = 0; k < c->amgSweeps; ++k) {
+        float* nxt = cur == x ? x2 : x;
+        sweep(cur, nxt);
+        cur = nxt;
+    }
+}
+
+// Chooses the level whose coarse correction (restriction, the whole cycle below, prolongation)
+// runs as one coarse_cycle_kernel launch: the first level >= 1 whose next coarser level has at
+// most kClusterMaxNodes nodes; builds and uploads its phase program (before a graph capture).
+static ef_status amg_prepare_cluster(ef_ctx* c) {
+    constexpr int kClusterMaxNodes = 2048;
+    c->clusterLevel = -1;
+    c->nCoarseOps = 0;
+    const int nL = (int)c->amg.size();
+    if (!c->amgCluster || c->amgCheb) return EF_OK;
+    int lc = -1;
+    for (int l = 1; l < nL; ++l)
+        if (c->amg[l].nN <= kClusterMaxNodes) {
+            lc = l;
+            break;
+        }
+    if (lc < 0) return EF_OK;
+    const AmgLevel& L = c->amg[lc - 1];
+    const AmgLevel& Cn = c->amg[lc];
+    // level lc's iterate at its coarse correction: amg_vcycle's buffer alternation of the
+    // pre-smoothing replayed (level lc's output vector is L.x, its second vector L.x2)
+    float* x = L.x;
+    float* cur = ((2 * c->amgSweeps - 1) & 1) ? L.x2 : x;
+    for (int k = 1; k < c->amgSweeps; ++k) cur = cur == x ? L.x2 : x;
+    std::vector<ef::CoarseOp> ops;
+    ef::CoarseOp rs{};
+    rs.type = ef::COP_RESTRICT;
+    rs.n = Cn.nN;
+    rs.p0 = Cn.aggPtr;
+    rs.p1 = Cn.aggIdx;
+    rs.f0 = Cn.offs;
+    rs.mask = Cn.dead;
+    rs.in = L.t;
+    rs.out = Cn.r;
+    ops.push_back(rs);
+    amg_cycle_ops(c, lc + 1, Cn.r, Cn.x, ops);
+    ef::CoarseOp pr{};
+    pr.type = ef::COP_PROLONG;
+    pr.n = L.nN;
+    pr.p0 = Cn.agg;
+    pr.f0 = Cn.offs;
+    pr.mask = L.dead;
+    pr.in = Cn.x;
+    pr.out = cur;
+    pr.omega = c->amgAlpha;
+    ops.push_back(pr);
+    if (!c->dCoarseOps || (int)ops.size() > c->nCoarseOpsCap) {
+        if (c->dCoarseOps) cudaFree(c->dCoarseOps);
+        c->dCoarseOps = nullptr;
+        ef_status st = EF_OK;
+        c->dCoarseOps = dalloc<ef::CoarseOp>(ops.size(), &st);
+        if (!c->dCoarseOps) return st;
+        c->nCoarseOpsCap = (int)ops.size();
+    }
+    EF_CUDA(cudaMemcpy(c->dCoarseOps, ops.data(), sizeof(ef::CoarseOp) * ops.size(), cudaMemcpyHostToDevice));
+    c->nCoarseOps = (int)ops.size();
+    c->clusterLevel = lc;
+    c->clusterCur = cur;
+    return EF_OK;
+}
+
 static ef_status amg_capture(ef_ctx* c) {
     if (c->vcGraph) return EF_OK;
-    EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
+    EF_CHECK(amg_prepare_cluster(c));
+    if (!c->capStream) EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
     EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
     long long captured = 0;
     t_captureCount = &captured;
@@ -1939,31 +2109,65 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
         }
         return EF_OK;
     };
+    // one fused damped block-Jacobi sweep xout = xin + omega D^-1 (r - A xin)
+    auto sweep = [&](const float* xin, float* xout) -> ef_status {
+        if (fine && c->dBsrValsH)
+            return ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, xin, r, mask, xout, s,
+                                                 binv, omega);
+        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega);
+    };
+    // The sweeps alternate between x and a second vector; 2 * sweeps - 1 of them follow the first
+    // (from zero), so the first goes to the second vector when that count is odd and the last
+    // one lands in x.
+    float* x2 = fine ? c->fineX : c->amg[l - 1].x2;
+    float* cur = x;
+    if (!c->amgCheb) cur = ((2 * c->amgSweeps - 1) & 1) ? x2 : x;
     // pre-smoothing from zero
     if (c->amgCheb) {
         EF_CHECK(chebyshev(true));
     } else {
-        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x, 0, s));
+        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, cur, 0, s));
         for (int k = 1; k < c->amgSweeps; ++k) {
-            EF_CHECK(residual());
-            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+            float* nxt = cur == x ? x2 : x;
+            EF_CHECK(sweep(cur, nxt));
+            cur = nxt;
         }
     }
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = (l > 0 && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
-        EF_CHECK(residual());
+        if (!c->amgCheb) {
+            EF_CHECK(fine && c->dBsrValsH
+                         ? ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, cur, r, mask, t, s)
+                         : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s));
+        } else {
+            EF_CHECK(residual());
+        }
+        if (l == c->clusterLevel) {
+            // restriction, the whole cycle below and the prolongation as one cluster launch
+            if (cur != c->clusterCur || x != c->amg[l - 1].x) {
+                ef_set_error("multigrid: cluster program built for other buffers");
+                return EF_ERR_ARG;
+            }
+            EF_CHECK(ef_launch_coarse_cycle(c->dCoarseOps, c->nCoarseOps, s));
+            continue;
+        }
         EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, x, s, c->amgAlpha));
+        EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, cur, s, c->amgAlpha));
     }
     // post-smoothing
     if (c->amgCheb) {
         EF_CHECK(chebyshev(false));
     } else {
         for (int k = 0; k < c->amgSweeps; ++k) {
-            EF_CHECK(residual());
-            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, t, x, 1, s));
+            float* nxt = cur == x ? x2 : x;
+            EF_CHECK(sweep(cur, nxt));
+            cur = nxt;
+        }
+        if (cur != x) {
+            ef_set_error("multigrid: smoothing sweeps did not end in the output vector");
+            return EF_ERR_ARG;
         }
     }
     return EF_OK;
@@ -2010,18 +2214,20 @@ static ef_status nn_capture(ef_ctx* c) {
     return EF_OK;
 }
 
-static ef_status fgmres_precond(ef_ctx* c, const float* v, float* z, cudaStream_t s) {
+static ef_status fgmres_precond(ef_ctx* c, const float* v, const float** out, cudaStream_t s) {
     EF_CHECK(amg_capture(c));
-    EF_CUDA(cudaMemcpyAsync(c->vcIn, v, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+    if (c->vcInStale) {  // otherwise the previous column's normalisation wrote v into vcIn
+        EF_CUDA(cudaMemcpyAsync(c->vcIn, v, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+        c->vcInStale = false;
+    }
     ef::note_launches(c->vcGraphKernels);
     EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
+    *out = c->vcOut;
     if (c->nnOn) {
         EF_CHECK(nn_capture(c));
         ef::note_launches(c->nnGraphKernels);
         EF_CUDA(cudaGraphLaunch(c->nnGraph, s));
-        EF_CUDA(cudaMemcpyAsync(z, c->vcOut2, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
-    } else {
-        EF_CUDA(cudaMemcpyAsync(z, c->vcOut, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
+        *out = c->vcOut2;
     }
     return EF_OK;
 }
@@ -2161,6 +2367,7 @@ static ef_status nn_add_sample(ef_ctx* c, const float* r, const float* e, cudaSt
     const float inv = (float)sqrt(inv2);
     EF_CHECK(amg_capture(c));
     EF_CUDA(cudaMemcpyAsync(c->vcIn, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    c->vcInStale = true;
     ef::note_launches(c->vcGraphKernels);
     EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
     EF_CHECK(ef_launch_spmv_f32((int)nN, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->vcOut, c->dMask,
@@ -2316,26 +2523,40 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
     }
     if (!c->fgW) {
         c->fgW = dalloc<float>(n, &st);
-        c->fgPart = dalloc<double>((size_t)c->nPart * ef_fgmres_max_basis(), &st);
+        c->fgNPart = 4 * c->nSM;  // 1024 threads per SM
+        c->fgPart = dalloc<double>((size_t)c->fgNPart * ef_fgmres_max_basis(), &st);
+        c->fgPartN = dalloc<double>((size_t)c->fgNPart, &st);
         c->fgH = dalloc<double>(4 * (size_t)ef_fgmres_max_basis(), &st);
-        if (!c->fgW || !c->fgPart || !c->fgH) return st;
+        if (!c->fgW || !c->fgPart || !c->fgPartN || !c->fgH) return st;
+        if (const char* e = getenv("EF_FGMRES_ETA")) c->fgEta2 = atof(e) * atof(e);
     }
-    double* dh = c->fgH;                                // pass-1 coefficients (accumulated)
-    double* dh2 = c->fgH + ef_fgmres_max_basis();      // pass-2 coefficients
-    double* dnrm = c->fgH + 2 * ef_fgmres_max_basis(); // squared norm
-    double* dy = c->fgH + 3 * ef_fgmres_max_basis();   // solution coefficients
-    float* dinv = (float*)(c->fgH + 2 * ef_fgmres_max_basis() + 1);  // 1 / norm as float
+    const int MB = ef_fgmres_max_basis();
+    double* hG = c->fgH;            // first-pass coefficients and |w|^2 (the DGKS gate)
+    double* hTmp = c->fgH + MB;     // second-pass coefficients
+    double* hAcc = c->fgH + 2 * MB; // column of the Hessenberg matrix
+    double* dy = c->fgH + 3 * MB;   // solution coefficients
     float* V = c->fgV;
     float* Z = c->fgZ;
-    float* w = c->fgW;
+    // Results of a column reach the host through mapped pinned memory written by the
+    // normalisation kernel: [0, j] coefficients, ldh - 2 re-orthogonalised flag, ldh - 1 |w|^2.
+    const int ldh = MB + 2;
+    if (!c->fgPin) {
+        EF_CUDA(cudaHostAlloc(&c->fgPin, sizeof(double) * 3 * ldh, cudaHostAllocMapped));
+        EF_CUDA(cudaHostGetDevicePointer((void**)&c->fgPinDev, c->fgPin, 0));
+        for (int k = 0; k < 2; ++k) {
+            EF_CUDA(cudaEventCreateWithFlags(&c->fgDone[k], cudaEventDisableTiming));
+            for (int e = 0; e < 4; ++e) EF_CUDA(cudaEventCreate(&c->fgEv[k][e]));
+        }
+    }
+    double* pinRestart = c->fgPin + 2 * ldh;
+    double* pinRestartDev = c->fgPinDev + 2 * ldh;
     EF_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, s));
-    // r0 = b (x = 0)
-    EF_CUDA(cudaMemcpyAsync(w, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-    double beta2 = 0.0;
-    EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
-    EF_CUDA(cudaMemcpyAsync(&beta2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+    // r0 = b (x = 0); v0 = r0 / |r0| (also into the preconditioner's input)
+    EF_CUDA(cudaMemcpyAsync(V, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s));
+    c->vcInStale = false;
     EF_CUDA(cudaStreamSynchronize(s));
-    const double bnorm = sqrt(beta2);
+    const double bnorm = sqrt(pinRestart[0]);
     *iters = 0;
     if (!(bnorm > 0.0)) return EF_OK;
     double beta = bnorm;
@@ -2353,41 +2574,26 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
     // The GPU work of column j+1 is enqueued before the host waits for column j's coefficients
     // (Givens rotations and the convergence test run on the host), so the GPU never idles on the
     // host; a converged cycle computes at most one column it does not use.
-    const int ldh = ef_fgmres_max_basis() + 2;
-    if (!c->fgPin) {
-        EF_CUDA(cudaMallocHost(&c->fgPin, sizeof(double) * 2 * ldh));
-        for (int k = 0; k < 2; ++k) {
-            EF_CUDA(cudaEventCreateWithFlags(&c->fgDone[k], cudaEventDisableTiming));
-            for (int e = 0; e < 4; ++e) EF_CUDA(cudaEventCreate(&c->fgEv[k][e]));
-        }
-    }
     auto enqueue_column = [&](int j) -> ef_status {
         const int sl = j & 1;
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][0], s));
-        EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, Z + (int64_t)j * n, s));
+        const float* pz = nullptr;
+        EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, &pz, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][2], s));
-        EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals,
-                                    Z + (int64_t)j * n, c->dMask, w, s));
+        // w = K z_j straight into the next basis slot; z_j kept in Z
+        EF_CHECK(ef_launch_spmv_f32_copy((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, pz,
+                                         c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][3], s));
-        // classical Gram-Schmidt, twice
-        EF_CUDA(cudaMemsetAsync(dh, 0, sizeof(double) * (j + 1), s));
-        EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
-        EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
-        EF_CHECK(ef_launch_multidot(n, j + 1, V, n, w, c->fgPart, c->nPart, dh2, dh, nullptr, s));
-        EF_CHECK(ef_launch_multiaxpy(n, j + 1, V, n, dh2, w, s));
-        EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
-        EF_CHECK(ef_launch_scale(n, w, dinv, V + (int64_t)(j + 1) * n, s));
+        EF_CHECK(ef_launch_cgs_column(n, j + 1, V, n, c->fgPart, c->fgPartN, c->fgNPart, hG, hTmp, hAcc, c->fgEta2,
+                                      c->vcIn, c->fgPinDev + sl * ldh, ldh - 1, s));
+        c->vcInStale = false;
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][1], s));
-        double* hp = c->fgPin + sl * ldh;
-        EF_CUDA(cudaMemcpyAsync(hp, dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
-        EF_CUDA(cudaMemcpyAsync(hp + ldh - 1, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
         EF_CUDA(cudaEventRecord(c->fgDone[sl], s));
         return EF_OK;
     };
     int total = 0;
     bool converged = false;
     while (total < maxIter && !converged) {
-        EF_CHECK(ef_launch_scale(n, w, dinv, V, s));  // v0 = r / ||r||
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
@@ -2406,7 +2612,12 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
                 EF_CUDA(cudaEventElapsedTime(&ms, c->fgEv[sl][2], c->fgEv[sl][3]));
                 prof->spmvMs += ms;
                 prof->spmvLaunches += 1;
+                EF_CUDA(cudaEventElapsedTime(&ms, c->fgEv[sl][0], c->fgEv[sl][2]));
+                prof->precondMs += ms;
+                EF_CUDA(cudaEventElapsedTime(&ms, c->fgEv[sl][3], c->fgEv[sl][1]));
+                prof->orthoMs += ms;
             }
+            if (prof && hcol[ldh - 2] != 0.0) prof->reorths += 1;
             ++total;
             double* Hj = &H[(size_t)j * (m + 1)];  // column j
             for (int i = 0; i <= j; ++i) Hj[i] = hcol[i];
@@ -2464,11 +2675,11 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         // restart: r = b - K x
         EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, x, c->dMask,
                                     c->fineT, s));
-        EF_CHECK(ef_launch_sub(n, b, c->fineT, w, s));
-        EF_CHECK(ef_launch_multidot(n, 1, w, n, w, c->fgPart, c->nPart, dnrm, nullptr, dinv, s));
-        EF_CUDA(cudaMemcpyAsync(&beta2, dnrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+        EF_CHECK(ef_launch_sub(n, b, c->fineT, V, s));
+        EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s));
+        c->vcInStale = false;
         EF_CUDA(cudaStreamSynchronize(s));
-        beta = sqrt(beta2);
+        beta = sqrt(pinRestart[0]);
         if (beta <= rtol * bnorm) {
             converged = true;
             break;

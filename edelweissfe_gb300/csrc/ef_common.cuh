@@ -63,6 +63,27 @@ struct PropsArg {
     double v[8];
 };
 
+// One phase of the multigrid cycle below a level, run by coarse_cycle_kernel (amg.cu) with a
+// cluster barrier after each phase.  All coarse nodes carry 6 DOFs.
+enum CoarseOpType {
+    COP_BJ = 0,        // out = omega D^-1 in (masked -> 0)                 thread per row
+    COP_SWEEP = 1,     // out = in + omega D^-1 (rhs - A in)                warp per row
+    COP_RESID = 2,     // out = rhs - A in (masked -> 0)                    warp per row
+    COP_RESTRICT = 3,  // out[I] = sum_{m in I} P_m^T in[m] (dead -> 0)     warp per aggregate
+    COP_PROLONG = 4,   // out[m] += omega P_m in[agg(m)] (free DOFs)       thread per row
+    COP_COARSEST = 5,  // out = inv in (dead -> 0)                          warp per DOF
+};
+struct CoarseOp {
+    int type, n;
+    const int32_t *p0, *p1;  // rowPtr, colIdx | aggPtr, aggIdx | agg
+    const float *f0, *f1;    // vals, binv | offs | inv
+    const uint8_t* mask;     // row mask / dead coarse DOFs
+    const float* in;
+    const float* rhs;
+    float* out;
+    float omega;
+};
+
 }  // namespace ef
 
 #define EF_CUDA(call)                                                     \

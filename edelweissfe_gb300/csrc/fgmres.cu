@@ -1,7 +1,9 @@
 // Flexible GMRES building blocks (FP32 vectors, FP64 reductions): masked BSR SpMV, classical
-// Gram-Schmidt with re-orthogonalisation as two passes of multi-dot products and a multi-axpy,
-// normalisation and the final x += Z y.  Reductions are per-CTA partials summed in a fixed
-// order, so every FGMRES run is bit-reproducible.
+// Gram-Schmidt as multi-dot products and a multi-axpy (re-orthogonalised when the DGKS test asks
+// for it), normalisation and the final x += Z y.  Reductions are per-CTA partials summed in a
+// fixed order, so every FGMRES run is bit-reproducible.
+
+#include <algorithm>
 
 #include "ef_common.cuh"
 
@@ -10,11 +12,14 @@ namespace ef {
 constexpr int kFB = 256;
 constexpr int kMaxBasis = 128;  // cap on the Krylov basis size (restart length + 1)
 
-// y = A x on the free DOFs (masked rows -> 0); 8 lanes per block row, batched loads
+// y = A x on the free DOFs (masked rows -> 0); 8 lanes per block row.  The column indices and the
+// block values of a row are loaded together (predicated on the row bounds only), then the x
+// gathers that depend on the column indices: two dependent memory steps per row, not three.
 __global__ void __launch_bounds__(kFB) spmv_f32_kernel(int nN, const int32_t* __restrict__ rowPtr,
                                                         const int32_t* __restrict__ colIdx,
                                                         const float* __restrict__ vals, const float* __restrict__ x,
-                                                        const uint8_t* __restrict__ mask, float* __restrict__ y) {
+                                                        const uint8_t* __restrict__ mask, float* __restrict__ y,
+                                                        float* __restrict__ xcopy) {
     const int lane = threadIdx.x & 7;
     const int m0 = (blockIdx.x * kFB + threadIdx.x) >> 3;
     const int m = m0 < nN ? m0 : nN - 1;
@@ -22,26 +27,26 @@ __global__ void __launch_bounds__(kFB) spmv_f32_kernel(int nN, const int32_t* __
     const int s = rowPtr[m], e = rowPtr[m + 1];
     for (int base = s; base < e; base += 32) {
         int cc[4];
+        float v[4][9];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int k = base + lane + 8 * j;
-            cc[j] = k < e ? 3 * colIdx[k] : -1;
-        }
-        float xv[4][3];
+            if (k < e) {
+                cc[j] = 3 * colIdx[k];
+                const float* src = vals + (int64_t)k * 9;
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (cc[j] >= 0) {
-                xv[j][0] = x[cc[j]];
-                xv[j][1] = x[cc[j] + 1];
-                xv[j][2] = x[cc[j] + 2];
+                for (int q = 0; q < 9; ++q) v[j][q] = src[q];
+            } else {
+                cc[j] = -1;
             }
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (cc[j] >= 0) {
-                const float* v = vals + (int64_t)(base + lane + 8 * j) * 9;
-                y0 += v[0] * xv[j][0] + v[1] * xv[j][1] + v[2] * xv[j][2];
-                y1 += v[3] * xv[j][0] + v[4] * xv[j][1] + v[5] * xv[j][2];
-                y2 += v[6] * xv[j][0] + v[7] * xv[j][1] + v[8] * xv[j][2];
+                const float x0 = x[cc[j]], x1 = x[cc[j] + 1], x2 = x[cc[j] + 2];
+                y0 += v[j][0] * x0 + v[j][1] * x1 + v[j][2] * x2;
+                y1 += v[j][3] * x0 + v[j][4] * x1 + v[j][5] * x2;
+                y2 += v[j][6] * x0 + v[j][7] * x1 + v[j][8] * x2;
             }
     }
 #pragma unroll
@@ -54,77 +59,183 @@ __global__ void __launch_bounds__(kFB) spmv_f32_kernel(int nN, const int32_t* __
         const int d = 3 * m + lane;
         const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
         y[d] = (mask && mask[d]) ? 0.f : yy;
+        if (xcopy) xcopy[d] = x[d];
     }
 }
 
-// part[cta * kMaxBasis + k] = sum over this CTA's chunk of V[k] . w, k < nv.  Each thread
-// accumulates all nv products of its elements (nv <= kMaxBasis, in registers in groups of 8).
-__global__ void __launch_bounds__(kFB) multidot_partial_kernel(int64_t n, int nv, const float* __restrict__ V,
+// DGKS test (Daniel, Gragg, Kaufman, Stewart 1976) of classical Gram-Schmidt: after the first
+// projection w' = w - V h of w (|w|^2 = h[nv]), re-orthogonalise only when the Pythagorean
+// estimate |w'|^2 = |w|^2 - |h|^2 shows cancellation, |w'|^2 < eta2 |w|^2.  Every thread that
+// asks computes the same sum in the same order, so all kernels of one column agree.
+__device__ __forceinline__ bool dgks_reorth(const double* __restrict__ h, int nv, double eta2) {
+    if (!(eta2 > 0.0)) return false;
+    double hh = 0.0;
+    for (int k = 0; k < nv; ++k) hh += h[k] * h[k];
+    const double w2 = h[nv];
+    return w2 - hh < eta2 * w2;
+}
+
+// FP64 is a narrow pipe on this GPU (2 lanes per SM and cycle), so the reductions below run in
+// FP32 inside a CTA (the vectors themselves are FP32) and in FP64 only across CTAs, where the
+// sums are long.  All orders are fixed.
+
+// fixed-order FP64 sum over the CTA of one value per thread (every thread gets it)
+__device__ __forceinline__ double cta_sum_fixed(double v, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < kFB / 32; ++q) t += red[q];
+    return t;
+}
+
+// fixed-order FP32 sum over a warp (every lane gets it)
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// part[k * gridDim.x + cta] = sum over this CTA's elements of V[k] . w, k < nv.  The vectors go
+// in groups of 8 (8 accumulators per thread), two elements per thread and step, so that 16
+// independent loads are in flight per thread.
+__global__ void __launch_bounds__(kFB, 4) multidot_partial_kernel(int64_t n, int nv, const float* __restrict__ V,
                                                                 int64_t ldv, const float* __restrict__ w,
-                                                                double* __restrict__ part) {
-    __shared__ double red[kFB / 32][kMaxBasis];
+                                                                double* __restrict__ part,
+                                                                const double* __restrict__ gate, int gateNv,
+                                                                double eta2) {
+    if (gate && !dgks_reorth(gate, gateNv, eta2)) return;
+    __shared__ float red[kFB / 32][kMaxBasis];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int64_t stride = (int64_t)gridDim.x * kFB;
     for (int k0 = 0; k0 < nv; k0 += 8) {
+        const int kn = min(8, nv - k0);
         float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int64_t i = (int64_t)blockIdx.x * kFB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kFB) {
-            const float wi = w[i];
+        int64_t i = (int64_t)blockIdx.x * kFB + threadIdx.x;
+        for (; i + stride < n; i += 2 * stride) {
+            const float wa = w[i], wb = w[i + stride];
+            float va[8], vb[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k)
-                if (k0 + k < nv) acc[k] = fmaf(V[(k0 + k) * ldv + i], wi, acc[k]);
+                if (k < kn) {
+                    va[k] = V[(k0 + k) * ldv + i];
+                    vb[k] = V[(k0 + k) * ldv + i + stride];
+                }
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kn) acc[k] = fmaf(vb[k], wb, fmaf(va[k], wa, acc[k]));
+        }
+        if (i < n) {
+            const float wa = w[i];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kn) acc[k] = fmaf(V[(k0 + k) * ldv + i], wa, acc[k]);
         }
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            double a = (double)acc[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-            if (lane == 0 && k0 + k < nv) red[wp][k0 + k] = a;
+            const float a = warp_sum(acc[k]);
+            if (lane == 0 && k < kn) red[wp][k0 + k] = a;
         }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < nv; k += kFB) {
-        double s = 0.0;
+        float s = 0.f;
+#pragma unroll
         for (int q = 0; q < kFB / 32; ++q) s += red[q][k];
-        part[(int64_t)blockIdx.x * kMaxBasis + k] = s;
+        part[(int64_t)k * gridDim.x + blockIdx.x] = (double)s;
     }
 }
 
-// h[k] = sum_c part[c][k] (fixed order, one warp per k); also accumulates into hAcc[k];
-// optionally writes 1/sqrt(h[0]) as a float to invNorm (normalisation factor)
-__global__ void multidot_final_kernel(int nPart, int nv, const double* __restrict__ part, double* __restrict__ h,
-                                      double* __restrict__ hAcc, float* __restrict__ invNorm) {
-    const int lane = threadIdx.x & 31;
-    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// h[k] = sum_c part[k * nPart + c], one CTA per k, fixed order
+__global__ void __launch_bounds__(kFB) multidot_final_kernel(int nPart, int nv, const double* __restrict__ part,
+                                                              double* __restrict__ h, const double* __restrict__ gate,
+                                                              int gateNv, double eta2) {
+    if (gate && !dgks_reorth(gate, gateNv, eta2)) return;
+    __shared__ double red[kFB / 32];
+    const int k = blockIdx.x;
     if (k >= nv) return;
     double s = 0.0;
-    for (int c = lane; c < nPart; c += 32) s += part[(int64_t)c * kMaxBasis + k];
+    for (int c = threadIdx.x; c < nPart; c += kFB) s += part[(int64_t)k * nPart + c];
+    s = cta_sum_fixed(s, red);
+    if (threadIdx.x == 0) h[k] = s;
+}
+
+// w -= sum_k h[k] V[k] over a fixed grid, and partN[cta] = this CTA's part of |w|^2 (fixed
+// order).  With a gate (the first-pass coefficients and |w|^2) the pass runs only when the DGKS
+// test asks for re-orthogonalisation.
+__global__ void __launch_bounds__(kFB) cgs_axpy_kernel(int64_t n, int nv, const float* __restrict__ V, int64_t ldv,
+                                                        const double* __restrict__ h, float* __restrict__ w,
+                                                        double* __restrict__ partN, const double* __restrict__ gate,
+                                                        double eta2) {
+    if (gate && !dgks_reorth(gate, nv, eta2)) return;
+    __shared__ float hs[kMaxBasis];
+    __shared__ float red[kFB / 32];
+    for (int k = threadIdx.x; k < nv; k += kFB) hs[k] = (float)h[k];
+    __syncthreads();
+    float nrm = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * kFB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kFB) {
+        float s = w[i];
+        int k = 0;
+        for (; k + 8 <= nv; k += 8) {
+            float v[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-        h[k] = s;
-        if (hAcc) hAcc[k] += s;
-        if (invNorm && k == 0) invNorm[0] = s > 0.0 ? (float)(1.0 / sqrt(s)) : 0.f;
+            for (int q = 0; q < 8; ++q) v[q] = V[(k + q) * ldv + i];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s -= hs[k + q] * v[q];
+        }
+        for (; k < nv; ++k) s -= hs[k] * V[k * ldv + i];
+        w[i] = s;
+        nrm = fmaf(s, s, nrm);
+    }
+    nrm = warp_sum(nrm);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nrm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+#pragma unroll
+        for (int q = 0; q < kFB / 32; ++q) t += red[q];
+        partN[blockIdx.x] = (double)t;
     }
 }
 
-// w -= sum_k h[k] V[k]
-__global__ void multiaxpy_kernel(int64_t n, int nv, const float* __restrict__ V, int64_t ldv,
-                                 const double* __restrict__ h, float* __restrict__ w) {
-    __shared__ float hs[kMaxBasis];
-    for (int k = threadIdx.x; k < nv; k += blockDim.x) hs[k] = (float)h[k];
-    __syncthreads();
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float s = w[i];
-    for (int k = 0; k < nv; ++k) s -= hs[k] * V[k * ldv + i];
-    w[i] = s;
+// hAcc = hG + hTmp when the DGKS test on hG fired, else hG (k < nv)
+__global__ void cgs_accumulate_kernel(int nv, const double* __restrict__ hG, const double* __restrict__ hTmp,
+                                      double* __restrict__ hAcc, double eta2) {
+    const bool re = dgks_reorth(hG, nv, eta2);
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) hAcc[k] = re ? hG[k] + hTmp[k] : hG[k];
 }
 
-// v = w * invNorm
-__global__ void scale_kernel(int64_t n, const float* __restrict__ w, const float* __restrict__ invNorm,
-                             float* __restrict__ v) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    v[i] = w[i] * invNorm[0];
+// Normalisation of the new basis vector: every CTA sums the |w|^2 parts np[0..nParts) in the
+// same order, w *= 1/|w|, copy to w2 (the preconditioner's input buffer).  CTA 0 publishes |w|^2
+// and the column's coefficients hAcc[0..nv) to host-mapped memory: hostOut[0..nv) = hAcc,
+// hostOut[slotNorm] = |w|^2, hostOut[slotNorm - 1] = 1 when the column was re-orthogonalised
+// (gate, eta2: the DGKS test of cgs_axpy_kernel).
+__global__ void __launch_bounds__(kFB) normalize_kernel(int64_t n, float* __restrict__ w, float* __restrict__ w2,
+                                                         const double* __restrict__ np, int nParts,
+                                                         const double* __restrict__ hAcc, int nv,
+                                                         volatile double* hostOut, int slotNorm,
+                                                         const double* __restrict__ gate, double eta2) {
+    __shared__ double red[kFB / 32];
+    double t = 0.0;
+    for (int c = threadIdx.x; c < nParts; c += kFB) t += np[c];
+    t = cta_sum_fixed(t, red);
+    const float inv = t > 0.0 ? (float)(1.0 / sqrt(t)) : 0.f;
+    if (blockIdx.x == 0 && hostOut) {
+        if (threadIdx.x == 0) {
+            hostOut[slotNorm] = t;
+            if (gate) hostOut[slotNorm - 1] = dgks_reorth(gate, nv, eta2) ? 1.0 : 0.0;
+        }
+        if (hAcc)
+            for (int k = threadIdx.x; k < nv; k += kFB) hostOut[k] = hAcc[k];
+    }
+    for (int64_t i = (int64_t)blockIdx.x * kFB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kFB) {
+        const float v = w[i] * inv;
+        w[i] = v;
+        if (w2) w2[i] = v;
+    }
 }
 
 // x += sum_k y[k] Z[k]   (y in FP64)
@@ -156,29 +267,60 @@ int ef_fgmres_max_basis() { return kMaxBasis; }
 
 ef_status ef_launch_spmv_f32(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals, const float* x,
                              const uint8_t* mask, float* y, cudaStream_t s) {
-    spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y);
+    spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y,
+                                                                           nullptr);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
-// h[0..nv) = V^T w (deterministic); part: [nPart][kMaxBasis] doubles
-ef_status ef_launch_multidot(int64_t n, int nv, const float* V, int64_t ldv, const float* w, double* part, int nPart,
-                             double* h, double* hAcc, float* invNorm, cudaStream_t s) {
-    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, w, part);
-    multidot_final_kernel<<<(nv + 7) / 8, 256, 0, ef::counted(s)>>>(nPart, nv, part, h, hAcc, invNorm);
+// y = A x and xcopy = x (the FGMRES product that also stores the preconditioned vector)
+ef_status ef_launch_spmv_f32_copy(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
+                                  const float* x, const uint8_t* mask, float* y, float* xcopy, cudaStream_t s) {
+    spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y,
+                                                                           xcopy);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
-ef_status ef_launch_multiaxpy(int64_t n, int nv, const float* V, int64_t ldv, const double* h, float* w,
-                              cudaStream_t s) {
-    multiaxpy_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, nv, V, ldv, h, w);
+// One Gram-Schmidt step of column j (nv = j + 1 basis vectors V[0..nv), the new vector w =
+// V[nv] in place), classical with DGKS-selective re-orthogonalisation:
+//   hG = [V^T w, |w|^2] (one pass, nv + 1 products), w -= V hG (+ |w|^2 parts),
+//   when the DGKS test on hG fires: hTmp = V^T w, w -= V hTmp (+ |w|^2 parts),
+//   hAcc = hG (+ hTmp), w /= |w|, w2 = w, hAcc and |w|^2 to hostOut.
+// With eta2 > 0 the re-orthogonalisation kernels are always launched (a fixed launch sequence)
+// and return at once when the test does not fire; eta2 = 0 leaves them out.  part:
+// [kMaxBasis][nPart], partN: [nPart], hG, hTmp, hAcc: [kMaxBasis].
+ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double* part, double* partN, int nPart,
+                               double* hG, double* hTmp, double* hAcc, double eta2, float* w2, double* hostOut,
+                               int slotNorm, cudaStream_t s) {
+    if (nv + 1 > kMaxBasis) {
+        ef_set_error("FGMRES: basis larger than the compiled maximum");
+        return EF_ERR_ARG;
+    }
+    float* w = V + (int64_t)nv * ldv;
+    const bool re = eta2 > 0.0;
+    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv + 1, V, ldv, w, part, nullptr, 0, 0.0);
+    multidot_final_kernel<<<nv + 1, kFB, 0, ef::counted(s)>>>(nPart, nv + 1, part, hG, nullptr, 0, 0.0);
+    cgs_axpy_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, hG, w, partN, nullptr, 0.0);
+    if (re) {
+        multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, w, part, hG, nv, eta2);
+        multidot_final_kernel<<<nv, kFB, 0, ef::counted(s)>>>(nPart, nv, part, hTmp, hG, nv, eta2);
+        cgs_axpy_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, hTmp, w, partN, hG, eta2);
+        cgs_accumulate_kernel<<<1, kMaxBasis, 0, ef::counted(s)>>>(nv, hG, hTmp, hAcc, eta2);
+    }
+    // every normalisation CTA sums all nPart parts: a quarter of the CTAs
+    normalize_kernel<<<std::max(1, nPart / 4), kFB, 0, ef::counted(s)>>>(
+        n, w, w2, partN, nPart, re ? hAcc : hG, nv, hostOut, slotNorm, re ? hG : nullptr, eta2);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
-ef_status ef_launch_scale(int64_t n, const float* w, const float* invNorm, float* v, cudaStream_t s) {
-    scale_kernel<<<nbf(n, 256), 256, 0, ef::counted(s)>>>(n, w, invNorm, v);
+// w /= |w| with |w|^2 from a one-vector multidot (the restart vector); w2 = w; |w|^2 to hostOut
+ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
+                                    int slotNorm, cudaStream_t s) {
+    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, 1, w, n, w, part, nullptr, 0, 0.0);
+    normalize_kernel<<<std::max(1, nPart / 4), kFB, 0, ef::counted(s)>>>(n, w, w2, part, nPart, nullptr, 0, hostOut,
+                                                                         slotNorm, nullptr, 0.0);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

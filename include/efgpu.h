@@ -78,6 +78,9 @@ typedef struct ef_solve_info {
     int kernelLaunches;  /* number of Krylov kernel launches timed (PCG: solves; FGMRES: iterations) */
     double spmvMs;       /* FGMRES: summed duration of its fine-level FP32 SpMV launches (profile = 1) */
     int spmvLaunches;    /* number of those SpMV launches */
+    double precondMs;    /* FGMRES: summed duration of the preconditioner applications (profile = 1) */
+    double orthoMs;      /* FGMRES: summed duration of the Gram-Schmidt steps (profile = 1) */
+    int reorths;         /* FGMRES: columns that the DGKS test re-orthogonalised (profile = 1) */
 } ef_solve_info;
 
 int ef_abi_version(void);

@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol():
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
-    assert lib.ef_abi_version() == 2
+    assert lib.ef_abi_version() == 3
 
 
 def test_argument_validation_without_gpu():

@@ -276,6 +276,39 @@ def test_fgmres_multigrid_solves_to_tolerance_with_fewer_iterations(gpu_lib):
     assert 3 * itf <= ip, (itf, ip)
 
 
+def test_fgmres_cluster_coarse_cycle_and_reorthogonalisation(gpu_lib, monkeypatch):
+    """The cycle below the first coarse level as one cluster launch gives bit-identical FGMRES
+    results to the launch-per-phase cycle (same operations in the same order); classical
+    Gram-Schmidt with DGKS re-orthogonalisation reaches the same 1e-8 solution."""
+    rng = np.random.default_rng(5)
+    out = {}
+    for key, env in (("phases", {"EF_AMG_CLUSTER": "0"}), ("cluster", {"EF_AMG_CLUSTER": "1"}),
+                     ("dgks", {"EF_AMG_CLUSTER": "1", "EF_FGMRES_ETA": "0.7071"})):  # fmt: skip
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
+        if key == "phases":
+            b = rng.normal(size=s.nDof)
+            b[s.dirIdxHost] = 1e-3 * rng.normal(size=s.dirIdxHost.size)
+        R = torch.as_tensor(b, device="cuda")
+        s.linsolver.method = "fgmres"
+        s.linsolver.rtol = 1e-8
+        s.linsolver.profile = True
+        l0 = s.lib.ef_kernel_launches()
+        x = s.linearSolve(R).cpu().numpy()
+        per_it = (s.lib.ef_kernel_launches() - l0) / s.lastSolveInfo.iterations
+        assert s.lastSolveInfo.relResidual <= 1e-8
+        out[key] = (x, s.lastSolveInfo.iterations, s.lastSolveInfo.reorths, per_it)
+        monkeypatch.delenv("EF_FGMRES_ETA", raising=False)
+    xp, ip, rp, lp = out["phases"]
+    xc, ic, rc, lc = out["cluster"]
+    xd, idg, rd, _ = out["dgks"]
+    assert lc < lp, (lc, lp)  # the cluster launch replaces the per-phase kernels
+    assert ic == ip and np.array_equal(xc, xp)
+    assert rp == 0 and rc == 0 and rd > 0
+    assert np.max(np.abs(xd - xp)) <= 1e-6 * np.max(np.abs(xp))
+
+
 def test_nist_gpu_fgmres_matches_reference_iteration_counts(gpu_lib):
     from edelweissfe_gb300.solver import LinSolverOptions, Step
 
