@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
+    ap.add_argument("--restart", type=int, default=64, help="FGMRES restart length")
+    ap.add_argument("--inner-rtol", type=float, default=1e-5, help="relative tolerance of one inner (FP32) solve")
     ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")
     ap.add_argument("--workload", default="box", choices=["box", "cubes", "tied"],
                     help="box: the 160k-element J2 box (default); cubes: 1024 independent J2 cubes in one batch; "
@@ -182,7 +184,7 @@ def run_ours(a):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     t0 = time.time()
-    s = build_solver(a, LinSolverOptions(method="fgmres", rtol=1e-8))
+    s = build_solver(a, LinSolverOptions(method="fgmres", rtol=1e-8, restart=a.restart, innerRtol=a.inner_rtol))
     setup_s = time.time() - t0
     info = s.info
     lib = s.lib
@@ -278,7 +280,7 @@ def run_ours(a):
             x = orig(R)
             i = s.lastSolveInfo
             infos.append((i.kernelMs, i.iterations, i.kernelLaunches, i.spmvMs, i.spmvLaunches, i.precondMs,
-                          i.orthoMs, i.reorths))
+                          i.orthoMs, i.reorths, i.refinements, 1))
             return x
 
         s.linsolver.profile = True
@@ -288,9 +290,9 @@ def run_ours(a):
         finally:
             s.linearSolve = orig
             s.linsolver.profile = False
-        return [sum(x[i] for x in infos) for i in range(8)]
+        return [sum(x[i] for x in infos) for i in range(10)]
 
-    fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth = profiled_step()
+    fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth, n_refine, n_solves = profiled_step()
 
     # comparison arm: block-Jacobi PCG on the same load step
     s.linsolver.method = "pcg"
@@ -394,7 +396,8 @@ def run_ours(a):
                            "precond_ms_per_iteration": pre_ms / fg_it if fg_it else None,
                            "spmv_ms_per_iteration": sp_ms / fg_it if fg_it else None,
                            "ortho_ms_per_iteration": orth_ms / fg_it if fg_it else None,
-                           "reorthogonalised_columns": int(n_reorth)},
+                           "reorthogonalised_columns": int(n_reorth), "solves": int(n_solves),
+                           "refinement_sweeps": int(n_refine), "restart": a.restart, "inner_rtol": a.inner_rtol},
         "dof_iterations_per_s": info.nDof * fg_it / (fg_kms * 1e-3) if fg_kms > 0 else None,
         "setup_s": setup_s,
         "history_s": history_s,

@@ -438,6 +438,8 @@ struct ef_ctx {
     int amgSweeps = 2;
     float amgAlpha = 1.5f;
     int amgCycle = 2;  // 1: V-cycle, 2: W-cycle below the finest level
+    int amgPre = 2, amgPost = 2;  // block-Jacobi sweeps before / after the coarse correction
+    int amgWLevels = 1;           // coarse levels 1..amgWLevels repeat their coarse correction
     // the whole preconditioner application captured once as a CUDA graph (fixed in/out buffers)
     float *vcIn = nullptr, *vcOut = nullptr;
     cudaStream_t capStream = nullptr;
@@ -1608,6 +1610,10 @@ static ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
     if (const char* e = getenv("EF_AMG_OMEGA")) c->amgOmega = (float)atof(e);
     if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
+    c->amgPre = c->amgPost = c->amgSweeps;
+    if (const char* e = getenv("EF_AMG_PRE")) c->amgPre = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_POST")) c->amgPost = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_WLEVELS")) c->amgWLevels = std::max(0, atoi(e));
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
@@ -1787,7 +1793,7 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         ops.push_back(o);
     };
     float* x2 = L.x2;
-    float* cur = ((2 * c->amgSweeps - 1) & 1) ? x2 : x;
+    float* cur = ((c->amgPre + c->amgPost) & 1) ? x : x2;
     {
         ef::CoarseOp o = op(ef::COP_BJ, L.nN);
         o.f1 = L.binv;
@@ -1797,12 +1803,12 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         o.omega = omega;
         ops.push_back(o);
     }
-    for (int k = 1; k < c->amgSweeps; ++k) {
+    for (int k = 1; k < c->amgPre; ++k) {
         float* nxt = cur == x ? x2 : x;
         sweep(cur, nxt);
         cur = nxt;
     }
-    const int reps = c->amgCycle > 1 ? c->amgCycle : 1;
+    const int reps = (c->amgCycle > 1 && l <= c->amgWLevels) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
         ef::CoarseOp o = op(ef::COP_RESID, L.nN);
         o.p0 = L.rowPtr;
@@ -1831,7 +1837,7 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         pr.omega = c->amgAlpha;
         ops.push_back(pr);
     }
-    for (int k = 0; k < c->amgSweeps; ++k) {
+    for (int k = 0; k < c->amgPost; ++k) {
         float* nxt = cur == x ? x2 : x;
         sweep(cur, nxt);
         cur = nxt;
@@ -1859,8 +1865,8 @@ static ef_status amg_prepare_cluster(ef_ctx* c) {
     // level lc's iterate at its coarse correction: amg_vcycle's buffer alternation of the
     // pre-smoothing replayed (level lc's output vector is L.x, its second vector L.x2)
     float* x = L.x;
-    float* cur = ((2 * c->amgSweeps - 1) & 1) ? L.x2 : x;
-    for (int k = 1; k < c->amgSweeps; ++k) cur = cur == x ? L.x2 : x;
+    float* cur = ((c->amgPre + c->amgPost) & 1) ? x : L.x2;
+    for (int k = 1; k < c->amgPre; ++k) cur = cur == x ? L.x2 : x;
     std::vector<ef::CoarseOp> ops;
     ef::CoarseOp rs{};
     rs.type = ef::COP_RESTRICT;
@@ -2116,25 +2122,24 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
                                                  binv, omega);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega);
     };
-    // The sweeps alternate between x and a second vector; 2 * sweeps - 1 of them follow the first
-    // (from zero), so the first goes to the second vector when that count is odd and the last
-    // one lands in x.
+    // The sweeps (the first from zero) alternate between x and a second vector; the first goes
+    // to the second vector when their total count is even, so that the last one lands in x.
     float* x2 = fine ? c->fineX : c->amg[l - 1].x2;
     float* cur = x;
-    if (!c->amgCheb) cur = ((2 * c->amgSweeps - 1) & 1) ? x2 : x;
+    if (!c->amgCheb) cur = ((c->amgPre + c->amgPost) & 1) ? x : x2;
     // pre-smoothing from zero
     if (c->amgCheb) {
         EF_CHECK(chebyshev(true));
     } else {
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, cur, 0, s));
-        for (int k = 1; k < c->amgSweeps; ++k) {
+        for (int k = 1; k < c->amgPre; ++k) {
             float* nxt = cur == x ? x2 : x;
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;
         }
     }
     // coarse correction (repeated for a W-cycle below the finest level)
-    const int reps = (l > 0 && c->amgCycle > 1) ? c->amgCycle : 1;
+    const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
         if (!c->amgCheb) {
             EF_CHECK(fine && c->dBsrValsH
@@ -2160,7 +2165,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     if (c->amgCheb) {
         EF_CHECK(chebyshev(false));
     } else {
-        for (int k = 0; k < c->amgSweeps; ++k) {
+        for (int k = 0; k < c->amgPost; ++k) {
             float* nxt = cur == x ? x2 : x;
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;

@@ -36,11 +36,16 @@ __device__ __forceinline__ bool grid_sync(BarrierState*, unsigned int, int* flag
     return !(*((volatile int*)flags) & EF_FLAG_BARRIER);
 }
 
-// block reduction of NV doubles in a fixed order (warp shuffles, then warp 0); result in all threads
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+// FP64 is a narrow pipe on this GPU (2 lanes per SM and cycle): per-thread partial sums and the
+// warp trees run in the vector type AT (FP32 for the FP32 solve), the CTA's warp sums and the
+// sum over CTAs in FP64, all in a fixed order.
+
+// CTA sum of NV values per thread, returned in FP64 to every thread
+template <typename AT, int NV>
+__device__ __forceinline__ void block_sum(AT (&v)[NV], double (&out)[NV]) {
     constexpr int NW = kKB / 32;
-    __shared__ double red[NV][NW];
+    __shared__ AT red[NV][NW];
+    __shared__ double res[NV];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
@@ -52,31 +57,37 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
         for (int j = 0; j < NV; ++j) red[j][w] = v[j];
     }
     __syncthreads();
-    if (w == 0) {
+    if (threadIdx.x < NV) {
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < NW; ++q) t += (double)red[threadIdx.x][q];
+        res[threadIdx.x] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) out[j] = res[j];
+    __syncthreads();
+}
+
+// sum of the per-CTA partials slot[c*4 + j], j < NV, identical in every CTA (one warp sums,
+// lane-strided then a fixed shuffle tree)
+template <int NV>
+__device__ __forceinline__ void reduce_partials(const double* part, int nCTA, double (&v)[NV]) {
+    __shared__ double res[NV];
+    if (threadIdx.x < 32) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
-            double t = lane < NW ? red[j][lane] : 0.0;
+            double a = 0.0;
+            for (int c = threadIdx.x; c < nCTA; c += 32) a += __ldcg(part + c * 4 + j);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0) red[j][0] = t;
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (threadIdx.x == 0) res[j] = a;
         }
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = red[j][0];
+    for (int j = 0; j < NV; ++j) v[j] = res[j];
     __syncthreads();
-}
-
-// sum of the per-CTA partials slot[c*4 + j], j < NV, identical in every CTA
-template <int NV>
-__device__ __forceinline__ void reduce_partials(const double* part, int nCTA, double (&v)[NV]) {
-#pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = 0.0;
-    for (int c = threadIdx.x; c < nCTA; c += kKB) {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) v[j] += __ldcg(part + c * 4 + j);
-    }
-    block_sum<NV>(v);
 }
 
 // y_row = A_row x for the block row `m`, lanes l = 0..7 of a row group; returns partial sums
@@ -184,7 +195,7 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
     const int nGroups = gridDim.x * groupsPerCTA;
 
     // init: x = 0, r = b, z = M^-1 r
-    double loc[2] = {0.0, 0.0};
+    VT loc[2] = {(VT)0, (VT)0};
     for (int m = tidg; m < nNodes; m += nThr) {
         const int d = 3 * m;
         VT rv[3];
@@ -200,14 +211,17 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
             VT zi = B[3 * i] * rv[0] + B[3 * i + 1] * rv[1] + B[3 * i + 2] * rv[2];
             if (mask[d + i]) zi = (VT)0;
             z[d + i] = zi;
-            loc[0] += (double)rv[i] * (double)zi;
-            loc[1] += (double)rv[i] * (double)rv[i];
+            loc[0] += rv[i] * zi;
+            loc[1] += rv[i] * rv[i];
         }
     }
-    block_sum<2>(loc);
-    if (threadIdx.x == 0) {
-        partB[blockIdx.x * 4 + 0] = loc[0];
-        partB[blockIdx.x * 4 + 1] = loc[1];
+    {
+        double cs[2];
+        block_sum<VT, 2>(loc, cs);
+        if (threadIdx.x == 0) {
+            partB[blockIdx.x * 4 + 0] = cs[0];
+            partB[blockIdx.x * 4 + 1] = cs[1];
+        }
     }
     if (!grid_sync(bar, nCTA, flags)) return;
     double tot[2];
@@ -225,7 +239,7 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
             // q = A p_k with p_k = z + beta p_{k-1} formed on the fly; p_k stored for own rows.
             // Loads are batched (up to kBatch blocks per lane issued before any use) so that a
             // row costs three dependent memory latencies instead of one per block.
-            double pq = 0.0;
+            VT pq = (VT)0;
             {
                 const int iters = (nNodes + nGroups - 1) / nGroups;
                 int g = blockIdx.x * groupsPerCTA + threadIdx.x / kRowLanes;
@@ -279,13 +293,14 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
                         if (mask[d]) yy = (VT)0;
                         q[d] = yy;
                         pCur[d] = pd;
-                        pq += (double)pd * (double)yy;
+                        pq += pd * yy;
                     }
                 }
             }
-            double v1[1] = {pq};
-            block_sum<1>(v1);
-            if (threadIdx.x == 0) partA[blockIdx.x * 4] = v1[0];
+            VT v1[1] = {pq};
+            double c1[1];
+            block_sum<VT, 1>(v1, c1);
+            if (threadIdx.x == 0) partA[blockIdx.x * 4] = c1[0];
             if (!grid_sync(bar, nCTA, flags)) return;
             double t1[1];
             reduce_partials<1>(partA, nCTA, t1);
@@ -298,7 +313,7 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
                 break;
             }
             const VT alpha = (VT)(rz / t1[0]);
-            double l2[2] = {0.0, 0.0};
+            VT l2[2] = {(VT)0, (VT)0};
             for (int m = tidg; m < nNodes; m += nThr) {
                 const int d = 3 * m;
                 VT rv[3];
@@ -314,14 +329,17 @@ __global__ void __launch_bounds__(kKB) pcg_persistent_kernel(
                     VT zi = B[3 * i] * rv[0] + B[3 * i + 1] * rv[1] + B[3 * i + 2] * rv[2];
                     if (mask[d + i]) zi = (VT)0;
                     z[d + i] = zi;
-                    l2[0] += (double)rv[i] * (double)zi;
-                    l2[1] += (double)rv[i] * (double)rv[i];
+                    l2[0] += rv[i] * zi;
+                    l2[1] += rv[i] * rv[i];
                 }
             }
-            block_sum<2>(l2);
-            if (threadIdx.x == 0) {
-                partB[blockIdx.x * 4 + 0] = l2[0];
-                partB[blockIdx.x * 4 + 1] = l2[1];
+            {
+                double c2[2];
+                block_sum<VT, 2>(l2, c2);
+                if (threadIdx.x == 0) {
+                    partB[blockIdx.x * 4 + 0] = c2[0];
+                    partB[blockIdx.x * 4 + 1] = c2[1];
+                }
             }
             if (!grid_sync(bar, nCTA, flags)) return;
             reduce_partials<2>(partB, nCTA, tot);
@@ -356,8 +374,9 @@ __global__ void __launch_bounds__(kKB) dot2_partial_kernel(int64_t n, const doub
     double v[1] = {0.0};
     for (int64_t i = (int64_t)blockIdx.x * kKB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kKB)
         v[0] += a[i] * b[i];
-    block_sum<1>(v);
-    if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+    double o[1];
+    block_sum<double, 1>(v, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = o[0];
 }
 
 __global__ void sum_final_kernel(int n, const double* __restrict__ part, double* __restrict__ out) {
