@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
+    ap.add_argument("--no-learned-jacobi", action="store_true",
+                    help="skip the learned correction's measurement over the block-Jacobi base")
+    ap.add_argument("--learned-jacobi-rtol", type=float, default=1e-6,
+                    help="relative residual of the solves of that measurement")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--restart", type=int, default=64, help="FGMRES restart length")
     ap.add_argument("--inner-rtol", type=float, default=1e-5, help="relative tolerance of one inner (FP32) solve")
@@ -164,6 +168,56 @@ def assembly_bytes(info, nEl, fp32=True):
     cond = nEl * 24 * 8 + nEl * 8 * 8 + info.nDof * 8 * 2  # Pe read, map, P and F write
     scatter = nEl * 36 * 9 * s + nEl * 64 * 8 + info.nBlocks * (9 * s + 8)  # Ke read, map, BSR write
     return elem, cond, scatter
+
+
+def learned_over_jacobi(s, rtol, epochs=60, lr=1e-3):
+    """FGMRES + block Jacobi with and without the network trained on that solver's own pairs,
+    each solve to the relative residual rtol."""
+    import torch
+
+    s.enableLearnedPreconditioner(False)
+    s.setFgmresPreconditioner("jacobi")
+    saved = s.learnedParameters()
+    saved_rtol = s.linsolver.rtol
+    s.linsolver.rtol = rtol
+
+    def rhs(seed):
+        b = np.random.default_rng(seed).normal(size=s.nDof)
+        b[s.dirIdxHost] = 0.0
+        return torch.as_tensor(b, device="cuda")
+
+    def solve(seed):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.linearSolve(rhs(seed))
+        torch.cuda.synchronize()
+        return s.lastSolveInfo.iterations, time.perf_counter() - t
+
+    try:
+        off_k, off_s = solve(100)
+        s.clearTrainingPairs()
+        s.initLearnedPreconditioner(seed=1, maxSamples=32)
+        s.collectTrainingPairs(every=max(5, off_k // 10), maxPerSolve=8, kind="iterates")
+        for k in range(4):
+            s.linearSolve(rhs(k))
+        s.collectTrainingPairs(0, 0)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        lf, ll = s.trainLearnedPreconditioner(epochs=epochs, lr=lr, norm="energy")
+        torch.cuda.synchronize()
+        train_s = time.time() - t0
+        s.enableLearnedPreconditioner(True)
+        on_k, on_s = solve(100)
+        return {"base": "block Jacobi", "rtol": rtol, "pairs": s.numTrainingPairs(), "epochs": epochs, "loss_first": lf,
+                "loss_last": ll, "train_s": train_s, "off_krylov": off_k, "on_krylov": on_k, "off_s": off_s,
+                "on_s": on_s, "krylov_ratio": off_k / on_k if on_k else None}  # fmt: skip
+    except Exception as ex:  # a solve that stalls is reported, not fatal to the bench
+        return {"base": "block Jacobi", "rtol": rtol, "error": f"{type(ex).__name__}: {ex}"}
+    finally:
+        s.linsolver.rtol = saved_rtol
+        s.enableLearnedPreconditioner(False)
+        s.setFgmresPreconditioner("multigrid")
+        s.setLearnedParameters(*saved)
 
 
 def run_ours(a):
@@ -348,6 +402,12 @@ def run_ours(a):
     f1.record(stream)
     torch.cuda.synchronize()
     e2e_s = f0.elapsed_time(f1) / 1e3 / e2e_steps
+
+    # the learned correction over the block-Jacobi base on this model's last Newton system: pairs
+    # from the plain FGMRES + block-Jacobi solves of random right-hand sides, GPU training, then
+    # one solve of a new right-hand side with and without the trained network
+    if learned and not a.no_learned_jacobi:
+        learned_info["over_jacobi"] = learned_over_jacobi(s, a.learned_jacobi_rtol)
 
     peaks, peak_kind = measured_peaks()
     sb = spmv_bytes(info)

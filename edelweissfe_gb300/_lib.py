@@ -32,6 +32,9 @@ EF_OPT_NO_SCALAR_CSR = 2
 EF_SOLVE_PCG = 0
 EF_SOLVE_FGMRES = 1
 
+EF_FGMRES_PC_MULTIGRID = 0
+EF_FGMRES_PC_JACOBI = 1
+
 
 class EfInfo(ctypes.Structure):
     _fields_ = [
@@ -102,6 +105,7 @@ SIGNATURES = {
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
     "ef_kernel_launches": (c_i64, []),
+    "ef_fgmres_set_preconditioner": (c_int, [c_vp, c_int]),
     "ef_set_group_props": (c_int, [c_vp, c_int, c_vp, c_int, c_int, c_vp]),
     "ef_set_ties": (c_int, [c_vp, c_vp, c_vp, c_vp, c_i64]),
     "ef_mpnn_dense_eval": (c_int, [c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -14,6 +14,8 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "ef_common.cuh"
 
 namespace ef {
@@ -642,6 +644,125 @@ __global__ void __launch_bounds__(256) level_residual3_bf16_kernel(int nN, const
     }
 }
 
+// Staged form of level_residual3_bf16_kernel for the fine level.  Persistent CTAs walk chunks of
+// kStageRows block rows; the blocks of the next chunk (16-byte words, the ninth values and the
+// column indices, contiguous in memory) are copied into shared memory with cp.async while the
+// current chunk is computed, so that every CTA keeps a whole chunk of loads in flight.  Each row
+// is then computed by 8 lanes from shared memory, as in the unstaged kernel (same order of
+// operations, same results).  Stage layout (cap = the largest chunk's block count): cap uint4
+// words | cap + 16 BF16 values | cap + 8 column indices; the index and BF16 ranges start on
+// 16-byte boundaries below the chunk's first block and end on 16-byte boundaries above its last.
+constexpr int kStageRows = 32;
+constexpr int kStageThreads = kStageRows * 8;
+
+__host__ __device__ inline size_t stage_v1_bytes(int cap) { return (((size_t)cap + 16) * 2 + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t stage_bytes_bf16(int cap) {
+    return (size_t)cap * 16 + stage_v1_bytes(cap) + ((size_t)cap + 8) * 4;
+}
+
+__device__ __forceinline__ void stage_chunk_bf16(int b0, int b1, const uint4* __restrict__ v8,
+                                                 const __nv_bfloat16* __restrict__ v1,
+                                                 const int32_t* __restrict__ colIdx, char* stage, int cap) {
+    uint4* s8 = reinterpret_cast<uint4*>(stage);
+    __nv_bfloat16* s1 = reinterpret_cast<__nv_bfloat16*>(stage + (size_t)cap * 16);
+    int32_t* sc = reinterpret_cast<int32_t*>(stage + (size_t)cap * 16 + stage_v1_bytes(cap));
+    const int n8 = b1 - b0;
+    for (int i = threadIdx.x; i < n8; i += kStageThreads) cp_async16(s8 + i, v8 + b0 + i);
+    const int v1s = b0 & ~7;
+    const int n1 = (b1 - v1s + 7) >> 3;  // 16-byte pieces of 8 BF16 values
+    for (int i = threadIdx.x; i < n1; i += kStageThreads) cp_async16(s1 + 8 * i, v1 + v1s + 8 * i);
+    const int cs = b0 & ~3;
+    const int nc = (b1 - cs + 3) >> 2;  // 16-byte pieces of 4 indices
+    for (int i = threadIdx.x; i < nc; i += kStageThreads) cp_async16(sc + 4 * i, colIdx + cs + 4 * i);
+}
+
+__global__ void __launch_bounds__(kStageThreads) level_residual3_bf16_staged_kernel(
+    int nN, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx, const uint4* __restrict__ v8,
+    const __nv_bfloat16* __restrict__ v1, const float* __restrict__ x, const float* __restrict__ r,
+    const uint8_t* __restrict__ mask, float* __restrict__ t, const float* __restrict__ binv, float omega, int cap) {
+    extern __shared__ __align__(16) char smem[];
+    const size_t sb = (stage_bytes_bf16(cap) + 15) & ~(size_t)15;
+    const int nChunks = (nN + kStageRows - 1) / kStageRows;
+    const int lane = threadIdx.x & 7;
+    const int rowInChunk = threadIdx.x >> 3;
+    int ch = blockIdx.x;
+    if (ch >= nChunks) return;
+    int b0 = rowPtr[ch * kStageRows];
+    int b1 = rowPtr[min((ch + 1) * kStageRows, nN)];
+    stage_chunk_bf16(b0, b1, v8, v1, colIdx, smem, cap);
+    cp_async_commit();
+    int st = 0;
+    for (; ch < nChunks; ch += gridDim.x, st ^= 1) {
+        const int nx = ch + gridDim.x;
+        int nb0 = 0, nb1 = 0;
+        if (nx < nChunks) {
+            nb0 = rowPtr[nx * kStageRows];
+            nb1 = rowPtr[min((nx + 1) * kStageRows, nN)];
+            stage_chunk_bf16(nb0, nb1, v8, v1, colIdx, smem + (st ^ 1) * sb, cap);
+        }
+        cp_async_commit();  // (an empty group when there is no next chunk)
+        // this row's own entries and bounds, fetched while the stage completes
+        const int m0 = ch * kStageRows + rowInChunk;
+        const int m = m0 < nN ? m0 : nN - 1;
+        const int s = rowPtr[m], e = rowPtr[m + 1];
+        cp_async_wait<1>();
+        __syncthreads();
+        const char* sg = smem + st * sb;
+        const uint4* s8 = reinterpret_cast<const uint4*>(sg);
+        const __nv_bfloat16* s1 = reinterpret_cast<const __nv_bfloat16*>(sg + (size_t)cap * 16);
+        const int32_t* sc = reinterpret_cast<const int32_t*>(sg + (size_t)cap * 16 + stage_v1_bytes(cap));
+        const int o8 = b0, o1 = b0 & ~7, oc = b0 & ~3;
+        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        for (int base = s; base < e; base += 32) {
+            int cc[4];
+            uint4 q[4];
+            float w8[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = base + lane + 8 * j;
+                if (k < e) {
+                    cc[j] = 3 * sc[k - oc];
+                    q[j] = s8[k - o8];
+                    w8[j] = __bfloat162float(s1[k - o1]);
+                } else {
+                    cc[j] = -1;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cc[j] >= 0) {
+                    const float x0 = x[cc[j]], x1 = x[cc[j] + 1], x2 = x[cc[j] + 2];
+                    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q[j]);
+                    const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
+                    const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
+                    y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
+                    y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
+                    y2 += a67.x * x0 + a67.y * x1 + w8[j] * x2;
+                }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+            y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+            y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+        }
+        if (m0 < nN && lane < 3) {
+            if (binv) {
+                const float yv[3] = {y0, y1, y2};
+                smooth_row<3>(m, lane, yv, x, r, mask, binv, omega, t);
+            } else {
+                const int d = 3 * m + lane;
+                const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
+                t[d] = (mask && mask[d]) ? 0.f : r[d] - yy;
+            }
+        }
+        __syncthreads();  // the stage is free for the chunk after next
+        b0 = nb0;
+        b1 = nb1;
+    }
+    cp_async_wait<0>();
+}
+
 // split BF16 copy of 3x3 blocks for level_residual3_bf16_kernel
 __global__ void to_bf16_split_kernel(int64_t nb, const float* __restrict__ src, uint4* __restrict__ v8,
                                      __nv_bfloat16* __restrict__ v1) {
@@ -774,6 +895,43 @@ ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* 
     const __nv_bfloat16* v1 = (const __nv_bfloat16*)(v8 + nBlocks);
     level_residual3_bf16_kernel<<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, v8, v1, x,
                                                                                      r, mask, t, binv, omega);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// largest block count of a chunk of kStageRows rows (host)
+int ef_stage_cap(int nN, const int32_t* rowPtrHost) {
+    int cap = 0;
+    for (int m0 = 0; m0 < nN; m0 += kStageRows)
+        cap = std::max(cap, rowPtrHost[std::min(m0 + kStageRows, nN)] - rowPtrHost[m0]);
+    return cap;
+}
+
+// staged fine-level BF16 residual / sweep; nSM CTAs x the resident count for the stage size
+ef_status ef_launch_level_residual_bf16_staged(int nSM, int cap, int nN, int64_t nBlocks, const int32_t* rowPtr,
+                                               const int32_t* colIdx, const void* vals, const float* x, const float* r,
+                                               const uint8_t* mask, float* t, cudaStream_t s, const float* binv,
+                                               float omega) {
+    const uint4* v8 = (const uint4*)vals;
+    const __nv_bfloat16* v1 = (const __nv_bfloat16*)(v8 + nBlocks);
+    const size_t smem = 2 * ((stage_bytes_bf16(cap) + 15) & ~(size_t)15);
+    static size_t attrSet = 0;
+    if (smem > 48 * 1024 && smem > attrSet) {
+        EF_CUDA(cudaFuncSetAttribute(level_residual3_bf16_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        attrSet = smem;
+    }
+    int perSM = 0;
+    EF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, level_residual3_bf16_staged_kernel, kStageThreads,
+                                                          smem));
+    if (perSM < 1) {
+        ef_set_error("staged BF16 residual: chunk does not fit in shared memory");
+        return EF_ERR_ARG;
+    }
+    const int nChunks = (nN + kStageRows - 1) / kStageRows;
+    const int grid = std::max(1, std::min(nChunks, perSM * nSM));
+    level_residual3_bf16_staged_kernel<<<grid, kStageThreads, smem, ef::counted(s)>>>(
+        nN, rowPtr, colIdx, v8, v1, x, r, mask, t, binv, omega, cap);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

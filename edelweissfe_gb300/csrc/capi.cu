@@ -72,6 +72,11 @@ ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* 
                                         const void* vals, const float* x, const float* r, const uint8_t* mask,
                                         float* t, cudaStream_t s, const float* binv = nullptr, float omega = 0.f);
 ef_status ef_launch_to_bf16_split(int64_t nBlocks, const float* src, void* dst, cudaStream_t s);
+int ef_stage_cap(int nN, const int32_t* rowPtrHost);
+ef_status ef_launch_level_residual_bf16_staged(int nSM, int cap, int nN, int64_t nBlocks, const int32_t* rowPtr,
+                                               const int32_t* colIdx, const void* vals, const float* x, const float* r,
+                                               const uint8_t* mask, float* t, cudaStream_t s, const float* binv,
+                                               float omega);
 ef_status ef_launch_coarse_cycle(const ef::CoarseOp* ops, int nOps, cudaStream_t s);
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s);
@@ -124,6 +129,10 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
                                int slotNorm, cudaStream_t s);
 ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
                                     int slotNorm, cudaStream_t s);
+int ef_sp_stage_cap(int nN, const int32_t* rowPtrHost);
+ef_status ef_launch_spmv_f32_staged(int nSM, int cap, int nN, const int32_t* rowPtr, const int32_t* colIdx,
+                                    const float* vals, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                                    cudaStream_t s);
 ef_status ef_launch_combine(int64_t n, int nv, const float* Z, int64_t ldz, const double* y, float* x, cudaStream_t s);
 ef_status ef_launch_sub(int64_t n, const float* b, const float* y, float* r, cudaStream_t s);
 
@@ -418,6 +427,7 @@ struct ef_ctx {
     int32_t* dRowOfBlock0 = nullptr;     // fine-level block -> block row
     float *fineX = nullptr, *fineT = nullptr;  // level-0 V-cycle work vectors
     bool amgStale = true;                // coarse values need a refresh (new system or mask)
+    bool nnEdgeStale = true;             // the learned correction's edge weights need a refresh
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
     // V-cycle parameters: damping, smoothing sweeps per side, coarse over-correction, cycle type
@@ -428,6 +438,7 @@ struct ef_ctx {
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
+    int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel
     ef::CoarseOp* dCoarseOps = nullptr;     // its phase program (device)
     int nCoarseOps = 0, nCoarseOpsCap = 0;
@@ -499,6 +510,8 @@ struct ef_ctx {
     double* fgH = nullptr;               // device scratch: [hG | hTmp | hAcc | y], 128 each
     double* fgPartN = nullptr;           // per-CTA parts of |w|^2
     int fgNPart = 0;                     // CTAs of the orthogonalisation kernels
+    int spCap = 0;                       // > 0: FGMRES SpMV through shared-memory staging (EF_SPMV_STAGED=1)
+    int fgPc = 0;                        // FGMRES base preconditioner: EF_FGMRES_PC_MULTIGRID / _JACOBI
     double* fgPinDev = nullptr;          // device address of fgPin
     bool vcInStale = true;               // vcIn does not hold the next basis vector
     double fgEta2 = 0.0;                 // DGKS threshold squared (EF_FGMRES_ETA; 0: one pass)
@@ -1064,11 +1077,11 @@ ef_status ef_finalize(ef_ctx* c, int options) {
                 return EF_ERR_ARG;
             }
         c->dRowPtr = dalloc<int32_t>(nNodes + 1, &st);
-        c->dColIdx = dalloc<int32_t>(nBlocks, &st);
+        c->dColIdx = dalloc<int32_t>(nBlocks + 16, &st);  // padding: staged loads round the end up to 16 bytes
         c->dBsrSeg = dalloc<int64_t>(nBlocks + 1, &st);
         c->dBsrSrc = dalloc<int64_t>(nSrc, &st);
         c->dDiagPos = dalloc<int64_t>(nNodes, &st);
-        c->dBsrVals = dalloc<char>((size_t)nBlocks * 9 * ks, &st);
+        c->dBsrVals = dalloc<char>((size_t)nBlocks * 9 * ks + 64, &st);  // + padding for staged loads
         c->dBinv = dalloc<char>((size_t)nNodes * 9 * ks, &st);
         c->dMask = dalloc<uint8_t>(c->nDof, &st);
         if (!c->dRowPtr || !c->dColIdx || !c->dBsrSeg || !c->dBsrSrc || !c->dDiagPos || !c->dBsrVals || !c->dBinv ||
@@ -1475,6 +1488,7 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
     EF_CUDA(cudaMemcpy(c->dMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
     c->hMask = std::move(m);
     c->amgStale = true;
+    c->nnEdgeStale = true;
     c->nnVersion++;
     return EF_OK;
 }
@@ -1486,6 +1500,7 @@ ef_status ef_assemble_bsr(ef_ctx* c, void* stream) {
     EF_CHECK(ef_launch_bj_setup(c->nNodes, c->dDiagPos, c->dNodeDof, c->dMask, c->dBsrVals, c->keFp64, c->dBinv,
                                 c->dFlags, s));
     c->amgStale = true;
+    c->nnEdgeStale = true;
     c->nnVersion++;
     return EF_OK;
 }
@@ -1606,6 +1621,17 @@ static ef_status upload(T** dst, const std::vector<T>& v) {
     return EF_OK;
 }
 
+// vectors of the FGMRES preconditioner (input, output) and the fine-level work vectors (also
+// the FGMRES restart residual), whichever base preconditioner runs
+static ef_status amg_workspace(ef_ctx* c) {
+    ef_status st = EF_OK;
+    if (!c->vcIn) c->vcIn = dalloc<float>(c->nDof, &st);
+    if (!c->vcOut) c->vcOut = dalloc<float>(c->nDof, &st);
+    if (!c->fineX) c->fineX = dalloc<float>(c->nDof, &st);
+    if (!c->fineT) c->fineT = dalloc<float>(c->nDof, &st);
+    return (c->vcIn && c->vcOut && c->fineX && c->fineT) ? EF_OK : st;
+}
+
 static ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
     if (const char* e = getenv("EF_AMG_OMEGA")) c->amgOmega = (float)atof(e);
@@ -1627,12 +1653,14 @@ static ef_status amg_build(ef_ctx* c) {
     for (int m = 0; m < n0; ++m)
         for (int k = c->hRowPtr0[m]; k < c->hRowPtr0[m + 1]; ++k) rob0[k] = m;
     EF_CHECK(upload(&c->dRowOfBlock0, rob0));
-    c->fineX = dalloc<float>(c->nDof, &st);
-    c->fineT = dalloc<float>(c->nDof, &st);
-    if (!c->fineX || !c->fineT) return st;
+    EF_CHECK(amg_workspace(c));
     if (c->amgBf16) {
-        c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9, &st);  // 16-byte words + 1 value per block
+        c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9 + 32, &st);  // 16-byte words + 1 value per block (+ padding)
         if (!c->dBsrValsH) return st;
+        bool staged = false;  // measured slower than the unstaged kernel (EF_AMG_STAGED=1 turns it on)
+        if (const char* e = getenv("EF_AMG_STAGED")) staged = atoi(e) != 0;
+        c->stageCap = staged ? ef_stage_cap(n0, c->hRowPtr0.data()) : 0;
+        if (c->stageCap > 4096) c->stageCap = 0;  // rows too long for a shared-memory stage: unstaged kernel
     }
     const std::vector<int32_t>* pRow = &c->hRowPtr0;
     const std::vector<int32_t>* pCol = &c->hColIdx0;
@@ -1745,9 +1773,7 @@ static ef_status amg_build(ef_ctx* c) {
     const int nc = BCo * c->amg.back().nN;
     c->amgCoarsestInv = dalloc<float>((size_t)nc * nc, &st);
     if (!c->amgCoarsestInv) return st;
-    c->vcIn = dalloc<float>(c->nDof, &st);
-    c->vcOut = dalloc<float>(c->nDof, &st);
-    if (!c->vcIn || !c->vcOut) return st;
+    EF_CHECK(amg_workspace(c));
     c->amgStale = true;
     return EF_OK;
 }
@@ -2034,6 +2060,15 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
 
 // dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses and
 // the coarsest inverse for the current fine system
+// edge weights of the learned correction for the current system
+static ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
+    if (!c->nnInit || !c->nnEdgeStale) return EF_OK;
+    EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
+    EF_CHECK(ef_launch_gather_f32(c->nBlocks, c->nnTpos, c->nnA, c->nnAT, s));
+    c->nnEdgeStale = false;
+    return EF_OK;
+}
+
 static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     if (!c->amgStale) return EF_OK;
     const int BCo = ef_amg_coarse_dofs();
@@ -2060,12 +2095,8 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     if (c->dBsrValsH)
         EF_CHECK(ef_launch_to_bf16_split(c->nBlocks, (const float*)c->dBsrVals, c->dBsrValsH, s));
     EF_CHECK(amg_damping(c, s));
-    if (c->nnInit) {
-        EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
-        EF_CHECK(ef_launch_gather_f32(c->nBlocks, c->nnTpos, c->nnA, c->nnAT, s));
-    }
     c->amgStale = false;
-    return EF_OK;
+    return nn_edge_refresh(c, s);
 }
 
 // x = V-cycle(r) on level l (l = 0: the fine system); one damped block-Jacobi sweep before and
@@ -2088,9 +2119,16 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
     float* t = fine ? c->fineT : c->amg[l - 1].t;
     AmgLevel& Cn = c->amg[l];
+    // fine level from the BF16 copy: staged through shared memory when the chunks fit
+    auto fine_bf16 = [&](const float* xin, float* out, const float* bj, float om) -> ef_status {
+        if (c->stageCap > 0)
+            return ef_launch_level_residual_bf16_staged(c->nSM, c->stageCap, nN, c->nBlocks, rowPtr, colIdx,
+                                                        c->dBsrValsH, xin, r, mask, out, s, bj, om);
+        return ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, xin, r, mask, out, s, bj,
+                                             om);
+    };
     auto residual = [&]() -> ef_status {
-        if (fine && c->dBsrValsH)
-            return ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, x, r, mask, t, s);
+        if (fine && c->dBsrValsH) return fine_bf16(x, t, nullptr, 0.f);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s);
     };
     // Chebyshev smoothing of degree amgSweeps on [lmax / 30, 1.1 lmax] of D^-1 A; from zero the
@@ -2117,9 +2155,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     };
     // one fused damped block-Jacobi sweep xout = xin + omega D^-1 (r - A xin)
     auto sweep = [&](const float* xin, float* xout) -> ef_status {
-        if (fine && c->dBsrValsH)
-            return ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, xin, r, mask, xout, s,
-                                                 binv, omega);
+        if (fine && c->dBsrValsH) return fine_bf16(xin, xout, binv, omega);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega);
     };
     // The sweeps (the first from zero) alternate between x and a second vector; the first goes
@@ -2142,9 +2178,8 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
         if (!c->amgCheb) {
-            EF_CHECK(fine && c->dBsrValsH
-                         ? ef_launch_level_residual_bf16(nN, c->nBlocks, rowPtr, colIdx, c->dBsrValsH, cur, r, mask, t, s)
-                         : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s));
+            EF_CHECK(fine && c->dBsrValsH ? fine_bf16(cur, t, nullptr, 0.f)
+                                          : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s));
         } else {
             EF_CHECK(residual());
         }
@@ -2201,6 +2236,7 @@ static ef_status nn_apply(ef_ctx* c, cudaStream_t s) {
 
 static ef_status nn_capture(ef_ctx* c) {
     if (c->nnGraph) return EF_OK;
+    if (!c->capStream) EF_CUDA(cudaStreamCreateWithFlags(&c->capStream, cudaStreamNonBlocking));
     EF_CUDA(cudaStreamBeginCapture(c->capStream, cudaStreamCaptureModeThreadLocal));
     long long captured = 0;
     t_captureCount = &captured;
@@ -2219,14 +2255,23 @@ static ef_status nn_capture(ef_ctx* c) {
     return EF_OK;
 }
 
-static ef_status fgmres_precond(ef_ctx* c, const float* v, const float** out, cudaStream_t s) {
+// vcOut = M vcIn with the base preconditioner: the multigrid cycle (captured graph) or one
+// block-Jacobi step D^-1 (free DOFs)
+static ef_status apply_base(ef_ctx* c, cudaStream_t s) {
+    if (c->fgPc == EF_FGMRES_PC_JACOBI)
+        return ef_launch_bj_apply(3, (int)c->nNodes, (const float*)c->dBinv, c->dMask, 1.f, c->vcIn, c->vcOut, 0, s);
     EF_CHECK(amg_capture(c));
+    ef::note_launches(c->vcGraphKernels);
+    EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
+    return EF_OK;
+}
+
+static ef_status fgmres_precond(ef_ctx* c, const float* v, const float** out, cudaStream_t s) {
     if (c->vcInStale) {  // otherwise the previous column's normalisation wrote v into vcIn
         EF_CUDA(cudaMemcpyAsync(c->vcIn, v, sizeof(float) * c->nDof, cudaMemcpyDeviceToDevice, s));
         c->vcInStale = false;
     }
-    ef::note_launches(c->vcGraphKernels);
-    EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
+    EF_CHECK(apply_base(c, s));
     *out = c->vcOut;
     if (c->nnOn) {
         EF_CHECK(nn_capture(c));
@@ -2370,11 +2415,9 @@ static ef_status nn_add_sample(ef_ctx* c, const float* r, const float* e, cudaSt
     S.er = h[1] * inv2;
     S.rr = h[2] * inv2;
     const float inv = (float)sqrt(inv2);
-    EF_CHECK(amg_capture(c));
     EF_CUDA(cudaMemcpyAsync(c->vcIn, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
     c->vcInStale = true;
-    ef::note_launches(c->vcGraphKernels);
-    EF_CUDA(cudaGraphLaunch(c->vcGraph, s));
+    EF_CHECK(apply_base(c, s));
     EF_CHECK(ef_launch_spmv_f32((int)nN, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->vcOut, c->dMask,
                                 c->nnKd, s));
     EF_CHECK(ef_launch_sub(n, c->vcIn, c->nnKd, c->nnRho, s));
@@ -2534,6 +2577,10 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         c->fgH = dalloc<double>(4 * (size_t)ef_fgmres_max_basis(), &st);
         if (!c->fgW || !c->fgPart || !c->fgPartN || !c->fgH) return st;
         if (const char* e = getenv("EF_FGMRES_ETA")) c->fgEta2 = atof(e) * atof(e);
+        bool staged = false;  // measured slower than the unstaged kernel (EF_SPMV_STAGED=1 turns it on)
+        if (const char* e = getenv("EF_SPMV_STAGED")) staged = atoi(e) != 0;
+        c->spCap = staged ? ef_sp_stage_cap((int)c->nNodes, c->hRowPtr0.data()) : 0;
+        if (c->spCap > 2048) c->spCap = 0;  // rows too long for a shared-memory stage
     }
     const int MB = ef_fgmres_max_basis();
     double* hG = c->fgH;            // first-pass coefficients and |w|^2 (the DGKS gate)
@@ -2586,8 +2633,13 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, &pz, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][2], s));
         // w = K z_j straight into the next basis slot; z_j kept in Z
-        EF_CHECK(ef_launch_spmv_f32_copy((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, pz,
-                                         c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
+        if (c->spCap > 0)
+            EF_CHECK(ef_launch_spmv_f32_staged(c->nSM, c->spCap, (int)c->nNodes, c->dRowPtr, c->dColIdx,
+                                               (const float*)c->dBsrVals, pz, c->dMask, V + (int64_t)(j + 1) * n,
+                                               Z + (int64_t)j * n, s));
+        else
+            EF_CHECK(ef_launch_spmv_f32_copy((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, pz,
+                                             c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][3], s));
         EF_CHECK(ef_launch_cgs_column(n, j + 1, V, n, c->fgPart, c->fgPartN, c->fgNPart, hG, hTmp, hAcc, c->fgEta2,
                                       c->vcIn, c->fgPinDev + sl * ldh, ldh - 1, s));
@@ -2766,8 +2818,13 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
             PcgResultHost pr;
             if (o->method == EF_SOLVE_FGMRES) {
-                EF_CHECK(amg_build(c));
-                EF_CHECK(amg_refresh(c, s));
+                if (c->fgPc == EF_FGMRES_PC_MULTIGRID) {
+                    EF_CHECK(amg_build(c));
+                    EF_CHECK(amg_refresh(c, s));
+                } else {
+                    EF_CHECK(amg_workspace(c));
+                    EF_CHECK(nn_edge_refresh(c, s));
+                }
                 int its = 0;
                 const ef_status fs = run_fgmres(c, (const float*)wv[0], (float*)wv[1], o->maxIter - total,
                                                 std::min(inner, 0.5), o->restart, &its, o->profile ? &inf : nullptr, s);
@@ -2805,6 +2862,20 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     inf.status = result;
     if (info) *info = inf;
     return result;
+}
+
+ef_status ef_fgmres_set_preconditioner(ef_ctx* c, int kind) {
+    EF_REQUIRE_FINALIZED(c);
+    if (kind != EF_FGMRES_PC_MULTIGRID && kind != EF_FGMRES_PC_JACOBI) {
+        ef_set_error("ef_fgmres_set_preconditioner: unknown kind");
+        return EF_ERR_ARG;
+    }
+    if (kind != c->fgPc && c->nnGraph) {  // the correction's captured graph reads the base output
+        cudaGraphExecDestroy(c->nnGraph);
+        c->nnGraph = nullptr;
+    }
+    c->fgPc = kind;
+    return EF_OK;
 }
 
 ef_status ef_batch_setup(ef_ctx* c, int nProb, const int32_t* nodePtr) {
@@ -2981,7 +3052,8 @@ ef_status ef_mpnn_init(ef_ctx* c, uint64_t seed, int maxSamples) {
         EF_CHECK(nn_transpose_map(c->hRowPtr0, c->hColIdx0, tpos));
         EF_CUDA(cudaMemcpy(c->nnTpos, tpos.data(), sizeof(int64_t) * tpos.size(), cudaMemcpyHostToDevice));
         c->nnInit = true;
-        c->amgStale = true;  // edge weights are computed with the next multigrid refresh
+        c->amgStale = true;  // edge weights are computed with the next refresh
+        c->nnEdgeStale = true;
     }
     // He-scaled normal weights; residual branches damped; output layer zero (z = Mv at start)
     std::mt19937_64 g(seed);
@@ -3066,8 +3138,13 @@ ef_status ef_mpnn_add_sample(ef_ctx* c, const double* r, const double* e, void* 
     }
     if (c->nnMaxSamples == 0) return EF_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    EF_CHECK(amg_build(c));
-    EF_CHECK(amg_refresh(c, s));
+    if (c->fgPc == EF_FGMRES_PC_MULTIGRID) {
+        EF_CHECK(amg_build(c));
+        EF_CHECK(amg_refresh(c, s));
+    } else {
+        EF_CHECK(amg_workspace(c));
+        EF_CHECK(nn_edge_refresh(c, s));
+    }
     const int64_t n = c->nDof;
     float* rf = (float*)c->w32[5];
     float* ef = (float*)c->w32[6];

@@ -63,6 +63,20 @@ struct PropsArg {
     double v[8];
 };
 
+#ifdef __CUDACC__
+// 16-byte asynchronous global -> shared copy (cp.async, cached in L2 only) and its group waits;
+// both addresses 16-byte aligned
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+#endif
+
 // One phase of the multigrid cycle below a level, run by coarse_cycle_kernel (amg.cu) with a
 // cluster barrier after each phase.  All coarse nodes carry 6 DOFs.
 enum CoarseOpType {

@@ -63,6 +63,103 @@ __global__ void __launch_bounds__(kFB) spmv_f32_kernel(int nN, const int32_t* __
     }
 }
 
+// Staged form of spmv_f32_kernel: persistent CTAs walk chunks of kSpRows block rows, copying the
+// next chunk's block values and column indices (contiguous in memory) into shared memory with
+// cp.async while the current one is computed; the rows are then computed by 8 lanes each from
+// shared memory, with the same order of operations as the unstaged kernel.  Stage layout
+// (cap = the largest chunk's block count): 9 cap + 8 floats | cap + 8 indices, both ranges
+// starting on the 16-byte boundary below the chunk's first block.
+constexpr int kSpRows = kFB / 8;
+
+__host__ __device__ inline size_t sp_stage_bytes(int cap) {
+    return (((size_t)9 * cap + 8) * 4 + 15) / 16 * 16 + ((size_t)cap + 8) * 4;
+}
+
+__device__ __forceinline__ void sp_stage_chunk(int b0, int b1, const float* __restrict__ vals,
+                                               const int32_t* __restrict__ colIdx, char* stage, int cap) {
+    float* sv = reinterpret_cast<float*>(stage);
+    int32_t* sc = reinterpret_cast<int32_t*>(stage + (((size_t)9 * cap + 8) * 4 + 15) / 16 * 16);
+    const int vs = (9 * b0) & ~3;
+    const int nv = (9 * b1 - vs + 3) >> 2;  // 16-byte pieces of 4 values
+    for (int i = threadIdx.x; i < nv; i += kFB) cp_async16(sv + 4 * i, vals + (int64_t)vs + 4 * i);
+    const int cs = b0 & ~3;
+    const int nc = (b1 - cs + 3) >> 2;
+    for (int i = threadIdx.x; i < nc; i += kFB) cp_async16(sc + 4 * i, colIdx + cs + 4 * i);
+}
+
+__global__ void __launch_bounds__(kFB) spmv_f32_staged_kernel(int nN, const int32_t* __restrict__ rowPtr,
+                                                               const int32_t* __restrict__ colIdx,
+                                                               const float* __restrict__ vals,
+                                                               const float* __restrict__ x,
+                                                               const uint8_t* __restrict__ mask, float* __restrict__ y,
+                                                               float* __restrict__ xcopy, int cap) {
+    extern __shared__ __align__(16) char smem[];
+    const size_t sb = (sp_stage_bytes(cap) + 15) & ~(size_t)15;
+    const int nChunks = (nN + kSpRows - 1) / kSpRows;
+    const int lane = threadIdx.x & 7;
+    const int rowInChunk = threadIdx.x >> 3;
+    int ch = blockIdx.x;
+    if (ch >= nChunks) return;
+    int b0 = rowPtr[ch * kSpRows];
+    int b1 = rowPtr[min((ch + 1) * kSpRows, nN)];
+    sp_stage_chunk(b0, b1, vals, colIdx, smem, cap);
+    cp_async_commit();
+    int st = 0;
+    for (; ch < nChunks; ch += gridDim.x, st ^= 1) {
+        const int nx = ch + gridDim.x;
+        int nb0 = 0, nb1 = 0;
+        if (nx < nChunks) {
+            nb0 = rowPtr[nx * kSpRows];
+            nb1 = rowPtr[min((nx + 1) * kSpRows, nN)];
+            sp_stage_chunk(nb0, nb1, vals, colIdx, smem + (st ^ 1) * sb, cap);
+        }
+        cp_async_commit();
+        const int m0 = ch * kSpRows + rowInChunk;
+        const int m = m0 < nN ? m0 : nN - 1;
+        const int s = rowPtr[m], e = rowPtr[m + 1];
+        cp_async_wait<1>();
+        __syncthreads();
+        const char* sg = smem + st * sb;
+        const float* sv = reinterpret_cast<const float*>(sg);
+        const int32_t* sc = reinterpret_cast<const int32_t*>(sg + (((size_t)9 * cap + 8) * 4 + 15) / 16 * 16);
+        const int vs = (9 * b0) & ~3, cs = b0 & ~3;
+        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        for (int base = s; base < e; base += 32) {
+            int cc[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = base + lane + 8 * j;
+                cc[j] = k < e ? 3 * sc[k - cs] : -1;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cc[j] >= 0) {
+                    const float* v = sv + (9 * (base + lane + 8 * j) - vs);
+                    const float x0 = x[cc[j]], x1 = x[cc[j] + 1], x2 = x[cc[j] + 2];
+                    y0 += v[0] * x0 + v[1] * x1 + v[2] * x2;
+                    y1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
+                    y2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
+                }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+            y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+            y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+        }
+        if (m0 < nN && lane < 3) {
+            const int d = 3 * m + lane;
+            const float yy = lane == 0 ? y0 : (lane == 1 ? y1 : y2);
+            y[d] = (mask && mask[d]) ? 0.f : yy;
+            if (xcopy) xcopy[d] = x[d];
+        }
+        __syncthreads();
+        b0 = nb0;
+        b1 = nb1;
+    }
+    cp_async_wait<0>();
+}
+
 // DGKS test (Daniel, Gragg, Kaufman, Stewart 1976) of classical Gram-Schmidt: after the first
 // projection w' = w - V h of w (|w|^2 = h[nv]), re-orthogonalise only when the Pythagorean
 // estimate |w'|^2 = |w|^2 - |h|^2 shows cancellation, |w'|^2 < eta2 |w|^2.  Every thread that
@@ -278,6 +375,35 @@ ef_status ef_launch_spmv_f32_copy(int nN, const int32_t* rowPtr, const int32_t* 
                                   const float* x, const uint8_t* mask, float* y, float* xcopy, cudaStream_t s) {
     spmv_f32_kernel<<<nbf((int64_t)nN * 8, kFB), kFB, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y,
                                                                            xcopy);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// staged SpMV (cap: the largest block count of a chunk of kSpRows rows, ef_sp_stage_cap)
+int ef_sp_stage_cap(int nN, const int32_t* rowPtrHost) {
+    int cap = 0;
+    for (int m0 = 0; m0 < nN; m0 += kSpRows) cap = std::max(cap, rowPtrHost[std::min(m0 + kSpRows, nN)] - rowPtrHost[m0]);
+    return cap;
+}
+
+ef_status ef_launch_spmv_f32_staged(int nSM, int cap, int nN, const int32_t* rowPtr, const int32_t* colIdx,
+                                    const float* vals, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                                    cudaStream_t s) {
+    const size_t smem = 2 * ((sp_stage_bytes(cap) + 15) & ~(size_t)15);
+    static size_t attrSet = 0;
+    if (smem > 48 * 1024 && smem > attrSet) {
+        EF_CUDA(cudaFuncSetAttribute(spmv_f32_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attrSet = smem;
+    }
+    int perSM = 0;
+    EF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, spmv_f32_staged_kernel, kFB, smem));
+    if (perSM < 1) {
+        ef_set_error("staged SpMV: chunk does not fit in shared memory");
+        return EF_ERR_ARG;
+    }
+    const int nChunks = (nN + kSpRows - 1) / kSpRows;
+    const int grid = std::max(1, std::min(nChunks, perSM * nSM));
+    spmv_f32_staged_kernel<<<grid, kFB, smem, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, mask, y, xcopy, cap);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -260,6 +260,14 @@ class NISTGPU:
 
     # ---- learned preconditioner correction (FGMRES only) ----------------------------------------
 
+    FGMRES_PRECONDITIONERS = {"multigrid": 0, "jacobi": 1}
+
+    def setFgmresPreconditioner(self, kind="multigrid"):
+        """Base preconditioner of the FGMRES solves (and of the learned correction's inputs):
+        "multigrid" (aggregation cycle) or "jacobi" (one block-Jacobi step)."""
+        _lib.check(self.lib.ef_fgmres_set_preconditioner(self.ctx, self.FGMRES_PRECONDITIONERS[kind]),
+                   "ef_fgmres_set_preconditioner")  # fmt: skip
+
     def initLearnedPreconditioner(self, seed=0, maxSamples=64):
         """Allocates the message-passing correction applied after the multigrid cycle and sets
         its initial weights (zero output layer: no correction until trained)."""
@@ -276,6 +284,9 @@ class NISTGPU:
         """One pair of device FP64 vectors with K e = r on the free DOFs."""
         _lib.check(self.lib.ef_mpnn_add_sample(self.ctx, r.data_ptr(), e.data_ptr(), self._stream()),
                    "ef_mpnn_add_sample")  # fmt: skip
+
+    def clearTrainingPairs(self):
+        _lib.check(self.lib.ef_mpnn_clear_samples(self.ctx), "ef_mpnn_clear_samples")
 
     def numTrainingPairs(self):
         n = ctypes.c_int()

@@ -242,6 +242,13 @@ ef_status ef_batch_autotune(ef_ctx* ctx, double rtol, int maxIter, const double*
 ef_status ef_batch_norms(ef_ctx* ctx, const double* R, const double* F, const double* ddU, double* out,
                          void* stream);
 
+/* Base preconditioner of EF_SOLVE_FGMRES (and of the learned correction's inputs):
+ * EF_FGMRES_PC_MULTIGRID (default) the aggregation multigrid cycle, EF_FGMRES_PC_JACOBI one
+ * block-Jacobi step D^-1. */
+#define EF_FGMRES_PC_MULTIGRID 0
+#define EF_FGMRES_PC_JACOBI 1
+ef_status ef_fgmres_set_preconditioner(ef_ctx* ctx, int kind);
+
 /* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----
  * The reference solves every Newton system with a direct or plain Krylov solver
  * (solvers/nonlinearimplicitstatic.py:547-571, linearSolve; utils/linearsolve.py:35-77); this

@@ -277,13 +277,17 @@ def test_fgmres_multigrid_solves_to_tolerance_with_fewer_iterations(gpu_lib):
 
 
 def test_fgmres_cluster_coarse_cycle_and_reorthogonalisation(gpu_lib, monkeypatch):
-    """The cycle below the first coarse level as one cluster launch gives bit-identical FGMRES
-    results to the launch-per-phase cycle (same operations in the same order); classical
-    Gram-Schmidt with DGKS re-orthogonalisation reaches the same 1e-8 solution."""
+    """The cycle below the first coarse level as one cluster launch, and the fine-level kernels
+    with or without shared-memory staging, give bit-identical FGMRES results (same operations in
+    the same order); classical Gram-Schmidt with DGKS re-orthogonalisation reaches the same 1e-8
+    solution."""
     rng = np.random.default_rng(5)
     out = {}
     for key, env in (("phases", {"EF_AMG_CLUSTER": "0"}), ("cluster", {"EF_AMG_CLUSTER": "1"}),
+                     ("staged", {"EF_AMG_CLUSTER": "0", "EF_AMG_STAGED": "1", "EF_SPMV_STAGED": "1"}),
                      ("dgks", {"EF_AMG_CLUSTER": "1", "EF_FGMRES_ETA": "0.7071"})):  # fmt: skip
+        for k in ("EF_FGMRES_ETA", "EF_AMG_STAGED", "EF_SPMV_STAGED"):
+            monkeypatch.delenv(k, raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)
         s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
@@ -299,12 +303,13 @@ def test_fgmres_cluster_coarse_cycle_and_reorthogonalisation(gpu_lib, monkeypatc
         per_it = (s.lib.ef_kernel_launches() - l0) / s.lastSolveInfo.iterations
         assert s.lastSolveInfo.relResidual <= 1e-8
         out[key] = (x, s.lastSolveInfo.iterations, s.lastSolveInfo.reorths, per_it)
-        monkeypatch.delenv("EF_FGMRES_ETA", raising=False)
     xp, ip, rp, lp = out["phases"]
     xc, ic, rc, lc = out["cluster"]
     xd, idg, rd, _ = out["dgks"]
+    xu, iu, _, _ = out["staged"]
     assert lc < lp, (lc, lp)  # the cluster launch replaces the per-phase kernels
     assert ic == ip and np.array_equal(xc, xp)
+    assert iu == ip and np.array_equal(xu, xp)  # shared-memory staging changes no result
     assert rp == 0 and rc == 0 and rd > 0
     assert np.max(np.abs(xd - xp)) <= 1e-6 * np.max(np.abs(xp))
 

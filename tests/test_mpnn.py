@@ -1,5 +1,6 @@
 """Learned preconditioner correction: the float64 oracle against finite differences (CPU), the
-CUDA forward/backward against the oracle, and the iteration gain of the trained network (GPU)."""
+CUDA forward/backward against the oracle, the tensor-core layer against the CUDA-core one, and
+the iteration gain of the network trained on the GPU (GPU)."""
 
 import ctypes
 
@@ -130,3 +131,54 @@ def test_gpu_dense_layer_tensor_cores_match_cuda_cores(gpu_lib, nN):
     assert np.max(np.abs(out[0][0] - qr)) <= 1e-5 * np.max(np.abs(qr))
     assert np.max(np.abs(out[1][0] - out[0][0])) <= 1e-2 * np.max(np.abs(out[0][0]))
     assert np.max(np.abs(out[1][1] - out[0][1])) <= 1e-2 * np.max(np.abs(out[0][1]))
+
+
+@pytest.mark.gpu
+def test_gpu_trained_network_cuts_fgmres_iterations(gpu_lib):
+    """The network trained on the GPU (own forward, backward and Adam kernels) on (residual,
+    correction) pairs that the plain FGMRES + block-Jacobi solver produces, then used as the
+    correction of that preconditioner: at least 40 % fewer FGMRES iterations to 1e-8 on new
+    right-hand sides of the same system than the same solver without it (measured on GB300:
+    about 2.7x fewer), and a lower training loss at the end than at the start."""
+    import torch
+    from cases import build_gpu_solver, j2_box_spec
+    from edelweissfe_gb300 import _lib
+    from edelweissfe_gb300.solver import TimeStep
+
+    s = build_gpu_solver(j2_box_spec(16, 8, 8, 1.6, 0.8, 0.8))
+    _lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+    dU = torch.zeros(s.nDof, dtype=torch.float64, device="cuda")
+    P, F = s._vec(), s._vec()
+    s.computeElements(dU, dU, P, F, TimeStep(1, 0.1, 0.1, 0.1, 0.1, 0.1))
+    s.assembleStiffnessCSR()
+    s.linsolver.method = "fgmres"
+    s.linsolver.rtol = 1e-8
+    s.linsolver.innerRtol = 1e-6
+    s.linsolver.restart = 40
+    s.setFgmresPreconditioner("jacobi")
+
+    def rhs(seed):
+        b = np.random.default_rng(seed).normal(size=s.nDof)
+        b[s.dirIdxHost] = 0.0
+        return torch.as_tensor(b, device="cuda")
+
+    def iterations(seeds):
+        out = []
+        for k in seeds:
+            s.linearSolve(rhs(k))
+            assert s.lastSolveInfo.relResidual <= 1e-8
+            out.append(s.lastSolveInfo.iterations)
+        return np.array(out)
+
+    off = iterations([100, 101, 102])
+    s.initLearnedPreconditioner(seed=0, maxSamples=48)
+    s.collectTrainingPairs(every=5, maxPerSolve=8, kind="iterates")
+    iterations(range(6))  # the plain solver's own iterates give the pairs
+    s.collectTrainingPairs(every=0)
+    assert s.numTrainingPairs() == 48
+    first, last = s.trainLearnedPreconditioner(epochs=100, lr=1e-3, norm="energy")
+    assert last < first
+    s.enableLearnedPreconditioner(True)
+    on = iterations([100, 101, 102])
+    s.enableLearnedPreconditioner(False)
+    assert on.mean() <= 0.6 * off.mean(), (off, on)
