@@ -560,6 +560,7 @@ void ef_destroy(ef_ctx* c) {
         F((void*)g.propsTable);
         F((void*)g.elemRow);
         F(g.geo);
+        F(g.geoS);
     }
     for (auto* t : c->dTables) F(t);
     F(c->Pe);
@@ -856,6 +857,10 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         }
         g.geo = dalloc<double>((size_t)h.nEl * h.nQP * (3 * h.nNodes + 1), &st);
         if (!g.geo) return st;
+        if (!g.tl) {
+            g.geoS = dalloc<float2>((size_t)h.nEl * h.nQP * (3 * h.nNodes + 1), &st);
+            if (!g.geoS) return st;
+        }
         EF_CHECK(ef_launch_geometry(g, c->dTables[gi], c->dX, c->dFlags, 0));
         g.peOffset = peOff;
         g.keOffset = keOff;

@@ -55,6 +55,7 @@ struct Group {
     int64_t keOffset;     // offset of this group's Ke blocks (units of 3x3 blocks)
     int tablesSlot;       // index of the group's element table
     double* geo;          // geometry cache [nEl*nQP][3*nNodes + 1]: dN/dx and w*detJ (FP64)
+    float2* geoS;         // the same values split into FP32 pairs (hi, lo = d - hi), small-strain groups
     const double* propsTable;  // optional per-element material rows [nRows][8] (null: props)
     const int32_t* elemRow;    // element -> row of propsTable
 };

@@ -130,6 +130,36 @@ __device__ __forceinline__ bool mat_von_mises(const double* props, double* sig, 
     return true;
 }
 
+// Double-float arithmetic (Dekker 1971; Knuth's TwoSum): a value is an unevaluated pair of
+// FP32 numbers hi + lo with |lo| <= ulp(hi) / 2, about 48 significant bits.  The element kernel
+// forms its strain and residual contractions this way on the FP32 pipe, because the FP64 pipe
+// of this GPU (2 lanes per SM and cycle) bounds the kernel.  The rounded operations are written
+// with the _rn intrinsics so that the compiler cannot contract them into FMAs.
+struct DF {
+    float hi, lo;
+};
+
+__host__ __device__ __forceinline__ float2 df_split(double d) {
+    const float hi = (float)d;
+    return make_float2(hi, (float)(d - (double)hi));
+}
+
+__device__ __forceinline__ double df_value(const DF& a) { return (double)a.hi + (double)a.lo; }
+
+// acc += a * b for a = (ah, al), b = (bh, bl): the product ah bh exactly (its rounding error from
+// an FMA), the cross terms ah bl + al bh in FP32 (relative 2^-24 of the product), al bl dropped
+// (2^-48); the sum with acc.hi by TwoSum, every error term into acc.lo
+__device__ __forceinline__ void df_fma(DF& acc, float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    const float pe = __fmaf_rn(a.x, b.x, -p);
+    const float x = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));
+    const float s = __fadd_rn(acc.hi, p);
+    const float bv = __fsub_rn(s, acc.hi);
+    const float err = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+    acc.hi = s;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(err, __fadd_rn(pe, x)));
+}
+
 // Gauss-point geometry in FP64: J = dN/dS x (reference formulation, including the C3D20
 // row-2 Jacobian term), det J and g_a = dN_a/dx = inv(J) dN_a/dS.
 template <int NN>
@@ -177,7 +207,8 @@ __device__ __forceinline__ double qp_geometry(const ElemTables* __restrict__ T, 
 // geo[(e*NQ + q) * (3*NN + 1) + 3a + c] = dN_a/dx_c, last entry = w_q det J.
 template <int NN, int NQ>
 __global__ void geometry_kernel(const ElemTables* __restrict__ T, int nEl, const int32_t* __restrict__ nodeDof,
-                                const double* __restrict__ X, double* __restrict__ geo, int* __restrict__ flags) {
+                                const double* __restrict__ X, double* __restrict__ geo, float2* __restrict__ geoS,
+                                int* __restrict__ flags) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nEl * NQ) return;
     const int64_t e = t / NQ;
@@ -197,23 +228,27 @@ __global__ void geometry_kernel(const ElemTables* __restrict__ T, int nEl, const
 #pragma unroll
         for (int c = 0; c < 3; ++c) o[3 * a + c] = g[a][c];
     o[3 * NN] = T->w[q] * det;
+    if (geoS) {
+        float2* os = geoS + t * (3 * NN + 1);
+        for (int k = 0; k <= 3 * NN; ++k) os[k] = df_split(o[k]);
+    }
 }
 
 template <int NN, int NQ, typename KT>
 struct SSShared {
     static constexpr int TPE = (NQ <= 8) ? 8 : 32;
     static constexpr int EPB = kBlock / TPE;
-    double du[EPB][NN][3];
-    double g[EPB][NQ][NN][3];
-    KT gk[EPB][NQ][NN][3];  // g in the stiffness precision, converted once per Gauss point and node
-    double sw[EPB][NQ][6];
-    KT tn[EPB][NQ][9];  // lt*w, mt*w, c1*w, n[6]
+    float2 du[EPB][NN][3];     // dU split into FP32 pairs
+    float2 g[EPB][NQ][NN][3];  // dN/dx split into FP32 pairs
+    KT gk[EPB][NQ][NN][3];     // g in the stiffness precision
+    float2 sw[EPB][NQ][6];     // sigma w detJ split into FP32 pairs
+    KT tn[EPB][NQ][9];         // lt*w, mt*w, c1*w, n[6]
 };
 
 // Element loop of one group: strain increment, constitutive update, Pe (FP64) and Ke blocks (KT).
 template <int NN, int NQ, typename KT, int MAT, bool VIJ>
 __global__ void __launch_bounds__(kBlock) small_strain_kernel(
-    int nEl, const int32_t* __restrict__ nodeDof, const double* __restrict__ geo, const double* __restrict__ dU,
+    int nEl, const int32_t* __restrict__ nodeDof, const float2* __restrict__ geoS, const double* __restrict__ dU,
     const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props,
     const double* __restrict__ propsTable, const int32_t* __restrict__ elemRow, KT* __restrict__ Kout,
     double* __restrict__ Pe, double* __restrict__ tang, int* __restrict__ flags) {
@@ -233,9 +268,9 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
     if (valid) {
         for (int a = lane; a < NN; a += TPE) {
             const int d = nodeDof[(int64_t)e * NN + a];
-            sh.du[le][a][0] = dU[d + 0];
-            sh.du[le][a][1] = dU[d + 1];
-            sh.du[le][a][2] = dU[d + 2];
+            sh.du[le][a][0] = df_split(dU[d + 0]);
+            sh.du[le][a][1] = df_split(dU[d + 1]);
+            sh.du[le][a][2] = df_split(dU[d + 2]);
         }
     }
     __syncthreads();
@@ -243,24 +278,34 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
     // ---- Gauss-point phase ---------------------------------------------------
     if (valid && lane < NQ) {
         const int q = lane;
-        const double* gq = geo + ((int64_t)e * NQ + q) * NG;
-        double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        const float2* gq = geoS + ((int64_t)e * NQ + q) * NG;
+        // displacement-increment gradient H = sum_a dU_a (x) g_a in double-float arithmetic
+        DF H[3][3];
 #pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) H[i][j] = DF{0.f, 0.f};
+#pragma unroll 4
         for (int a = 0; a < NN; ++a) {
-            double ga[3];
+            float2 ga[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 ga[c] = gq[3 * a + c];
                 sh.g[le][q][a][c] = ga[c];
-                sh.gk[le][q][a][c] = (KT)ga[c];
+                sh.gk[le][q][a][c] = sizeof(KT) == sizeof(float) ? (KT)ga[c].x : (KT)((double)ga[c].x + (double)ga[c].y);
             }
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
+            for (int i = 0; i < 3; ++i) {
+                const float2 u = sh.du[le][a][i];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) H[i][j] += sh.du[le][a][i] * ga[j];
+                for (int j = 0; j < 3; ++j) df_fma(H[i][j], u, ga[j]);
+            }
         }
-        const double wdet = gq[3 * NN];
-        const double de[6] = {H[0][0], H[1][1], H[2][2], H[0][1] + H[1][0], H[0][2] + H[2][0], H[1][2] + H[2][1]};
+        const float2 wq = gq[3 * NN];
+        const double wdet = (double)wq.x + (double)wq.y;
+        const double de[6] = {df_value(H[0][0]), df_value(H[1][1]), df_value(H[2][2]),
+                              df_value(H[0][1]) + df_value(H[1][0]), df_value(H[0][2]) + df_value(H[2][0]),
+                              df_value(H[1][2]) + df_value(H[2][1])};
         const int64_t nQPtot = (int64_t)nEl * NQ;
         const int64_t qi = (int64_t)e * NQ + q;
         double sig[6];
@@ -283,7 +328,7 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
             if (!(sig[i] == sig[i])) atomicOr(flags, EF_FLAG_NAN);
         }
 #pragma unroll
-        for (int i = 0; i < 6; ++i) sh.sw[le][q][i] = sig[i] * wdet;
+        for (int i = 0; i < 6; ++i) sh.sw[le][q][i] = df_split(sig[i] * wdet);
         if (tang) {
             // FP64 tangent of this Gauss point for the exact (matrix-free) refinement residual
             tang[0 * nQPtot + qi] = mo.lt * wdet;
@@ -303,21 +348,27 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
     __syncthreads();
     if (!valid) return;
 
-    // ---- residual: Pe_a = -sum_q (sigma w detJ) . g_qa  (FP64 accumulation) ----
+    // ---- residual: Pe_a = -sum_q (sigma w detJ) . g_qa  (double-float accumulation) ----
     for (int a = lane; a < NN; a += TPE) {
-        double f0 = 0, f1 = 0, f2 = 0;
-#pragma unroll 4
+        DF f0{0.f, 0.f}, f1{0.f, 0.f}, f2{0.f, 0.f};
+#pragma unroll 2
         for (int q = 0; q < NQ; ++q) {
-            const double* s = sh.sw[le][q];
-            const double gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
-            f0 += s[0] * gx + s[3] * gy + s[4] * gz;
-            f1 += s[3] * gx + s[1] * gy + s[5] * gz;
-            f2 += s[4] * gx + s[5] * gy + s[2] * gz;
+            const float2* s = sh.sw[le][q];
+            const float2 gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
+            df_fma(f0, s[0], gx);
+            df_fma(f0, s[3], gy);
+            df_fma(f0, s[4], gz);
+            df_fma(f1, s[3], gx);
+            df_fma(f1, s[1], gy);
+            df_fma(f1, s[5], gz);
+            df_fma(f2, s[4], gx);
+            df_fma(f2, s[5], gy);
+            df_fma(f2, s[2], gz);
         }
         double* pe = Pe + (int64_t)e * ND + 3 * a;
-        pe[0] = -f0;
-        pe[1] = -f1;
-        pe[2] = -f2;
+        pe[0] = -df_value(f0);
+        pe[1] = -df_value(f1);
+        pe[2] = -df_value(f2);
     }
 
     // ---- stiffness: K_ab = sum_q lt ga(x)gb + mt (gb(x)ga + ga.gb I) - c1 va(x)vb ----
@@ -493,16 +544,20 @@ static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, d
     const double* sIn = g.state[g.cur];
     double* sOut = g.state[1 - g.cur];
     if (grid == 0) return EF_OK;
+    if (!g.geoS) {
+        ef_set_error("small-strain kernel: split geometry cache missing");
+        return EF_ERR_STATE;
+    }
     const size_t smem = sizeof(SSShared<NN, NQ, KT>);
     if (vij) {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, true>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geoS, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
                                                   (KT*)K, Pe, tang, flags);
     } else {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, false>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geo, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
+        k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geoS, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
                                                   (KT*)K, Pe, tang, flags);
     }
     EF_CUDA(cudaGetLastError());
@@ -539,7 +594,8 @@ template <int NN, int NQ>
 static ef_status launch_geometry(const Group& g, const ElemTables* T, const double* X, int* flags, cudaStream_t s) {
     const int64_t n = (int64_t)g.nEl * NQ;
     if (n == 0) return EF_OK;
-    geometry_kernel<NN, NQ><<<(int)((n + 127) / 128), 128, 0, ef::counted(s)>>>(T, g.nEl, g.nodeDof, X, g.geo, flags);
+    geometry_kernel<NN, NQ><<<(int)((n + 127) / 128), 128, 0, ef::counted(s)>>>(T, g.nEl, g.nodeDof, X, g.geo, g.geoS,
+                                                                              flags);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
