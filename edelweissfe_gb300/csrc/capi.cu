@@ -766,6 +766,15 @@ ef_status ef_set_ties(ef_ctx* c, const int64_t* slave, const int64_t* masterA, c
     return EF_OK;
 }
 
+// slots 6 and 7 of a small-strain material's property row: lambda and G of (E, nu), formed once
+// (the element kernel reads them instead of dividing per Gauss point)
+static void derived_props(int mat, double* p) {
+    if (mat != MAT_LINEAR_ELASTIC && mat != MAT_VON_MISES) return;
+    const double E = p[0], nu = p[1];
+    p[6] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    p[7] = E / (2.0 * (1.0 + nu));
+}
+
 ef_status ef_set_group_props(ef_ctx* c, int groupId, const double* table, int nRows, int nProps,
                              const int32_t* elemRow) {
     if (!c) return EF_ERR_ARG;
@@ -787,8 +796,10 @@ ef_status ef_set_group_props(ef_ctx* c, int groupId, const double* table, int nR
         return EF_ERR_ARG;
     }
     h.propsTable.assign((size_t)nRows * 8, 0.0);
-    for (int r = 0; r < nRows; ++r)
+    for (int r = 0; r < nRows; ++r) {
         for (int i = 0; i < nProps; ++i) h.propsTable[(size_t)r * 8 + i] = table[(size_t)r * nProps + i];
+        derived_props(h.mat, &h.propsTable[(size_t)r * 8]);
+    }
     h.elemRow.assign(elemRow, elemRow + h.nEl);
     for (int32_t r : h.elemRow)
         if (r < 0 || r >= nRows) {
@@ -835,7 +846,8 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         g.mat = h.mat;
         g.tl = h.tl;
         g.nState = 12 + ((h.mat == MAT_VON_MISES || h.mat == MAT_NEOHOOKE_WA) ? 1 : 0);
-        for (size_t i = 0; i < h.props.size(); ++i) g.props[i] = h.props[i];
+        for (size_t i = 0; i < h.props.size() && i < 8; ++i) g.props[i] = h.props[i];
+        derived_props(h.mat, g.props);
         g.nodeDof = dalloc<int32_t>(h.nodeDof.size(), &st);
         if (!g.nodeDof) return st;
         EF_CUDA(cudaMemcpy(g.nodeDof, h.nodeDof.data(), sizeof(int32_t) * h.nodeDof.size(), cudaMemcpyHostToDevice));
