@@ -277,8 +277,8 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
 
 // t = r - A x for 6x6 blocks, one warp per block row: lane 6g + i (g < 5, i < 6) takes row i of
 // the blocks g, g + 5, g + 10, ... of the row (three 8-byte loads of the block row, so that the
-// warp reads five consecutive blocks per step), the five slots of each i are combined by a
-// fixed shuffle sequence.  With binv set: one smoothing sweep, t = x + omega D^-1 (r - A x).
+// warp reads five consecutive blocks per slot, three slots per step), the five slots of each i
+// are combined by a fixed shuffle sequence.  With binv set: one smoothing sweep, t = x + omega D^-1 (r - A x).
 template <bool CG>
 __device__ __forceinline__ float2 ldv2(const float* p) {
     if (CG) return __ldcg(reinterpret_cast<const float2*>(p));
@@ -292,13 +292,30 @@ __device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __res
     const int g = lane / BC, ri = lane - BC * g;
     float acc = 0.f;
     if (g < 5) {
+        // three blocks per lane and step (15 per warp), their loads issued together
         const int e = rowPtr[m + 1];
-        for (int k = rowPtr[m] + g; k < e; k += 5) {
-            const int c = BC * colIdx[k];
-            const float2* v = reinterpret_cast<const float2*>(vals + (int64_t)k * BC * BC + BC * ri);
-            const float2 a0 = v[0], a1 = v[1], a2 = v[2];
-            const float2 x0 = ldv2<CG>(x + c), x1 = ldv2<CG>(x + c + 2), x2 = ldv2<CG>(x + c + 4);
-            acc += a0.x * x0.x + a0.y * x0.y + a1.x * x1.x + a1.y * x1.y + a2.x * x2.x + a2.y * x2.y;
+        for (int k0 = rowPtr[m] + g; k0 < e; k0 += 15) {
+            int c[3];
+            float2 a[3][3];
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {
+                const int k = k0 + 5 * u;
+                c[u] = -1;
+                if (k < e) {
+                    c[u] = BC * colIdx[k];
+                    const float2* v = reinterpret_cast<const float2*>(vals + (int64_t)k * BC * BC + BC * ri);
+                    a[u][0] = v[0];
+                    a[u][1] = v[1];
+                    a[u][2] = v[2];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+                if (c[u] >= 0) {
+                    const float2 x0 = ldv2<CG>(x + c[u]), x1 = ldv2<CG>(x + c[u] + 2), x2 = ldv2<CG>(x + c[u] + 4);
+                    acc += a[u][0].x * x0.x + a[u][0].y * x0.y + a[u][1].x * x1.x + a[u][1].y * x1.y +
+                           a[u][2].x * x2.x + a[u][2].y * x2.y;
+                }
         }
     }
     // lanes i < 6: acc(i) + acc(i + 6) + acc(i + 12) + acc(i + 18) + acc(i + 24)
@@ -500,7 +517,7 @@ __global__ void coarsest_apply_kernel(int n, const float* __restrict__ inv, cons
 // and written through L2 only.  Every thread runs every phase loop and every barrier, so the
 // barrier count is uniform over the cluster.
 constexpr int kCoarseCtas = 8;
-constexpr int kCoarseThreads = 1024;
+constexpr int kCoarseThreads = 512;
 __global__ void __cluster_dims__(kCoarseCtas, 1, 1) __launch_bounds__(kCoarseThreads, 1)
     coarse_cycle_kernel(const CoarseOp* __restrict__ ops, int nOps) {
     const int tid = blockIdx.x * kCoarseThreads + threadIdx.x;
