@@ -431,7 +431,7 @@ struct ef_ctx {
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
     // V-cycle parameters: damping, smoothing sweeps per side, coarse over-correction, cycle type
-    float amgOmega = 0.65f;                 // upper bound of the smoothing damping
+    float amgOmega = 1.0f;                  // upper bound of the smoothing damping
     std::vector<float> levelOmega;          // per smoothed level: amgOmega, or 4 / (3 lambda_max(D^-1 A)) when smaller
     float* amgPow[2] = {nullptr, nullptr};  // power-iteration vectors (fine size)
     float* amgZero = nullptr;
