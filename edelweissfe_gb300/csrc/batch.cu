@@ -19,18 +19,29 @@
 
 namespace ef {
 
-template <int TPB>
-__device__ __forceinline__ double cta_sum(double v, double* red) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// CTA sums of NV values per thread in a fixed order.  FP64 is a narrow pipe on this GPU, so one
+// warp does the adds (TPB / 32 strided adds per lane and value, then a shuffle tree) instead of
+// every warp; red holds NV * TPB doubles.
+template <int TPB, int NV>
+__device__ __forceinline__ void cta_sum(double (&v)[NV], double* red) {
     __syncthreads();  // red is free again (previous readers are done)
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double s = 0.0;
 #pragma unroll
-    for (int i = 0; i < TPB / 32; ++i) s += red[i];
-    return s;
+    for (int j = 0; j < NV; ++j) red[j * TPB + threadIdx.x] = v[j];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double s = 0.0;
+#pragma unroll
+            for (int i = 0; i < TPB / 32; ++i) s += red[j * TPB + 32 * i + threadIdx.x];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (threadIdx.x == 0) red[NV * TPB + j] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = red[NV * TPB + j];
 }
 
 // TPB threads per CTA; the products use LPR lanes per block row (strided over the row's blocks,
@@ -42,7 +53,7 @@ __global__ void __launch_bounds__(TPB) batched_pcg_kernel(
     const double* __restrict__ binv, const uint8_t* __restrict__ mask, const double* __restrict__ b,
     double* __restrict__ x, double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
     double* __restrict__ q, int maxIter, double rtol2, int* __restrict__ itersOut, double* __restrict__ relOut) {
-    __shared__ double red[TPB / 32];
+    __shared__ double red[2 * TPB + 2];
     constexpr int RPI = TPB / LPR;  // block rows per pass of the product
     const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
     for (int k = blockIdx.x; k < nProb; k += gridDim.x) {
@@ -69,8 +80,10 @@ __global__ void __launch_bounds__(TPB) batched_pcg_kernel(
                 lbb += rv[i] * rv[i];
             }
         }
-        double rz = cta_sum<TPB>(lrz, red);
-        const double bb = cta_sum<TPB>(lbb, red);
+        double t0[2] = {lrz, lbb};
+        cta_sum<TPB, 2>(t0, red);
+        double rz = t0[0];
+        const double bb = t0[1];
         int it = 0;
         double rr = bb;
         bool ok = true;
@@ -107,7 +120,9 @@ __global__ void __launch_bounds__(TPB) batched_pcg_kernel(
                         }
                     }
                 }
-                const double pq = cta_sum<TPB>(lpq, red);
+                double t1[1] = {lpq};
+                cta_sum<TPB, 1>(t1, red);
+                const double pq = t1[0];
                 if (!(pq > 0.0)) {  // breakdown or NaN: stop with the current iterate
                     ok = pq == pq;
                     break;
@@ -134,8 +149,10 @@ __global__ void __launch_bounds__(TPB) batched_pcg_kernel(
                         lrz2 += rv[i] * zi;
                     }
                 }
-                rr = cta_sum<TPB>(lrr, red);
-                const double rz2 = cta_sum<TPB>(lrz2, red);
+                double t2[2] = {lrr, lrz2};
+                cta_sum<TPB, 2>(t2, red);
+                rr = t2[0];
+                const double rz2 = t2[1];
                 const double beta = rz2 / rz;
                 rz = rz2;
                 for (int m = n0 + (int)threadIdx.x; m < n1; m += TPB)
