@@ -234,20 +234,31 @@ __global__ void geometry_kernel(const ElemTables* __restrict__ T, int nEl, const
     }
 }
 
+// a split value in the stiffness precision: hi for FP32, hi + lo for FP64
+template <typename KT>
+__device__ __forceinline__ KT gk_value(float2 v);
+template <>
+__device__ __forceinline__ float gk_value<float>(float2 v) {
+    return v.x;
+}
+template <>
+__device__ __forceinline__ double gk_value<double>(float2 v) {
+    return (double)v.x + (double)v.y;
+}
+
 template <int NN, int NQ, typename KT>
 struct SSShared {
     static constexpr int TPE = (NQ <= 8) ? 8 : 32;
     static constexpr int EPB = kBlock / TPE;
     float2 du[EPB][NN][3];     // dU split into FP32 pairs
-    float2 g[EPB][NQ][NN][3];  // dN/dx split into FP32 pairs
-    KT gk[EPB][NQ][NN][3];     // g in the stiffness precision
+    float2 g[EPB][NQ][NN][3];  // dN/dx split into FP32 pairs (the FP32 stiffness reads hi)
     float2 sw[EPB][NQ][6];     // sigma w detJ split into FP32 pairs
     KT tn[EPB][NQ][9];         // lt*w, mt*w, c1*w, n[6]
 };
 
 // Element loop of one group: strain increment, constitutive update, Pe (FP64) and Ke blocks (KT).
 template <int NN, int NQ, typename KT, int MAT, bool VIJ>
-__global__ void __launch_bounds__(kBlock) small_strain_kernel(
+__global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
     int nEl, const int32_t* __restrict__ nodeDof, const float2* __restrict__ geoS, const double* __restrict__ dU,
     const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props,
     const double* __restrict__ propsTable, const int32_t* __restrict__ elemRow, KT* __restrict__ Kout,
@@ -292,7 +303,6 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
             for (int c = 0; c < 3; ++c) {
                 ga[c] = gq[3 * a + c];
                 sh.g[le][q][a][c] = ga[c];
-                sh.gk[le][q][a][c] = sizeof(KT) == sizeof(float) ? (KT)ga[c].x : (KT)((double)ga[c].x + (double)ga[c].y);
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
@@ -378,8 +388,10 @@ __global__ void __launch_bounds__(kBlock) small_strain_kernel(
         KT k[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int q = 0; q < NQ; ++q) {
             const KT* tn = sh.tn[le][q];
-            const KT ga0 = sh.gk[le][q][a][0], ga1 = sh.gk[le][q][a][1], ga2 = sh.gk[le][q][a][2];
-            const KT gb0 = sh.gk[le][q][b][0], gb1 = sh.gk[le][q][b][1], gb2 = sh.gk[le][q][b][2];
+            const KT ga0 = gk_value<KT>(sh.g[le][q][a][0]), ga1 = gk_value<KT>(sh.g[le][q][a][1]),
+                     ga2 = gk_value<KT>(sh.g[le][q][a][2]);
+            const KT gb0 = gk_value<KT>(sh.g[le][q][b][0]), gb1 = gk_value<KT>(sh.g[le][q][b][1]),
+                     gb2 = gk_value<KT>(sh.g[le][q][b][2]);
             const KT lt = tn[0], mt = tn[1], c1 = tn[2];
             const KT s = mt * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
             const KT la[3] = {lt * ga0, lt * ga1, lt * ga2};
