@@ -250,10 +250,11 @@ template <int NN, int NQ, typename KT>
 struct SSShared {
     static constexpr int TPE = (NQ <= 8) ? 8 : 32;
     static constexpr int EPB = kBlock / TPE;
-    float2 du[EPB][NN][3];     // dU split into FP32 pairs
-    float2 g[EPB][NQ][NN][3];  // dN/dx split into FP32 pairs (the FP32 stiffness reads hi)
-    float2 sw[EPB][NQ][6];     // sigma w detJ split into FP32 pairs
-    KT tn[EPB][NQ][9];         // lt*w, mt*w, c1*w, n[6]
+    // per-element rows padded by one entry, so that the elements of a warp fall on different banks
+    float2 du[EPB][NN * 3 + 1];       // dU split into FP32 pairs, [3a + i]
+    float2 g[EPB][NQ * NN * 3 + 1];   // dN/dx split into FP32 pairs, [(q NN + a) 3 + c] (the FP32 stiffness reads hi)
+    float2 sw[EPB][NQ * 6 + 1];       // sigma w detJ split into FP32 pairs, [6q + i]
+    KT tn[EPB][NQ][9];                // lt*w, mt*w, c1*w, n[6]
 };
 
 // Element loop of one group: strain increment, constitutive update, Pe (FP64) and Ke blocks (KT).
@@ -279,9 +280,9 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
     if (valid) {
         for (int a = lane; a < NN; a += TPE) {
             const int d = nodeDof[(int64_t)e * NN + a];
-            sh.du[le][a][0] = df_split(dU[d + 0]);
-            sh.du[le][a][1] = df_split(dU[d + 1]);
-            sh.du[le][a][2] = df_split(dU[d + 2]);
+            sh.du[le][3 * a + 0] = df_split(dU[d + 0]);
+            sh.du[le][3 * a + 1] = df_split(dU[d + 1]);
+            sh.du[le][3 * a + 2] = df_split(dU[d + 2]);
         }
     }
     __syncthreads();
@@ -302,11 +303,11 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 ga[c] = gq[3 * a + c];
-                sh.g[le][q][a][c] = ga[c];
+                sh.g[le][(q * NN + a) * 3 + c] = ga[c];
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                const float2 u = sh.du[le][a][i];
+                const float2 u = sh.du[le][3 * a + i];
 #pragma unroll
                 for (int j = 0; j < 3; ++j) df_fma(H[i][j], u, ga[j]);
             }
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
             if (!(sig[i] == sig[i])) atomicOr(flags, EF_FLAG_NAN);
         }
 #pragma unroll
-        for (int i = 0; i < 6; ++i) sh.sw[le][q][i] = df_split(sig[i] * wdet);
+        for (int i = 0; i < 6; ++i) sh.sw[le][6 * q + i] = df_split(sig[i] * wdet);
         if (tang) {
             // FP64 tangent of this Gauss point for the exact (matrix-free) refinement residual
             tang[0 * nQPtot + qi] = mo.lt * wdet;
@@ -363,8 +364,9 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
         DF f0{0.f, 0.f}, f1{0.f, 0.f}, f2{0.f, 0.f};
 #pragma unroll 2
         for (int q = 0; q < NQ; ++q) {
-            const float2* s = sh.sw[le][q];
-            const float2 gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
+            const float2* s = &sh.sw[le][6 * q];
+            const float2* gg = &sh.g[le][(q * NN + a) * 3];
+            const float2 gx = gg[0], gy = gg[1], gz = gg[2];
             df_fma(f0, s[0], gx);
             df_fma(f0, s[3], gy);
             df_fma(f0, s[4], gz);
@@ -388,10 +390,10 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
         KT k[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int q = 0; q < NQ; ++q) {
             const KT* tn = sh.tn[le][q];
-            const KT ga0 = gk_value<KT>(sh.g[le][q][a][0]), ga1 = gk_value<KT>(sh.g[le][q][a][1]),
-                     ga2 = gk_value<KT>(sh.g[le][q][a][2]);
-            const KT gb0 = gk_value<KT>(sh.g[le][q][b][0]), gb1 = gk_value<KT>(sh.g[le][q][b][1]),
-                     gb2 = gk_value<KT>(sh.g[le][q][b][2]);
+            const float2* gA = &sh.g[le][(q * NN + a) * 3];
+            const float2* gB = &sh.g[le][(q * NN + b) * 3];
+            const KT ga0 = gk_value<KT>(gA[0]), ga1 = gk_value<KT>(gA[1]), ga2 = gk_value<KT>(gA[2]);
+            const KT gb0 = gk_value<KT>(gB[0]), gb1 = gk_value<KT>(gB[1]), gb2 = gk_value<KT>(gB[2]);
             const KT lt = tn[0], mt = tn[1], c1 = tn[2];
             const KT s = mt * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
             const KT la[3] = {lt * ga0, lt * ga1, lt * ga2};
@@ -443,9 +445,10 @@ template <int NN, int NQ>
 struct ApplyShared {
     static constexpr int TPE = (NQ <= 8) ? 8 : 32;
     static constexpr int EPB = kBlock / TPE;
-    double xv[EPB][NN][3];
-    double g[EPB][NQ][NN][3];
-    double sw[EPB][NQ][6];
+    // per-element rows padded by one entry (bank spread of the elements of a warp)
+    double xv[EPB][NN * 3 + 1];
+    double g[EPB][NQ * NN * 3 + 1];
+    double sw[EPB][NQ * 6 + 1];
 };
 
 template <int NN, int NQ>
@@ -468,9 +471,9 @@ __global__ void __launch_bounds__(kBlock) small_strain_apply_kernel(int nEl, con
     if (valid) {
         for (int a = lane; a < NN; a += TPE) {
             const int d = nodeDof[(int64_t)e * NN + a];
-            sh.xv[le][a][0] = x[d + 0];
-            sh.xv[le][a][1] = x[d + 1];
-            sh.xv[le][a][2] = x[d + 2];
+            sh.xv[le][3 * a + 0] = x[d + 0];
+            sh.xv[le][3 * a + 1] = x[d + 1];
+            sh.xv[le][3 * a + 2] = x[d + 2];
         }
     }
     __syncthreads();
@@ -481,11 +484,11 @@ __global__ void __launch_bounds__(kBlock) small_strain_apply_kernel(int nEl, con
 #pragma unroll
         for (int a = 0; a < NN; ++a) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sh.g[le][q][a][c] = gq[3 * a + c];
+            for (int c = 0; c < 3; ++c) sh.g[le][(q * NN + a) * 3 + c] = gq[3 * a + c];
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int j = 0; j < 3; ++j) H[i][j] += sh.xv[le][a][i] * sh.g[le][q][a][j];
+                for (int j = 0; j < 3; ++j) H[i][j] += sh.xv[le][3 * a + i] * sh.g[le][(q * NN + a) * 3 + j];
         }
         const double ep[6] = {H[0][0], H[1][1], H[2][2], H[0][1] + H[1][0], H[0][2] + H[2][0], H[1][2] + H[2][1]};
         const int64_t nQPtot = (int64_t)nEl * NQ;
@@ -504,17 +507,18 @@ __global__ void __launch_bounds__(kBlock) small_strain_apply_kernel(int nEl, con
         }
         // sigma = (lt 1x1 + 2 mt I_s - c1 n x n) eps   (weights already in lt, mt, c1)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) sh.sw[le][q][i] = lt * tr + 2.0 * mt * ep[i] - c1 * n[i] * ne;
+        for (int i = 0; i < 3; ++i) sh.sw[le][6 * q + i] = lt * tr + 2.0 * mt * ep[i] - c1 * n[i] * ne;
 #pragma unroll
-        for (int i = 3; i < 6; ++i) sh.sw[le][q][i] = mt * ep[i] - c1 * n[i] * ne;
+        for (int i = 3; i < 6; ++i) sh.sw[le][6 * q + i] = mt * ep[i] - c1 * n[i] * ne;
     }
     __syncthreads();
     if (!valid) return;
     for (int a = lane; a < NN; a += TPE) {
         double f0 = 0, f1 = 0, f2 = 0;
         for (int q = 0; q < NQ; ++q) {
-            const double* s = sh.sw[le][q];
-            const double gx = sh.g[le][q][a][0], gy = sh.g[le][q][a][1], gz = sh.g[le][q][a][2];
+            const double* s = &sh.sw[le][6 * q];
+            const double* gg = &sh.g[le][(q * NN + a) * 3];
+            const double gx = gg[0], gy = gg[1], gz = gg[2];
             f0 += s[0] * gx + s[3] * gy + s[4] * gz;
             f1 += s[3] * gx + s[1] * gy + s[5] * gz;
             f2 += s[4] * gx + s[5] * gy + s[2] * gz;
