@@ -450,6 +450,7 @@ struct ef_ctx {
     float amgAlpha = 1.5f;
     int amgCycle = 2;  // 1: V-cycle, 2: W-cycle below the finest level
     int amgPre = 2, amgPost = 2;  // block-Jacobi sweeps before / after the coarse correction
+    int amgPreC = 2, amgPostC = 2;  // the same on the coarse levels
     int amgWLevels = 1;           // coarse levels 1..amgWLevels repeat their coarse correction
     // the whole preconditioner application captured once as a CUDA graph (fixed in/out buffers)
     float *vcIn = nullptr, *vcOut = nullptr;
@@ -1657,6 +1658,10 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_PRE")) c->amgPre = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_POST")) c->amgPost = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_WLEVELS")) c->amgWLevels = std::max(0, atoi(e));
+    c->amgPreC = c->amgPre;
+    c->amgPostC = c->amgPost;
+    if (const char* e = getenv("EF_AMG_PRE_COARSE")) c->amgPreC = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_POST_COARSE")) c->amgPostC = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
@@ -1836,7 +1841,7 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         ops.push_back(o);
     };
     float* x2 = L.x2;
-    float* cur = ((c->amgPre + c->amgPost) & 1) ? x : x2;
+    float* cur = ((c->amgPreC + c->amgPostC) & 1) ? x : x2;
     {
         ef::CoarseOp o = op(ef::COP_BJ, L.nN);
         o.f1 = L.binv;
@@ -1846,7 +1851,7 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         o.omega = omega;
         ops.push_back(o);
     }
-    for (int k = 1; k < c->amgPre; ++k) {
+    for (int k = 1; k < c->amgPreC; ++k) {
         float* nxt = cur == x ? x2 : x;
         sweep(cur, nxt);
         cur = nxt;
@@ -1880,7 +1885,7 @@ static void amg_cycle_ops(const ef_ctx* c, int l, const float* r, float* x, std:
         pr.omega = c->amgAlpha;
         ops.push_back(pr);
     }
-    for (int k = 0; k < c->amgPost; ++k) {
+    for (int k = 0; k < c->amgPostC; ++k) {
         float* nxt = cur == x ? x2 : x;
         sweep(cur, nxt);
         cur = nxt;
@@ -1908,8 +1913,8 @@ static ef_status amg_prepare_cluster(ef_ctx* c) {
     // level lc's iterate at its coarse correction: amg_vcycle's buffer alternation of the
     // pre-smoothing replayed (level lc's output vector is L.x, its second vector L.x2)
     float* x = L.x;
-    float* cur = ((c->amgPre + c->amgPost) & 1) ? x : L.x2;
-    for (int k = 1; k < c->amgPre; ++k) cur = cur == x ? L.x2 : x;
+    float* cur = ((c->amgPreC + c->amgPostC) & 1) ? x : L.x2;
+    for (int k = 1; k < c->amgPreC; ++k) cur = cur == x ? L.x2 : x;
     std::vector<ef::CoarseOp> ops;
     ef::CoarseOp rs{};
     rs.type = ef::COP_RESTRICT;
@@ -2178,14 +2183,15 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     // The sweeps (the first from zero) alternate between x and a second vector; the first goes
     // to the second vector when their total count is even, so that the last one lands in x.
     float* x2 = fine ? c->fineX : c->amg[l - 1].x2;
+    const int nPre = fine ? c->amgPre : c->amgPreC, nPost = fine ? c->amgPost : c->amgPostC;
     float* cur = x;
-    if (!c->amgCheb) cur = ((c->amgPre + c->amgPost) & 1) ? x : x2;
+    if (!c->amgCheb) cur = ((nPre + nPost) & 1) ? x : x2;
     // pre-smoothing from zero
     if (c->amgCheb) {
         EF_CHECK(chebyshev(true));
     } else {
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, cur, 0, s));
-        for (int k = 1; k < c->amgPre; ++k) {
+        for (int k = 1; k < nPre; ++k) {
             float* nxt = cur == x ? x2 : x;
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;
@@ -2217,7 +2223,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     if (c->amgCheb) {
         EF_CHECK(chebyshev(false));
     } else {
-        for (int k = 0; k < c->amgPost; ++k) {
+        for (int k = 0; k < nPost; ++k) {
             float* nxt = cur == x ? x2 : x;
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;
