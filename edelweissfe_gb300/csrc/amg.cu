@@ -60,8 +60,8 @@ __device__ __forceinline__ void pblock(const float* __restrict__ d, float P[BF][
     }
 }
 
-// coarse block S = sum over finer blocks f = (m, n) of P_m^T A_f P_n; on level 0 masked fine
-// rows/columns are left out; dead coarse DOFs get identity rows/columns
+// coarse block S = sum over finer blocks f = (m, n) of P_m^T A_f P_n (fixed order); on level 0
+// masked fine rows/columns are left out; dead coarse DOFs get identity rows/columns
 template <int BF>
 __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict__ seg, const int32_t* __restrict__ src,
                                 const int32_t* __restrict__ fineRowOfBlock, const int32_t* __restrict__ fineCol,
@@ -71,11 +71,13 @@ __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict
                                 float* __restrict__ coarseVals) {
     const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (S >= nCoarseBlocks) return;
-    double acc[BC][BC];
+    // compensated FP32 sums (TwoSum: value hi + lo), no FP64: on this GPU the FP64 pipe, and in
+    // particular its FP32 -> FP64 conversions, bounded this kernel
+    float acc[BC][BC], lo[BC][BC];
 #pragma unroll
     for (int i = 0; i < BC; ++i)
 #pragma unroll
-        for (int j = 0; j < BC; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < BC; ++j) acc[i][j] = lo[i][j] = 0.f;
     for (int64_t t = seg[S]; t < seg[S + 1]; ++t) {
         const int32_t f = src[t];
         const int m = fineRowOfBlock[f], n = fineCol[f];
@@ -109,7 +111,10 @@ __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict
                 float s = 0.f;
 #pragma unroll
                 for (int k = 0; k < BF; ++k) s += Pm[k][i] * AP[k][j];
-                acc[i][j] += (double)s;
+                const float t = __fadd_rn(acc[i][j], s);
+                const float bv = __fsub_rn(t, acc[i][j]);
+                lo[i][j] = __fadd_rn(lo[i][j], __fadd_rn(__fsub_rn(acc[i][j], __fsub_rn(t, bv)), __fsub_rn(s, bv)));
+                acc[i][j] = t;
             }
     }
     const int I = coarseRowOfBlock[S], J = coarseCol[S];
@@ -117,9 +122,9 @@ __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict
     for (int i = 0; i < BC; ++i)
 #pragma unroll
         for (int j = 0; j < BC; ++j) {
-            double a = acc[i][j];
-            if (coarseDead[BC * I + i] || coarseDead[BC * J + j]) a = (I == J && i == j) ? 1.0 : 0.0;
-            coarseVals[S * BC * BC + i * BC + j] = (float)a;
+            float a = __fadd_rn(acc[i][j], lo[i][j]);
+            if (coarseDead[BC * I + i] || coarseDead[BC * J + j]) a = (I == J && i == j) ? 1.f : 0.f;
+            coarseVals[S * BC * BC + i * BC + j] = a;
         }
 }
 
@@ -425,69 +430,73 @@ __global__ void prolong_kernel(int nN, const int32_t* __restrict__ agg, const fl
 constexpr int kMaxCoarsestDof = 96;
 __global__ void coarsest_inverse_kernel(int nN, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
                                         const float* __restrict__ vals, float* __restrict__ inv) {
-    extern __shared__ double smemA[];
+    // FP32 Gauss-Jordan on [A | I] in shared memory (one CTA; the FP64 version spent ~1.5 ms in
+    // the FP64 pipe of a single SM); pivots below 1e-6 of the largest diagonal entry mark a null
+    // direction (FP32 round-off of a zero pivot is ~1e-7 of it)
+    extern __shared__ float smemF[];
     const int n = BC * nN;
     const int ld = 2 * n + 1;
-    auto A = [&](int r, int c) -> double& { return smemA[r * ld + c]; };
+    auto A = [&](int r, int c) -> float& { return smemF[r * ld + c]; };
     __shared__ int piv;
-    __shared__ double dmax;
+    __shared__ float dmax;
     __shared__ unsigned char drop[kMaxCoarsestDof];
-    for (int i = threadIdx.x; i < n * 2 * n; i += blockDim.x) {
-        const int r = i / (2 * n), c = i % (2 * n);
-        A(r, c) = (c >= n && c - n == r) ? 1.0 : 0.0;
-    }
+    for (int r = threadIdx.y; r < n; r += blockDim.y)
+        for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) A(r, c) = (c >= n && c - n == r) ? 1.f : 0.f;
     __syncthreads();
-    for (int m = threadIdx.x; m < nN; m += blockDim.x)
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    for (int m = tid; m < nN; m += nt)
         for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k) {
             const int cn = colIdx[k];
             for (int i = 0; i < BC; ++i)
-                for (int j = 0; j < BC; ++j) A(BC * m + i, BC * cn + j) = (double)vals[(int64_t)k * BC * BC + i * BC + j];
+                for (int j = 0; j < BC; ++j) A(BC * m + i, BC * cn + j) = vals[(int64_t)k * BC * BC + i * BC + j];
         }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double d = 0.0;
-        for (int i = 0; i < n; ++i) d = fmax(d, fabs(A(i, i)));
+    if (tid == 0) {
+        float d = 0.f;
+        for (int i = 0; i < n; ++i) d = fmaxf(d, fabsf(A(i, i)));
         dmax = d;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) drop[i] = 0;
+    for (int i = tid; i < n; i += nt) drop[i] = 0;
     __syncthreads();
     for (int col = 0; col < n; ++col) {
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             int p = col;
-            double best = fabs(A(col, col));
+            float best = fabsf(A(col, col));
             for (int r = col + 1; r < n; ++r)
-                if (fabs(A(r, col)) > best) {
-                    best = fabs(A(r, col));
+                if (fabsf(A(r, col)) > best) {
+                    best = fabsf(A(r, col));
                     p = r;
                 }
-            piv = best > 1e-10 * dmax ? p : -1;
+            piv = best > 1e-6f * dmax ? p : -1;
             if (piv < 0) drop[col] = 1;
         }
         __syncthreads();
         if (piv < 0) continue;
         if (piv != col)
-            for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) {
-                const double tmp = A(col, c);
+            for (int c = tid; c < 2 * n; c += nt) {
+                const float tmp = A(col, c);
                 A(col, c) = A(piv, c);
                 A(piv, c) = tmp;
             }
         __syncthreads();
-        const double d = A(col, col);
+        const float d = A(col, col);
         __syncthreads();
-        for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) A(col, c) /= d;
+        for (int c = tid; c < 2 * n; c += nt) A(col, c) /= d;
         __syncthreads();
-        for (int i = threadIdx.x; i < n * 2 * n; i += blockDim.x) {
-            const int r = i / (2 * n), c = i % (2 * n);
-            if (r != col && c != col) A(r, c) -= A(r, col) * A(col, c);
+        for (int r = threadIdx.y; r < n; r += blockDim.y) {
+            if (r == col) continue;
+            const float f = A(r, col);
+            for (int c = threadIdx.x; c < 2 * n; c += blockDim.x)
+                if (c != col) A(r, c) -= f * A(col, c);
         }
         __syncthreads();
-        for (int r = threadIdx.x; r < n; r += blockDim.x)
-            if (r != col) A(r, col) = 0.0;
+        for (int r = tid; r < n; r += nt)
+            if (r != col) A(r, col) = 0.f;
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+    for (int i = tid; i < n * n; i += nt) {
         const int r = i / n, c = i % n;
-        inv[i] = (drop[r] || drop[c]) ? 0.f : (float)A(r, n + c);
+        inv[i] = (drop[r] || drop[c]) ? 0.f : A(r, n + c);
     }
 }
 
@@ -874,9 +883,9 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
         ef_set_error("coarsest level too large for the dense solve");
         return EF_ERR_ARG;
     }
-    const size_t smem = sizeof(double) * BC * nN * (2 * BC * nN + 1);
+    const size_t smem = sizeof(float) * BC * nN * (2 * BC * nN + 1);
     EF_CUDA(cudaFuncSetAttribute(coarsest_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    coarsest_inverse_kernel<<<1, 256, smem, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, inv);
+    coarsest_inverse_kernel<<<1, dim3(32, 32), smem, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, inv);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

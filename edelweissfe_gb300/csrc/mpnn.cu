@@ -523,28 +523,30 @@ __global__ void bf16_to_f32_kernel(int n, const __nv_bfloat16* __restrict__ pb, 
 // mode 0: z . e; mode 3: z^2 per 3-wide feature group of f ([n][9], no mask)
 __global__ void sumsq_partial_kernel(int64_t n, int groups, const float* __restrict__ z, const float* __restrict__ e,
                                      const uint8_t* __restrict__ mask, double* __restrict__ part) {
-    __shared__ double red[8][3];
-    double acc[3] = {0.0, 0.0, 0.0};
+    // per-thread and per-warp sums in FP32 (a thread holds a few elements), the CTA's warp sums
+    // and the sum over CTAs in FP64: FP64 is a narrow pipe on this GPU
+    __shared__ float red[8][3];
+    float acc[3] = {0.f, 0.f, 0.f};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (groups == 0) {
             if (mask && mask[i]) continue;
-            acc[0] += (double)z[i] * (double)e[i];
+            acc[0] = fmaf(z[i], e[i], acc[0]);
         } else if (groups == 3) {
             const int g = (int)((i % FIN) / 3);
-            const double v = z[i];
-            acc[0] += g == 0 ? v * v : 0.0;
-            acc[1] += g == 1 ? v * v : 0.0;
-            acc[2] += g == 2 ? v * v : 0.0;
+            const float v = z[i];
+            acc[0] += g == 0 ? v * v : 0.f;
+            acc[1] += g == 1 ? v * v : 0.f;
+            acc[2] += g == 2 ? v * v : 0.f;
         } else {
             if (mask && mask[i]) continue;
-            const double d = (double)z[i] - (e ? (double)e[i] : 0.0);
-            acc[0] += d * d;
+            const float d = z[i] - (e ? e[i] : 0.f);
+            acc[0] = fmaf(d, d, acc[0]);
         }
     }
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 #pragma unroll
     for (int g = 0; g < 3; ++g) {
-        double a = acc[g];
+        float a = acc[g];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) red[wp][g] = a;
@@ -552,17 +554,20 @@ __global__ void sumsq_partial_kernel(int64_t n, int groups, const float* __restr
     __syncthreads();
     if (threadIdx.x < 3) {
         double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += (double)red[w][threadIdx.x];
         part[(int64_t)blockIdx.x * 3 + threadIdx.x] = t;
     }
 }
 
+// out[g] = sum_c part[c][g], one warp per g: lane-strided sums, then a fixed shuffle tree
 __global__ void sumsq_final_kernel(int nPart, const double* __restrict__ part, double* __restrict__ out) {
-    const int g = threadIdx.x;
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (g >= 3) return;
     double t = 0.0;
-    for (int c = 0; c < nPart; ++c) t += part[(int64_t)c * 3 + g];
-    out[g] = t;
+    for (int c = lane; c < nPart; c += 32) t += part[(int64_t)c * 3 + g];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[g] = t;
 }
 
 __global__ void scale_inplace_kernel(int64_t n, float* __restrict__ x, float a) {
@@ -720,7 +725,7 @@ ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s) 
 ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
                         int nPart, double* out, cudaStream_t s) {
     sumsq_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, groups, z, e, mask, part);
-    sumsq_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
+    sumsq_final_kernel<<<1, 96, 0, ef::counted(s)>>>(nPart, part, out);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
