@@ -60,8 +60,8 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
     ap.add_argument("--no-learned-jacobi", action="store_true",
                     help="skip the learned correction's measurement over the block-Jacobi base")
-    ap.add_argument("--learned-jacobi-rtol", type=float, default=1e-3,
-                    help="relative residual of the solves of that measurement")
+    ap.add_argument("--learned-jacobi-budget", type=int, default=2000,
+                    help="Krylov iterations of each solve of that measurement")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--restart", type=int, default=64, help="FGMRES restart length")
     ap.add_argument("--inner-rtol", type=float, default=1e-5, help="relative tolerance of one inner (FP32) solve")
@@ -173,34 +173,48 @@ def assembly_bytes(info, nEl, fp32=True):
     return elem, cond, scatter
 
 
-def learned_over_jacobi(s, rtol, epochs=60, lr=1e-3):
-    """FGMRES + block Jacobi with and without the network trained on that solver's own pairs,
-    each solve to the relative residual rtol."""
+def learned_over_jacobi(s, budget, epochs=60, lr=1e-3):
+    """FGMRES + block Jacobi with and without the network trained on that solver's own pairs:
+    the FP64 relative residual that each reaches in the same number of Krylov iterations (the
+    plastic system makes FGMRES + block Jacobi stall before tight tolerances).  The pairs come
+    from solves to 1e-2."""
+    import ctypes
+
     import torch
+
+    from edelweissfe_gb300 import _lib
 
     s.enableLearnedPreconditioner(False)
     s.setFgmresPreconditioner("jacobi")
     saved = s.learnedParameters()
     saved_rtol = s.linsolver.rtol
-    s.linsolver.rtol = rtol
 
     def rhs(seed):
         b = np.random.default_rng(seed).normal(size=s.nDof)
         b[s.dirIdxHost] = 0.0
         return torch.as_tensor(b, device="cuda")
 
-    def solve(seed):
+    def capped(seed):
+        o = s.linsolver
+        opts = _lib.EfSolveOpts(_lib.EF_SOLVE_FGMRES, 1, 1e-8, o.innerRtol, budget, o.restart, o.maxRefine, 0)
+        info = _lib.EfSolveInfo()
+        b = rhs(seed)
+        x = torch.empty_like(b)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        s.linearSolve(rhs(seed))
+        st = s.lib.ef_solve(s.ctx, ctypes.byref(opts), b.data_ptr(), x.data_ptr(), ctypes.byref(info),
+                            s._stream())  # fmt: skip
         torch.cuda.synchronize()
-        return s.lastSolveInfo.iterations, time.perf_counter() - t
+        if st not in (_lib.EF_OK, _lib.EF_NOT_CONVERGED):
+            _lib.check(st, "ef_solve")
+        return info.relResidual, info.iterations, time.perf_counter() - t
 
     try:
-        off_k, off_s = solve(100)
+        off_r, off_k, off_s = capped(100)
         s.clearTrainingPairs()
         s.initLearnedPreconditioner(seed=1, maxSamples=32)
-        s.collectTrainingPairs(every=max(5, off_k // 10), maxPerSolve=8, kind="iterates")
+        s.linsolver.rtol = 1e-2
+        s.collectTrainingPairs(every=10, maxPerSolve=8, kind="iterates")
         for k in range(4):
             s.linearSolve(rhs(k))
         s.collectTrainingPairs(0, 0)
@@ -210,12 +224,12 @@ def learned_over_jacobi(s, rtol, epochs=60, lr=1e-3):
         torch.cuda.synchronize()
         train_s = time.time() - t0
         s.enableLearnedPreconditioner(True)
-        on_k, on_s = solve(100)
-        return {"base": "block Jacobi", "rtol": rtol, "pairs": s.numTrainingPairs(), "epochs": epochs, "loss_first": lf,
-                "loss_last": ll, "train_s": train_s, "off_krylov": off_k, "on_krylov": on_k, "off_s": off_s,
-                "on_s": on_s, "krylov_ratio": off_k / on_k if on_k else None}  # fmt: skip
-    except Exception as ex:  # a solve that stalls is reported, not fatal to the bench
-        return {"base": "block Jacobi", "rtol": rtol, "error": f"{type(ex).__name__}: {ex}"}
+        on_r, on_k, on_s = capped(100)
+        return {"base": "block Jacobi", "krylov_budget": budget, "pairs": s.numTrainingPairs(), "epochs": epochs,
+                "loss_first": lf, "loss_last": ll, "train_s": train_s, "off_relres": off_r, "on_relres": on_r,
+                "off_krylov": off_k, "on_krylov": on_k, "off_s": off_s, "on_s": on_s}  # fmt: skip
+    except Exception as ex:  # reported, not fatal to the bench
+        return {"base": "block Jacobi", "krylov_budget": budget, "error": f"{type(ex).__name__}: {ex}"}
     finally:
         s.linsolver.rtol = saved_rtol
         s.enableLearnedPreconditioner(False)
@@ -410,7 +424,7 @@ def run_ours(a):
     # from the plain FGMRES + block-Jacobi solves of random right-hand sides, GPU training, then
     # one solve of a new right-hand side with and without the trained network
     if learned and not a.no_learned_jacobi:
-        learned_info["over_jacobi"] = learned_over_jacobi(s, a.learned_jacobi_rtol)
+        learned_info["over_jacobi"] = learned_over_jacobi(s, a.learned_jacobi_budget)
 
     peaks, peak_kind = measured_peaks()
     sb = spmv_bytes(info)
