@@ -569,6 +569,15 @@ __global__ void __cluster_dims__(kCoarseCtas, 1, 1) __launch_bounds__(kCoarseThr
     }
 }
 
+// x /= sqrt(*n2) (x stays when *n2 is not positive): the power iteration's normalisation with the
+// norm left on the device
+__global__ void scale_rnorm_kernel(int64_t n, float* __restrict__ x, const double* __restrict__ n2) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = *n2;
+    if (v > 0.0) x[i] *= (float)(1.0 / sqrt(v));
+}
+
 // deterministic pseudo-random start vector in [-0.5, 0.5) (integer hash of the index)
 __global__ void fill_hash_kernel(int64_t n, float* __restrict__ x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -901,6 +910,13 @@ int ef_coarse_cycle_threads() { return kCoarseCtas * kCoarseThreads; }
 
 ef_status ef_launch_coarse_cycle(const ef::CoarseOp* ops, int nOps, cudaStream_t s) {
     coarse_cycle_kernel<<<kCoarseCtas, kCoarseThreads, 0, ef::counted(s)>>>(ops, nOps);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_scale_rnorm(int64_t n, float* x, const double* n2, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    scale_rnorm_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, x, n2);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -66,6 +66,7 @@ ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* off
 ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                      float* inv, cudaStream_t s);
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
+ef_status ef_launch_scale_rnorm(int64_t n, float* x, const double* n2, cudaStream_t s);
 ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* mask, float a, float b, const float* t,
                               float* d, float* x, int first, cudaStream_t s);
 ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
@@ -443,6 +444,8 @@ struct ef_ctx {
     ef::CoarseOp* dCoarseOps = nullptr;     // its phase program (device)
     int nCoarseOps = 0, nCoarseOpsCap = 0;
     float* clusterCur = nullptr;            // level clusterLevel's iterate that the program updates
+    double* amgNorms = nullptr;             // power-iteration norms of the damping estimate
+    int amgNormsCap = 0;
     std::vector<float> levelLam;            // per smoothed level: estimated lambda_max(D^-1 A), quantised
     std::vector<float*> chebD;              // per smoothed level: Chebyshev direction vector
     void* dBsrValsH = nullptr;
@@ -631,6 +634,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->vcOut);
     if (c->vcGraph) cudaGraphExecDestroy(c->vcGraph);
     if (c->dCoarseOps) cudaFree(c->dCoarseOps);
+    if (c->amgNorms) cudaFree(c->amgNorms);
     if (c->egExec) cudaGraphExecDestroy(c->egExec);
     if (c->nnGraph) cudaGraphExecDestroy(c->nnGraph);
     for (void* p : {(void*)c->nnP, (void*)c->nnPf, (void*)c->nnM1, (void*)c->nnM2, (void*)c->nnG, c->nnPb,
@@ -2029,8 +2033,16 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
     }
     const int nL = (int)c->amg.size();
     const int BCo = ef_amg_coarse_dofs();
+    constexpr int kPow = 13;  // power-iteration steps per level
+    if (!c->amgNorms || c->amgNormsCap < 3 * kPow * nL) {
+        if (c->amgNorms) cudaFree(c->amgNorms);
+        c->amgNorms = dalloc<double>((size_t)3 * kPow * nL, &st);
+        if (!c->amgNorms) return st;
+        c->amgNormsCap = 3 * kPow * nL;
+    }
     std::vector<float> om(nL), lamq(nL);
-    double* out = c->nnRed + 3 * c->nnPartN;
+    // all levels' iterations stay on the device (normalisation by the device-side norm); one
+    // transfer of the norms at the end
     for (int l = 0; l < nL; ++l) {
         const bool fine = l == 0;
         const int bs = fine ? 3 : BCo;
@@ -2044,20 +2056,22 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
         float* a = c->amgPow[0];
         float* b = c->amgPow[1];
         EF_CHECK(ef_launch_fill_hash(n, a, s));
-        double prev = 0.0, lam = 0.0;
-        for (int it = 0; it < 13; ++it) {
-            EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, out, s));
-            double nn2 = 0.0;
-            EF_CUDA(cudaMemcpyAsync(&nn2, out, sizeof(double), cudaMemcpyDeviceToHost, s));
-            EF_CUDA(cudaStreamSynchronize(s));
-            const double nrm = sqrt(nn2);
-            if (it > 0) lam = nrm / prev;
-            if (!(nrm > 0.0)) break;
-            EF_CHECK(ef_mpnn_scale(n, a, (float)(1.0 / nrm), s));
-            prev = 1.0;
+        for (int it = 0; it < kPow; ++it) {
+            double* n2 = c->amgNorms + 3 * (l * kPow + it);
+            EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, n2, s));
+            if (it + 1 == kPow) break;
+            EF_CHECK(ef_launch_scale_rnorm(n, a, n2, s));
             EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, a, c->amgZero, mask, b, s));  // -A a
             EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
         }
+    }
+    std::vector<double> hn(3 * (size_t)kPow * nL);
+    EF_CUDA(cudaMemcpyAsync(hn.data(), c->amgNorms, sizeof(double) * hn.size(), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    for (int l = 0; l < nL; ++l) {
+        // lambda: |D^-1 A a| for the unit vector a of the last step
+        const double n2 = hn[3 * (l * kPow + kPow - 1)];
+        const double lam = n2 > 0.0 ? sqrt(n2) : 0.0;
         float w = c->amgOmega;
         if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.85)  // close to the stability limit 2
             w = std::max(1.f, std::round((float)(4.0 / (3.0 * lam)) * 64.f)) / 64.f;
