@@ -289,11 +289,13 @@ __device__ __forceinline__ float2 ldv2(const float* p) {
     if (CG) return __ldcg(reinterpret_cast<const float2*>(p));
     return *reinterpret_cast<const float2*>(p);
 }
-template <bool CG>
+// H: the block values come from a BF16 copy (valsH, 6 values = three 4-byte words per block row)
+template <bool CG, bool H = false>
 __device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __restrict__ rowPtr,
                                            const int32_t* __restrict__ colIdx, const float* __restrict__ vals,
                                            const float* x, const float* r, const uint8_t* __restrict__ mask, float* t,
-                                           const float* __restrict__ binv, float omega) {
+                                           const float* __restrict__ binv, float omega,
+                                           const uint32_t* __restrict__ valsH = nullptr) {
     const int g = lane / BC, ri = lane - BC * g;
     float acc = 0.f;
     if (g < 5) {
@@ -308,10 +310,19 @@ __device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __res
                 c[u] = -1;
                 if (k < e) {
                     c[u] = BC * colIdx[k];
-                    const float2* v = reinterpret_cast<const float2*>(vals + (int64_t)k * BC * BC + BC * ri);
-                    a[u][0] = v[0];
-                    a[u][1] = v[1];
-                    a[u][2] = v[2];
+                    if (H) {
+                        const uint32_t* v = valsH + ((int64_t)k * BC * BC + BC * ri) / 2;
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const uint32_t w = v[q];
+                            a[u][q] = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+                        }
+                    } else {
+                        const float2* v = reinterpret_cast<const float2*>(vals + (int64_t)k * BC * BC + BC * ri);
+                        a[u][0] = v[0];
+                        a[u][1] = v[1];
+                        a[u][2] = v[2];
+                    }
                 }
             }
 #pragma unroll
@@ -345,11 +356,21 @@ __global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int3
                                                                const float* __restrict__ vals,
                                                                const float* __restrict__ x, const float* __restrict__ r,
                                                                const uint8_t* __restrict__ mask, float* __restrict__ t,
-                                                               const float* __restrict__ binv, float omega) {
+                                                               const float* __restrict__ binv, float omega,
+                                                               const uint32_t* __restrict__ valsH) {
     const int lane = threadIdx.x & 31;
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (m >= nN) return;
-    resid6_row<false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega);
+    if (valsH)
+        resid6_row<false, true>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, valsH);
+    else
+        resid6_row<false, false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega);
+}
+
+// BF16 copy of FP32 values (coarse-level blocks for the smoothing residuals)
+__global__ void to_bf16_kernel(int64_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = __float2bfloat16(src[i]);
 }
 
 // rc[I] = sum over members m of aggregate I of P_m^T t[m]; one warp per aggregate, members
@@ -855,13 +876,13 @@ ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* m
 // binv == nullptr: t = r - A x; otherwise one smoothing sweep t = x + omega D^-1 (r - A x)
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
-                                   const float* binv, float omega) {
+                                   const float* binv, float omega, const void* valsH) {
     if (bs == 3)
         level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r,
                                                                                         mask, t, binv, omega);
     else
-        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r,
-                                                                                       mask, t, binv, omega);
+        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(
+            nN, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, (const uint32_t*)valsH);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -910,6 +931,13 @@ int ef_coarse_cycle_threads() { return kCoarseCtas * kCoarseThreads; }
 
 ef_status ef_launch_coarse_cycle(const ef::CoarseOp* ops, int nOps, cudaStream_t s) {
     coarse_cycle_kernel<<<kCoarseCtas, kCoarseThreads, 0, ef::counted(s)>>>(ops, nOps);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    to_bf16_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, src, (__nv_bfloat16*)dst);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

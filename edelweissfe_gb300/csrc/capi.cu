@@ -58,7 +58,8 @@ ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* m
                              float* x, int accumulate, cudaStream_t s);
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
-                                   const float* binv = nullptr, float omega = 0.f);
+                                   const float* binv = nullptr, float omega = 0.f, const void* valsH = nullptr);
+ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
                              const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s);
 ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
@@ -356,6 +357,7 @@ struct AmgLevel {
     int32_t* gsrc = nullptr;
     float *x = nullptr, *r = nullptr, *t = nullptr;  // V-cycle work vectors of this level
     float* x2 = nullptr;                             // second smoothing iterate (sweeps alternate)
+    uint16_t* valsH = nullptr;                       // BF16 copy of vals for the smoothing residuals
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
 };
@@ -438,6 +440,7 @@ struct ef_ctx {
     float* amgZero = nullptr;
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
+    bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
     int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel
@@ -619,6 +622,7 @@ void ef_destroy(ef_ctx* c) {
         F(L.gsrc);
         F(L.x);
         F(L.x2);
+        F(L.valsH);
         F(L.r);
         F(L.t);
     }
@@ -1671,6 +1675,7 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
     if (const char* e = getenv("EF_AMG_SMOOTHER")) c->amgCheb = strcmp(e, "cheb") == 0;
     if (const char* e = getenv("EF_AMG_CLUSTER")) c->amgCluster = atoi(e) != 0;
+    if (const char* e = getenv("EF_AMG_BF16_COARSE")) c->amgBf16Coarse = atoi(e) != 0;
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;
     const int BCo = ef_amg_coarse_dofs();
@@ -1780,6 +1785,10 @@ static ef_status amg_build(ef_ctx* c) {
         L.t = dalloc<float>((size_t)BCo * nC, &st);
         L.x2 = dalloc<float>((size_t)BCo * nC, &st);
         if (!L.vals || !L.binv || !L.dead || !L.x || !L.r || !L.t || !L.x2) return st;
+        if (c->amgBf16Coarse) {
+            L.valsH = dalloc<uint16_t>((size_t)L.nBlocks * BCo * BCo, &st);
+            if (!L.valsH) return st;
+        }
         c->amg.push_back(std::move(L));
         pRow = &c->amg.back().hRowPtr;
         pCol = &c->amg.back().hColIdx;
@@ -2125,6 +2134,7 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
         EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
                                     L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
         EF_CHECK(ef_launch_bj6_setup(L.nN, L.diagPos, L.vals, L.binv, s));
+        if (L.valsH) EF_CHECK(ef_launch_to_bf16(L.nBlocks * BCo * BCo, L.vals, L.valsH, s));
     }
     const AmgLevel& C = c->amg.back();
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
@@ -2154,6 +2164,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     const float* binv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
     const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
     float* t = fine ? c->fineT : c->amg[l - 1].t;
+    const void* valsH = fine ? nullptr : c->amg[l - 1].valsH;
     AmgLevel& Cn = c->amg[l];
     // fine level from the BF16 copy: staged through shared memory when the chunks fit
     auto fine_bf16 = [&](const float* xin, float* out, const float* bj, float om) -> ef_status {
@@ -2165,7 +2176,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     };
     auto residual = [&]() -> ef_status {
         if (fine && c->dBsrValsH) return fine_bf16(x, t, nullptr, 0.f);
-        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s);
+        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s, nullptr, 0.f, valsH);
     };
     // Chebyshev smoothing of degree amgSweeps on [lmax / 30, 1.1 lmax] of D^-1 A; from zero the
     // first residual is r itself
@@ -2192,7 +2203,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     // one fused damped block-Jacobi sweep xout = xin + omega D^-1 (r - A xin)
     auto sweep = [&](const float* xin, float* xout) -> ef_status {
         if (fine && c->dBsrValsH) return fine_bf16(xin, xout, binv, omega);
-        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega);
+        return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega, valsH);
     };
     // The sweeps (the first from zero) alternate between x and a second vector; the first goes
     // to the second vector when their total count is even, so that the last one lands in x.
@@ -2216,7 +2227,8 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     for (int rep = 0; rep < reps; ++rep) {
         if (!c->amgCheb) {
             EF_CHECK(fine && c->dBsrValsH ? fine_bf16(cur, t, nullptr, 0.f)
-                                          : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s));
+                                          : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s,
+                                                                     nullptr, 0.f, valsH));
         } else {
             EF_CHECK(residual());
         }
