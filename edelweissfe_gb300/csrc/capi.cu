@@ -854,6 +854,7 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         g.nPair = h.nNodes * (h.nNodes + 1) / 2;
         g.mat = h.mat;
         g.tl = h.tl;
+        if (const char* e = getenv("EF_ELEM_INTCONV")) g.intConv = atoi(e) != 0;
         g.nState = 12 + ((h.mat == MAT_VON_MISES || h.mat == MAT_NEOHOOKE_WA) ? 1 : 0);
         for (size_t i = 0; i < h.props.size() && i < 8; ++i) g.props[i] = h.props[i];
         derived_props(h.mat, g.props);

@@ -56,6 +56,7 @@ struct Group {
     int tablesSlot;       // index of the group's element table
     double* geo;          // geometry cache [nEl*nQP][3*nNodes + 1]: dN/dx and w*detJ (FP64)
     float2* geoS;         // the same values split into FP32 pairs (hi, lo = d - hi), small-strain groups
+    int intConv;          // 1: the element kernel converts FP64 <-> FP32 pairs by integer operations
     const double* propsTable;  // optional per-element material rows [nRows][8] (null: props)
     const int32_t* elemRow;    // element -> row of propsTable
 };

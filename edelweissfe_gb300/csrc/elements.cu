@@ -21,6 +21,7 @@
 
 #include <math.h>
 
+#include "dfloat_bits.h"
 #include "ef_common.cuh"
 
 namespace ef {
@@ -146,6 +147,20 @@ __host__ __device__ __forceinline__ float2 df_split(double d) {
 
 __device__ __forceinline__ double df_value(const DF& a) { return (double)a.hi + (double)a.lo; }
 
+// the same conversions by integer operations on the bit patterns (dfloat_bits.h), which keep them
+// off the FP64 pipe; hi is truncated instead of rounded (the pair still holds 47 bits)
+__device__ __forceinline__ float2 df_split_i(double d) {
+    uint32_t h, l;
+    split_bits((uint64_t)__double_as_longlong(d), &h, &l);
+    return make_float2(__uint_as_float(h), __uint_as_float(l));
+}
+__device__ __forceinline__ double widen_i(float f) { return __longlong_as_double((long long)widen_bits(__float_as_uint(f))); }
+__device__ __forceinline__ double df_value_i(const DF& a) { return widen_i(a.hi) + widen_i(a.lo); }
+__device__ __forceinline__ float2 df_split_sel(double d, int intConv) { return intConv ? df_split_i(d) : df_split(d); }
+__device__ __forceinline__ double df_value_sel(const DF& a, int intConv) {
+    return intConv ? df_value_i(a) : df_value(a);
+}
+
 // acc += a * b for a = (ah, al), b = (bh, bl): the product ah bh exactly (its rounding error from
 // an FMA), the cross terms ah bl + al bh in FP32 (relative 2^-24 of the product), al bl dropped
 // (2^-48); the sum with acc.hi by TwoSum, every error term into acc.lo
@@ -263,7 +278,7 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
     int nEl, const int32_t* __restrict__ nodeDof, const float2* __restrict__ geoS, const double* __restrict__ dU,
     const double* __restrict__ stateIn, double* __restrict__ stateOut, PropsArg props,
     const double* __restrict__ propsTable, const int32_t* __restrict__ elemRow, KT* __restrict__ Kout,
-    double* __restrict__ Pe, double* __restrict__ tang, int* __restrict__ flags) {
+    double* __restrict__ Pe, double* __restrict__ tang, int* __restrict__ flags, int intConv) {
     constexpr int TPE = (NQ <= 8) ? 8 : 32;
     constexpr int EPB = kBlock / TPE;
     constexpr int NP = PairTab<NN>::NP;
@@ -280,9 +295,9 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
     if (valid) {
         for (int a = lane; a < NN; a += TPE) {
             const int d = nodeDof[(int64_t)e * NN + a];
-            sh.du[le][3 * a + 0] = df_split(dU[d + 0]);
-            sh.du[le][3 * a + 1] = df_split(dU[d + 1]);
-            sh.du[le][3 * a + 2] = df_split(dU[d + 2]);
+            sh.du[le][3 * a + 0] = df_split_sel(dU[d + 0], intConv);
+            sh.du[le][3 * a + 1] = df_split_sel(dU[d + 1], intConv);
+            sh.du[le][3 * a + 2] = df_split_sel(dU[d + 2], intConv);
         }
     }
     __syncthreads();
@@ -313,10 +328,12 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
             }
         }
         const float2 wq = gq[3 * NN];
-        const double wdet = (double)wq.x + (double)wq.y;
-        const double de[6] = {df_value(H[0][0]), df_value(H[1][1]), df_value(H[2][2]),
-                              df_value(H[0][1]) + df_value(H[1][0]), df_value(H[0][2]) + df_value(H[2][0]),
-                              df_value(H[1][2]) + df_value(H[2][1])};
+        const double wdet = df_value_sel(DF{wq.x, wq.y}, intConv);
+        const double de[6] = {df_value_sel(H[0][0], intConv), df_value_sel(H[1][1], intConv),
+                              df_value_sel(H[2][2], intConv),
+                              df_value_sel(H[0][1], intConv) + df_value_sel(H[1][0], intConv),
+                              df_value_sel(H[0][2], intConv) + df_value_sel(H[2][0], intConv),
+                              df_value_sel(H[1][2], intConv) + df_value_sel(H[2][1], intConv)};
         const int64_t nQPtot = (int64_t)nEl * NQ;
         const int64_t qi = (int64_t)e * NQ + q;
         double sig[6];
@@ -339,7 +356,7 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
             if (!(sig[i] == sig[i])) atomicOr(flags, EF_FLAG_NAN);
         }
 #pragma unroll
-        for (int i = 0; i < 6; ++i) sh.sw[le][6 * q + i] = df_split(sig[i] * wdet);
+        for (int i = 0; i < 6; ++i) sh.sw[le][6 * q + i] = df_split_sel(sig[i] * wdet, intConv);
         if (tang) {
             // FP64 tangent of this Gauss point for the exact (matrix-free) refinement residual
             tang[0 * nQPtot + qi] = mo.lt * wdet;
@@ -378,9 +395,9 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
             df_fma(f2, s[2], gz);
         }
         double* pe = Pe + (int64_t)e * ND + 3 * a;
-        pe[0] = -df_value(f0);
-        pe[1] = -df_value(f1);
-        pe[2] = -df_value(f2);
+        pe[0] = -df_value_sel(f0, intConv);
+        pe[1] = -df_value_sel(f1, intConv);
+        pe[2] = -df_value_sel(f2, intConv);
     }
 
     // ---- stiffness: K_ab = sum_q lt ga(x)gb + mt (gb(x)ga + ga.gb I) - c1 va(x)vb ----
@@ -569,12 +586,12 @@ static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, d
         auto k = small_strain_kernel<NN, NQ, KT, MAT, true>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geoS, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
-                                                  (KT*)K, Pe, tang, flags);
+                                                  (KT*)K, Pe, tang, flags, g.intConv);
     } else {
         auto k = small_strain_kernel<NN, NQ, KT, MAT, false>;
         EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kBlock, smem, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geoS, dU, sIn, sOut, pa, g.propsTable, g.elemRow,
-                                                  (KT*)K, Pe, tang, flags);
+                                                  (KT*)K, Pe, tang, flags, g.intConv);
     }
     EF_CUDA(cudaGetLastError());
     return EF_OK;

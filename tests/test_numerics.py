@@ -55,3 +55,26 @@ def test_split_is_exact_to_48_bits():
     lo = (d - hi.astype(np.float64)).astype(np.float32)
     rel = np.abs(hi.astype(np.float64) + lo.astype(np.float64) - d) / np.abs(d)
     assert rel.max() < 2.0**-47
+
+
+def test_integer_fp64_fp32_pair_conversions(tmp_path):
+    """The integer-only FP64 -> FP32-pair split and FP32 -> FP64 widening of the element kernel's
+    double-float operands (edelweissfe_gb300/csrc/dfloat_bits.h), compiled for the host from the
+    same source and checked against the compiler's exact conversions on 2 million values and the
+    special cases (zero, subnormal, infinity, NaN, out of range)."""
+    import os
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("no C++ compiler")
+    here = os.path.dirname(os.path.abspath(__file__))
+    exe = str(tmp_path / "dfloat_bits_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-o", exe, os.path.join(here, "native", "dfloat_bits_check.cpp")],
+                   check=True)  # fmt: skip
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "failures 0" in out.stdout
