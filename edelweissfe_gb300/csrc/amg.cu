@@ -128,6 +128,214 @@ __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict
         }
 }
 
+// ---- smoothed aggregation (index maps from amg_sa_pattern.h) -------------------------------
+// P = P_t - w D^-1 A P_t on the live finer DOFs (masked finer rows of P are zero; A with masked
+// rows and columns dropped, as in the Galerkin product), AP = A P, A_c = P^T A P: segmented sums
+// in the fixed order of the maps, FP32 with compensated accumulation for the coarse operator.
+
+// one P block per thread: b = (m = pRow[b], J = pCol[b])
+template <int BF>
+__global__ void sa_prolongator_kernel(int64_t nP, const int32_t* __restrict__ pRow, const int32_t* __restrict__ pCol,
+                                      const int64_t* __restrict__ pSeg, const int32_t* __restrict__ pSrc,
+                                      const int32_t* __restrict__ fineCol, const float* __restrict__ fineVals,
+                                      const uint8_t* __restrict__ fineMask, const float* __restrict__ offs,
+                                      const int32_t* __restrict__ agg, const float* __restrict__ binv,
+                                      const float* __restrict__ wP, float* __restrict__ Pv) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nP) return;
+    const int m = pRow[b], J = pCol[b];
+    float acc[BF][BC];
+#pragma unroll
+    for (int i = 0; i < BF; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
+    for (int64_t t = pSeg[b]; t < pSeg[b + 1]; ++t) {
+        const int32_t k = pSrc[t];
+        const int n = fineCol[k];
+        float Pn[BF][BC];
+        pblock<BF>(offs + 3 * (int64_t)n, Pn);
+        const float* v = fineVals + (int64_t)k * BF * BF;
+#pragma unroll
+        for (int i = 0; i < BF; ++i) {
+            if (fineMask && fineMask[BF * m + i]) continue;
+#pragma unroll
+            for (int q = 0; q < BF; ++q) {
+                if (fineMask && fineMask[BF * n + q]) continue;
+                const float a = v[i * BF + q];
+#pragma unroll
+                for (int j = 0; j < BC; ++j) acc[i][j] += a * Pn[q][j];
+            }
+        }
+    }
+    const float w = *wP;
+    float Pm[BF][BC];
+    pblock<BF>(offs + 3 * (int64_t)m, Pm);
+    const bool own = J == agg[m];
+    const float* B = binv + (int64_t)m * BF * BF;
+    float* out = Pv + b * BF * BC;
+#pragma unroll
+    for (int i = 0; i < BF; ++i) {
+        const bool masked = fineMask && fineMask[BF * m + i];
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            float z = 0.f;
+#pragma unroll
+            for (int q = 0; q < BF; ++q) z += B[i * BF + q] * acc[q][j];
+            out[i * BC + j] = masked ? 0.f : (own ? Pm[i][j] : 0.f) - w * z;
+        }
+    }
+}
+
+// one AP block per thread: a = (m = apRow[a], J); sum over pairs (finer block k of row m, P block)
+template <int BF>
+__global__ void sa_ap_kernel(int64_t nAP, const int32_t* __restrict__ apRow, const int64_t* __restrict__ apSeg,
+                             const int32_t* __restrict__ apK, const int32_t* __restrict__ apP,
+                             const int32_t* __restrict__ fineCol, const float* __restrict__ fineVals,
+                             const uint8_t* __restrict__ fineMask, const float* __restrict__ Pv,
+                             float* __restrict__ APv) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nAP) return;
+    const int m = apRow[a];
+    float acc[BF][BC];
+#pragma unroll
+    for (int i = 0; i < BF; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
+    for (int64_t t = apSeg[a]; t < apSeg[a + 1]; ++t) {
+        const int32_t k = apK[t];
+        const int n = fineCol[k];
+        const float* v = fineVals + (int64_t)k * BF * BF;
+        const float* P = Pv + (int64_t)apP[t] * BF * BC;
+#pragma unroll
+        for (int i = 0; i < BF; ++i) {
+            if (fineMask && fineMask[BF * m + i]) continue;
+#pragma unroll
+            for (int q = 0; q < BF; ++q) {
+                if (fineMask && fineMask[BF * n + q]) continue;
+                const float av = v[i * BF + q];
+#pragma unroll
+                for (int j = 0; j < BC; ++j) acc[i][j] += av * P[q * BC + j];
+            }
+        }
+    }
+    float* out = APv + a * BF * BC;
+#pragma unroll
+    for (int i = 0; i < BF; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) out[i * BC + j] = acc[i][j];
+}
+
+// one coarse block per thread: S = (I, J), sum over pairs (P block (m, I), AP block (m, J)) of
+// P^T AP in compensated FP32; dead coarse DOFs get identity rows and columns
+template <int BF>
+__global__ void sa_galerkin_kernel(int64_t nC, const int64_t* __restrict__ cSeg, const int32_t* __restrict__ cP,
+                                   const int32_t* __restrict__ cAP, const float* __restrict__ Pv,
+                                   const float* __restrict__ APv, const int32_t* __restrict__ coarseRowOfBlock,
+                                   const int32_t* __restrict__ coarseCol, const uint8_t* __restrict__ coarseDead,
+                                   float* __restrict__ coarseVals) {
+    const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (S >= nC) return;
+    float hi[BC][BC], lo[BC][BC];
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) hi[i][j] = lo[i][j] = 0.f;
+    for (int64_t t = cSeg[S]; t < cSeg[S + 1]; ++t) {
+        const float* P = Pv + (int64_t)cP[t] * BF * BC;
+        const float* Q = APv + (int64_t)cAP[t] * BF * BC;
+#pragma unroll
+        for (int i = 0; i < BC; ++i)
+#pragma unroll
+            for (int j = 0; j < BC; ++j) {
+                float s = 0.f;
+#pragma unroll
+                for (int q = 0; q < BF; ++q) s += P[q * BC + i] * Q[q * BC + j];
+                const float tt = __fadd_rn(hi[i][j], s);
+                const float bv = __fsub_rn(tt, hi[i][j]);
+                lo[i][j] = __fadd_rn(lo[i][j], __fadd_rn(__fsub_rn(hi[i][j], __fsub_rn(tt, bv)), __fsub_rn(s, bv)));
+                hi[i][j] = tt;
+            }
+    }
+    const int I = coarseRowOfBlock[S], J = coarseCol[S];
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            float a = __fadd_rn(hi[i][j], lo[i][j]);
+            if (coarseDead[BC * I + i] || coarseDead[BC * J + j]) a = (I == J && i == j) ? 1.f : 0.f;
+            coarseVals[S * BC * BC + i * BC + j] = a;
+        }
+}
+
+// rc[I] = sum over the P blocks b of column I (increasing finer row) of P_b^T t[row(b)]; one warp
+// per coarse node, blocks strided over the lanes, fixed shuffle tree; dead coarse DOFs -> 0
+template <int BF>
+__global__ void sa_restrict_kernel(int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ tIdx,
+                                   const int32_t* __restrict__ pRow, const float* __restrict__ Pv,
+                                   const float* __restrict__ t, const uint8_t* __restrict__ coarseDead,
+                                   float* __restrict__ rc) {
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= nC) return;
+    float a[BC];
+#pragma unroll
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    for (int k = tPtr[I] + lane; k < tPtr[I + 1]; k += 32) {
+        const int32_t b = tIdx[k];
+        const int m = pRow[b];
+        const float* P = Pv + (int64_t)b * BF * BC;
+#pragma unroll
+        for (int i = 0; i < BF; ++i) {
+            const float ti = t[BF * m + i];
+#pragma unroll
+            for (int j = 0; j < BC; ++j) a[j] += P[i * BC + j] * ti;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < BC; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+    if (lane < BC) {
+        float v = a[0];
+#pragma unroll
+        for (int j = 1; j < BC; ++j)
+            if (lane == j) v = a[j];
+        rc[BC * I + lane] = coarseDead[BC * I + lane] ? 0.f : v;
+    }
+}
+
+// x[m] += alpha sum over the P blocks of row m of P_b xc[col(b)] on free finer DOFs
+template <int BF>
+__global__ void sa_prolong_kernel(int nF, const int32_t* __restrict__ pRowPtr, const int32_t* __restrict__ pCol,
+                                  const float* __restrict__ Pv, const float* __restrict__ xc,
+                                  const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nF) return;
+    float s[BF];
+#pragma unroll
+    for (int i = 0; i < BF; ++i) s[i] = 0.f;
+    for (int b = pRowPtr[m]; b < pRowPtr[m + 1]; ++b) {
+        const float* P = Pv + (int64_t)b * BF * BC;
+        const float* c = xc + BC * (int64_t)pCol[b];
+        float cv[BC];
+#pragma unroll
+        for (int j = 0; j < BC; ++j) cv[j] = c[j];
+#pragma unroll
+        for (int i = 0; i < BF; ++i)
+#pragma unroll
+            for (int j = 0; j < BC; ++j) s[i] += P[i * BC + j] * cv[j];
+    }
+#pragma unroll
+    for (int i = 0; i < BF; ++i)
+        if (!(mask && mask[BF * m + i])) x[BF * m + i] += alpha * s[i];
+}
+
+// *wP = 4 / (3 lambda) with lambda = sqrt(*n2), the prolongator damping from the power iteration
+__global__ void sa_damping_kernel(const double* __restrict__ n2, float* __restrict__ wP) {
+    const double v = *n2;
+    *wP = v > 0.0 ? (float)(4.0 / (3.0 * sqrt(v))) : 0.f;
+}
+
 // inverse of each 6x6 diagonal block (pseudo-inverse: pivots below 1e-9 of the largest
 // diagonal entry are dropped), FP64 Gauss-Jordan in registers
 __global__ void bj6_setup_kernel(int nN, const int64_t* __restrict__ diagPos, const float* __restrict__ vals,
@@ -883,6 +1091,64 @@ ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const 
     else
         level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(
             nN, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, (const uint32_t*)valsH);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// ---- smoothed aggregation launchers ----
+ef_status ef_launch_sa_damping(const double* n2, float* wP, cudaStream_t s) {
+    sa_damping_kernel<<<1, 1, 0, ef::counted(s)>>>(n2, wP);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int32_t* pCol, const int64_t* pSeg,
+                             const int32_t* pSrc, int64_t nAP, const int32_t* apRow, const int64_t* apSeg,
+                             const int32_t* apK, const int32_t* apP, const int32_t* fineCol, const float* fineVals,
+                             const uint8_t* fineMask, const float* offs, const int32_t* agg, const float* binv,
+                             const float* wP, float* Pv, float* APv, int64_t nC, const int64_t* cSeg,
+                             const int32_t* cP, const int32_t* cAP, const int32_t* coarseRowOfBlock,
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals,
+                             cudaStream_t s) {
+#define EF_SA(BF_)                                                                                             \
+    sa_prolongator_kernel<BF_><<<nb_(nP, 128), 128, 0, ef::counted(s)>>>(nP, pRow, pCol, pSeg, pSrc, fineCol, \
+                                                                        fineVals, fineMask, offs, agg, binv,  \
+                                                                        wP, Pv);                              \
+    sa_ap_kernel<BF_><<<nb_(nAP, 128), 128, 0, ef::counted(s)>>>(nAP, apRow, apSeg, apK, apP, fineCol,        \
+                                                                fineVals, fineMask, Pv, APv);                 \
+    sa_galerkin_kernel<BF_><<<nb_(nC, 64), 64, 0, ef::counted(s)>>>(nC, cSeg, cP, cAP, Pv, APv,               \
+                                                                   coarseRowOfBlock, coarseCol, coarseDead,   \
+                                                                   coarseVals)
+    if (nP == 0 || nC == 0) return EF_OK;
+    if (bf == 3) {
+        EF_SA(3);
+    } else {
+        EF_SA(6);
+    }
+#undef EF_SA
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_restrict(int bf, int nC, const int32_t* tPtr, const int32_t* tIdx, const int32_t* pRow,
+                                const float* Pv, const float* t, const uint8_t* coarseDead, float* rc,
+                                cudaStream_t s) {
+    if (bf == 3)
+        sa_restrict_kernel<3><<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, tPtr, tIdx, pRow, Pv, t,
+                                                                                      coarseDead, rc);
+    else
+        sa_restrict_kernel<6><<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, tPtr, tIdx, pRow, Pv, t,
+                                                                                      coarseDead, rc);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_prolong(int bf, int nF, const int32_t* pRowPtr, const int32_t* pCol, const float* Pv,
+                               const float* xc, const uint8_t* mask, float* x, float alpha, cudaStream_t s) {
+    if (bf == 3)
+        sa_prolong_kernel<3><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, pCol, Pv, xc, mask, x, alpha);
+    else
+        sa_prolong_kernel<6><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, pCol, Pv, xc, mask, x, alpha);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -11,6 +11,7 @@
 #include <thread>
 #include <vector>
 
+#include "amg_sa_pattern.h"
 #include "ef_common.cuh"
 
 #include <atomic>
@@ -60,6 +61,20 @@ ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const 
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
                                    const float* binv = nullptr, float omega = 0.f, const void* valsH = nullptr);
 ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
+ef_status ef_launch_sa_damping(const double* n2, float* wP, cudaStream_t s);
+ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int32_t* pCol, const int64_t* pSeg,
+                             const int32_t* pSrc, int64_t nAP, const int32_t* apRow, const int64_t* apSeg,
+                             const int32_t* apK, const int32_t* apP, const int32_t* fineCol, const float* fineVals,
+                             const uint8_t* fineMask, const float* offs, const int32_t* agg, const float* binv,
+                             const float* wP, float* Pv, float* APv, int64_t nC, const int64_t* cSeg,
+                             const int32_t* cP, const int32_t* cAP, const int32_t* coarseRowOfBlock,
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals,
+                             cudaStream_t s);
+ef_status ef_launch_sa_restrict(int bf, int nC, const int32_t* tPtr, const int32_t* tIdx, const int32_t* pRow,
+                                const float* Pv, const float* t, const uint8_t* coarseDead, float* rc,
+                                cudaStream_t s);
+ef_status ef_launch_sa_prolong(int bf, int nF, const int32_t* pRowPtr, const int32_t* pCol, const float* Pv,
+                               const float* xc, const uint8_t* mask, float* x, float alpha, cudaStream_t s);
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
                              const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s);
 ef_status ef_launch_prolong(int bf, int nN, const int32_t* agg, const float* offs, const float* xc,
@@ -358,6 +373,13 @@ struct AmgLevel {
     float *x = nullptr, *r = nullptr, *t = nullptr;  // V-cycle work vectors of this level
     float* x2 = nullptr;                             // second smoothing iterate (sweeps alternate)
     uint16_t* valsH = nullptr;                       // BF16 copy of vals for the smoothing residuals
+    // smoothed aggregation (transition from the finer level to this one): index maps and values
+    int64_t saNP = 0, saNAP = 0;
+    int32_t *saPRowPtr = nullptr, *saPCol = nullptr, *saPRow = nullptr, *saPSrc = nullptr;
+    int32_t *saTPtr = nullptr, *saTIdx = nullptr, *saApRow = nullptr, *saApK = nullptr, *saApP = nullptr;
+    int32_t *saCP = nullptr, *saCAP = nullptr;
+    int64_t *saPSeg = nullptr, *saApSeg = nullptr, *saCSeg = nullptr;
+    float *saPv = nullptr, *saAPv = nullptr, *saW = nullptr;
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
 };
@@ -441,6 +463,7 @@ struct ef_ctx {
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
+    bool amgSmoothed = false;               // smoothed-aggregation prolongators (EF_AMG_SMOOTHED)
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
     int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel
@@ -623,6 +646,11 @@ void ef_destroy(ef_ctx* c) {
         F(L.x);
         F(L.x2);
         F(L.valsH);
+        for (void* q : {(void*)L.saPRowPtr, (void*)L.saPCol, (void*)L.saPRow, (void*)L.saPSrc, (void*)L.saTPtr,
+                        (void*)L.saTIdx, (void*)L.saApRow, (void*)L.saApK, (void*)L.saApP, (void*)L.saCP,
+                        (void*)L.saCAP, (void*)L.saPSeg, (void*)L.saApSeg, (void*)L.saCSeg, (void*)L.saPv,
+                        (void*)L.saAPv, (void*)L.saW})
+            F(q);
         F(L.r);
         F(L.t);
     }
@@ -1677,6 +1705,8 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_SMOOTHER")) c->amgCheb = strcmp(e, "cheb") == 0;
     if (const char* e = getenv("EF_AMG_CLUSTER")) c->amgCluster = atoi(e) != 0;
     if (const char* e = getenv("EF_AMG_BF16_COARSE")) c->amgBf16Coarse = atoi(e) != 0;
+    if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
+    if (c->amgSmoothed && !getenv("EF_AMG_ALPHA")) c->amgAlpha = 1.0f;  // smoothed prolongators need no over-correction
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;
     const int BCo = ef_amg_coarse_dofs();
@@ -1725,10 +1755,17 @@ static ef_status amg_build(ef_ctx* c) {
         L.hOffs.resize(3 * (size_t)nFine);
         for (int m = 0; m < nFine; ++m)
             for (int k = 0; k < 3; ++k) L.hOffs[3 * m + k] = (float)((*pPos)[3 * m + k] - L.hCentroid[3 * L.hAgg[m] + k]);
-        // coarse pattern
+        // coarse pattern: aggregate adjacency, or with smoothed prolongators the pattern of P^T A P
+        // (a superset)
         std::vector<std::vector<int32_t>> cols(nC);
-        for (int m = 0; m < nFine; ++m)
-            for (int k = (*pRow)[m]; k < (*pRow)[m + 1]; ++k) cols[L.hAgg[m]].push_back(L.hAgg[(*pCol)[k]]);
+        SAPattern SA;
+        if (c->amgSmoothed) {
+            build_sa_pattern(nFine, pRow->data(), pCol->data(), L.hAgg.data(), nC, SA);
+            for (int I = 0; I < nC; ++I) cols[I].assign(SA.cCol.begin() + SA.cRowPtr[I], SA.cCol.begin() + SA.cRowPtr[I + 1]);
+        } else {
+            for (int m = 0; m < nFine; ++m)
+                for (int k = (*pRow)[m]; k < (*pRow)[m + 1]; ++k) cols[L.hAgg[m]].push_back(L.hAgg[(*pCol)[k]]);
+        }
         L.hRowPtr.assign(nC + 1, 0);
         for (int I = 0; I < nC; ++I) {
             auto& v = cols[I];
@@ -1778,6 +1815,32 @@ static ef_status amg_build(ef_ctx* c) {
         EF_CHECK(upload(&L.aggIdx, L.hAggIdx));
         EF_CHECK(upload(&L.gseg, gcount));
         EF_CHECK(upload(&L.gsrc, gsrc));
+        if (c->amgSmoothed) {
+            L.saNP = (int64_t)SA.pCol.size();
+            L.saNAP = (int64_t)SA.apCol.size();
+            std::vector<int32_t> apRow(L.saNAP);
+            for (int m = 0; m < nFine; ++m)
+                for (int32_t a = SA.apRowPtr[m]; a < SA.apRowPtr[m + 1]; ++a) apRow[a] = m;
+            EF_CHECK(upload(&L.saPRowPtr, SA.pRowPtr));
+            EF_CHECK(upload(&L.saPCol, SA.pCol));
+            EF_CHECK(upload(&L.saPRow, SA.pRow));
+            EF_CHECK(upload(&L.saPSeg, SA.pSeg));
+            EF_CHECK(upload(&L.saPSrc, SA.pSrc));
+            EF_CHECK(upload(&L.saTPtr, SA.tPtr));
+            EF_CHECK(upload(&L.saTIdx, SA.tIdx));
+            EF_CHECK(upload(&L.saApRow, apRow));
+            EF_CHECK(upload(&L.saApSeg, SA.apSeg));
+            EF_CHECK(upload(&L.saApK, SA.apK));
+            EF_CHECK(upload(&L.saApP, SA.apP));
+            EF_CHECK(upload(&L.saCSeg, SA.cSeg));
+            EF_CHECK(upload(&L.saCP, SA.cP));
+            EF_CHECK(upload(&L.saCAP, SA.cAP));
+            const int bfL = c->amg.empty() ? 3 : BCo;
+            L.saPv = dalloc<float>((size_t)std::max<int64_t>(1, L.saNP) * bfL * BCo, &st);
+            L.saAPv = dalloc<float>((size_t)std::max<int64_t>(1, L.saNAP) * bfL * BCo, &st);
+            L.saW = dalloc<float>(1, &st);
+            if (!L.saPv || !L.saAPv || !L.saW) return st;
+        }
         L.vals = dalloc<float>((size_t)L.nBlocks * BCo * BCo, &st);
         L.binv = dalloc<float>((size_t)nC * BCo * BCo, &st);
         L.dead = dalloc<uint8_t>((size_t)BCo * nC, &st);
@@ -1914,7 +1977,7 @@ static ef_status amg_prepare_cluster(ef_ctx* c) {
     c->clusterLevel = -1;
     c->nCoarseOps = 0;
     const int nL = (int)c->amg.size();
-    if (!c->amgCluster || c->amgCheb) return EF_OK;
+    if (!c->amgCluster || c->amgCheb || c->amgSmoothed) return EF_OK;
     int lc = -1;
     for (int l = 1; l < nL; ++l)
         if (c->amg[l].nN <= kClusterMaxNodes) {
@@ -2027,7 +2090,10 @@ static void amg_dead_mask(const AmgLevel& L, int bf, const uint8_t* fineDead, st
 // smoothing is stable for omega lambda < 2.  Where amgOmega lambda exceeds 1.85 (quadratic
 // elements raise lambda well above its hex8 value of about 2) the level uses 4 / (3 lambda),
 // quantised to 1/64 so that small changes keep the captured cycle; any change re-captures it.
-static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
+static constexpr int kPowerSteps = 13;  // power-iteration steps per level
+
+// scratch of the damping estimate (allocated once)
+static ef_status amg_power_alloc(ef_ctx* c) {
     ef_status st = EF_OK;
     if (!c->amgPow[0]) {
         c->amgPow[0] = dalloc<float>(c->nDof, &st);
@@ -2042,45 +2108,54 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
         if (!c->nnRed) return st;
     }
     const int nL = (int)c->amg.size();
-    const int BCo = ef_amg_coarse_dofs();
-    constexpr int kPow = 13;  // power-iteration steps per level
-    if (!c->amgNorms || c->amgNormsCap < 3 * kPow * nL) {
+    if (!c->amgNorms || c->amgNormsCap < 3 * kPowerSteps * nL) {
         if (c->amgNorms) cudaFree(c->amgNorms);
-        c->amgNorms = dalloc<double>((size_t)3 * kPow * nL, &st);
+        c->amgNorms = dalloc<double>((size_t)3 * kPowerSteps * nL, &st);
         if (!c->amgNorms) return st;
-        c->amgNormsCap = 3 * kPow * nL;
+        c->amgNormsCap = 3 * kPowerSteps * nL;
     }
+    return EF_OK;
+}
+
+// lambda_max(D^-1 A) of level l by power iteration, entirely on the device (normalised by the
+// device-side norm); the last step's squared norm, lambda^2, is left at
+// amgNorms[3 (l kPowerSteps + kPowerSteps - 1)]
+static ef_status amg_power(ef_ctx* c, int l, cudaStream_t s) {
+    const int BCo = ef_amg_coarse_dofs();
+    const bool fine = l == 0;
+    const int bs = fine ? 3 : BCo;
+    const int nN = fine ? (int)c->nNodes : c->amg[l - 1].nN;
+    const int32_t* rowPtr = fine ? c->dRowPtr : c->amg[l - 1].rowPtr;
+    const int32_t* colIdx = fine ? c->dColIdx : c->amg[l - 1].colIdx;
+    const float* vals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
+    const float* binv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
+    const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
+    const int64_t n = (int64_t)bs * nN;
+    float* a = c->amgPow[0];
+    float* b = c->amgPow[1];
+    EF_CHECK(ef_launch_fill_hash(n, a, s));
+    for (int it = 0; it < kPowerSteps; ++it) {
+        double* n2 = c->amgNorms + 3 * (l * kPowerSteps + it);
+        EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, n2, s));
+        if (it + 1 == kPowerSteps) break;
+        EF_CHECK(ef_launch_scale_rnorm(n, a, n2, s));
+        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, a, c->amgZero, mask, b, s));  // -A a
+        EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
+    }
+    return EF_OK;
+}
+
+// per-level smoothing damping from the power-iteration norms (one transfer); the captured cycle
+// graphs are dropped when a damping changes
+static ef_status amg_damping_finish(ef_ctx* c, cudaStream_t s) {
+    const int nL = (int)c->amg.size();
     std::vector<float> om(nL), lamq(nL);
-    // all levels' iterations stay on the device (normalisation by the device-side norm); one
-    // transfer of the norms at the end
-    for (int l = 0; l < nL; ++l) {
-        const bool fine = l == 0;
-        const int bs = fine ? 3 : BCo;
-        const int nN = fine ? (int)c->nNodes : c->amg[l - 1].nN;
-        const int32_t* rowPtr = fine ? c->dRowPtr : c->amg[l - 1].rowPtr;
-        const int32_t* colIdx = fine ? c->dColIdx : c->amg[l - 1].colIdx;
-        const float* vals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
-        const float* binv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
-        const uint8_t* mask = fine ? c->dMask : c->amg[l - 1].dead;
-        const int64_t n = (int64_t)bs * nN;
-        float* a = c->amgPow[0];
-        float* b = c->amgPow[1];
-        EF_CHECK(ef_launch_fill_hash(n, a, s));
-        for (int it = 0; it < kPow; ++it) {
-            double* n2 = c->amgNorms + 3 * (l * kPow + it);
-            EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, n2, s));
-            if (it + 1 == kPow) break;
-            EF_CHECK(ef_launch_scale_rnorm(n, a, n2, s));
-            EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, a, c->amgZero, mask, b, s));  // -A a
-            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
-        }
-    }
-    std::vector<double> hn(3 * (size_t)kPow * nL);
+    std::vector<double> hn(3 * (size_t)kPowerSteps * nL);
     EF_CUDA(cudaMemcpyAsync(hn.data(), c->amgNorms, sizeof(double) * hn.size(), cudaMemcpyDeviceToHost, s));
     EF_CUDA(cudaStreamSynchronize(s));
     for (int l = 0; l < nL; ++l) {
         // lambda: |D^-1 A a| for the unit vector a of the last step
-        const double n2 = hn[3 * (l * kPow + kPow - 1)];
+        const double n2 = hn[3 * (l * kPowerSteps + kPowerSteps - 1)];
         const double lam = n2 > 0.0 ? sqrt(n2) : 0.0;
         float w = c->amgOmega;
         if (lam > 0.0 && lam == lam && c->amgOmega * lam > 1.85)  // close to the stability limit 2
@@ -2104,6 +2179,12 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
     return EF_OK;
 }
 
+static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
+    EF_CHECK(amg_power_alloc(c));
+    for (int l = 0; l < (int)c->amg.size(); ++l) EF_CHECK(amg_power(c, l, s));
+    return amg_damping_finish(c, s);
+}
+
 // dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses and
 // the coarsest inverse for the current fine system
 // edge weights of the learned correction for the current system
@@ -2125,6 +2206,7 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
         EF_CUDA(cudaMemcpyAsync(L.dead, L.hDead.data(), L.hDead.size(), cudaMemcpyHostToDevice, s));
         fineDead = L.hDead.data();
     }
+    if (c->amgSmoothed) EF_CHECK(amg_power_alloc(c));
     for (size_t l = 0; l < c->amg.size(); ++l) {
         AmgLevel& L = c->amg[l];
         const bool fine = l == 0;
@@ -2132,8 +2214,20 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
         const int32_t* fCol = fine ? c->dColIdx : c->amg[l - 1].colIdx;
         const float* fVals = fine ? (const float*)c->dBsrVals : c->amg[l - 1].vals;
         const uint8_t* fMask = fine ? c->dMask : c->amg[l - 1].dead;
-        EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
-                                    L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+        if (c->amgSmoothed) {
+            // smoothed prolongator P = P_t - 4 / (3 lambda) D^-1 A P_t of the finer level (its lambda
+            // from the power iteration on the device), then A P and P^T A P
+            const float* fBinv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
+            EF_CHECK(amg_power(c, (int)l, s));
+            EF_CHECK(ef_launch_sa_damping(c->amgNorms + 3 * ((int)l * kPowerSteps + kPowerSteps - 1), L.saW, s));
+            EF_CHECK(ef_launch_sa_setup(fine ? 3 : BCo, L.saNP, L.saPRow, L.saPCol, L.saPSeg, L.saPSrc, L.saNAP,
+                                        L.saApRow, L.saApSeg, L.saApK, L.saApP, fCol, fVals, fMask, L.offs, L.agg,
+                                        fBinv, L.saW, L.saPv, L.saAPv, L.nBlocks, L.saCSeg, L.saCP, L.saCAP,
+                                        L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+        } else {
+            EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
+                                        L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+        }
         EF_CHECK(ef_launch_bj6_setup(L.nN, L.diagPos, L.vals, L.binv, s));
         if (L.valsH) EF_CHECK(ef_launch_to_bf16(L.nBlocks * BCo * BCo, L.vals, L.valsH, s));
     }
@@ -2141,7 +2235,11 @@ static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
     if (c->dBsrValsH)
         EF_CHECK(ef_launch_to_bf16_split(c->nBlocks, (const float*)c->dBsrVals, c->dBsrValsH, s));
-    EF_CHECK(amg_damping(c, s));
+    if (c->amgSmoothed) {
+        EF_CHECK(amg_damping_finish(c, s));  // every level's power iteration ran above
+    } else {
+        EF_CHECK(amg_damping(c, s));
+    }
     c->amgStale = false;
     return nn_edge_refresh(c, s);
 }
@@ -2242,9 +2340,15 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
             EF_CHECK(ef_launch_coarse_cycle(c->dCoarseOps, c->nCoarseOps, s));
             continue;
         }
-        EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
+        if (c->amgSmoothed)
+            EF_CHECK(ef_launch_sa_restrict(bs, Cn.nN, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t, Cn.dead, Cn.r, s));
+        else
+            EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, cur, s, c->amgAlpha));
+        if (c->amgSmoothed)
+            EF_CHECK(ef_launch_sa_prolong(bs, nN, Cn.saPRowPtr, Cn.saPCol, Cn.saPv, Cn.x, mask, cur, c->amgAlpha, s));
+        else
+            EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, cur, s, c->amgAlpha));
     }
     // post-smoothing
     if (c->amgCheb) {
