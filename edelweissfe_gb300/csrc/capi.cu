@@ -2185,8 +2185,6 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
     return amg_damping_finish(c, s);
 }
 
-// dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses and
-// the coarsest inverse for the current fine system
 // edge weights of the learned correction for the current system
 static ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
     if (!c->nnInit || !c->nnEdgeStale) return EF_OK;
@@ -2196,6 +2194,8 @@ static ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
     return EF_OK;
 }
 
+// dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses, the
+// coarsest inverse and the smoothing damping for the current fine system
 static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     if (!c->amgStale) return EF_OK;
     const int BCo = ef_amg_coarse_dofs();
