@@ -8,7 +8,8 @@
 //   level 0 -> 1 (3 DOFs):  P_m = [ I | R(d) ]               (3 x 6)
 //   level l -> l+1 (6 DOFs): P_m = [ I R(d) ; 0 I ]          (6 x 6)
 // with R(d) = [e_x x d, e_y x d, e_z x d].  The Galerkin operators P^T A P are sums of
-// P_m^T A_mn P_n over the finer blocks, formed by an atomic-free segmented sum in FP64.
+// P_m^T A_mn P_n over the finer blocks, formed by an atomic-free segmented sum in compensated
+// FP32.
 // Smoothing is damped block Jacobi; the coarsest level is solved with a dense
 // pseudo-inverse (Gauss-Jordan, pivots below a relative threshold dropped).
 
@@ -16,11 +17,10 @@
 
 #include <algorithm>
 
+#include "amg_sa_body.h"
 #include "ef_common.cuh"
 
 namespace ef {
-
-constexpr int BC = 6;  // DOFs of a coarse node
 
 // Vector loads/stores of the multigrid phases: plain, or through L2 only (CG) in the cluster
 // kernel, whose CTAs read vectors that other CTAs of the cluster wrote in the same launch.
@@ -35,29 +35,6 @@ __device__ __forceinline__ void stv(float* p, float v) {
         __stcg(p, v);
     else
         *p = v;
-}
-
-// finer-node prolongation block, BF x 6
-template <int BF>
-__device__ __forceinline__ void pblock(const float* __restrict__ d, float P[BF][BC]) {
-    const float dx = d[0], dy = d[1], dz = d[2];
-#pragma unroll
-    for (int i = 0; i < BF; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) P[i][j] = 0.f;
-    P[0][0] = P[1][1] = P[2][2] = 1.f;
-    // rotation columns: e_x x d = (0,-dz,dy), e_y x d = (dz,0,-dx), e_z x d = (-dy,dx,0)
-    P[1][3] = -dz;
-    P[2][3] = dy;
-    P[0][4] = dz;
-    P[2][4] = -dx;
-    P[0][5] = -dy;
-    P[1][5] = dx;
-    if (BF == 6) {
-        P[3 % BF][3] = 1.f;
-        P[4 % BF][4] = 1.f;
-        P[5 % BF][5] = 1.f;
-    }
 }
 
 // coarse block S = sum over finer blocks f = (m, n) of P_m^T A_f P_n (fixed order); on level 0
@@ -132,8 +109,9 @@ __global__ void galerkin_kernel(int64_t nCoarseBlocks, const int64_t* __restrict
 // P = P_t - w D^-1 A P_t on the live finer DOFs (masked finer rows of P are zero; A with masked
 // rows and columns dropped, as in the Galerkin product), AP = A P, A_c = P^T A P: segmented sums
 // in the fixed order of the maps, FP32 with compensated accumulation for the coarse operator.
+// The per-thread bodies are in amg_sa_body.h.
 
-// one P block per thread: b = (m = pRow[b], J = pCol[b])
+// one P block per thread
 template <int BF>
 __global__ void sa_prolongator_kernel(int64_t nP, const int32_t* __restrict__ pRow, const int32_t* __restrict__ pCol,
                                       const int64_t* __restrict__ pSeg, const int32_t* __restrict__ pSrc,
@@ -143,50 +121,10 @@ __global__ void sa_prolongator_kernel(int64_t nP, const int32_t* __restrict__ pR
                                       const float* __restrict__ wP, float* __restrict__ Pv) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nP) return;
-    const int m = pRow[b], J = pCol[b];
-    float acc[BF][BC];
-#pragma unroll
-    for (int i = 0; i < BF; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
-    for (int64_t t = pSeg[b]; t < pSeg[b + 1]; ++t) {
-        const int32_t k = pSrc[t];
-        const int n = fineCol[k];
-        float Pn[BF][BC];
-        pblock<BF>(offs + 3 * (int64_t)n, Pn);
-        const float* v = fineVals + (int64_t)k * BF * BF;
-#pragma unroll
-        for (int i = 0; i < BF; ++i) {
-            if (fineMask && fineMask[BF * m + i]) continue;
-#pragma unroll
-            for (int q = 0; q < BF; ++q) {
-                if (fineMask && fineMask[BF * n + q]) continue;
-                const float a = v[i * BF + q];
-#pragma unroll
-                for (int j = 0; j < BC; ++j) acc[i][j] += a * Pn[q][j];
-            }
-        }
-    }
-    const float w = *wP;
-    float Pm[BF][BC];
-    pblock<BF>(offs + 3 * (int64_t)m, Pm);
-    const bool own = J == agg[m];
-    const float* B = binv + (int64_t)m * BF * BF;
-    float* out = Pv + b * BF * BC;
-#pragma unroll
-    for (int i = 0; i < BF; ++i) {
-        const bool masked = fineMask && fineMask[BF * m + i];
-#pragma unroll
-        for (int j = 0; j < BC; ++j) {
-            float z = 0.f;
-#pragma unroll
-            for (int q = 0; q < BF; ++q) z += B[i * BF + q] * acc[q][j];
-            out[i * BC + j] = masked ? 0.f : (own ? Pm[i][j] : 0.f) - w * z;
-        }
-    }
+    sa_prolongator_block<BF>(b, pRow, pCol, pSeg, pSrc, fineCol, fineVals, fineMask, offs, agg, binv, *wP, Pv);
 }
 
-// one AP block per thread: a = (m = apRow[a], J); sum over pairs (finer block k of row m, P block)
+// one AP block per thread
 template <int BF>
 __global__ void sa_ap_kernel(int64_t nAP, const int32_t* __restrict__ apRow, const int64_t* __restrict__ apSeg,
                              const int32_t* __restrict__ apK, const int32_t* __restrict__ apP,
@@ -195,38 +133,10 @@ __global__ void sa_ap_kernel(int64_t nAP, const int32_t* __restrict__ apRow, con
                              float* __restrict__ APv) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nAP) return;
-    const int m = apRow[a];
-    float acc[BF][BC];
-#pragma unroll
-    for (int i = 0; i < BF; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
-    for (int64_t t = apSeg[a]; t < apSeg[a + 1]; ++t) {
-        const int32_t k = apK[t];
-        const int n = fineCol[k];
-        const float* v = fineVals + (int64_t)k * BF * BF;
-        const float* P = Pv + (int64_t)apP[t] * BF * BC;
-#pragma unroll
-        for (int i = 0; i < BF; ++i) {
-            if (fineMask && fineMask[BF * m + i]) continue;
-#pragma unroll
-            for (int q = 0; q < BF; ++q) {
-                if (fineMask && fineMask[BF * n + q]) continue;
-                const float av = v[i * BF + q];
-#pragma unroll
-                for (int j = 0; j < BC; ++j) acc[i][j] += av * P[q * BC + j];
-            }
-        }
-    }
-    float* out = APv + a * BF * BC;
-#pragma unroll
-    for (int i = 0; i < BF; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) out[i * BC + j] = acc[i][j];
+    sa_ap_block<BF>(a, apRow, apSeg, apK, apP, fineCol, fineVals, fineMask, Pv, APv);
 }
 
-// one coarse block per thread: S = (I, J), sum over pairs (P block (m, I), AP block (m, J)) of
-// P^T AP in compensated FP32; dead coarse DOFs get identity rows and columns
+// one coarse block per thread
 template <int BF>
 __global__ void sa_galerkin_kernel(int64_t nC, const int64_t* __restrict__ cSeg, const int32_t* __restrict__ cP,
                                    const int32_t* __restrict__ cAP, const float* __restrict__ Pv,
@@ -235,40 +145,11 @@ __global__ void sa_galerkin_kernel(int64_t nC, const int64_t* __restrict__ cSeg,
                                    float* __restrict__ coarseVals) {
     const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (S >= nC) return;
-    float hi[BC][BC], lo[BC][BC];
-#pragma unroll
-    for (int i = 0; i < BC; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) hi[i][j] = lo[i][j] = 0.f;
-    for (int64_t t = cSeg[S]; t < cSeg[S + 1]; ++t) {
-        const float* P = Pv + (int64_t)cP[t] * BF * BC;
-        const float* Q = APv + (int64_t)cAP[t] * BF * BC;
-#pragma unroll
-        for (int i = 0; i < BC; ++i)
-#pragma unroll
-            for (int j = 0; j < BC; ++j) {
-                float s = 0.f;
-#pragma unroll
-                for (int q = 0; q < BF; ++q) s += P[q * BC + i] * Q[q * BC + j];
-                const float tt = __fadd_rn(hi[i][j], s);
-                const float bv = __fsub_rn(tt, hi[i][j]);
-                lo[i][j] = __fadd_rn(lo[i][j], __fadd_rn(__fsub_rn(hi[i][j], __fsub_rn(tt, bv)), __fsub_rn(s, bv)));
-                hi[i][j] = tt;
-            }
-    }
-    const int I = coarseRowOfBlock[S], J = coarseCol[S];
-#pragma unroll
-    for (int i = 0; i < BC; ++i)
-#pragma unroll
-        for (int j = 0; j < BC; ++j) {
-            float a = __fadd_rn(hi[i][j], lo[i][j]);
-            if (coarseDead[BC * I + i] || coarseDead[BC * J + j]) a = (I == J && i == j) ? 1.f : 0.f;
-            coarseVals[S * BC * BC + i * BC + j] = a;
-        }
+    sa_galerkin_block<BF>(S, cSeg, cP, cAP, Pv, APv, coarseRowOfBlock, coarseCol, coarseDead, coarseVals);
 }
 
-// rc[I] = sum over the P blocks b of column I (increasing finer row) of P_b^T t[row(b)]; one warp
-// per coarse node, blocks strided over the lanes, fixed shuffle tree; dead coarse DOFs -> 0
+// one warp per coarse node: lane partial sums over strided P blocks, fixed shuffle tree; dead
+// coarse DOFs -> 0
 template <int BF>
 __global__ void sa_restrict_kernel(int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ tIdx,
                                    const int32_t* __restrict__ pRow, const float* __restrict__ Pv,
@@ -278,19 +159,7 @@ __global__ void sa_restrict_kernel(int nC, const int32_t* __restrict__ tPtr, con
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (I >= nC) return;
     float a[BC];
-#pragma unroll
-    for (int j = 0; j < BC; ++j) a[j] = 0.f;
-    for (int k = tPtr[I] + lane; k < tPtr[I + 1]; k += 32) {
-        const int32_t b = tIdx[k];
-        const int m = pRow[b];
-        const float* P = Pv + (int64_t)b * BF * BC;
-#pragma unroll
-        for (int i = 0; i < BF; ++i) {
-            const float ti = t[BF * m + i];
-#pragma unroll
-            for (int j = 0; j < BC; ++j) a[j] += P[i * BC + j] * ti;
-        }
-    }
+    sa_restrict_partial<BF>(I, lane, 32, tPtr, tIdx, pRow, Pv, t, a);
 #pragma unroll
     for (int j = 0; j < BC; ++j)
 #pragma unroll
@@ -304,30 +173,14 @@ __global__ void sa_restrict_kernel(int nC, const int32_t* __restrict__ tPtr, con
     }
 }
 
-// x[m] += alpha sum over the P blocks of row m of P_b xc[col(b)] on free finer DOFs
+// one finer node per thread
 template <int BF>
 __global__ void sa_prolong_kernel(int nF, const int32_t* __restrict__ pRowPtr, const int32_t* __restrict__ pCol,
                                   const float* __restrict__ Pv, const float* __restrict__ xc,
                                   const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nF) return;
-    float s[BF];
-#pragma unroll
-    for (int i = 0; i < BF; ++i) s[i] = 0.f;
-    for (int b = pRowPtr[m]; b < pRowPtr[m + 1]; ++b) {
-        const float* P = Pv + (int64_t)b * BF * BC;
-        const float* c = xc + BC * (int64_t)pCol[b];
-        float cv[BC];
-#pragma unroll
-        for (int j = 0; j < BC; ++j) cv[j] = c[j];
-#pragma unroll
-        for (int i = 0; i < BF; ++i)
-#pragma unroll
-            for (int j = 0; j < BC; ++j) s[i] += P[i * BC + j] * cv[j];
-    }
-#pragma unroll
-    for (int i = 0; i < BF; ++i)
-        if (!(mask && mask[BF * m + i])) x[BF * m + i] += alpha * s[i];
+    sa_prolong_row<BF>(m, pRowPtr, pCol, Pv, xc, mask, x, alpha);
 }
 
 // *wP = 4 / (3 lambda) with lambda = sqrt(*n2), the prolongator damping from the power iteration

@@ -81,9 +81,12 @@ def test_integer_fp64_fp32_pair_conversions(tmp_path):
 
 
 def test_smoothed_aggregation_index_maps(tmp_path):
-    """The smoothed-aggregation index maps (edelweissfe_gb300/csrc/amg_sa_pattern.h): the smoothed
-    prolongator, A P and P^T A P formed through them as segmented sums equal the dense products
-    on a masked random block system, and the dense products vanish outside the patterns."""
+    """The smoothed-aggregation index maps (edelweissfe_gb300/csrc/amg_sa_pattern.h) and the
+    per-thread bodies of the device kernels (edelweissfe_gb300/csrc/amg_sa_body.h, the same source
+    compiled for the host): the smoothed prolongator, A P, P^T A P, the restriction and the
+    prolongation equal the dense FP64 products to FP32 rounding on random block systems of 3-DOF
+    and 6-DOF nodes, with and without masked DOFs, and the dense products vanish outside the
+    patterns."""
     import os
     import shutil
     import subprocess
@@ -95,8 +98,8 @@ def test_smoothed_aggregation_index_maps(tmp_path):
         pytest.skip("no C++ compiler")
     here = os.path.dirname(os.path.abspath(__file__))
     exe = str(tmp_path / "amg_sa_check")
-    subprocess.run([gxx, "-O2", "-std=c++17", "-o", exe, os.path.join(here, "native", "amg_sa_check.cpp")],
-                   check=True)  # fmt: skip
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe,
+                    os.path.join(here, "native", "amg_sa_check.cpp")], check=True)  # fmt: skip
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "failures 0" in out.stdout
