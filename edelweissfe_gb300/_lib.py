@@ -92,6 +92,10 @@ SIGNATURES = {
     "ef_get_state_size": (c_int, [c_vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     "ef_set_state": (c_int, [c_vp, c_int, c_vp]),
     "ef_get_state": (c_int, [c_vp, c_int, c_int, c_vp]),
+    "ef_results_create": (c_int, [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_int, c_int, ctypes.POINTER(c_int)]),
+    "ef_results_update": (c_int, [c_vp, c_int, c_int, c_vp, c_vp]),
+    "ef_results_device": (c_int, [c_vp, c_int, ctypes.POINTER(c_vp), ctypes.POINTER(c_i64)]),
+    "ef_results_destroy": (c_int, [c_vp, c_int]),
     "ef_accept_state": (c_int, [c_vp]),
     "ef_add_body_force": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp]),
     "ef_export_vij": (c_int, [c_vp, c_vp, c_vp]),

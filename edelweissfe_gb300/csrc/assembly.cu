@@ -341,3 +341,29 @@ ef_status ef_launch_tie_fill(int64_t n, const int32_t* slave, const int32_t* ma,
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
+
+// element results (utils/elementresultcollector.pyx:38-120): one thread per requested
+// (element, quadrature point) p = i * nQ + j, table[p * count + k] = state var first + k of point
+// elements[i] * nQP + qps[j]; the SoA state makes the reads of a warp contiguous for consecutive
+// points, the strided writes of a thread merge in L2
+__global__ void results_gather_kernel(int64_t nPts, int nQ, int nQP, int64_t nq, int first, int count,
+                                      const int32_t* __restrict__ elements, const int32_t* __restrict__ qps,
+                                      const double* __restrict__ state, double* __restrict__ table) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nPts) return;
+    const int64_t i = p / nQ;
+    const int j = (int)(p - i * nQ);
+    const double* src = state + (int64_t)first * nq + (int64_t)elements[i] * nQP + qps[j];
+    double* out = table + p * count;
+    for (int k = 0; k < count; ++k) out[k] = src[(int64_t)k * nq];
+}
+
+ef_status ef_launch_results_gather(int64_t nPts, int nQ, int nQP, int64_t nq, int first, int count,
+                                   const int32_t* elements, const int32_t* qps, const double* state, double* table,
+                                   cudaStream_t s) {
+    if (nPts == 0) return EF_OK;
+    results_gather_kernel<<<nblk(nPts, 256), 256, 0, ef::counted(s)>>>(nPts, nQ, nQP, nq, first, count, elements, qps,
+                                                                        state, table);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}

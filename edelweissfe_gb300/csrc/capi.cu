@@ -384,6 +384,16 @@ struct AmgLevel {
     std::vector<uint8_t> hDead;
 };
 
+// element result collector: device lists of elements and quadrature points of one group, the
+// state slice [first, first + count) and the gathered table [nEls][nQ][count]
+struct ResultCollector {
+    int group = -1;  // -1: free slot
+    int nEls = 0, nQ = 0, first = 0, count = 0;
+    int32_t* dEl = nullptr;
+    int32_t* dQp = nullptr;
+    double* dTable = nullptr;
+};
+
 struct ef_ctx {
     int64_t nDof = 0, nNodes = 0, nElements = 0;
     std::vector<double> hX;
@@ -391,6 +401,7 @@ struct ef_ctx {
     std::vector<HostGroup> hg;
     std::vector<Group> groups;
     std::vector<ElemTables*> dTables;
+    std::vector<ResultCollector> results;
     bool finalized = false;
     int keFp64 = 0;
     int nSM = 0;
@@ -593,6 +604,11 @@ void ef_destroy(ef_ctx* c) {
         F(g.geoS);
     }
     for (auto* t : c->dTables) F(t);
+    for (auto& r : c->results) {
+        F(r.dEl);
+        F(r.dQp);
+        F(r.dTable);
+    }
     F(c->Pe);
     F(c->Kblk);
     F(c->dFlags);
@@ -3434,6 +3450,119 @@ ef_status ef_norms(ef_ctx* c, const double* R, const double* F, const double* dd
     EF_CHECK(ef_launch_norms(c->nDof, R, F, ddU, c->dPart, c->nPart, c->dRed, s));
     EF_CUDA(cudaMemcpyAsync(out, c->dRed, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     EF_CUDA(cudaStreamSynchronize(s));
+    return EF_OK;
+}
+
+// ---- element result collectors (utils/elementresultcollector.pyx:38-120) ----------------------
+
+static ResultCollector* result_collector(ef_ctx* c, int id) {
+    if (id < 0 || id >= (int)c->results.size() || c->results[id].group < 0) {
+        ef_set_error("element result collector: unknown id");
+        return nullptr;
+    }
+    return &c->results[id];
+}
+
+ef_status ef_results_create(ef_ctx* c, int groupId, const int32_t* elements, int nEls, const int32_t* qps, int nQps,
+                            int first, int count, int* collectorId) {
+    EF_REQUIRE_FINALIZED(c);
+    if (groupId < 0 || groupId >= (int)c->groups.size() || !collectorId) {
+        ef_set_error("ef_results_create: invalid group or output");
+        return EF_ERR_ARG;
+    }
+    const Group& g = c->groups[groupId];
+    if (first < 0 || count < 1 || first + count > g.nState) {
+        ef_set_error("ef_results_create: state slice outside [0, nState)");
+        return EF_ERR_ARG;
+    }
+    std::vector<int32_t> el, qp;
+    if (elements) {
+        if (nEls < 1) {
+            ef_set_error("ef_results_create: empty element list");
+            return EF_ERR_ARG;
+        }
+        el.assign(elements, elements + nEls);
+    } else {
+        el.resize(g.nEl);
+        for (int e = 0; e < g.nEl; ++e) el[e] = e;
+    }
+    if (qps) {
+        if (nQps < 1) {
+            ef_set_error("ef_results_create: empty quadrature point list");
+            return EF_ERR_ARG;
+        }
+        qp.assign(qps, qps + nQps);
+    } else {
+        qp.resize(g.nQP);
+        for (int q = 0; q < g.nQP; ++q) qp[q] = q;
+    }
+    for (int32_t e : el)
+        if (e < 0 || e >= g.nEl) {
+            ef_set_error("ef_results_create: element index outside the group");
+            return EF_ERR_ARG;
+        }
+    for (int32_t q : qp)
+        if (q < 0 || q >= g.nQP) {
+            ef_set_error("ef_results_create: quadrature point outside the element");
+            return EF_ERR_ARG;
+        }
+    ResultCollector r;
+    r.nEls = (int)el.size();
+    r.nQ = (int)qp.size();
+    r.first = first;
+    r.count = count;
+    ef_status st = upload(&r.dEl, el);
+    if (st == EF_OK) st = upload(&r.dQp, qp);
+    if (st == EF_OK) r.dTable = dalloc<double>((size_t)r.nEls * r.nQ * count, &st);
+    if (st != EF_OK) {
+        for (void* p : {(void*)r.dEl, (void*)r.dQp, (void*)r.dTable})
+            if (p) cudaFree(p);
+        return st;
+    }
+    r.group = groupId;
+    int id = 0;
+    while (id < (int)c->results.size() && c->results[id].group >= 0) ++id;
+    if (id == (int)c->results.size())
+        c->results.push_back(r);
+    else
+        c->results[id] = r;
+    *collectorId = id;
+    return EF_OK;
+}
+
+ef_status ef_results_update(ef_ctx* c, int collectorId, int trial, double* hostOut, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    const ResultCollector* r = result_collector(c, collectorId);
+    if (!r) return EF_ERR_ARG;
+    const Group& g = c->groups[r->group];
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t nPts = (int64_t)r->nEls * r->nQ;
+    EF_CHECK(ef_launch_results_gather(nPts, r->nQ, g.nQP, (int64_t)g.nEl * g.nQP, r->first, r->count, r->dEl, r->dQp,
+                                      g.state[trial ? 1 - g.cur : g.cur], r->dTable, s));
+    if (hostOut) {
+        EF_CUDA(cudaMemcpyAsync(hostOut, r->dTable, sizeof(double) * nPts * r->count, cudaMemcpyDeviceToHost, s));
+        EF_CUDA(cudaStreamSynchronize(s));
+    }
+    return EF_OK;
+}
+
+ef_status ef_results_device(ef_ctx* c, int collectorId, const double** table, int64_t* nValues) {
+    EF_REQUIRE_FINALIZED(c);
+    const ResultCollector* r = result_collector(c, collectorId);
+    if (!r || !table) return EF_ERR_ARG;
+    *table = r->dTable;
+    if (nValues) *nValues = (int64_t)r->nEls * r->nQ * r->count;
+    return EF_OK;
+}
+
+ef_status ef_results_destroy(ef_ctx* c, int collectorId) {
+    EF_REQUIRE_FINALIZED(c);
+    ResultCollector* r = result_collector(c, collectorId);
+    if (!r) return EF_ERR_ARG;
+    EF_CUDA(cudaFree(r->dEl));
+    EF_CUDA(cudaFree(r->dQp));
+    EF_CUDA(cudaFree(r->dTable));
+    *r = ResultCollector();
     return EF_OK;
 }
 

@@ -133,6 +133,9 @@ ef_status ef_launch_condense(int64_t nNodes, const int32_t* nodeDof, const int64
 ef_status ef_launch_condense_add(int64_t nNodes, const int32_t* nodeDof, const int64_t* ptr, const int64_t* src,
                                  const float* w, const double* Pe, int64_t lo, int64_t hi, double* V, cudaStream_t s);
 ef_status ef_launch_vij_export(int nEl, int nn, int np, const void* Kblk, int kDouble, double* Kvij, cudaStream_t s);
+ef_status ef_launch_results_gather(int64_t nPts, int nQ, int nQP, int64_t nq, int first, int count,
+                                   const int32_t* elements, const int32_t* qps, const double* state, double* table,
+                                   cudaStream_t s);
 ef_status ef_launch_csr_scatter(int64_t nnz, const int64_t* seg, const int32_t* perm, const double* V, double* data,
                                 cudaStream_t s);
 ef_status ef_launch_csr_dirichlet_rows(int64_t nRows, const int64_t* rows, const int32_t* indptr,

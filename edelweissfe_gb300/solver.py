@@ -258,6 +258,26 @@ class NISTGPU:
         _lib.check(st, "ef_solve")
         return ddU
 
+    # ---- element results ---------------------------------------------------------------------------
+
+    def getResultArray(self, groupId: int, element: int, result: str, quadraturePoint: int, trial: bool = False):
+        """One element's result at one quadrature point (elements/displacementelement/element.py:386-409),
+        as a copy of the committed state (trial=True: the current iteration's state)."""
+        from .results import ElementResultCollector
+
+        c = ElementResultCollector(self, groupId, [element], [quadraturePoint], result, trial=trial)
+        try:
+            return c.getCurrentResults()[0].copy()
+        finally:
+            c.close()
+
+    def resultCollector(self, groupId: int, elements, quadraturePoints, result: str, trial: bool = False):
+        """An ElementResultCollector over elements (indices within the group, None: all) and
+        quadrature points of one group (utils/elementresultcollector.pyx)."""
+        from .results import ElementResultCollector
+
+        return ElementResultCollector(self, groupId, elements, quadraturePoints, result, trial=trial)
+
     # ---- learned preconditioner correction (FGMRES only) ----------------------------------------
 
     FGMRES_PRECONDITIONERS = {"multigrid": 0, "jacobi": 1}

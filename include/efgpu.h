@@ -131,6 +131,24 @@ ef_status ef_get_state_size(const ef_ctx* ctx, int groupId, int* nQP, int* nStat
 ef_status ef_set_state(ef_ctx* ctx, int groupId, const double* state);
 ef_status ef_get_state(ef_ctx* ctx, int groupId, int trial, double* state);
 
+/* Element results (utils/elementresultcollector.pyx:38-120 ElementResultCollector, over
+ * elements/displacementelement/element.py:386-409 getResultArray, whose names map to state
+ * slices: "stress" [0, 6), "strain" [6, 12), "materialstate" [12, nState), the J2 "kappa" and
+ * the NeoHookeWa "energy" [12, 13)).  A collector gathers, for a list of elements of one group
+ * (indices within the group; NULL: all, in order) and a list of their quadrature points (NULL:
+ * all), the state entries [first, first + count) of every point into one FP64 table
+ * [nEls][nQps][count] on the device.  ef_results_create checks and uploads the lists (EF_ERR_ARG
+ * for an index outside the group or a slice outside the state).  ef_results_update gathers the
+ * committed (trial = 0, what the reference's result views show) or trial (trial = 1) state on
+ * `stream` and, with hostOut non-NULL, copies the table there (host [nEls*nQps*count]; the call
+ * then synchronises the stream).  ef_results_device returns the device table and its length.
+ * Collectors belong to their context: ef_destroy frees those still open. */
+ef_status ef_results_create(ef_ctx* ctx, int groupId, const int32_t* elements, int nEls, const int32_t* qps,
+                            int nQps, int first, int count, int* collectorId);
+ef_status ef_results_update(ef_ctx* ctx, int collectorId, int trial, double* hostOut, void* stream);
+ef_status ef_results_device(ef_ctx* ctx, int collectorId, const double** table, int64_t* nValues);
+ef_status ef_results_destroy(ef_ctx* ctx, int collectorId);
+
 /* elements/displacementelement/element.py:373-379 acceptLastState for all elements: the trial
  * state is copied into the committed state (device-wide synchronous copy; the state buffers keep
  * their addresses, so element launches captured in a CUDA graph remain valid). */
