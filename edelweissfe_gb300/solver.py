@@ -434,3 +434,102 @@ class NISTGPU:
             if maxIncrements is not None and done >= maxIncrements:
                 break
         return U, P
+
+
+class IndirectControl:
+    """Indirect displacement control for the arc-length driver (stepactions/indirectcontrol.py:29-44):
+    the load-factor correction ddLambda that makes c . dU over the controlled DOFs (node 1's
+    components, then node 2's) grow by stepProgressIncrement * L in the increment."""
+
+    def __init__(self, dofs1, cVector1, dofs2, cVector2, L: float):
+        self.idcs = np.concatenate([np.asarray(dofs1, np.int64), np.asarray(dofs2, np.int64)])
+        self.c = np.concatenate([np.asarray(cVector1, float), np.asarray(cVector2, float)])
+        self.L = float(L)
+
+    def computeDDLambda(self, dU, ddU_0, ddU_f, timeStep):
+        """dU, ddU_0, ddU_f: host arrays of the controlled DOFs."""
+        dL = timeStep.stepProgressIncrement * self.L
+        return (dL - self.c.dot(dU + ddU_0)) / self.c.dot(ddU_f)
+
+
+class NISTGPUArcLength(NISTGPU):
+    """The arc-length driver of solvers/nonlinearimplicitstaticparallelarclength.py:120-320 over the
+    same GPU hot path.  Each Newton iteration evaluates the elements once, forms
+    R_0 = P_0 + (Lambda + dLambda) P_f + P from the dead loads P_0, the reference loads P_f (the
+    node and body forces at step progress 1 minus those at 0) and the internal forces P, and
+    solves the one assembled system twice (K ddU_0 = R_0, K ddU_f = P_f; the preconditioner set-up
+    is shared).  The controller gives ddLambda from the controlled DOFs (one small device-to-host
+    read) and ddU = ddU_0 + ddLambda ddU_f.  Dirichlet rows take the prescribed values scaled like
+    the load: zero in the first iteration of an extrapolated increment, else the increment over
+    [Lambda, Lambda + dLambda] in R_0 and the full value in P_f.  The convergence test runs on R_0
+    from the second iteration on, or from the first after an extrapolation, and the load factor
+    is extrapolated with the displacements (:355-368).  Without a controller the increments are
+    the plain Newton increments of NISTGPU, as in the reference."""
+
+    identification = "NISTGPUArcLength"
+
+    def __init__(self, *args, arcLengthController: IndirectControl = None, **kw):
+        super().__init__(*args, **kw)
+        self.arcLengthController = arcLengthController
+        self.Lambda = 0.0
+        self.dLambda = 0.0
+        self.lambdaHistory = []  # Lambda after each converged increment
+
+    def _dirichletAt(self, number, progressIncrement, progress):
+        return self._dirichletDelta(TimeStep(number, progressIncrement, progress, 0.0, 0.0, 0.0))
+
+    def solveIncrement(self, U_n, dU, P, timeStep, prevTimeStep, step: Step):
+        ctl = self.arcLengthController
+        if ctl is None:
+            return super().solveIncrement(U_n, dU, P, timeStep, prevTimeStep, step)
+        iterationCounter = 0
+        residualHistory = {"displacement": (0.0, 0)}
+        F = self._vec()
+        U_np = self._vec()
+        ddU = None
+        Lambda, dLambda = self.Lambda, self.dLambda
+        if step.extrapolation == "linear" and prevTimeStep is not None and prevTimeStep.stepProgressIncrement:
+            ratio = timeStep.stepProgressIncrement / prevTimeStep.stepProgressIncrement
+            dLambda = dLambda * ratio
+            dU *= ratio
+            isExtrapolated = True
+        else:
+            dLambda = 0.0
+            dU.zero_()
+            isExtrapolated = False
+        P_0 = self._externalLoads(TimeStep(timeStep.number, 0.0, 0.0, 0.0, 0.0, 0.0))
+        P_f = self._externalLoads(TimeStep(timeStep.number, 1.0, 1.0, 0.0, 0.0, 0.0)) - P_0
+        R_f = P_f.clone()
+        if self.dirichlets:
+            R_f[self.dirIdx] = self._dirichletAt(timeStep.number, 1.0, 1.0)
+        idx = torch.as_tensor(ctl.idcs, device=self.device)
+        while True:
+            torch.add(U_n, dU, out=U_np)
+            P, F = self.computeElements(U_np, dU, P, F, timeStep)
+            R_0 = P_0 + (Lambda + dLambda) * P_f + P
+            if self.dirichlets:
+                if isExtrapolated and iterationCounter == 0:
+                    R_0[self.dirIdx] = self._dirichletAt(timeStep.number, 0.0, 0.0)
+                else:
+                    R_0[self.dirIdx] = self._dirichletAt(timeStep.number, dLambda, Lambda + dLambda)
+            if iterationCounter > 0 or isExtrapolated:
+                if self.checkConvergence(R_0, ddU, F, iterationCounter, residualHistory):
+                    break
+                if residualHistory["displacement"][1] > step.maxGrowIter:
+                    raise DivergingSolution(f"Residual grew {step.maxGrowIter} times, cutting back")
+                if iterationCounter == step.maxIter:
+                    raise ReachedMaxIterations("Reached max. iterations in current increment, cutting back")
+            self.assembleStiffnessCSR()
+            self.applyDirichletK()
+            ddU_0 = self.linearSolve(R_0)
+            ddU_f = self.linearSolve(R_f)
+            ctlValues = torch.stack([dU[idx], ddU_0[idx], ddU_f[idx]]).cpu().numpy()
+            ddLambda = ctl.computeDDLambda(ctlValues[0], ctlValues[1], ctlValues[2], timeStep)
+            ddU = ddU_0 + ddLambda * ddU_f
+            dU += ddU
+            dLambda += ddLambda
+            iterationCounter += 1
+        self.Lambda += dLambda
+        self.dLambda = dLambda
+        self.lambdaHistory.append(self.Lambda)
+        return U_np, dU, P, iterationCounter

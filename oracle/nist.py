@@ -301,3 +301,85 @@ class NIST:
             if maxIncrements is not None and nDone >= maxIncrements:
                 break
         return U, P
+
+
+@dataclass
+class IndirectControl:
+    """Indirect displacement control of the arc-length driver (stepactions/indirectcontrol.py:29-44,
+    ``computeDDLambda``): the load-factor correction that makes c . dU over the controlled DOFs
+    (node 1's then node 2's displacement components) grow by stepProgressIncrement * L."""
+
+    idcs: np.ndarray
+    c: np.ndarray
+    L: float
+
+    def computeDDLambda(self, dU, ddU_0, ddU_f, ts):
+        dL = ts.stepProgressIncrement * self.L
+        return (dL - self.c.dot(dU[self.idcs] + ddU_0[self.idcs])) / self.c.dot(ddU_f[self.idcs])
+
+
+class NISTArcLength(NIST):
+    """Arc-length increment of ``solvers/nonlinearimplicitstaticparallelarclength.py:120-320``: per
+    Newton iteration the residual R_0 = P_0 + (Lambda + dLambda) P_f + P of the dead loads P_0, the
+    reference loads P_f (the loads at step progress 1 minus those at 0) and the internal forces,
+    two solves K ddU_0 = R_0 and K ddU_f = P_f, the controller's ddLambda, and
+    ddU = ddU_0 + ddLambda ddU_f.  Dirichlet rows take the prescribed values scaled like the load
+    (a zero increment in the first iteration of an extrapolated increment); the convergence test
+    runs on R_0 from the second iteration on, or from the first after an extrapolation; the load
+    factor and the displacement increment are extrapolated together (:355-368)."""
+
+    def __init__(self, model: Model, controller: IndirectControl, linsolve=spsolve_direct):
+        super().__init__(model, linsolve)
+        self.controller = controller
+        self.Lambda = 0.0
+        self.dLambda = 0.0
+        self.lambdaHistory = []  # Lambda after each converged increment
+
+    def _dirichletAt(self, number, progressIncrement, progress):
+        return self._dirichletDelta(TimeStep(number, progressIncrement, progress, 0.0, 0.0, 0.0))
+
+    def solveIncrement(self, U_n, dU, ts, prevTs, step):
+        it = 0
+        hist = [(0.0, 0)]
+        ddU = None
+        Lambda, dLambda = self.Lambda, self.dLambda
+        if step.extrapolation == "linear" and prevTs is not None and prevTs.stepProgressIncrement:
+            dLambda = dLambda * (ts.stepProgressIncrement / prevTs.stepProgressIncrement)
+            dU = dU * (ts.stepProgressIncrement / prevTs.stepProgressIncrement)
+            extrap = True
+        else:
+            dLambda = 0.0
+            dU = np.zeros_like(dU)
+            extrap = False
+        P_0 = self._externalLoads(TimeStep(ts.number, 0.0, 0.0, 0.0, 0.0, 0.0))
+        P_f = self._externalLoads(TimeStep(ts.number, 1.0, 1.0, 0.0, 0.0, 0.0)) - P_0
+        while True:
+            U_np = U_n + dU
+            P, V, F = self.computeElements(U_np, dU)
+            R_0 = P_0 + (Lambda + dLambda) * P_f + P
+            R_f = P_f.copy()
+            if self.dirIdx.size:
+                if extrap and it == 0:
+                    R_0[self.dirIdx] = self._dirichletAt(ts.number, 0.0, 0.0)
+                else:
+                    R_0[self.dirIdx] = self._dirichletAt(ts.number, dLambda, Lambda + dLambda)
+                R_f[self.dirIdx] = self._dirichletAt(ts.number, 1.0, 1.0)
+            if it > 0 or extrap:
+                if self.checkConvergence(R_0, ddU, F, it, hist):
+                    break
+                if hist[0][1] > step.maxGrowIter:
+                    raise DivergingSolution("Residual grew too often")
+                if it == step.maxIter:
+                    raise ReachedMaxIterations("Reached max. iterations")
+            A = self.applyDirichletK(self.assembleStiffnessCSR(V))
+            ddU_0 = self.linearSolve(A, R_0)
+            ddU_f = self.linearSolve(A, R_f)
+            ddLambda = self.controller.computeDDLambda(dU, ddU_0, ddU_f, ts)
+            ddU = ddU_0 + ddLambda * ddU_f
+            dU = dU + ddU
+            dLambda += ddLambda
+            it += 1
+        self.Lambda += dLambda
+        self.dLambda = dLambda
+        self.lambdaHistory.append(self.Lambda)
+        return U_np, dU, P, it

@@ -5,6 +5,7 @@ Run in a container where the reference sources are available (default
 
     python tests/golden/make_golden.py        # all fixtures
     python tests/golden/make_golden.py tl     # only the total-Lagrange ones
+    python tests/golden/make_golden.py arclength   # only the arc-length one
 
 What it does:
 
@@ -23,7 +24,9 @@ What it does:
      state, random increments),
    * ``csr_small.npz``: the CSR pattern and a scatter result of ``CSRGenerator``,
    * ``nist_<case>.npz``: final displacements and Newton iteration counts of
-     the reference NIST driver on 3D J2 / elastic boxes.
+     the reference NIST driver on 3D J2 / elastic boxes,
+   * ``nist_arclength_j2_10x2x2.npz``: the same of the reference arc-length
+     driver with indirect displacement control, plus its load factors.
 
 Nothing here is needed at test time; the tests only read the ``.npz`` files.
 """
@@ -375,11 +378,79 @@ def tl_fixtures(scratch):
         np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
 
 
+ARC_INP = """*material, name=vonmises, id=mat, provider=edelweiss
+{E}, {nu}, {fy}, {H}, 0.0, 0.0
+*job, name=job, domain=3d
+*solver, solver=NISTPArcLength, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX ={nX}
+nY ={nY}
+nZ ={nZ}
+lX ={lX}
+lY ={lY}
+lZ ={lZ}
+elProvider =edelweiss
+elType =C3D8
+*section, name=section1, material=mat, type=solid
+all
+*modelGenerator, generator=findClosestNode, name=closestN1, executeAfterManualGeneration=True
+location='{x1}, 0, 0'
+storeIn=IDC1
+*modelGenerator, generator=findClosestNode, name=closestN2, executeAfterManualGeneration=True
+location='{x2}, 0, 0'
+storeIn=IDC2
+*step, solver=theSolver, maxInc={maxInc}, startInc={maxInc}, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTArcLength, arcLengthController=indirectcontrol
+indirectcontrol, dof1='model.nodeSets["IDC1"][0].fields["displacement"]', cVector1='[-1,0,0]', dof2='model.nodeSets["IDC2"][0].fields["displacement"]', cVector2='[1,0,0]', L={L},
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0, 2=0.0, 3=0.0
+nodeforces, name=pull, nSet=gen_right, components='{f}, 0, 0', field=displacement
+"""
+
+ARC_CASE = dict(nX=10, nY=2, nZ=2, lX=1.0, lY=0.2, lZ=0.2, x1=0.3, x2=0.7, L=0.0016, f=10.0, maxInc=0.25)
+
+
+def arclength_fixtures(scratch):
+    """The reference's arc-length driver (solvers/nonlinearimplicitstaticparallelarclength.py) with
+    indirect displacement control (stepactions/indirectcontrol.py) on a J2 bar: the relative x
+    displacement of the nodes at x1 and x2 grows to L over the step while the load factor of the
+    node forces on the x = lX face follows.  The driver derives from NISTParallel, whose module
+    also holds the Marmot element loop (not buildable here); it is stubbed with the serial NIST,
+    whose element loop gives the same results as NISTParallel's at one thread.  Stores U, the
+    Newton iterations and the load factor Lambda after every increment."""
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    stub = types.ModuleType("edelweissfe.solvers.nonlinearimplicitstaticparallel")
+    stub.NISTParallel = NIST
+    sys.modules["edelweissfe.solvers.nonlinearimplicitstaticparallel"] = stub
+    from edelweissfe.solvers.nonlinearimplicitstaticparallelarclength import NISTPArcLength
+
+    rec = []
+    orig = NISTPArcLength.solveIncrement
+
+    def wrapped(self, *a, **k):
+        out = orig(self, *a, **k)
+        rec.append((out[3], self.Lambda))
+        return out
+
+    NISTPArcLength.solveIncrement = wrapped
+    try:
+        text = ARC_INP.format(E=210000.0, nu=0.3, fy=250.0, H=1000.0, **ARC_CASE)
+        U, _ = run_inp(text, scratch, "arclength")
+    finally:
+        NISTPArcLength.solveIncrement = orig
+    np.savez_compressed(os.path.join(HERE, "nist_arclength_j2_10x2x2.npz"), U=U, iters=np.array([r[0] for r in rec]),
+                        Lambda=np.array([r[1] for r in rec]), **{k: np.array(v) for k, v in ARC_CASE.items()})
+
+
 def main():
     scratch = tempfile.mkdtemp(prefix="efref_")
     prepare_reference(scratch)
     if sys.argv[1:] == ["tl"]:  # only the total-Lagrange fixtures
         tl_fixtures(scratch)
+        shutil.rmtree(scratch, ignore_errors=True)
+        return
+    if sys.argv[1:] == ["arclength"]:  # only the arc-length fixture
+        arclength_fixtures(scratch)
         shutil.rmtree(scratch, ignore_errors=True)
         return
     copy_uref()
@@ -391,6 +462,7 @@ def main():
     csr_fixture()
     nist_fixtures(scratch)
     tl_fixtures(scratch)
+    arclength_fixtures(scratch)
     shutil.rmtree(scratch, ignore_errors=True)
 
 

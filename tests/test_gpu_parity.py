@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from cases import UREF_CASES, build_gpu_solver, cantilever_spec, j2_box_spec, tl_box_spec, uref_spec
+from cases import J2_PROPS, UREF_CASES, build_gpu_solver, cantilever_spec, j2_box_spec, tl_box_spec, uref_spec
 from conftest import golden
 
 pytestmark = pytest.mark.gpu
@@ -162,6 +162,31 @@ def test_nist_gpu_j2_matches_reference(gpu_lib, case, mode):
     s = build_gpu_solver(spec, keFp64=fp64, linsolver=LinSolverOptions(mixed=not fp64))
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.iterationHistory] == list(g["iters"])
+    assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_nist_gpu_arclength_matches_reference(gpu_lib, mode):
+    """Arc-length driver with indirect displacement control on a J2 bar
+    (solvers/nonlinearimplicitstaticparallelarclength.py, stepactions/indirectcontrol.py):
+    identical Newton iteration counts, displacements and load factors within 1e-6 relative."""
+    from edelweissfe_gb300.mesh import box_mesh
+    from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model, NodeForces
+    from edelweissfe_gb300.solver import IndirectControl, LinSolverOptions, NISTGPUArcLength, Step
+
+    g = golden("nist_arclength_j2_10x2x2.npz")
+    m = box_mesh(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]))
+    model = Model(m["coords"], [ElementGroup("C3D8", m["elements"], "vonmises", np.array(J2_PROPS))])
+    n1, n2 = (int(np.argmin(np.linalg.norm(m["coords"] - [float(g[k]), 0.0, 0.0], axis=1))) for k in ("x1", "x2"))
+    ctl = IndirectControl(3 * n1 + np.arange(3), [-1.0, 0.0, 0.0], 3 * n2 + np.arange(3), [1.0, 0.0, 0.0], float(g["L"]))
+    fp64 = mode == "fp64"
+    s = NISTGPUArcLength(model, [DirichletBC(m["nodeSets"]["gen_left"], {0: 0.0, 1: 0.0, 2: 0.0})],
+                         [NodeForces(m["nodeSets"]["gen_right"], [float(g["f"]), 0.0, 0.0])], keFp64=fp64,
+                         linsolver=LinSolverOptions(mixed=not fp64), arcLengthController=ctl)  # fmt: skip
+    inc = float(g["maxInc"])
+    U, _ = s.solveStep(Step(startInc=inc, maxInc=inc, minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.iterationHistory] == list(g["iters"])
+    assert np.max(np.abs(np.array(s.lambdaHistory) - g["Lambda"])) <= 1e-6 * np.max(g["Lambda"])
     assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
 
 

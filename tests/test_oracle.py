@@ -6,7 +6,7 @@ import pytest
 from conftest import golden
 from oracle.element import SmallStrainElements, TLElements, make_elements
 from oracle.mesh import BoxMesh
-from oracle.nist import NIST, Model, Step
+from oracle.nist import NIST, IndirectControl, Model, NISTArcLength, Step
 from oracle.system import csr_slot_map, csr_update, element_dofs, vij_pattern
 
 
@@ -93,6 +93,31 @@ def test_oracle_nist_cantilever_matches_reference():
     assert np.max(np.abs(U - g["U"])) < 1e-12
     assert [it for _, it in s.history] == list(g["iters"])
     assert abs(U.min() - (-4.65324e-3)) < 1e-8
+
+
+def arclength_case(g):
+    """The J2 bar of the arc-length fixture: x = 0 clamped, reference node forces on the x = lX face,
+    indirect control of the x displacement of the nodes closest to (x1, 0, 0) and (x2, 0, 0)."""
+    mesh = BoxMesh(int(g["nX"]), int(g["nY"]), int(g["nZ"]), float(g["lX"]), float(g["lY"]), float(g["lZ"]))
+    n1, n2 = (int(np.argmin(np.linalg.norm(mesh.coords - [float(g[k]), 0.0, 0.0], axis=1))) for k in ("x1", "x2"))
+    idcs = np.concatenate([3 * n1 + np.arange(3), 3 * n2 + np.arange(3)])
+    return mesh, idcs, np.array([-1.0, 0.0, 0.0, 1.0, 0.0, 0.0])
+
+
+def test_oracle_arclength_indirect_control_matches_reference():
+    """solvers/nonlinearimplicitstaticparallelarclength.py with stepactions/indirectcontrol.py: the
+    reference's displacements, Newton iteration counts and load factors."""
+    g = golden("nist_arclength_j2_10x2x2.npz")
+    mesh, idcs, c = arclength_case(g)
+    model = _box_model(mesh, "C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], [("gen_left", [0, 1, 2])],
+                       nodeforces=[("gen_right", [float(g["f"]), 0.0, 0.0])])  # fmt: skip
+    s = NISTArcLength(model, IndirectControl(idcs, c, float(g["L"])))
+    U, _ = s.solveStep(Step(startInc=float(g["maxInc"]), maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
+    assert [it for _, it in s.history] == list(g["iters"])
+    assert np.max(np.abs(np.array(s.lambdaHistory) - g["Lambda"])) <= 1e-12 * np.max(g["Lambda"])
+    assert np.max(np.abs(U - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
+    # the control: c . U over the controlled DOFs reaches L at the end of the step
+    assert abs(c.dot(U[idcs]) - float(g["L"])) <= 1e-12
 
 
 @pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20"])
