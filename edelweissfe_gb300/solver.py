@@ -524,7 +524,7 @@ class NISTGPUArcLength(NISTGPU):
             ddU_0 = self.linearSolve(R_0)
             ddU_f = self.linearSolve(R_f)
             ctlValues = torch.stack([dU[idx], ddU_0[idx], ddU_f[idx]]).cpu().numpy()
-            ddLambda = ctl.computeDDLambda(ctlValues[0], ctlValues[1], ctlValues[2], timeStep)
+            ddLambda = float(ctl.computeDDLambda(ctlValues[0], ctlValues[1], ctlValues[2], timeStep))
             ddU = ddU_0 + ddLambda * ddU_f
             dU += ddU
             dLambda += ddLambda
