@@ -190,10 +190,12 @@ struct TypeInfo {
     int tl;
 };
 
+// elements/library.py:212-291 (small strain), :453-532 (total Lagrange) and the aliases of :535-551
 const TypeInfo kTypes[] = {
-    {"C3D8", 8, 1, 0},   {"C3D8R", 8, 0, 0},    {"C3D8E", 8, 2, 0},   {"C3D20", 20, 2, 0},
+    {"C3D8", 8, 1, 0},    {"C3D8R", 8, 0, 0},   {"C3D8E", 8, 2, 0},    {"C3D20", 20, 2, 0},
     {"C3D20R", 20, 1, 0}, {"C3D8TL", 8, 1, 1},  {"C3D20TL", 20, 2, 1}, {"C3D8RTL", 8, 0, 1},
-    {"C3D20RTL", 20, 1, 1},
+    {"C3D8ETL", 8, 2, 1}, {"C3D20RTL", 20, 1, 1}, {"C3D8N", 8, 1, 0},  {"C3D20N", 20, 2, 0},
+    {"C3D8NTL", 8, 1, 1}, {"C3D20NTL", 20, 2, 1},
 };
 
 bool ieq(const char* a, const char* b) {

@@ -368,7 +368,7 @@ static ef_status launch_tl_apply(const Group& g, const double* x, const double* 
 
 using namespace ef;
 
-#define EF_TL_TYPES(M) M(8, 8) M(8, 1) M(20, 27) M(20, 8)
+#define EF_TL_TYPES(M) M(8, 8) M(8, 1) M(8, 27) M(20, 27) M(20, 8)
 
 // Number of FP64 values per Gauss point that the total-Lagrange kernels keep for the
 // matrix-free refinement residual.

@@ -1,7 +1,8 @@
 """Hexahedral element library of the oracle: node tables, Gauss rules, shape functions.
 
-Follows ``elements/library.py`` (C3D8 :212-227, C3D8R :228-242, C3D20 :260-275,
-C3D20R :276-291, C3D8TL :453-467, C3D20TL :501-515, C3D20RTL :516-531) and the
+Follows ``elements/library.py`` (C3D8 :212-227, C3D8R :228-242, C3D8E :244-259, C3D20 :260-275,
+C3D20R :276-291, C3D8TL :453-467, C3D8RTL :469-484, C3D8ETL :485-500, C3D20TL :501-515,
+C3D20RTL :517-532) and the
 shape-function conventions of
 ``elements/displacementelement/_elementcomputationmatrices.py``:
 
@@ -107,6 +108,7 @@ ELEMENT_TYPES = {
     "C3D20R": (HEX20_NODES, _rule_2x2x2, False),
     "C3D8TL": (HEX8_NODES, _rule_2x2x2, True),
     "C3D8RTL": (HEX8_NODES, _rule_1, True),
+    "C3D8ETL": (HEX8_NODES, _rule_3x3x3, True),
     "C3D20TL": (HEX20_NODES, _rule_3x3x3, True),
     "C3D20RTL": (HEX20_NODES, _rule_2x2x2, True),
 }

@@ -6,6 +6,7 @@ Run in a container where the reference sources are available (default
     python tests/golden/make_golden.py        # all fixtures
     python tests/golden/make_golden.py tl     # only the total-Lagrange ones
     python tests/golden/make_golden.py arclength   # only the arc-length one
+    python tests/golden/make_golden.py variants    # only the other integration rules
 
 What it does:
 
@@ -442,6 +443,20 @@ def arclength_fixtures(scratch):
                         Lambda=np.array([r[1] for r in rec]), **{k: np.array(v) for k, v in ARC_CASE.items()})
 
 
+J2 = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
+
+
+def variant_fixtures():
+    """The other integration rules of elements/library.py: one point (C3D8R, C3D8RTL), 2x2x2 on
+    the 20-node hexahedron (C3D20R, C3D20RTL) and 3x3x3 on the 8-node one (C3D8E, C3D8ETL)."""
+    element_fixture("C3D8R", "vonmises", J2, 16, seed=21, plastic=True)
+    element_fixture("C3D8E", "vonmises", J2, 8, seed=22, plastic=True)
+    element_fixture("C3D20R", "vonmises", J2, 8, seed=23, plastic=True)
+    element_fixture_tl("C3D8RTL", [80.0, 200.0], 16, seed=24)
+    element_fixture_tl("C3D8ETL", [80.0, 200.0], 8, seed=25)
+    element_fixture_tl("C3D20RTL", [80.0, 200.0], 8, seed=26)
+
+
 def main():
     scratch = tempfile.mkdtemp(prefix="efref_")
     prepare_reference(scratch)
@@ -451,6 +466,10 @@ def main():
         return
     if sys.argv[1:] == ["arclength"]:  # only the arc-length fixture
         arclength_fixtures(scratch)
+        shutil.rmtree(scratch, ignore_errors=True)
+        return
+    if sys.argv[1:] == ["variants"]:  # only the reduced / enhanced integration element types
+        variant_fixtures()
         shutil.rmtree(scratch, ignore_errors=True)
         return
     copy_uref()
@@ -463,6 +482,7 @@ def main():
     nist_fixtures(scratch)
     tl_fixtures(scratch)
     arclength_fixtures(scratch)
+    variant_fixtures()
     shutil.rmtree(scratch, ignore_errors=True)
 
 

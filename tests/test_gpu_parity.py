@@ -372,3 +372,15 @@ def test_nist_gpu_tied_hex20_hex8_total_lagrange_matches_oracle(gpu_lib, mode):
     sl, a, b = spec["mesh"]["ties"]
     u = U.cpu().numpy().reshape(-1, 3)
     assert np.max(np.abs(u[sl] - 0.5 * (u[a] + u[b]))) <= 1e-14 * np.max(np.abs(u))
+
+
+ELEM_VARIANTS = [("C3D8R", "vonmises"), ("C3D8E", "vonmises"), ("C3D20R", "vonmises"), ("C3D8RTL", "neohookewa"),
+                 ("C3D8ETL", "neohookewa"), ("C3D20RTL", "neohookewa")]  # fmt: skip
+
+
+@pytest.mark.parametrize("keFp64", [True, False], ids=["fp64", "fp32K"])
+@pytest.mark.parametrize("elType,mat", ELEM_VARIANTS)
+def test_element_kernel_other_integration_rules_match_reference_fixture(gpu_lib, elType, mat, keFp64):
+    """One Gauss point (C3D8R, C3D8RTL), 2x2x2 on the 20-node hexahedron (C3D20R, C3D20RTL) and
+    3x3x3 on the 8-node one (C3D8E, C3D8ETL) against the reference's fixtures, as above."""
+    test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, keFp64)

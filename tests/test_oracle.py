@@ -53,6 +53,9 @@ ELEM_FIXTURES = [
     ("C3D8", "vonmisesexp"),
     ("C3D20", "linearelastic"),
     ("C3D20", "vonmises"),
+    ("C3D8R", "vonmises"),
+    ("C3D8E", "vonmises"),
+    ("C3D20R", "vonmises"),
 ]
 
 
@@ -135,7 +138,7 @@ def test_oracle_nist_j2_matches_reference(case):
     assert np.max(np.abs(U - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
 
 
-@pytest.mark.parametrize("elType", ["C3D8TL", "C3D20TL"])
+@pytest.mark.parametrize("elType", ["C3D8TL", "C3D20TL", "C3D8RTL", "C3D8ETL", "C3D20RTL"])
 def test_oracle_tl_element_matches_reference(elType):
     g = golden(f"elem_{elType}_neohookewa.npz")
     els = TLElements(elType, g["coords"], "neohookewa", g["props"])
