@@ -103,3 +103,89 @@ def test_smoothed_aggregation_index_maps(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "failures 0" in out.stdout
+
+
+def _material_points(rng, n, plastic):
+    sig = rng.normal(0.0, 120.0 if plastic else 50.0, (n, 6))
+    kap = rng.uniform(0.0, 0.01, n)
+    de = rng.normal(0.0, 1e-3, (n, 6)) * rng.uniform(0.0, 2.0, (n, 1))
+    de[::7] = 0.0  # the zero-increment shortcut
+    de[3::11] *= 1e-16  # below its threshold |de| < 1e-14
+    return sig, kap, de
+
+
+def _run_materials_check(tmp_path, exe, mat, props, sig, kap, de):
+    import subprocess
+
+    n = sig.shape[0]
+    p8 = np.zeros(8)
+    p8[: len(props)] = props
+    E, nu = props[0], props[1]
+    p8[6] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))  # lambda and G as the host forms them
+    p8[7] = E / (2.0 * (1.0 + nu))
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        f.write(np.array([n, mat], np.int32).tobytes())
+        f.write(p8.tobytes())
+        f.write(np.hstack([sig, kap[:, None], de]).astype(np.float64).tobytes())
+    r = subprocess.run([exe, str(fin), str(fout)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return np.fromfile(fout, np.float64).reshape(n, 17)
+
+
+def test_element_constitutive_updates_match_oracle(tmp_path):
+    """The element kernel's J2 return map and linear elasticity (edelweissfe_gb300/csrc/materials.h),
+    compiled for the host from the device source, against the oracle (oracle/materials.py, which
+    follows materials/vonmises/vonmises.py:186-254 and linearelastic.py:185-210) point by point:
+    stress, kappa and the consistent tangent to 1e-12, for linear and exponential hardening,
+    zero increments, and the points where the reference's Newton iteration fails (CutbackRequest)."""
+    import os
+    import shutil
+    import subprocess
+
+    from oracle.materials import ReturnMapFailed, linear_elastic, von_mises
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("no C++ compiler")
+    here = os.path.dirname(os.path.abspath(__file__))
+    exe = str(tmp_path / "materials_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe,
+                    os.path.join(here, "native", "materials_check.cpp")], check=True)  # fmt: skip
+    Is = np.diag([1.0, 1.0, 1.0, 0.5, 0.5, 0.5])
+    one = np.zeros((6, 6))
+    one[:3, :3] = 1.0
+    rng = np.random.default_rng(7)
+    cases = [(1, [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], True), (1, [210000.0, 0.3, 250.0, 1000.0, 80.0, 30.0], True),
+             (1, [210000.0, 0.3, 250.0, 0.0, -240.0, 2e5], True), (0, [210000.0, 0.3], False)]  # fmt: skip
+    nFailed = nPlastic = 0
+    for mat, props, plastic in cases:
+        sig, kap, de = _material_points(rng, 4000, plastic)
+        out = _run_materials_check(tmp_path, exe, mat, props, sig, kap, de)
+        for p in range(sig.shape[0]):
+            try:
+                with np.errstate(all="ignore"):
+                    if mat == 1:
+                        s1, k1, C = von_mises(props, sig[p : p + 1], kap[p : p + 1, None], de[p : p + 1])
+                    else:
+                        s1, k1, C = linear_elastic(props, sig[p : p + 1], np.zeros((1, 0)), de[p : p + 1])
+                        k1 = kap[p : p + 1, None]
+            except ReturnMapFailed:
+                assert out[p, 0] == 0.0, (props, p)
+                nFailed += 1
+                continue
+            assert out[p, 0] == 1.0, (props, p)
+            if not np.all(np.isfinite(s1)):  # the iteration ran into NaN: the kernel flags it
+                assert not np.all(np.isfinite(out[p, 1:7]))
+                continue
+            y = out[p]
+            scale = np.max(np.abs(s1)) + 1.0
+            assert np.max(np.abs(y[1:7] - s1[0])) <= 1e-12 * scale, (props, p)
+            assert abs(y[7] - k1[0, 0]) <= 1e-12 * (abs(k1[0, 0]) + 1e-6), (props, p)
+            n = y[11:17]
+            Cg = y[8] * one + 2.0 * y[9] * Is - y[10] * np.outer(n, n)
+            assert np.max(np.abs(Cg - C[0])) <= 1e-12 * np.max(np.abs(C[0])), (props, p)
+            nPlastic += y[10] != 0.0
+    assert nFailed > 0 and nPlastic > 1000
