@@ -74,6 +74,12 @@ __device__ __forceinline__ float2 df_split_sel(double d, int intConv) { return i
 __device__ __forceinline__ double df_value_sel(const DF& a, int intConv) {
     return intConv ? df_value_i(a) : df_value(a);
 }
+// NaN test: a floating-point compare (FP64 pipe), or with intConv the exponent-all-ones,
+// nonzero-fraction test on the bit pattern (integer pipe)
+__device__ __forceinline__ bool is_nan_sel(double x, int intConv) {
+    if (intConv) return ((unsigned long long)__double_as_longlong(x) << 1) > (0x7FF0000000000000ull << 1);
+    return !(x == x);
+}
 
 // acc += a * b for a = (ah, al), b = (bh, bl): the product ah bh exactly (its rounding error from
 // an FMA), the cross terms ah bl + al bh in FP32 (relative 2^-24 of the product), al bl dropped
@@ -259,7 +265,7 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
             double kap = stateIn[12 * nQPtot + qi];
             if (!mat_von_mises(pv, sig, &kap, de, mo)) atomicOr(flags, EF_FLAG_RETURNMAP);
             stateOut[12 * nQPtot + qi] = kap;
-            if (!(kap == kap)) atomicOr(flags, EF_FLAG_NAN);
+            if (is_nan_sel(kap, intConv)) atomicOr(flags, EF_FLAG_NAN);
         } else {
             mat_linear_elastic(pv, sig, de, mo);
         }
@@ -267,7 +273,7 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
         for (int i = 0; i < 6; ++i) {
             stateOut[i * nQPtot + qi] = sig[i];
             stateOut[(6 + i) * nQPtot + qi] = stateIn[(6 + i) * nQPtot + qi] + de[i];
-            if (!(sig[i] == sig[i])) atomicOr(flags, EF_FLAG_NAN);
+            if (is_nan_sel(sig[i], intConv)) atomicOr(flags, EF_FLAG_NAN);
         }
 #pragma unroll
         for (int i = 0; i < 6; ++i) sh.sw[le][6 * q + i] = df_split_sel(sig[i] * wdet, intConv);

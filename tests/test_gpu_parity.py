@@ -384,3 +384,12 @@ def test_element_kernel_other_integration_rules_match_reference_fixture(gpu_lib,
     """One Gauss point (C3D8R, C3D8RTL), 2x2x2 on the 20-node hexahedron (C3D20R, C3D20RTL) and
     3x3x3 on the 8-node one (C3D8E, C3D8ETL) against the reference's fixtures, as above."""
     test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, keFp64)
+
+
+@pytest.mark.parametrize("elType,mat", [("C3D8", "vonmises"), ("C3D8", "vonmisesexp"), ("C3D20", "vonmises"),
+                                        ("C3D8R", "vonmises")])  # fmt: skip
+def test_element_kernel_integer_conversions_match_reference_fixture(gpu_lib, elType, mat, monkeypatch):
+    """The element kernel with its FP64 <-> FP32-pair conversions and NaN tests done by integer
+    operations (EF_ELEM_INTCONV=1, csrc/dfloat_bits.h) against the reference's fixtures, as above."""
+    monkeypatch.setenv("EF_ELEM_INTCONV", "1")
+    test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, False)
