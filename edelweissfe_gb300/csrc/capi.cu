@@ -384,6 +384,17 @@ struct AmgLevel {
     float *saPv = nullptr, *saAPv = nullptr, *saW = nullptr;
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
+
+    // device arrays of the level (null ones are skipped)
+    void free_device() {
+        for (void* p : {(void*)rowPtr, (void*)colIdx, (void*)rowOfBlock, (void*)diagPos, (void*)vals, (void*)binv,
+                        (void*)dead, (void*)agg, (void*)offs, (void*)aggPtr, (void*)aggIdx, (void*)gseg, (void*)gsrc,
+                        (void*)x, (void*)x2, (void*)valsH, (void*)r, (void*)t, (void*)saPRowPtr, (void*)saPCol,
+                        (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
+                        (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
+                        (void*)saPv, (void*)saAPv, (void*)saW})
+            if (p) cudaFree(p);
+    }
 };
 
 // element result collector: device lists of elements and quadrature points of one group, the
@@ -647,31 +658,7 @@ void ef_destroy(ef_ctx* c) {
     for (auto* p : c->w64k) F(p);
     for (auto* p : c->dTang) F(p);
     F(c->dYe);
-    for (auto& L : c->amg) {
-        F(L.rowPtr);
-        F(L.colIdx);
-        F(L.rowOfBlock);
-        F(L.diagPos);
-        F(L.vals);
-        F(L.binv);
-        F(L.dead);
-        F(L.agg);
-        F(L.offs);
-        F(L.aggPtr);
-        F(L.aggIdx);
-        F(L.gseg);
-        F(L.gsrc);
-        F(L.x);
-        F(L.x2);
-        F(L.valsH);
-        for (void* q : {(void*)L.saPRowPtr, (void*)L.saPCol, (void*)L.saPRow, (void*)L.saPSrc, (void*)L.saTPtr,
-                        (void*)L.saTIdx, (void*)L.saApRow, (void*)L.saApK, (void*)L.saApP, (void*)L.saCP,
-                        (void*)L.saCAP, (void*)L.saPSeg, (void*)L.saApSeg, (void*)L.saCSeg, (void*)L.saPv,
-                        (void*)L.saAPv, (void*)L.saW})
-            F(q);
-        F(L.r);
-        F(L.t);
-    }
+    for (auto& L : c->amg) L.free_device();
     F(c->amgCoarsestInv);
     F(c->amgPow[0]);
     F(c->amgPow[1]);
@@ -1751,6 +1738,13 @@ static ef_status amg_build(ef_ctx* c) {
     int nFine = n0;
     while (nFine > ef_max_coarsest_nodes()) {
         AmgLevel L;
+        // frees the level's device arrays on an early error return, until the context owns them
+        struct Guard {
+            AmgLevel* L;
+            ~Guard() {
+                if (L) L->free_device();
+            }
+        } guard{&L};
         const int nC = aggregate(nFine, *pRow, *pCol, L.hAgg);
         if (nC >= nFine) break;  // no coarsening progress
         L.nN = nC;
@@ -1871,6 +1865,7 @@ static ef_status amg_build(ef_ctx* c) {
             L.valsH = dalloc<uint16_t>((size_t)L.nBlocks * BCo * BCo, &st);
             if (!L.valsH) return st;
         }
+        guard.L = nullptr;
         c->amg.push_back(std::move(L));
         pRow = &c->amg.back().hRowPtr;
         pCol = &c->amg.back().hColIdx;
