@@ -744,6 +744,13 @@ def run_reference(a):
         return
     t0 = time.time()
     procs = max(1, min(16, os.cpu_count() or 1))
+    warm = 0
+    for _ in range(max(0, a.warmup)):  # untimed, on a small sample (worker start-up, imports, caches)
+        cpu_baseline(a, newton_per_step=PCG_NEWTON_PER_STEP, krylov_per_step=PCG_KRYLOV_PER_STEP, procs=procs,
+                     sample=250 * procs)  # fmt: skip
+        warm += 1
+        if time.time() - t0 > 60:
+            break
     vals = []
     for _ in range(max(1, a.steps)):
         cb = cpu_baseline(a, newton_per_step=PCG_NEWTON_PER_STEP, krylov_per_step=PCG_KRYLOV_PER_STEP, procs=procs,
@@ -759,7 +766,7 @@ def run_reference(a):
         "unit": "s",
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": len(vals),
-        "warmup": 0,
+        "warmup": warm,
         "ms_per_step": v * 1e3,
         "higher_is_better": False,
         "scaling": "weak",
