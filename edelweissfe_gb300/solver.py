@@ -24,7 +24,7 @@ import torch
 
 from . import _lib
 from .exceptions import CutbackRequest, DivergingSolution, ReachedMaxIterations, StepFailed
-from .model import BodyForce, DirichletBC, Model, NodeForces
+from .model import Model
 
 
 @dataclass
