@@ -139,3 +139,108 @@ def test_newton_driver_host_logic_matches_reference():
     U, _ = s.solveStep(Step(maxInc=float(g["maxInc"]), minInc=1e-6, maxIter=25))
     assert [it for _, it in s.iterationHistory] == list(g["iters"])
     assert np.max(np.abs(U.numpy() - g["U"])) <= 1e-10 * np.max(np.abs(g["U"]))
+
+
+_NAN_DOF = 3 * ((2 * 3 + 1) * 3 + 1)  # x of the node (2, 1, 1) of a 4 x 2 x 2 box: a free DOF
+
+
+class _ElementLib(_OracleLib):
+    """ef_compute_elements / ef_element_status answered by the oracle's element loop, with a
+    return-map failure or a NaN injected at chosen element-loop calls (1-based), so that the
+    solver's own status mapping and cutback handling run."""
+
+    def __init__(self, nDof, elements, oracle, inject):
+        super().__init__(nDof, elements)
+        self.oracle = oracle
+        self.inject = inject
+        self.calls = 0
+        self.status = 0
+        self.V = None
+
+    def ef_compute_elements(self, ctx, U_np, dU, time2, dT, P, F, stream):
+        from oracle.materials import ReturnMapFailed
+
+        self.calls += 1
+        kind = self.inject.get(self.calls)
+        try:
+            if kind == "returnmap":
+                raise ReturnMapFailed("Von Mises Newton failed.")
+            p, self.V, f = self.oracle.computeElements(self._arr(U_np).copy(), self._arr(dU).copy())
+        except ReturnMapFailed:
+            self.status = 1  # EF_CUTBACK
+            return 0
+        if kind == "nan":
+            p = p.copy()
+            p[_NAN_DOF] = np.nan
+        self._arr(P)[:] = p
+        self._arr(F)[:] = f
+        self.status = 2 if np.isnan(p).any() else 0  # EF_NAN
+        return 0
+
+    def ef_element_status(self, ctx, stream, pNewDT):
+        st, self.status = self.status, 0
+        if pNewDT is not None:
+            pNewDT._obj.value = 0.5 if st == 1 else 1.0
+        return st
+
+
+def test_newton_driver_cutbacks_match_oracle():
+    """Failure handling of NISTGPU (solvers/nonlinearimplicitstatic.py:247-279): a return-map
+    failure reported by the element status (CutbackRequest, increment x max(0.5, cutbackFactor)),
+    a NaN in the element results (DivergingSolution, x cutbackFactor) and too many iterations
+    (ReachedMaxIterations), injected at the same element-loop calls of the oracle's NIST, give the
+    same increment sequence, iteration counts and displacements."""
+    import math
+
+    from edelweissfe_gb300.mesh import box_mesh
+    from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model
+    from edelweissfe_gb300.solver import NISTGPU, Step
+    from oracle.materials import ReturnMapFailed
+    from oracle.nist import Step as OracleStep
+
+    props = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
+    dims = (4, 2, 2, 1.0, 0.5, 0.5)
+    inject = {12: "returnmap", 20: "nan"}
+    results = {}
+    for side in ("oracle", "gpu-host"):
+        m = box_mesh(*dims)
+        mesh = BoxMesh(*dims)
+        elements = make_elements("C3D8", mesh.coords[mesh.elements], "vonmises", props)
+        dirs = [DirichletBC(m["nodeSets"]["gen_left"], {0: 0.0, 1: 0.0, 2: 0.0}),
+                DirichletBC(m["nodeSets"]["gen_right"], {0: 0.01})]  # fmt: skip
+        oracle = NIST(OracleModel(3 * mesh.nNodes, [(elements, element_dofs(mesh.elements))],
+                                  [(d.dofs, d.delta) for d in dirs], []))  # fmt: skip
+        if side == "oracle":
+            calls = [0]
+            base = oracle.computeElements
+
+            def computeElements(U_np, dU, base=base, calls=calls):
+                calls[0] += 1
+                kind = inject.get(calls[0])
+                if kind == "returnmap":
+                    raise ReturnMapFailed("Von Mises Newton failed.")
+                P, V, F = base(U_np, dU)
+                if kind == "nan":
+                    P = P.copy()
+                    P[_NAN_DOF] = np.nan
+                return P, V, F
+
+            oracle.computeElements = computeElements
+            with np.errstate(invalid="ignore"):
+                U, _ = oracle.solveStep(OracleStep(maxInc=0.5, minInc=1e-4, maxIter=4))
+            results[side] = ([(n, it if it >= 0 else math.inf) for n, it in oracle.history], U)
+        else:
+            model = Model(m["coords"], [ElementGroup("C3D8", m["elements"], "vonmises", np.array(props))])
+            s = _oracle_backed(NISTGPU, model, dirs, [], elements, element_dofs(mesh.elements))
+            lib = _ElementLib(3 * mesh.nNodes, elements, oracle, inject)
+            s.lib = lib
+            type(s).computeElements = NISTGPU.computeElements  # the solver's own status mapping
+            type(s).assembleStiffnessCSR = lambda self: setattr(self, "_A", oracle.applyDirichletK(
+                oracle.assembleStiffnessCSR(lib.V)))  # fmt: skip
+            with np.errstate(invalid="ignore"):
+                U, _ = s.solveStep(Step(maxInc=0.5, minInc=1e-4, maxIter=4))
+            results[side] = (list(s.iterationHistory), U.numpy())
+    (ho, Uo), (hg, Ug) = results["oracle"], results["gpu-host"]
+    assert hg == ho, (hg, ho)
+    assert sum(1 for _, it in ho if it == math.inf) >= 3  # the iteration limit and both injections
+    assert np.max(np.abs(Ug - Uo)) <= 1e-12 * np.max(np.abs(Uo))
