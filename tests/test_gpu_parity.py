@@ -425,3 +425,47 @@ def test_element_kernel_integer_conversions_match_reference_fixture(gpu_lib, elT
     operations (EF_ELEM_INTCONV=1, csrc/dfloat_bits.h) against the reference's fixtures, as above."""
     monkeypatch.setenv("EF_ELEM_INTCONV", "1")
     test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, False)
+
+
+def test_element_status_reports_return_map_failures_and_nan(gpu_lib):
+    """Failure detection on the device, mapped to the reference's exceptions by the host: with a
+    softening J2 law under which the consistency iteration of three Gauss points of the fixture's
+    elements exceeds its 15 iterations (the oracle raises there; materials/vonmises/vonmises.py:231
+    raises CutbackRequest(.., 0.5)), the element status is EF_CUTBACK with cutback size 0.5; a NaN
+    in the displacement increment gives EF_NAN (DivergingSolution); reading the status resets it;
+    a zero increment (the shortcut, no iteration) gives EF_OK."""
+    from edelweissfe_gb300 import _lib
+    from oracle.element import SmallStrainElements
+    from oracle.materials import ReturnMapFailed
+
+    g = golden("elem_C3D8_vonmises.npz")
+    props = np.array([210000.0, 0.3, 250.0, 0.0, -200.0, 1e5])
+    els = SmallStrainElements("C3D8", g["coords"], "vonmises", props)
+    els.stateRef[:] = g["state0"]
+    with pytest.raises(ReturnMapFailed), np.errstate(all="ignore"):
+        els.compute_yourself(g["U"], g["dU"])
+    ctx, nDof = _ctx_for_elements(gpu_lib, "C3D8", "vonmises", props, g["coords"], False)
+    try:
+        state0 = np.ascontiguousarray(g["state0"])
+        _lib.check(gpu_lib.ef_set_state(ctx, 0, state0.ctypes.data), "ef_set_state")
+        dev = torch.device("cuda")
+        U = torch.as_tensor(g["U"].reshape(-1), device=dev)
+        P = torch.zeros(nDof, dtype=torch.float64, device=dev)
+        F = torch.zeros_like(P)
+        t = np.array([0.5, 0.5])
+        newDT = ctypes.c_double(0.0)
+
+        def run(dU):
+            _lib.check(gpu_lib.ef_compute_elements(ctx, U.data_ptr(), dU.data_ptr(), t.ctypes.data, 0.1, P.data_ptr(),
+                                                   F.data_ptr(), None), "ef_compute_elements")  # fmt: skip
+            return gpu_lib.ef_element_status(ctx, None, ctypes.byref(newDT))
+
+        dU = torch.as_tensor(g["dU"].reshape(-1), device=dev)
+        assert run(dU) == _lib.EF_CUTBACK and newDT.value == 0.5
+        assert gpu_lib.ef_element_status(ctx, None, ctypes.byref(newDT)) == _lib.EF_OK and newDT.value == 1.0
+        dUn = dU.clone()
+        dUn[0] = float("nan")
+        assert run(dUn) == _lib.EF_NAN
+        assert run(torch.zeros_like(dU)) == _lib.EF_OK
+    finally:
+        gpu_lib.ef_destroy(ctx)
