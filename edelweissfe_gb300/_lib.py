@@ -97,6 +97,7 @@ SIGNATURES = {
     "ef_results_device": (c_int, [c_vp, c_int, ctypes.POINTER(c_vp), ctypes.POINTER(c_i64)]),
     "ef_results_destroy": (c_int, [c_vp, c_int]),
     "ef_accept_state": (c_int, [c_vp]),
+    "ef_reset_state": (c_int, [c_vp]),
     "ef_add_body_force": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp]),
     "ef_export_vij": (c_int, [c_vp, c_vp, c_vp]),
     "ef_csr_pattern": (c_int, [c_vp, c_vp, c_vp]),

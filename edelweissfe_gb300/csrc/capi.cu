@@ -1455,6 +1455,14 @@ ef_status ef_accept_state(ef_ctx* c) {
     return EF_OK;
 }
 
+ef_status ef_reset_state(ef_ctx* c) {
+    EF_REQUIRE_FINALIZED(c);
+    for (auto& g : c->groups)
+        EF_CUDA(cudaMemcpy(g.state[1 - g.cur], g.state[g.cur], sizeof(double) * g.nState * g.nEl * g.nQP,
+                           cudaMemcpyDeviceToDevice));
+    return EF_OK;
+}
+
 ef_status ef_add_body_force(ef_ctx* c, int groupId, const double* load3, double* PExt, void* stream) {
     EF_REQUIRE_FINALIZED(c);
     if (groupId < 0 || groupId >= (int)c->groups.size() || !load3 || !PExt) {

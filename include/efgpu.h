@@ -98,8 +98,9 @@ int64_t ef_kernel_launches(void);
 ef_status ef_create(int64_t nDof, const double* nodeCoords, ef_ctx** out);
 void ef_destroy(ef_ctx* ctx);
 
-/* elType: C3D8, C3D8R, C3D8E, C3D20, C3D20R (small strain) or C3D8TL, C3D20TL (total
- * Lagrange); material: linearelastic [E, nu], vonmises [E, nu, fy0, HLin, dfy, delta],
+/* elType (elements/library.py): C3D8, C3D8R, C3D8E, C3D20, C3D20R (small strain) or C3D8TL,
+ * C3D8RTL, C3D8ETL, C3D20TL, C3D20RTL (total Lagrange), and the aliases C3D8N, C3D20N, C3D8NTL,
+ * C3D20NTL; material: linearelastic [E, nu], vonmises [E, nu, fy0, HLin, dfy, delta],
  * neohookewa [mu, K].  elDofs: host [nEl][3*nNodes] global DOFs of each element in element
  * DOF order (DofManager.idcsOfHigherOrderEntitiesInDofVector); each node's three DOFs must
  * be consecutive.  Groups are appended in the reference's element order. */
@@ -153,6 +154,11 @@ ef_status ef_results_destroy(ef_ctx* ctx, int collectorId);
  * state is copied into the committed state (device-wide synchronous copy; the state buffers keep
  * their addresses, so element launches captured in a CUDA graph remain valid). */
 ef_status ef_accept_state(ef_ctx* ctx);
+/* elements/displacementelement/element.py:381-384 resetToLastValidState for all elements: the
+ * trial state is set back to the committed one (device-wide synchronous copy).  Every element
+ * pass starts from the committed state, so only a caller that reads the trial state
+ * (ef_get_state or ef_results_update with trial = 1) sees a difference. */
+ef_status ef_reset_state(ef_ctx* ctx);
 
 /* elements/displacementelement/element.py:348-371 computeBodyForce, added into PExt (device [nDof]) */
 ef_status ef_add_body_force(ef_ctx* ctx, int groupId, const double* load3, double* PExt, void* stream);

@@ -85,6 +85,14 @@ def test_result_collector_gathers_the_state(gpu_lib, elType, mat, name):
         # the whole state vector of one point
         cOne, full = collect([3], [1], 0, nState, 1)
         assert np.array_equal(full[0, 0], trial[3, 1])
+        # resetToLastValidState: the trial state is the committed one again; a new pass restores it
+        _lib.check(gpu_lib.ef_reset_state(ctx), "ef_reset_state")
+        back = np.zeros_like(trial)
+        _lib.check(gpu_lib.ef_get_state(ctx, 0, 1, back.ctypes.data), "ef_get_state")
+        assert np.array_equal(back, state0)
+        _lib.check(gpu_lib.ef_compute_elements(ctx, U.data_ptr(), dU.data_ptr(), t.ctypes.data, 0.1, P.data_ptr(),
+                                               F.data_ptr(), None), "ef_compute_elements")  # fmt: skip
+        assert gpu_lib.ef_element_status(ctx, None, None) == _lib.EF_OK
         # acceptLastState: the committed stress is the accepted trial stress
         _lib.check(gpu_lib.ef_accept_state(ctx), "ef_accept_state")
         out = np.full((nEl, nQP, 6), np.nan)
