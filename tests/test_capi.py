@@ -39,3 +39,11 @@ def test_argument_validation_without_gpu():
     assert lib.ef_create(0, X.ctypes.data, ctypes.byref(ctx)) == _lib.EF_ERR_ARG
     assert lib.ef_finalize(None, 0) == _lib.EF_ERR_ARG
     assert lib.ef_compute_elements(None, None, None, None, 0.0, None, None, None) == _lib.EF_ERR_STATE
+    # calls on a missing context fail with EF_ERR_STATE before touching the device
+    cid = ctypes.c_int(-1)
+    assert lib.ef_results_create(None, 0, None, 0, None, 0, 0, 6, ctypes.byref(cid)) == _lib.EF_ERR_STATE
+    assert cid.value == -1
+    assert lib.ef_results_update(None, 0, 0, None, None) == _lib.EF_ERR_STATE
+    assert lib.ef_results_destroy(None, 0) == _lib.EF_ERR_STATE
+    assert lib.ef_reset_state(None) == _lib.EF_ERR_STATE
+    assert lib.ef_accept_state(None) == _lib.EF_ERR_STATE
