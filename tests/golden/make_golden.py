@@ -351,6 +351,21 @@ def run_inp(text, scratch, name):
     return U, np.array(iters)
 
 
+NIST_VARIANT_CASES = {
+    "j2_box_4x2x2_c3d20r": dict(nX=4, nY=2, nZ=2, lX=0.4, lY=0.2, lZ=0.2, elType="C3D20R", maxInc=0.1, ux=0.0015),
+    "j2_box_8x3x3_c3d8e": dict(nX=8, nY=3, nZ=3, lX=0.8, lY=0.3, lZ=0.3, elType="C3D8E", maxInc=0.1, ux=0.0016),
+}
+
+
+def nist_variant_fixtures(scratch):
+    """NIST runs of J2 boxes with the 2x2x2 rule on the 20-node and the 3x3x3 rule on the 8-node
+    hexahedron (C3D20R, C3D8E)."""
+    for name, c in NIST_VARIANT_CASES.items():
+        text = BOX_J2_INP.format(E=210000.0, nu=0.3, fy=250.0, H=1000.0, **c)
+        U, it = run_inp(text, scratch, name)
+        np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
+
+
 def nist_fixtures(scratch):
     U, it = run_inp(CANTILEVER_INP, scratch, "cantilever")
     np.savez_compressed(os.path.join(HERE, "nist_cantilever_20x4x4.npz"), U=U, iters=it)
@@ -470,6 +485,7 @@ def main():
         return
     if sys.argv[1:] == ["variants"]:  # only the reduced / enhanced integration element types
         variant_fixtures()
+        nist_variant_fixtures(scratch)
         shutil.rmtree(scratch, ignore_errors=True)
         return
     copy_uref()
@@ -483,6 +499,7 @@ def main():
     tl_fixtures(scratch)
     arclength_fixtures(scratch)
     variant_fixtures()
+    nist_variant_fixtures(scratch)
     shutil.rmtree(scratch, ignore_errors=True)
 
 

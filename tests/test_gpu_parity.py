@@ -151,7 +151,7 @@ def test_nist_gpu_cantilever_config1(gpu_lib, mode):
 
 
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
-@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20"])
+@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20", "j2_box_4x2x2_c3d20r", "j2_box_8x3x3_c3d8e"])
 def test_nist_gpu_j2_matches_reference(gpu_lib, case, mode):
     """3D J2 boxes: identical Newton iteration counts, displacements within 1e-6 relative."""
     from edelweissfe_gb300.solver import LinSolverOptions, Step

@@ -123,7 +123,7 @@ def test_oracle_arclength_indirect_control_matches_reference():
     assert abs(c.dot(U[idcs]) - float(g["L"])) <= 1e-12
 
 
-@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20"])
+@pytest.mark.parametrize("case", ["j2_box_10x4x4", "j2_box_6x3x3_c3d20", "j2_box_4x2x2_c3d20r", "j2_box_8x3x3_c3d8e"])
 def test_oracle_nist_j2_matches_reference(case):
     g = golden(f"nist_{case}.npz")
     elType = str(g["elType"])
