@@ -359,10 +359,14 @@ NIST_VARIANT_CASES = {
 
 def nist_variant_fixtures(scratch):
     """NIST runs of J2 boxes with the 2x2x2 rule on the 20-node and the 3x3x3 rule on the 8-node
-    hexahedron (C3D20R, C3D8E)."""
+    hexahedron (C3D20R, C3D8E), and of NeoHookeWa boxes with the total-Lagrange counterparts
+    (C3D20RTL, C3D8ETL)."""
     for name, c in NIST_VARIANT_CASES.items():
         text = BOX_J2_INP.format(E=210000.0, nu=0.3, fy=250.0, H=1000.0, **c)
         U, it = run_inp(text, scratch, name)
+        np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
+    for name, c in TL_VARIANT_CASES.items():
+        U, it = run_inp(BOX_TL_INP.format(mu=80.0, K=200.0, **c), scratch, name)
         np.savez_compressed(os.path.join(HERE, f"nist_{name}.npz"), U=U, iters=it, **{k: np.array(v) for k, v in c.items()})
 
 
@@ -382,6 +386,10 @@ def nist_fixtures(scratch):
 TL_CASES = {
     "tl_box_6x3x3_c3d8tl": dict(nX=6, nY=3, nZ=3, lX=0.6, lY=0.3, lZ=0.3, elType="C3D8TL", maxInc=0.25, ux=-0.09),
     "tl_box_3x2x2_c3d20tl": dict(nX=3, nY=2, nZ=2, lX=0.3, lY=0.2, lZ=0.2, elType="C3D20TL", maxInc=0.5, ux=-0.045),
+}
+TL_VARIANT_CASES = {
+    "tl_box_3x2x2_c3d20rtl": dict(nX=3, nY=2, nZ=2, lX=0.3, lY=0.2, lZ=0.2, elType="C3D20RTL", maxInc=0.5, ux=-0.045),
+    "tl_box_4x2x2_c3d8etl": dict(nX=4, nY=2, nZ=2, lX=0.4, lY=0.2, lZ=0.2, elType="C3D8ETL", maxInc=0.25, ux=-0.06),
 }
 
 

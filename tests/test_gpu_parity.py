@@ -192,7 +192,8 @@ def test_nist_gpu_arclength_matches_reference(gpu_lib, mode):
 
 
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
-@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl"])
+@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl", "tl_box_3x2x2_c3d20rtl",
+                                  "tl_box_4x2x2_c3d8etl"])
 def test_nist_gpu_total_lagrange_matches_reference(gpu_lib, case, mode):
     """Total-Lagrange NeoHookeWa boxes compressed by 15 %: identical Newton iteration counts,
     displacements within 1e-6 relative."""

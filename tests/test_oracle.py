@@ -153,7 +153,8 @@ def test_oracle_tl_element_matches_reference(elType):
     assert np.max(np.abs(els.stateTemp - s1) / scale) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl"])
+@pytest.mark.parametrize("case", ["tl_box_6x3x3_c3d8tl", "tl_box_3x2x2_c3d20tl", "tl_box_3x2x2_c3d20rtl",
+                                  "tl_box_4x2x2_c3d8etl"])
 def test_oracle_nist_tl_matches_reference(case):
     g = golden(f"nist_{case}.npz")
     elType = str(g["elType"])
