@@ -84,7 +84,7 @@ class SmallStrainElements:
             st[:, q, 12:] = mstate
             B = self.B[:, q]
             f = self.detJ[:, q] * w[q]
-            Ke += np.einsum("eia,eij,ejb->eab", B, C, B) * f[:, None, None]
+            Ke += np.matmul(B.transpose(0, 2, 1), np.matmul(C, B)) * f[:, None, None]  # B^T (C B) per element
             Pe -= np.einsum("eia,ei->ea", B, stress) * f[:, None]
             st[:, q, 6:12] += dStrain[:, q]
         self.stateTemp = st

@@ -269,7 +269,9 @@ class NIST:
             it += 1
         return U_np, dU, P, it
 
-    def solveStep(self, step: Step, maxIncrements=None):
+    def solveStep(self, step: Step, maxIncrements=None, callback=None):
+        """The increment loop of solveStep (solvers/nonlinearimplicitstatic.py:185-316); callback(ts,
+        iterations, U) after every converged increment."""
         nDof = self.model.nDof
         U = np.zeros(nDof)
         dU = np.zeros(nDof)
@@ -297,6 +299,8 @@ class NIST:
             for els, _ in self.model.groups:
                 els.accept_last_state()
             self.history.append((ts.number, it))
+            if callback is not None:
+                callback(ts, it, U)
             nDone += 1
             if maxIncrements is not None and nDone >= maxIncrements:
                 break

@@ -7,6 +7,7 @@ Run in a container where the reference sources are available (default
     python tests/golden/make_golden.py tl     # only the total-Lagrange ones
     python tests/golden/make_golden.py arclength   # only the arc-length one
     python tests/golden/make_golden.py variants    # only the other integration rules
+    python tests/golden/make_golden.py headline    # only the scaled benchmark box history
 
 What it does:
 
@@ -27,7 +28,10 @@ What it does:
    * ``nist_<case>.npz``: final displacements and Newton iteration counts of
      the reference NIST driver on 3D J2 / elastic boxes,
    * ``nist_arclength_j2_10x2x2.npz``: the same of the reference arc-length
-     driver with indirect displacement control, plus its load factors.
+     driver with indirect displacement control, plus its load factors,
+   * ``nist_j2_box_25x10x10_history.npz``: the benchmark's J2 box at a quarter
+     of its edge counts, displacements after every increment and the final
+     stresses.
 
 Nothing here is needed at test time; the tests only read the ``.npz`` files.
 """
@@ -53,7 +57,12 @@ def copy_uref():
         np.savez_compressed(os.path.join(HERE, f"uref_{name}.npz"), U=U)
 
 
-def prepare_reference(scratch):
+CYTHON_MODULES = ["numerics/csrgenerator", "solvers/nonlinearimplicitstaticparallelmk2", "utils/elementresultcollector"]
+
+
+def prepare_reference(scratch, modules=None):
+    """Copies the reference package into `scratch`, builds its Cython modules there (all of
+    CYTHON_MODULES, or `modules`), installs the stubs and puts it first on sys.path."""
     shutil.copytree(os.path.join(REF, "edelweissfe"), os.path.join(scratch, "edelweissfe"))
     build = os.path.join(scratch, "build_ext.py")
     with open(build, "w") as f:
@@ -61,7 +70,7 @@ def prepare_reference(scratch):
             "from setuptools import setup, Extension\n"
             "from Cython.Build import cythonize\n"
             "import numpy as np\n"
-            "mods = ['numerics/csrgenerator', 'solvers/nonlinearimplicitstaticparallelmk2', 'utils/elementresultcollector']\n"
+            f"mods = {list(modules or CYTHON_MODULES)!r}\n"
             "exts = [Extension('edelweissfe.' + m.replace('/', '.'), ['edelweissfe/' + m + '.pyx'],\n"
             "        include_dirs=[np.get_include()], language='c++', extra_compile_args=['-fopenmp'], extra_link_args=['-fopenmp'])\n"
             "        for m in mods]\n"
@@ -468,6 +477,53 @@ def arclength_fixtures(scratch):
 
 J2 = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
 
+# The 160k-element J2 box of the benchmark (100x40x40 on 10x4x4, u_x = 0.002 lX over 20 increments
+# of at most 0.05) at a quarter of its edge counts with the same element size: 2500 C3D8, 9,438 DOFs.
+HEADLINE_SCALED_CASE = dict(nX=25, nY=10, nZ=10, lX=2.5, lY=1.0, lZ=1.0, elType="C3D8", maxInc=0.05, ux=0.005)
+
+
+def headline_scaled_fixture(scratch):
+    """The reference's NIST on the scaled benchmark box through its whole load history: the
+    displacements after every converged increment (rows of U_inc), the Newton iteration count of
+    each, and the committed stress of every Gauss point at the end (stress [nEl][8][6], element
+    label order)."""
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    c = HEADLINE_SCALED_CASE
+    rec = []
+    orig = NIST.solveIncrement
+
+    def wrapped(self, *a, **k):
+        out = orig(self, *a, **k)
+        rec.append(np.array(out[0], dtype=float, copy=True))
+        return out
+
+    NIST.solveIncrement = wrapped
+    holder = {}
+    from edelweissfe.drivers import inputfiledrivensimulation as ifs
+
+    orig_sim = ifs.finiteElementSimulation
+
+    def keep_model(*a, **k):
+        model, fo = orig_sim(*a, **k)
+        holder["model"] = model
+        return model, fo
+
+    ifs.finiteElementSimulation = keep_model
+    try:
+        text = BOX_J2_INP.format(E=210000.0, nu=0.3, fy=250.0, H=1000.0, **c)
+        U, it = run_inp(text, scratch, "headline_scaled")
+    finally:
+        NIST.solveIncrement = orig
+        ifs.finiteElementSimulation = orig_sim
+    model = holder["model"]
+    labels = sorted(model.elements)
+    stress = np.array([np.asarray(model.elements[e]._stateVarsRef)[:, 0:6] for e in labels])
+    U_inc = np.array(rec)
+    assert np.max(np.abs(U_inc[-1] - U)) == 0.0, "DofVector and node-field orders differ"
+    np.savez_compressed(os.path.join(HERE, "nist_j2_box_25x10x10_history.npz"), U=U, U_inc=U_inc, iters=it,
+                        stress=stress, **{k: np.array(v) for k, v in c.items()})
+
 
 def variant_fixtures():
     """The other integration rules of elements/library.py: one point (C3D8R, C3D8RTL), 2x2x2 on
@@ -496,6 +552,10 @@ def main():
         nist_variant_fixtures(scratch)
         shutil.rmtree(scratch, ignore_errors=True)
         return
+    if sys.argv[1:] == ["headline"]:  # only the scaled benchmark box history
+        headline_scaled_fixture(scratch)
+        shutil.rmtree(scratch, ignore_errors=True)
+        return
     copy_uref()
     element_fixture("C3D8", "linearelastic", [210000.0, 0.3], 24, seed=1)
     element_fixture("C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], 48, seed=2, plastic=True)
@@ -508,6 +568,7 @@ def main():
     arclength_fixtures(scratch)
     variant_fixtures()
     nist_variant_fixtures(scratch)
+    headline_scaled_fixture(scratch)
     shutil.rmtree(scratch, ignore_errors=True)
 
 
