@@ -487,7 +487,7 @@ struct ef_ctx {
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
-    bool amgSmoothed = false;               // smoothed-aggregation prolongators (EF_AMG_SMOOTHED)
+    bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
     int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel
@@ -1702,6 +1702,13 @@ static ef_status amg_workspace(ef_ctx* c) {
 
 static ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
+    if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
+    // smoothed prolongators: one sweep before and after, V-cycle (the fastest cfg 2 load step of
+    // 1/1, 2/2 x V, W on level 1); plain aggregation: two sweeps and a W-cycle on level 1
+    if (c->amgSmoothed) {
+        c->amgSweeps = 1;
+        c->amgWLevels = 0;
+    }
     if (const char* e = getenv("EF_AMG_OMEGA")) c->amgOmega = (float)atof(e);
     if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
     c->amgPre = c->amgPost = c->amgSweeps;
@@ -1718,7 +1725,6 @@ static ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_SMOOTHER")) c->amgCheb = strcmp(e, "cheb") == 0;
     if (const char* e = getenv("EF_AMG_CLUSTER")) c->amgCluster = atoi(e) != 0;
     if (const char* e = getenv("EF_AMG_BF16_COARSE")) c->amgBf16Coarse = atoi(e) != 0;
-    if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
     if (c->amgSmoothed && !getenv("EF_AMG_ALPHA")) c->amgAlpha = 1.0f;  // smoothed prolongators need no over-correction
     ef_status st = EF_OK;
     const int n0 = (int)c->nNodes;

@@ -1,7 +1,6 @@
 """GPU parity of the hot path (through the C ABI) against the reference's fixtures and the oracle."""
 
 import ctypes
-import os
 
 import numpy as np
 import pytest
@@ -277,19 +276,15 @@ def test_fgmres_multigrid_solves_to_tolerance_with_fewer_iterations(gpu_lib):
     assert 3 * itf <= ip, (itf, ip)
 
 
-@pytest.mark.skipif(os.environ.get("EF_TEST_SMOOTHED_AGGREGATION") != "1",
-                    reason="smoothed aggregation is built but not yet validated on the GPU; "
-                           "EF_TEST_SMOOTHED_AGGREGATION=1 runs this test")  # fmt: skip
 def test_fgmres_smoothed_aggregation_solves_with_fewer_iterations(gpu_lib, monkeypatch):
-    """FGMRES with the smoothed-aggregation hierarchy (EF_AMG_SMOOTHED=1): the solution of the
-    plain aggregation hierarchy at 1e-8 (FP64 residual of the exact tangent) in fewer Krylov
-    iterations, and the same bits when the solve is repeated."""
+    """FGMRES with the smoothed-aggregation hierarchy (the default): the solution of the plain
+    aggregation hierarchy (EF_AMG_SMOOTHED=0) at 1e-8 (FP64 residual of the exact tangent) in
+    fewer Krylov iterations, and the same bits when the solve is repeated."""
     spec = j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0)
     rng = np.random.default_rng(3)
     out = {}
     for smoothed in (False, True):
-        if smoothed:
-            monkeypatch.setenv("EF_AMG_SMOOTHED", "1")
+        monkeypatch.setenv("EF_AMG_SMOOTHED", "1" if smoothed else "0")
         s = _assembled(spec)
         if not out:
             out["b"] = rng.normal(size=s.nDof)
@@ -312,8 +307,9 @@ def test_fgmres_cluster_coarse_cycle_and_reorthogonalisation(gpu_lib, monkeypatc
     """The cycle below the first coarse level as one cluster launch, and the fine-level kernels
     with or without shared-memory staging, give bit-identical FGMRES results (same operations in
     the same order); classical Gram-Schmidt with DGKS re-orthogonalisation reaches the same 1e-8
-    solution."""
+    solution.  (The cluster launch serves the plain aggregation hierarchy.)"""
     rng = np.random.default_rng(5)
+    monkeypatch.setenv("EF_AMG_SMOOTHED", "0")
     out = {}
     for key, env in (("phases", {"EF_AMG_CLUSTER": "0"}), ("cluster", {"EF_AMG_CLUSTER": "1"}),
                      ("staged", {"EF_AMG_CLUSTER": "0", "EF_AMG_STAGED": "1", "EF_SPMV_STAGED": "1"}),
