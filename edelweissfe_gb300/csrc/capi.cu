@@ -181,6 +181,7 @@ struct HostGroup {
     std::vector<int32_t> nodeDof;  // [nEl][nNodes]
     std::vector<double> propsTable;  // optional per-element material rows [nRows][8]
     std::vector<int32_t> elemRow;    // element -> row
+    double cutback = 0.5;            // increment scale requested on a material failure (vonmises.py:231)
 };
 
 struct TypeInfo {
@@ -817,6 +818,20 @@ static void derived_props(int mat, double* p) {
     p[7] = E / (2.0 * (1.0 + nu));
 }
 
+ef_status ef_set_group_cutback(ef_ctx* c, int groupId, double scale) {
+    if (!c) return EF_ERR_ARG;
+    if (c->finalized) {
+        ef_set_error("ef_set_group_cutback: context already finalized");
+        return EF_ERR_STATE;
+    }
+    if (groupId < 0 || groupId >= (int)c->hg.size() || !(scale > 0.0 && scale < 1.0)) {
+        ef_set_error("ef_set_group_cutback: needs a group and a scale in (0, 1)");
+        return EF_ERR_ARG;
+    }
+    c->hg[groupId].cutback = scale;
+    return EF_OK;
+}
+
 ef_status ef_set_group_props(ef_ctx* c, int groupId, const double* table, int nRows, int nProps,
                              const int32_t* elemRow) {
     if (!c) return EF_ERR_ARG;
@@ -872,7 +887,12 @@ ef_status ef_finalize(ef_ctx* c, int options) {
 
     c->dFlags = dalloc<int>(4, &st);
     if (!c->dFlags) return st;
-    EF_CUDA(cudaMemset(c->dFlags, 0, 4 * sizeof(int)));
+    {
+        const float none = EF_PNEWDT_NONE;
+        int hf[4] = {0, 0, 0, 0};
+        memcpy(&hf[1], &none, sizeof(float));
+        EF_CUDA(cudaMemcpy(c->dFlags, hf, sizeof(hf), cudaMemcpyHostToDevice));
+    }
 
     // groups: device node maps and double-buffered SoA state
     int64_t peOff = 0, keOff = 0, nEl = 0, nVIJ = 0;
@@ -888,6 +908,7 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         g.mat = h.mat;
         g.tl = h.tl;
         if (const char* e = getenv("EF_ELEM_INTCONV")) g.intConv = atoi(e) != 0;
+        g.cutback = (float)h.cutback;
         g.nState = 12 + ((h.mat == MAT_VON_MISES || h.mat == MAT_NEOHOOKE_WA) ? 1 : 0);
         for (size_t i = 0; i < h.props.size() && i < 8; ++i) g.props[i] = h.props[i];
         derived_props(h.mat, g.props);
@@ -1390,14 +1411,24 @@ ef_status ef_compute_elements(ef_ctx* c, const double* U_np, const double* dU, c
 
 ef_status ef_element_status(ef_ctx* c, void* stream, double* pNewDT) {
     EF_REQUIRE_FINALIZED(c);
-    int f = 0;
-    EF_CUDA(cudaMemcpyAsync(&f, c->dFlags, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    int hf[2] = {0, 0};
+    EF_CUDA(cudaMemcpyAsync(hf, c->dFlags, sizeof(hf), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     EF_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-    EF_CUDA(cudaMemsetAsync(c->dFlags, 0, sizeof(int), (cudaStream_t)stream));
+    const int f = hf[0];
+    float req = EF_PNEWDT_NONE;
+    memcpy(&req, &hf[1], sizeof(float));
+    {
+        const float none = EF_PNEWDT_NONE;
+        int reset[2] = {0, 0};
+        memcpy(&reset[1], &none, sizeof(float));
+        EF_CUDA(cudaMemcpy(c->dFlags, reset, sizeof(reset), cudaMemcpyHostToDevice));
+    }
     if (pNewDT) *pNewDT = 1.0;
     if (f & EF_FLAG_NAN) return EF_NAN;
     if (f & EF_FLAG_RETURNMAP) {
-        if (pNewDT) *pNewDT = 0.5;
+        // the smallest scale any failing element asked for (min over elements, as the Marmot
+        // element loop's min over its threads' pNewDT, solvers/nonlinearimplicitstaticparallel.pyx:145-150)
+        if (pNewDT) *pNewDT = req < EF_PNEWDT_NONE ? (double)req : 0.5;
         return EF_CUTBACK;
     }
     if (f & EF_FLAG_BADDET) {
@@ -3042,6 +3073,25 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     if (result == EF_OK && !(inf.relResidual <= o->rtol)) result = (rr == rr) ? EF_NOT_CONVERGED : EF_NAN;
     inf.status = result;
     if (info) *info = inf;
+    if (o->method == EF_SOLVE_FGMRES && c->nnOn && c->nnTensorCores) {
+        // a tensor-core tile that gave up waiting freed its TMEM while its MMA may still have been
+        // running: the solve that used the network is discarded and the network continues on
+        // the CUDA-core layer for the rest of this context
+        int f = 0;
+        EF_CUDA(cudaMemcpy(&f, c->dFlags, sizeof(int), cudaMemcpyDeviceToHost));
+        if (f & EF_FLAG_TCWAIT) {
+            EF_CUDA(cudaMemset(c->dFlags, 0, sizeof(int)));
+            c->nnTensorCores = 0;
+            if (c->nnGraph) {  // the captured network pass holds the tensor-core layer: capture again
+                cudaGraphExecDestroy(c->nnGraph);
+                c->nnGraph = nullptr;
+            }
+            ef_set_error("ef_solve: the learned correction's tensor-core accumulator wait timed out; this solve is "
+                         "discarded and the network runs on the CUDA cores from now on");
+            if (info) info->status = EF_ERR_DEVICE;
+            return EF_ERR_DEVICE;
+        }
+    }
     return result;
 }
 

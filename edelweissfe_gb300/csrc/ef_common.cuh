@@ -15,6 +15,7 @@
 #define EF_FLAG_NAN 2          // NaN in an element result
 #define EF_FLAG_BARRIER 4      // a grid barrier gave up (bounded spin exhausted)
 #define EF_FLAG_BADDET 8       // non-positive Jacobian determinant
+#define EF_FLAG_TCWAIT 16      // a tensor-core tile of the network gave up waiting for its accumulator
 
 namespace ef {
 
@@ -59,11 +60,18 @@ struct Group {
     int intConv;          // 1: the element kernel converts FP64 <-> FP32 pairs by integer operations
     const double* propsTable;  // optional per-element material rows [nRows][8] (null: props)
     const int32_t* elemRow;    // element -> row of propsTable
+    float cutback;             // increment scale an element of this group asks for when its material fails
 };
 
 struct PropsArg {
     double v[8];
+    float cutback;  // the group's increment scale on a material failure (atomic min into flags[1])
 };
+
+// flags[1] holds the smallest increment scale requested by a failing element (float bits; positive
+// floats order like their bit patterns, so an integer atomicMin gives the minimum); this value
+// means "no request"
+#define EF_PNEWDT_NONE 1.0e30f
 
 #ifdef __CUDACC__
 // 16-byte asynchronous global -> shared copy (cp.async, cached in L2 only) and its group waits;

@@ -263,7 +263,10 @@ __global__ void __launch_bounds__(kBlock, 5) small_strain_kernel(
         const double* pv = propsTable ? propsTable + 8 * (int64_t)elemRow[e] : props.v;
         if (MAT == MAT_VON_MISES) {
             double kap = stateIn[12 * nQPtot + qi];
-            if (!mat_von_mises(pv, sig, &kap, de, mo)) atomicOr(flags, EF_FLAG_RETURNMAP);
+            if (!mat_von_mises(pv, sig, &kap, de, mo)) {
+                atomicOr(flags, EF_FLAG_RETURNMAP);
+                atomicMin(flags + 1, __float_as_int(props.cutback));
+            }
             stateOut[12 * nQPtot + qi] = kap;
             if (is_nan_sel(kap, intConv)) atomicOr(flags, EF_FLAG_NAN);
         } else {
@@ -494,6 +497,7 @@ static ef_status launch_ss(const Group& g, const double* dU, void* K, int vij, d
     const int grid = (g.nEl + EPB - 1) / EPB;
     PropsArg pa;
     for (int i = 0; i < 8; ++i) pa.v[i] = g.props[i];
+    pa.cutback = g.cutback;
     const double* sIn = g.state[g.cur];
     double* sOut = g.state[1 - g.cur];
     if (grid == 0) return EF_OK;

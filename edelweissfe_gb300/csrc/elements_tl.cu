@@ -334,6 +334,7 @@ static ef_status launch_tl(const Group& g, const double* U, void* K, int vij, do
     if (grid == 0) return EF_OK;
     PropsArg pa;
     for (int i = 0; i < 8; ++i) pa.v[i] = g.props[i];
+    pa.cutback = g.cutback;
     double* sOut = g.state[1 - g.cur];
     const size_t smem = sizeof(TLShared<NN, NQ, KT>);
     if (vij) {

@@ -12,6 +12,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdio>
 
 #include "ef_common.cuh"
 
@@ -599,13 +600,20 @@ extern "C" ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr,
     PcgResult hr;
     EF_CUDA(cudaMemcpyAsync(&hr, res, sizeof(hr), cudaMemcpyDeviceToHost, s));
     EF_CUDA(cudaStreamSynchronize(s));
+    const double rel = hr.bb > 0.0 ? sqrt(hr.rr / hr.bb) : 0.0;
     if (info) {
         info->iterations = hr.iterations;
         info->refinements = 0;
-        info->relResidual = hr.bb > 0.0 ? sqrt(hr.rr / hr.bb) : 0.0;
+        info->relResidual = rel;
         info->status = hr.status;
         info->kernelMs = 0.0;
         info->kernelLaunches = 1;
+    }
+    if (hr.status != EF_OK) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "ef_pcg_solve_noalloc: status %d after %d iterations, relative residual %.3e",
+                 hr.status, hr.iterations, rel);
+        ef_set_error(msg);
     }
     return hr.status == EF_OK ? EF_OK : (ef_status)hr.status;
 }

@@ -332,7 +332,10 @@ __global__ void __launch_bounds__(128) dense_tc_kernel(int nN, const float* __re
             hout[(int64_t)m * H + c] = h[(int64_t)m * H + c] + qq;
         }
     } else if (tid == 0) {
-        atomicOr(flags, EF_FLAG_BARRIER);
+        // the accumulator never became ready: this tile's output is skipped, and an MMA still in
+        // flight may write TMEM columns after the dealloc below, so the host must discard the
+        // whole network pass and stop using the tensor-core layer (see EF_FLAG_TCWAIT)
+        atomicOr(flags, EF_FLAG_TCWAIT);
     }
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
@@ -758,7 +761,7 @@ ef_status ef_mpnn_alpha_combine(int64_t n, const float* Mv, const float* N, cons
 }
 
 // one dense layer, q = relu(Ws h + Wn agg), hout = h + q, on the tensor cores (tc != 0) or the
-// FP32 CUDA cores; flags receives EF_FLAG_BARRIER if a tensor-core tile gave up waiting
+// FP32 CUDA cores; flags receives EF_FLAG_TCWAIT if a tensor-core tile gave up waiting
 ef_status ef_mpnn_dense(int tc, int nN, const float* h, const float* agg, const float* Wl, float* q, float* hout,
                         int* flags, cudaStream_t s) {
     if (nN == 0) return EF_OK;

@@ -26,6 +26,7 @@ class ElementGroup:
     props: np.ndarray
     propsTable: np.ndarray = None  # optional per-element material rows [nRows, nProps]
     elemRow: np.ndarray = None  # element -> row of propsTable
+    cutback: float = None  # increment scale requested when the material fails (None: the library's 0.5)
 
 
 class Model:

@@ -152,6 +152,8 @@ class NISTGPU:
                 "ef_add_group",
             )  # fmt: skip
             self.groupIds.append(gid.value)
+            if g.cutback is not None:
+                _lib.check(self.lib.ef_set_group_cutback(self.ctx, gid.value, float(g.cutback)), "ef_set_group_cutback")
             if g.propsTable is not None:
                 tab = np.ascontiguousarray(np.asarray(g.propsTable, dtype=float))
                 rows = np.ascontiguousarray(np.asarray(g.elemRow, dtype=np.int32))

@@ -119,9 +119,11 @@ ef_status ef_compute_elements(ef_ctx* ctx, const double* U_np, const double* dU,
                               double* P, double* F, void* stream);
 
 /* Synchronises `stream` and returns the element status of the last ef_compute_elements:
- * EF_OK, EF_CUTBACK (J2 return map failed; the reference raises CutbackRequest(.., 0.5),
+ * EF_OK, EF_CUTBACK (a material update failed: the reference's J2 raises CutbackRequest(.., 0.5),
  * materials/vonmises/vonmises.py:231) or EF_NAN.  *pNewDT receives the suggested increment
- * scale (1.0, or 0.5 on cutback).  Resets the flags. */
+ * scale: 1.0, or on cutback the smallest scale any failing element asked for (its group's
+ * ef_set_group_cutback value, default 0.5), the min over elements of the Marmot element loop
+ * (solvers/nonlinearimplicitstaticparallel.pyx:136-150).  Resets the flags. */
 ef_status ef_element_status(ef_ctx* ctx, void* stream, double* pNewDT);
 
 /* Per-Gauss-point state of a group, host [nEl][nQP][nState] with the reference layout
@@ -238,6 +240,11 @@ ef_status ef_norms(ef_ctx* ctx, const double* R, const double* F, const double* 
  * the scalar reference CSR. */
 ef_status ef_set_ties(ef_ctx* ctx, const int64_t* slave, const int64_t* masterA, const int64_t* masterB, int64_t n);
 
+/* Increment scale in (0, 1) that an element of group `groupId` requests when its material update
+ * fails (before ef_finalize; default 0.5, the reference's J2, materials/vonmises/vonmises.py:231;
+ * a Marmot material sets its own pNewDT, elements/marmotelement/element.pyx:233-239). */
+ef_status ef_set_group_cutback(ef_ctx* ctx, int groupId, double scale);
+
 /* Per-element material rows for group `groupId` (before ef_finalize): table host
  * [nRows][nProps] (the material's property order), elemRow host [nEl] (row of each element). */
 ef_status ef_set_group_props(ef_ctx* ctx, int groupId, const double* table, int nRows, int nProps,
@@ -325,8 +332,12 @@ ef_status ef_mpnn_eval(int nNodes, const int32_t* rowPtr, const int32_t* colIdx,
 /* One dense layer of the network, q = relu(Ws h + Wn agg), hout = h + q, on HOST arrays h, agg
  * [nNodes][64], W [2][64][64] (Ws then Wn, row = output channel), q, hout [nNodes][64]: on the
  * tensor cores (tcgen05, BF16 operands, FP32 accumulation; tensorCores != 0) or the FP32 CUDA
- * cores.  flags (host) receives the kernel's status bits (EF_FLAG_BARRIER 4: a tile gave up
- * waiting for its accumulator).  For verification; synchronises `stream`. */
+ * cores.  flags (host) receives the kernel's status bits (16: a tile gave up waiting for its
+ * accumulator; its TMEM was freed while the MMA may still run, so the results of the call are
+ * to be discarded).  For verification; synchronises `stream`.
+ * In an FGMRES solve with the network enabled the same event makes ef_solve return
+ * EF_ERR_DEVICE: that solve is discarded and the context's network runs on the FP32 CUDA cores
+ * from then on. */
 ef_status ef_mpnn_dense_eval(int tensorCores, int nNodes, const float* h, const float* agg, const float* W,
                              float* q, float* hout, int* flags, void* stream);
 

@@ -481,3 +481,46 @@ def test_nist_gpu_arclength_matches_reference(gpu_lib, mode):
     assert [it for _, it in s.iterationHistory] == list(g["iters"])
     assert np.max(np.abs(np.array(s.lambdaHistory) - g["Lambda"])) <= 1e-6 * np.max(g["Lambda"])
     assert np.max(np.abs(U.cpu().numpy() - g["U"])) <= 1e-6 * np.max(np.abs(g["U"]))
+
+
+def test_element_status_returns_the_smallest_requested_cutback(gpu_lib):
+    """Two groups of the same failing J2 elements (the softening law above) with their own
+    increment scales (ef_set_group_cutback 0.4 and 0.3): EF_CUTBACK with the smaller one, the min
+    over elements of the Marmot element loop (solvers/nonlinearimplicitstaticparallel.pyx:145-150)."""
+    from edelweissfe_gb300 import _lib
+
+    g = golden("elem_C3D8_vonmises.npz")
+    props = np.ascontiguousarray([210000.0, 0.3, 250.0, 0.0, -200.0, 1e5])
+    coords = g["coords"]
+    nEl = coords.shape[0]
+    nDof = 2 * 24 * nEl
+    X = np.ascontiguousarray(np.concatenate([coords.reshape(-1), coords.reshape(-1)]))
+    ctx = ctypes.c_void_p()
+    _lib.check(gpu_lib.ef_create(nDof, X.ctypes.data, ctypes.byref(ctx)), "ef_create")
+    try:
+        for k, scale in enumerate((0.4, 0.3)):
+            ed = np.ascontiguousarray(np.arange(k * 24 * nEl, (k + 1) * 24 * nEl, dtype=np.int32).reshape(nEl, 24))
+            gid = ctypes.c_int()
+            _lib.check(gpu_lib.ef_add_group(ctx, b"C3D8", b"vonmises", props.ctypes.data, props.size, nEl,
+                                            ed.ctypes.data, ctypes.byref(gid)), "ef_add_group")  # fmt: skip
+            _lib.check(gpu_lib.ef_set_group_cutback(ctx, gid.value, scale), "ef_set_group_cutback")
+        assert gpu_lib.ef_set_group_cutback(ctx, 0, 1.5) == _lib.EF_ERR_ARG
+        _lib.check(gpu_lib.ef_finalize(ctx, _lib.EF_OPT_NO_SCALAR_CSR), "ef_finalize")
+        assert gpu_lib.ef_set_group_cutback(ctx, 0, 0.2) == _lib.EF_ERR_STATE
+        state0 = np.ascontiguousarray(g["state0"])
+        for gid in (0, 1):
+            _lib.check(gpu_lib.ef_set_state(ctx, gid, state0.ctypes.data), "ef_set_state")
+        dev = torch.device("cuda")
+        U = torch.as_tensor(np.tile(g["U"].reshape(-1), 2), device=dev)
+        dU = torch.as_tensor(np.tile(g["dU"].reshape(-1), 2), device=dev)
+        P = torch.zeros(nDof, dtype=torch.float64, device=dev)
+        F = torch.zeros_like(P)
+        t = np.array([0.5, 0.5])
+        newDT = ctypes.c_double(0.0)
+        _lib.check(gpu_lib.ef_compute_elements(ctx, U.data_ptr(), dU.data_ptr(), t.ctypes.data, 0.1, P.data_ptr(),
+                                               F.data_ptr(), None), "ef_compute_elements")  # fmt: skip
+        assert gpu_lib.ef_element_status(ctx, None, ctypes.byref(newDT)) == _lib.EF_CUTBACK
+        assert abs(newDT.value - 0.3) < 1e-7
+        assert gpu_lib.ef_element_status(ctx, None, ctypes.byref(newDT)) == _lib.EF_OK and newDT.value == 1.0
+    finally:
+        gpu_lib.ef_destroy(ctx)
