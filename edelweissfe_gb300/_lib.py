@@ -78,6 +78,16 @@ class EfSolveInfo(ctypes.Structure):
     ]
 
 
+class EfNewtonOpts(ctypes.Structure):
+    _fields_ = [("fluxTol", c_dbl), ("fluxTolAlt", c_dbl), ("corrTol", c_dbl), ("fluxFloor", c_dbl),
+                ("nAccFluxes", c_dbl)]  # fmt: skip
+
+
+class EfNewtonCheck(ctypes.Structure):
+    _fields_ = [("converged", c_int), ("nGrew", c_int), ("fluxResidual", c_dbl), ("fieldCorrection", c_dbl),
+                ("spatialAveragedFlux", c_dbl)]  # fmt: skip
+
+
 # name -> (restype, argtypes); the exported surface of include/efgpu.h
 SIGNATURES = {
     "ef_abi_version": (c_int, []),
@@ -108,6 +118,11 @@ SIGNATURES = {
     "ef_solve": (c_int, [c_vp, ctypes.POINTER(EfSolveOpts), c_vp, c_vp, ctypes.POINTER(EfSolveInfo), c_vp]),
     "ef_bsr_matvec": (c_int, [c_vp, c_vp, c_vp, c_vp]),
     "ef_norms": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ef_newton_residual": (
+        c_int,
+        [c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_dbl, c_int, ctypes.POINTER(EfNewtonOpts), c_vp,
+         ctypes.POINTER(EfNewtonCheck), c_vp],
+    ),
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
     "ef_kernel_launches": (c_i64, []),
     "ef_fgmres_set_preconditioner": (c_int, [c_vp, c_int]),

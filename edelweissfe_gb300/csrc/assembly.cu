@@ -226,6 +226,78 @@ __global__ void norms_final_kernel(int nPart, const double* __restrict__ part, d
     out[2] = c;
 }
 
+// R = P + PExt with the Dirichlet rows set to 0 (dir[i] != 0), and the partial norms of the
+// convergence check: max |R|, sum |F|, max |ddU| (solvers/nonlinearimplicitstatic.py:418-436,
+// :625-725)
+__global__ void newton_residual_kernel(int64_t n, const double* __restrict__ P, const double* __restrict__ PExt,
+                                       const uint8_t* __restrict__ dir, const double* __restrict__ F,
+                                       const double* __restrict__ D, double* __restrict__ R,
+                                       double* __restrict__ part) {
+    __shared__ double s0[256], s1[256], s2[256];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double r = dir[i] ? 0.0 : (PExt ? P[i] + PExt[i] : P[i]);
+        R[i] = r;
+        a = fmax(a, fabs(r));
+        b += fabs(F[i]);
+        if (D) c = fmax(c, fabs(D[i]));
+    }
+    s0[threadIdx.x] = a;
+    s1[threadIdx.x] = b;
+    s2[threadIdx.x] = c;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s0[threadIdx.x] = fmax(s0[threadIdx.x], s0[threadIdx.x + w]);
+            s1[threadIdx.x] += s1[threadIdx.x + w];
+            s2[threadIdx.x] = fmax(s2[threadIdx.x], s2[threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x + 0] = s0[0];
+        part[3 * blockIdx.x + 1] = s1[0];
+        part[3 * blockIdx.x + 2] = s2[0];
+    }
+}
+
+// The reference's convergence test for the displacement field (solvers/nonlinearimplicitstatic.py
+// :656-682, computeSpatialAveragedFluxes :771-792), decided on the device from the partial norms:
+// q = {fluxTol, fluxTolAlt, corrTol, fluxFloor, nAccFluxes, prevResidual, iteration, nGrew, hasDdU}
+// out = {converged, nGrew, fluxResidual, fieldCorrection, spatialAveragedFlux}
+__global__ void newton_decide_kernel(int nPart, const double* __restrict__ part, const double* __restrict__ q,
+                                     double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = 0; i < nPart; ++i) {
+        a = fmax(a, part[3 * i]);
+        b += part[3 * i + 1];
+        c = fmax(c, part[3 * i + 2]);
+    }
+    const double avg = fmax(1e-10, b / q[4]);
+    const double tol = q[6] < 15.0 ? q[0] : q[1];
+    const double corr = q[8] != 0.0 ? c : 0.0;
+    const bool convCorr = corr < q[2];
+    const bool convFlux = a <= fmax(tol * avg, q[3]);
+    out[0] = (convCorr && convFlux) ? 1.0 : 0.0;
+    out[1] = q[7] + (a > q[5] ? 1.0 : 0.0);
+    out[2] = a;
+    out[3] = corr;
+    out[4] = avg;
+}
+
+// R = P + PExt, then R[dofs[k]] = values[k] (the prescribed increments of the first iteration)
+__global__ void newton_first_residual_kernel(int64_t n, const double* __restrict__ P, const double* __restrict__ PExt,
+                                             double* __restrict__ R) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) R[i] = PExt ? P[i] + PExt[i] : P[i];
+}
+__global__ void scatter_values_kernel(int64_t n, const int64_t* __restrict__ dofs, const double* __restrict__ v,
+                                      double* __restrict__ R) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) R[dofs[k]] = v[k];
+}
+
 // x[slave] = (x[a] + x[b]) / 2 per component (tied nodes)
 __global__ void tie_fill_kernel(int64_t n, const int32_t* __restrict__ slave, const int32_t* __restrict__ ma,
                                 const int32_t* __restrict__ mb, double* __restrict__ x) {
@@ -330,6 +402,23 @@ ef_status ef_launch_norms(int64_t n, const double* R, const double* F, const dou
                           double* out, cudaStream_t s) {
     norms_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, R, F, D, part);
     norms_final_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, out);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_newton_check(int64_t n, const double* P, const double* PExt, const uint8_t* dir, const double* F,
+                                 const double* D, double* R, double* part, int nPart, const double* q, double* out,
+                                 cudaStream_t s) {
+    newton_residual_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, P, PExt, dir, F, D, R, part);
+    newton_decide_kernel<<<1, 32, 0, ef::counted(s)>>>(nPart, part, q, out);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_newton_first(int64_t n, const double* P, const double* PExt, int64_t nDir, const int64_t* dofs,
+                                 const double* values, double* R, cudaStream_t s) {
+    if (n > 0) newton_first_residual_kernel<<<nblk(n, 256), 256, 0, ef::counted(s)>>>(n, P, PExt, R);
+    if (nDir > 0) scatter_values_kernel<<<nblk(nDir, 256), 256, 0, ef::counted(s)>>>(nDir, dofs, values, R);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

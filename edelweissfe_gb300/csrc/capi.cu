@@ -152,6 +152,19 @@ ef_status ef_launch_spmv_f32_staged(int nSM, int cap, int nN, const int32_t* row
                                     cudaStream_t s);
 ef_status ef_launch_combine(int64_t n, int nv, const float* Z, int64_t ldz, const double* y, float* x, cudaStream_t s);
 ef_status ef_launch_sub(int64_t n, const float* b, const float* y, float* r, cudaStream_t s);
+ef_status ef_launch_newton_check(int64_t n, const double* P, const double* PExt, const uint8_t* dir, const double* F,
+                                 const double* D, double* R, double* part, int nPart, const double* q, double* out,
+                                 cudaStream_t s);
+ef_status ef_launch_newton_first(int64_t n, const double* P, const double* PExt, int64_t nDir, const int64_t* dofs,
+                                 const double* values, double* R, cudaStream_t s);
+ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
+                                 cudaStream_t s);
+ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                               cudaStream_t s);
+ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                                     const void* v8, const void* v1, const float* x, const float* r,
+                                     const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s);
 
 using namespace ef;
 
@@ -445,6 +458,11 @@ struct ef_ctx {
     void* dBinv = nullptr;
     uint8_t* dMask = nullptr;
     bool anyDirichlet = false;
+    // the Dirichlet DOFs of ef_set_dirichlet (without tied DOFs) for the residual of the Newton check
+    int64_t nDir = 0;
+    int64_t* dDirIdx = nullptr;
+    uint8_t* dDirMask = nullptr;
+    double* dNewton = nullptr;  // [16]: decision inputs (9) and outputs (5) of ef_newton_residual
     // scalar CSR (reference layout)
     bool scalar = false;
     int64_t nVIJ = 0, nnz = 0;
@@ -480,6 +498,18 @@ struct ef_ctx {
     bool nnEdgeStale = true;             // the learned correction's edge weights need a refresh
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
+    // sliced-ELL copy of the fine system (sell.cu): FGMRES product and fine smoothing
+    int sellMode = -1;                     // -1 not decided, 0 off (EF_SELL=0 or too much padding), 1 on
+    bool sellStale = true;                 // values need a refresh from the assembled blocks
+    int sellSlices = 0;
+    int64_t sellE = 0;                     // slots (32 x the sum of the slice widths)
+    int64_t* dSellOff = nullptr;           // [sellSlices + 1] first slot of each slice
+    int32_t* dSellPerm = nullptr;          // [nNodes] block row of each SELL row (null: identity)
+    int32_t* dSellCol = nullptr;           // [sellE] block column (padding: the row itself)
+    int32_t* dSellSrc = nullptr;           // [sellE] source block in the BSR values (-1: padding)
+    float* dSellV9 = nullptr;              // FP32 values, nine planes per slot column
+    void* dSellV8 = nullptr;               // BF16 values 0..7 per slot (16-byte words)
+    void* dSellV1 = nullptr;               // BF16 value 8 per slot
     // V-cycle parameters: damping, smoothing sweeps per side, coarse over-correction, cycle type
     float amgOmega = 1.0f;                  // upper bound of the smoothing damping
     std::vector<float> levelOmega;          // per smoothed level: amgOmega, or 4 / (3 lambda_max(D^-1 A)) when smaller
@@ -626,6 +656,16 @@ void ef_destroy(ef_ctx* c) {
     F(c->Pe);
     F(c->Kblk);
     F(c->dFlags);
+    F(c->dDirIdx);
+    F(c->dDirMask);
+    F(c->dNewton);
+    F(c->dSellOff);
+    F(c->dSellPerm);
+    F(c->dSellCol);
+    F(c->dSellSrc);
+    F(c->dSellV9);
+    F(c->dSellV8);
+    F(c->dSellV1);
     F(c->dNodeDof);
     F(c->dCondPtr);
     F(c->dCondSrc);
@@ -1581,6 +1621,22 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
         }
         m[dofs[i]] = 1;
     }
+    {
+        ef_status st = EF_OK;
+        if (c->dDirIdx) cudaFree(c->dDirIdx);
+        if (c->dDirMask) cudaFree(c->dDirMask);
+        c->dDirIdx = nullptr;
+        c->dDirMask = nullptr;
+        c->nDir = n;
+        if (n > 0) {
+            c->dDirIdx = dalloc<int64_t>((size_t)n, &st);
+            if (!c->dDirIdx) return st;
+            EF_CUDA(cudaMemcpy(c->dDirIdx, dofs, sizeof(int64_t) * n, cudaMemcpyHostToDevice));
+        }
+        c->dDirMask = dalloc<uint8_t>((size_t)c->nDof, &st);
+        if (!c->dDirMask) return st;
+        EF_CUDA(cudaMemcpy(c->dDirMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
+    }
     for (int32_t sN : c->hTieS)
         for (int k = 0; k < 3; ++k) m[3 * (int64_t)sN + k] = 1;
     c->anyDirichlet = n > 0 || !c->hTieS.empty();
@@ -1595,6 +1651,7 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
 ef_status ef_assemble_bsr(ef_ctx* c, void* stream) {
     EF_REQUIRE_FINALIZED(c);
     cudaStream_t s = (cudaStream_t)stream;
+    c->sellStale = true;
     EF_CHECK(ef_launch_bsr_scatter(c->nBlocks, c->dBsrSeg, c->dBsrSrc, c->dBsrW, c->Kblk, c->keFp64, c->dBsrVals, s));
     EF_CHECK(ef_launch_bj_setup(c->nNodes, c->dDiagPos, c->dNodeDof, c->dMask, c->dBsrVals, c->keFp64, c->dBinv,
                                 c->dFlags, s));
@@ -1731,6 +1788,99 @@ static ef_status amg_workspace(ef_ctx* c) {
     return (c->vcIn && c->vcOut && c->fineX && c->fineT) ? EF_OK : st;
 }
 
+// ---- sliced-ELL copy of the fine system (kernels in sell.cu) ---------------------------------
+
+// Layout, decided once: slices of 32 block rows in their natural order; when that pads the slots
+// by more than 15 % over the blocks, rows are sorted by length (longest first) within windows of
+// 4096 rows and the permutation is kept if it pads less; above 50 % padding after that (or with
+// EF_SELL=0, or an FP64 system) the CSR kernels stay in use.
+static ef_status sell_build(ef_ctx* c) {
+    if (c->sellMode >= 0) return EF_OK;
+    c->sellMode = 0;
+    if (const char* e = getenv("EF_SELL"))
+        if (atoi(e) == 0) return EF_OK;
+    const int n0 = (int)c->nNodes;
+    const std::vector<int32_t>& rp = c->hRowPtr0;
+    const std::vector<int32_t>& ci = c->hColIdx0;
+    if (c->keFp64 || n0 <= 0 || (int64_t)rp.size() != (int64_t)n0 + 1) return EF_OK;
+    auto len = [&](int m) { return rp[m + 1] - rp[m]; };
+    auto slots = [&](const std::vector<int32_t>& order) {
+        int64_t tot = 0;
+        for (int s0 = 0; s0 < n0; s0 += 32) {
+            int w = 0;
+            for (int r = s0; r < std::min(s0 + 32, n0); ++r) w = std::max(w, len(order.empty() ? r : order[r]));
+            tot += 32 * (int64_t)w;
+        }
+        return tot;
+    };
+    std::vector<int32_t> perm;
+    int64_t nE = slots(perm);
+    const double nb = (double)c->nBlocks;
+    if (nE > 1.15 * nb) {
+        std::vector<int32_t> p(n0);
+        for (int m = 0; m < n0; ++m) p[m] = m;
+        const int W = 4096;
+        for (int w0 = 0; w0 < n0; w0 += W)
+            std::stable_sort(p.begin() + w0, p.begin() + std::min(w0 + W, n0),
+                             [&](int a, int b) { return len(a) > len(b); });
+        const int64_t nE2 = slots(p);
+        if (nE2 < nE) {
+            nE = nE2;
+            perm.swap(p);
+        }
+    }
+    if (nE > 1.5 * nb || nE >= ((int64_t)1 << 31) / 9) return EF_OK;
+    const int nS = (n0 + 31) / 32;
+    std::vector<int64_t> off(nS + 1, 0);
+    std::vector<int32_t> col(nE), src(nE);
+    for (int s = 0; s < nS; ++s) {
+        int w = 0;
+        for (int r = 32 * s; r < std::min(32 * s + 32, n0); ++r) w = std::max(w, len(perm.empty() ? r : perm[r]));
+        off[s + 1] = off[s] + 32 * (int64_t)w;
+        for (int j = 0; j < w; ++j)
+            for (int i = 0; i < 32; ++i) {
+                const int r = 32 * s + i;
+                const int64_t t = off[s] + 32 * (int64_t)j + i;
+                if (r < n0) {
+                    const int m = perm.empty() ? r : perm[r];
+                    const bool real = j < len(m);
+                    src[t] = real ? rp[m] + j : -1;
+                    col[t] = real ? ci[rp[m] + j] : m;
+                } else {
+                    src[t] = -1;
+                    col[t] = n0 - 1;
+                }
+            }
+    }
+    ef_status st = EF_OK;
+    EF_CHECK(upload(&c->dSellOff, off));
+    EF_CHECK(upload(&c->dSellCol, col));
+    EF_CHECK(upload(&c->dSellSrc, src));
+    if (!perm.empty()) EF_CHECK(upload(&c->dSellPerm, perm));
+    c->dSellV9 = dalloc<float>(9 * (size_t)nE, &st);
+    if (!c->dSellV9) return st;
+    if (c->amgBf16) {
+        c->dSellV8 = dalloc<uint4>((size_t)nE, &st);
+        c->dSellV1 = dalloc<uint16_t>((size_t)nE, &st);
+        if (!c->dSellV8 || !c->dSellV1) return st;
+    }
+    c->sellSlices = nS;
+    c->sellE = nE;
+    c->sellMode = 1;
+    c->sellStale = true;
+    return EF_OK;
+}
+
+// the SELL values from the assembled FP32 blocks (after every assembly)
+static ef_status sell_refresh(ef_ctx* c, cudaStream_t s) {
+    EF_CHECK(sell_build(c));
+    if (c->sellMode != 1 || !c->sellStale) return EF_OK;
+    EF_CHECK(ef_launch_sell_refresh(c->sellE, c->dSellSrc, (const float*)c->dBsrVals, c->dSellV9, c->dSellV8,
+                                    c->dSellV1, s));
+    c->sellStale = false;
+    return EF_OK;
+}
+
 static ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
     if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
@@ -1766,7 +1916,8 @@ static ef_status amg_build(ef_ctx* c) {
         for (int k = c->hRowPtr0[m]; k < c->hRowPtr0[m + 1]; ++k) rob0[k] = m;
     EF_CHECK(upload(&c->dRowOfBlock0, rob0));
     EF_CHECK(amg_workspace(c));
-    if (c->amgBf16) {
+    EF_CHECK(sell_build(c));
+    if (c->amgBf16 && c->sellMode != 1) {  // (with the SELL copy the fine level reads its BF16 values)
         c->dBsrValsH = dalloc<uint16_t>((size_t)c->nBlocks * 9 + 32, &st);  // 16-byte words + 1 value per block (+ padding)
         if (!c->dBsrValsH) return st;
         bool staged = false;  // measured slower than the unstaged kernel (EF_AMG_STAGED=1 turns it on)
@@ -2255,6 +2406,7 @@ static ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
 // dead coarse DOFs from the current Dirichlet mask, then Galerkin values, block inverses, the
 // coarsest inverse and the smoothing damping for the current fine system
 static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
+    EF_CHECK(sell_refresh(c, s));
     if (!c->amgStale) return EF_OK;
     const int BCo = ef_amg_coarse_dofs();
     const uint8_t* fineDead = c->hMask.data();
@@ -2323,8 +2475,13 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     float* t = fine ? c->fineT : c->amg[l - 1].t;
     const void* valsH = fine ? nullptr : c->amg[l - 1].valsH;
     AmgLevel& Cn = c->amg[l];
-    // fine level from the BF16 copy: staged through shared memory when the chunks fit
+    // fine level from a BF16 copy: the sliced-ELL one, else the BSR split copy (staged through
+    // shared memory when the chunks fit)
+    const bool fineH = fine && c->amgBf16 && (c->sellMode == 1 || c->dBsrValsH);
     auto fine_bf16 = [&](const float* xin, float* out, const float* bj, float om) -> ef_status {
+        if (c->sellMode == 1)
+            return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
+                                              c->dSellV1, xin, r, mask, out, bj, om, s);
         if (c->stageCap > 0)
             return ef_launch_level_residual_bf16_staged(c->nSM, c->stageCap, nN, c->nBlocks, rowPtr, colIdx,
                                                         c->dBsrValsH, xin, r, mask, out, s, bj, om);
@@ -2332,7 +2489,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
                                              om);
     };
     auto residual = [&]() -> ef_status {
-        if (fine && c->dBsrValsH) return fine_bf16(x, t, nullptr, 0.f);
+        if (fineH) return fine_bf16(x, t, nullptr, 0.f);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x, r, mask, t, s, nullptr, 0.f, valsH);
     };
     // Chebyshev smoothing of degree amgSweeps on [lmax / 30, 1.1 lmax] of D^-1 A; from zero the
@@ -2359,7 +2516,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     };
     // one fused damped block-Jacobi sweep xout = xin + omega D^-1 (r - A xin)
     auto sweep = [&](const float* xin, float* xout) -> ef_status {
-        if (fine && c->dBsrValsH) return fine_bf16(xin, xout, binv, omega);
+        if (fineH) return fine_bf16(xin, xout, binv, omega);
         return ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, xin, r, mask, xout, s, binv, omega, valsH);
     };
     // The sweeps (the first from zero) alternate between x and a second vector; the first goes
@@ -2383,7 +2540,7 @@ static ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStre
     const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
         if (!c->amgCheb) {
-            EF_CHECK(fine && c->dBsrValsH ? fine_bf16(cur, t, nullptr, 0.f)
+            EF_CHECK(fineH ? fine_bf16(cur, t, nullptr, 0.f)
                                           : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s,
                                                                      nullptr, 0.f, valsH));
         } else {
@@ -2845,7 +3002,10 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CHECK(fgmres_precond(c, V + (int64_t)j * n, &pz, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][2], s));
         // w = K z_j straight into the next basis slot; z_j kept in Z
-        if (c->spCap > 0)
+        if (c->sellMode == 1)
+            EF_CHECK(ef_launch_sell_spmv3((int)c->nNodes, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol,
+                                          c->dSellV9, pz, c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
+        else if (c->spCap > 0)
             EF_CHECK(ef_launch_spmv_f32_staged(c->nSM, c->spCap, (int)c->nNodes, c->dRowPtr, c->dColIdx,
                                                (const float*)c->dBsrVals, pz, c->dMask, V + (int64_t)(j + 1) * n,
                                                Z + (int64_t)j * n, s));
@@ -3030,6 +3190,7 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
             PcgResultHost pr;
             if (o->method == EF_SOLVE_FGMRES) {
+                EF_CHECK(sell_refresh(c, s));
                 if (c->fgPc == EF_FGMRES_PC_MULTIGRID) {
                     EF_CHECK(amg_build(c));
                     EF_CHECK(amg_refresh(c, s));
@@ -3502,6 +3663,42 @@ ef_status ef_mpnn_eval(int nNodes, const int32_t* rowPtr, const int32_t* colIdx,
 #undef EV_CUDA
 #undef EV_CHECK
     return finish(EF_OK);
+}
+
+ef_status ef_newton_residual(ef_ctx* c, int mode, const double* P, const double* PExt, const double* dirValues,
+                             const double* F, const double* ddU, int iteration, double prevResidual, int nGrew,
+                             const ef_newton_opts* o, double* R, ef_newton_check* out, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (!P || !R || (mode != 0 && mode != 1) || (mode == 1 && (!F || !o || !out)) ||
+        (mode == 0 && c->nDir > 0 && !dirValues)) {
+        ef_set_error("ef_newton_residual: bad arguments");
+        return EF_ERR_ARG;
+    }
+    if (!c->dDirMask) {
+        ef_set_error("ef_newton_residual: call ef_set_dirichlet first");
+        return EF_ERR_STATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (mode == 0) return ef_launch_newton_first(c->nDof, P, PExt, c->nDir, c->dDirIdx, dirValues, R, s);
+    if (!c->dNewton) {
+        ef_status st = EF_OK;
+        c->dNewton = dalloc<double>(16, &st);
+        if (!c->dNewton) return st;
+    }
+    const double q[9] = {o->fluxTol, o->fluxTolAlt, o->corrTol, o->fluxFloor, o->nAccFluxes, prevResidual,
+                         (double)iteration, (double)nGrew, ddU ? 1.0 : 0.0};
+    EF_CUDA(cudaMemcpyAsync(c->dNewton, q, sizeof(q), cudaMemcpyHostToDevice, s));
+    EF_CHECK(ef_launch_newton_check(c->nDof, P, PExt, c->dDirMask, F, ddU, R, c->dPart, c->nPart, c->dNewton,
+                                    c->dNewton + 9, s));
+    double r[5];
+    EF_CUDA(cudaMemcpyAsync(r, c->dNewton + 9, sizeof(r), cudaMemcpyDeviceToHost, s));
+    EF_CUDA(cudaStreamSynchronize(s));
+    out->converged = r[0] != 0.0;
+    out->nGrew = (int)r[1];
+    out->fluxResidual = r[2];
+    out->fieldCorrection = r[3];
+    out->spatialAveragedFlux = r[4];
+    return EF_OK;
 }
 
 ef_status ef_norms(ef_ctx* c, const double* R, const double* F, const double* ddU, double* out, void* stream) {

@@ -1,0 +1,188 @@
+// Sliced-ELL copies of the fine 3x3-block system and the fine-level kernels that stream them.
+//
+// The fine system's block rows are grouped into slices of 32; a slice is as wide as its longest
+// row (shorter rows are padded with zero blocks whose column is the row itself) and its entries
+// are stored column-major: entry j of the slice's row i sits at slot e0 + 32 j + i.  A warp takes
+// one slice, a lane one row, so at every step j the warp reads 32 consecutive column indices and
+// 32 consecutive blocks -- fully coalesced, with no row-pointer load ahead of them -- and, on a
+// mesh numbered along a grid line, gathers x from 32 consecutive nodes.  An optional row
+// permutation (rows sorted by length within windows) keeps the padding small on meshes whose row
+// lengths vary; on the structured hex8 box it is the identity and costs one coalesced load.
+//
+// Two value copies, refreshed from the FP32 block values after every assembly:
+//  * FP32, nine planes per slot column: value k of slot t at 9 (t - i) + 32 k + i (i = t mod 32),
+//    for the FGMRES product y = K z;
+//  * BF16 split: one 16-byte word with values 0..7 per slot and value 8 in a second array, for the
+//    multigrid's fine smoothing sweeps and residuals (a preconditioner only).
+// Summation per row runs over the row's blocks in column order with one accumulator per output
+// component: deterministic, not the same rounding as the CSR kernels.
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "ef_common.cuh"
+
+namespace ef {
+
+constexpr int kSellThreads = 128;  // four slices per CTA
+constexpr int kSellSlicesPerCta = kSellThreads / 32;
+
+__global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src, const float* __restrict__ bsr,
+                                    float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nE) return;
+    const int64_t b = src[t];
+    float a[9];
+    if (b >= 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = bsr[b * 9 + k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = 0.f;
+    }
+    const int64_t i = t & 31;
+    float* d = v9 + 9 * (t - i) + i;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[32 * k] = a[k];
+    if (v8) {
+        __nv_bfloat162 h[4] = {__floats2bfloat162_rn(a[0], a[1]), __floats2bfloat162_rn(a[2], a[3]),
+                               __floats2bfloat162_rn(a[4], a[5]), __floats2bfloat162_rn(a[6], a[7])};
+        v8[t] = *reinterpret_cast<const uint4*>(h);
+        v1[t] = __float2bfloat16_rn(a[8]);
+    }
+}
+
+// y = K x on the free DOFs (0 on masked rows); COPY: xcopy = x as well
+template <bool COPY>
+__global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nSlices, const int64_t* __restrict__ off,
+                                                                  const int32_t* __restrict__ perm,
+                                                                  const int32_t* __restrict__ col,
+                                                                  const float* __restrict__ v9,
+                                                                  const float* __restrict__ x,
+                                                                  const uint8_t* __restrict__ mask,
+                                                                  float* __restrict__ y, float* __restrict__ xcopy) {
+    const int lane = threadIdx.x & 31;
+    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
+    if (sl >= nSlices) return;
+    const int64_t e0 = off[sl];
+    const int w = (int)((off[sl + 1] - e0) >> 5);
+    const int32_t* cs = col + e0 + lane;
+    const float* vs = v9 + 9 * e0 + lane;
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll 3
+    for (int j = 0; j < w; ++j) {
+        const int c3 = 3 * __ldcs(cs + 32 * j);
+        const float* vv = vs + 288 * j;
+        const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
+        const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
+        const float a6 = __ldcs(vv + 192), a7 = __ldcs(vv + 224), a8 = __ldcs(vv + 256);
+        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+        y0 += a0 * x0 + a1 * x1 + a2 * x2;
+        y1 += a3 * x0 + a4 * x1 + a5 * x2;
+        y2 += a6 * x0 + a7 * x1 + a8 * x2;
+    }
+    const int r = sl * 32 + lane;
+    if (r >= nN) return;
+    const int m = perm ? perm[r] : r;
+    const int d = 3 * m;
+    y[d + 0] = mask[d + 0] ? 0.f : y0;
+    y[d + 1] = mask[d + 1] ? 0.f : y1;
+    y[d + 2] = mask[d + 2] ? 0.f : y2;
+    if (COPY) {
+        xcopy[d + 0] = x[d + 0];
+        xcopy[d + 1] = x[d + 1];
+        xcopy[d + 2] = x[d + 2];
+    }
+}
+
+// t = r - K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
+// t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy
+__global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
+    int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
+    const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
+    const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
+    const float* __restrict__ binv, float omega) {
+    const int lane = threadIdx.x & 31;
+    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
+    if (sl >= nSlices) return;
+    const int64_t e0 = off[sl];
+    const int w = (int)((off[sl + 1] - e0) >> 5);
+    const int32_t* cs = col + e0 + lane;
+    const uint4* qs = v8 + e0 + lane;
+    const __nv_bfloat16* ws = v1 + e0 + lane;
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < w; ++j) {
+        const int c3 = 3 * __ldcs(cs + 32 * j);
+        const uint4 q = __ldcs(qs + 32 * j);
+        const float w8 = __bfloat162float(ws[32 * j]);
+        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+        const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
+        const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
+        y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
+        y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
+        y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
+    }
+    const int rr = sl * 32 + lane;
+    if (rr >= nN) return;
+    const int m = perm ? perm[rr] : rr;
+    const int d = 3 * m;
+    const bool k0 = mask[d], k1 = mask[d + 1], k2 = mask[d + 2];
+    const float t0 = k0 ? 0.f : r[d] - y0, t1 = k1 ? 0.f : r[d + 1] - y1, t2 = k2 ? 0.f : r[d + 2] - y2;
+    if (!binv) {
+        t[d] = t0;
+        t[d + 1] = t1;
+        t[d + 2] = t2;
+        return;
+    }
+    const float* B = binv + 9 * (int64_t)m;
+    const float z0 = B[0] * t0 + B[1] * t1 + B[2] * t2;
+    const float z1 = B[3] * t0 + B[4] * t1 + B[5] * t2;
+    const float z2 = B[6] * t0 + B[7] * t1 + B[8] * t2;
+    const float x0 = x[d], x1 = x[d + 1], x2 = x[d + 2];
+    t[d] = k0 ? x0 : x0 + omega * z0;
+    t[d + 1] = k1 ? x1 : x1 + omega * z1;
+    t[d + 2] = k2 ? x2 : x2 + omega * z2;
+}
+
+}  // namespace ef
+
+using namespace ef;
+
+static inline unsigned sell_grid(int nSlices) {
+    return (unsigned)((nSlices + kSellSlicesPerCta - 1) / kSellSlicesPerCta);
+}
+
+ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
+                                 cudaStream_t s) {
+    if (nE <= 0) return EF_OK;
+    sell_refresh_kernel<<<(unsigned)((nE + 255) / 256), 256, 0, ef::counted(s)>>>(
+        nE, src, bsr, v9, (uint4*)v8, (__nv_bfloat16*)v1);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                               cudaStream_t s) {
+    if (nSlices <= 0) return EF_OK;
+    if (xcopy)
+        sell_spmv3_kernel<true><<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(nN, nSlices, off, perm, col,
+                                                                                          v9, x, mask, y, xcopy);
+    else
+        sell_spmv3_kernel<false><<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(nN, nSlices, off, perm, col,
+                                                                                           v9, x, mask, y, nullptr);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                                     const void* v8, const void* v1, const float* x, const float* r,
+                                     const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s) {
+    if (nSlices <= 0) return EF_OK;
+    sell_level3_bf16_kernel<<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(
+        nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}

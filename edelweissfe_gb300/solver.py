@@ -171,6 +171,10 @@ class NISTGPU:
         dirDofs = [d.dofs for d in self.dirichlets]
         self.dirIdxHost = np.concatenate(dirDofs).astype(np.int64) if dirDofs else np.zeros(0, np.int64)
         self.dirIdx = torch.as_tensor(self.dirIdxHost, device=self.device)
+        _lib.check(self.lib.ef_set_dirichlet(self.ctx, self.dirIdxHost.ctypes.data, self.dirIdxHost.size),
+                   "ef_set_dirichlet")  # fmt: skip
+        self.newtonOpts = _lib.EfNewtonOpts(self.fluxResidualTolerance, self.fluxResidualToleranceAlternative,
+                                            self.fieldCorrectionTolerance, 1e-7, float(self.nAccumulatedFluxes))
         self.computationTimes = {}
         self.iterationHistory = []  # (increment number, Newton iterations) per converged increment
         self.krylovIterations = []  # per linear solve
@@ -360,6 +364,26 @@ class NISTGPU:
         residualHistory["displacement"] = (fluxResidual, nGrew)
         return convergedCorrection and convergedFlux
 
+    def newtonResidual(self, first, P, PExt, R, F, ddU, iterationCounter, residualHistory, timeStep):
+        """R = P + PExt with the Dirichlet rows of solvers/nonlinearimplicitstatic.py:418-436 and,
+        unless `first` (the first iteration of an increment that was not extrapolated: the
+        prescribed increments go into R, nothing is checked), checkConvergence (:625-725) decided on
+        the device (ef_newton_residual: one read per Newton iteration).  Returns converged."""
+        if first:
+            vals = self._dirichletDelta(timeStep)
+            _lib.check(self.lib.ef_newton_residual(self.ctx, 0, P.data_ptr(), PExt.data_ptr(), vals.data_ptr(), None,
+                                                   None, 0, 0.0, 0, None, R.data_ptr(), None, self._stream()),
+                       "ef_newton_residual")  # fmt: skip
+            return False
+        prev, nGrew = residualHistory["displacement"]
+        out = _lib.EfNewtonCheck()
+        _lib.check(self.lib.ef_newton_residual(self.ctx, 1, P.data_ptr(), PExt.data_ptr(), None, F.data_ptr(),
+                                               None if ddU is None else ddU.data_ptr(), iterationCounter, prev, nGrew,
+                                               ctypes.byref(self.newtonOpts), R.data_ptr(), ctypes.byref(out),
+                                               self._stream()), "ef_newton_residual")  # fmt: skip
+        residualHistory["displacement"] = (out.fluxResidual, out.nGrew)
+        return bool(out.converged)
+
     # -- Newton loop (same control flow as NIST.solveIncrement) ------------------------
     def extrapolateLastIncrement(self, extrapolation, timeStep, dU, prevTimeStep):
         if extrapolation == "linear" and prevTimeStep is not None and prevTimeStep.timeIncrement:
@@ -382,13 +406,10 @@ class NISTGPU:
         while True:
             torch.add(U_n, dU, out=U_np)
             P, F = self.computeElements(U_np, dU, P, F, timeStep)
-            torch.add(P, PExt, out=R)
-            if iterationCounter == 0 and not isExtrapolated and self.dirichlets:
-                R[self.dirIdx] = self._dirichletDelta(timeStep)
-            else:
-                if self.dirichlets:
-                    R[self.dirIdx] = 0.0
-                if self.checkConvergence(R, ddU, F, iterationCounter, residualHistory):
+            first = iterationCounter == 0 and not isExtrapolated and bool(self.dirichlets)
+            converged = self.newtonResidual(first, P, PExt, R, F, ddU, iterationCounter, residualHistory, timeStep)
+            if not first:
+                if converged:
                     break
                 if residualHistory["displacement"][1] > step.maxGrowIter:
                     raise DivergingSolution(f"Residual grew {step.maxGrowIter} times, cutting back")

@@ -226,6 +226,39 @@ ef_status ef_pcg_solve_noalloc(int64_t nNodes, const int32_t* rowPtr, const int3
  * Deterministic; synchronises `stream`. */
 ef_status ef_norms(ef_ctx* ctx, const double* R, const double* F, const double* ddU, double* out, void* stream);
 
+/* Tolerances of the convergence check (config/phenomena.py: 1e-8, 5e-3, 1e-8; the flux floor 1e-7
+ * of solvers/nonlinearimplicitstatic.py:680) and the accumulated nodal flux count of the field
+ * (numerics/dofmanager.py:354-380, the sum of the elements' DOF counts). */
+typedef struct ef_newton_opts {
+    double fluxTol;
+    double fluxTolAlt;   /* from the 15th iteration on */
+    double corrTol;
+    double fluxFloor;
+    double nAccFluxes;
+} ef_newton_opts;
+
+typedef struct ef_newton_check {
+    int converged;               /* the increment's Newton iteration converged */
+    int nGrew;                   /* residual growth count after this check */
+    double fluxResidual;         /* max |R| */
+    double fieldCorrection;      /* max |ddU| (0 without ddU) */
+    double spatialAveragedFlux;  /* max(1e-10, sum |F| / nAccFluxes) */
+} ef_newton_check;
+
+/* The Newton iteration's residual and convergence decision on the device
+ * (solvers/nonlinearimplicitstatic.py:418-440 and checkConvergence :625-725), for the
+ * displacement field.  R, P, PExt (may be NULL), F, ddU (may be NULL), dirValues: device [nDof]
+ * (dirValues [nDir], in the order of the ef_set_dirichlet list).
+ * mode 0 (the first iteration of an increment that was not extrapolated): R = P + PExt with the
+ * prescribed increments dirValues at the Dirichlet DOFs; no check, out unused, no synchronisation.
+ * mode 1: R = P + PExt with 0 at the Dirichlet DOFs, then the reference's test: converged when
+ * max |ddU| < corrTol and max |R| <= max(tol * max(1e-10, sum |F| / nAccFluxes), fluxFloor) with
+ * tol = fluxTol below iteration 15, else fluxTolAlt; nGrew counts max |R| > prevResidual.  One
+ * synchronising read of `out`. */
+ef_status ef_newton_residual(ef_ctx* ctx, int mode, const double* P, const double* PExt, const double* dirValues,
+                             const double* F, const double* ddU, int iteration, double prevResidual, int nGrew,
+                             const ef_newton_opts* opts, double* R, ef_newton_check* out, void* stream);
+
 /* ---- batches of independent small problems ----
  * The reference runs one model per job; a batch is many independent meshes held in one context
  * (one element group may carry a material row per element), each with its own Newton checks.

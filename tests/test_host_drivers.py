@@ -23,6 +23,7 @@ class _OracleLib:
     def __init__(self, nDof, elements):
         self.nDof = nDof
         self.elements = elements
+        self.dirIdx = np.zeros(0, np.int64)
 
     def _arr(self, ptr):
         return np.ctypeslib.as_array((ctypes.c_double * self.nDof).from_address(ptr))
@@ -35,6 +36,25 @@ class _OracleLib:
         return 0
 
     def ef_set_dirichlet(self, ctx, dofs, n):
+        self.dirIdx = np.ctypeslib.as_array((ctypes.c_int64 * n).from_address(dofs)).copy() if n else np.zeros(0, int)
+        return 0
+
+    def ef_newton_residual(self, ctx, mode, P, PExt, dirValues, F, ddU, iteration, prev, nGrew, opts, R, out, stream):
+        """The device check's arithmetic (solvers/nonlinearimplicitstatic.py:418-436, :625-725) on host memory."""
+        r = self._arr(R)
+        r[:] = self._arr(P) + (self._arr(PExt) if PExt else 0.0)
+        if mode == 0:
+            r[self.dirIdx] = np.ctypeslib.as_array((ctypes.c_double * self.dirIdx.size).from_address(dirValues))
+            return 0
+        r[self.dirIdx] = 0.0
+        o, res = opts._obj, out._obj
+        flux = np.max(np.abs(r))
+        avg = max(1e-10, np.sum(np.abs(self._arr(F))) / o.nAccFluxes)
+        corr = np.max(np.abs(self._arr(ddU))) if ddU else 0.0
+        tol = o.fluxTol if iteration < 15 else o.fluxTolAlt
+        res.converged = int(corr < o.corrTol and flux <= max(tol * avg, o.fluxFloor))
+        res.nGrew = nGrew + (1 if flux > prev else 0)
+        res.fluxResidual, res.fieldCorrection, res.spatialAveragedFlux = flux, corr, avg
         return 0
 
     def ef_accept_state(self, ctx):
@@ -79,6 +99,10 @@ def _oracle_backed(cls, model, dirichlets, nodeforces, elements, elDofs, **kw):
     s.device = torch.device("cpu")
     s.nDof = nDof
     s.nAccumulatedFluxes = model.n_accumulated_fluxes()
+    from edelweissfe_gb300 import _lib
+
+    s.newtonOpts = _lib.EfNewtonOpts(s.fluxResidualTolerance, s.fluxResidualToleranceAlternative,
+                                     s.fieldCorrectionTolerance, 1e-7, float(s.nAccumulatedFluxes))
     s.dirIdxHost = np.concatenate([d.dofs for d in s.dirichlets]).astype(np.int64)
     s.dirIdx = torch.as_tensor(s.dirIdxHost)
     s.computationTimes = {}
