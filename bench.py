@@ -59,14 +59,16 @@ def parse():
     ap.add_argument("--increment", type=int, default=13, help="load increment re-solved in the timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the all-FP64 solve of the timed increment")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="skip the tied-box and cube-batch records nested in the headline line")
     ap.add_argument("--no-learned", action="store_true", help="FGMRES + multigrid without the learned correction")
-    ap.add_argument("--no-learned-jacobi", action="store_true",
-                    help="skip the learned correction's measurement over the block-Jacobi base")
-    ap.add_argument("--learned-jacobi-budget", type=int, default=2000,
-                    help="Krylov iterations of each solve of that measurement")
+    ap.add_argument("--no-learned-family", action="store_true",
+                    help="skip the learned correction's cross-seed measurement on the seeded J2 family")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--restart", type=int, default=64, help="FGMRES restart length")
     ap.add_argument("--inner-rtol", type=float, default=1e-5, help="relative tolerance of one inner (FP32) solve")
+    ap.add_argument("--precond-reuse", type=int, default=0,
+                    help="Newton systems of an increment that reuse the coarse multigrid levels of its first one")
     ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")
     ap.add_argument("--workload", default="box", choices=["box", "cubes", "tied"],
                     help="box: the 160k-element J2 box (default); cubes: 1024 independent J2 cubes in one batch; "
@@ -78,7 +80,7 @@ def parse():
     return ap.parse_args()
 
 
-def multigrid_description():
+def multigrid_description(reuse=0):
     """The multigrid cycle as the library sets it up (its environment options, defaults otherwise)."""
     smoothed = os.environ.get("EF_AMG_SMOOTHED", "1") not in ("", "0")
     wl = int(os.environ.get("EF_AMG_WLEVELS", "0" if smoothed else "1"))
@@ -86,7 +88,8 @@ def multigrid_description():
     pre, post = os.environ.get("EF_AMG_PRE", sweeps), os.environ.get("EF_AMG_POST", sweeps)
     kind = "smoothed-aggregation" if smoothed else "rigid-body aggregation"
     cycle = "V-cycle" if wl == 0 else ("W-cycle on level 1" if wl == 1 else f"W-cycle on levels 1-{wl}")
-    return f"{kind} multigrid, {cycle}, {pre}/{post} block-Jacobi sweeps"
+    lag = f", coarse levels built once per increment and reused by up to {reuse} Newton systems" if reuse else ""
+    return f"{kind} multigrid, {cycle}, {pre}/{post} block-Jacobi sweeps{lag}"
 
 
 def workload(a):
@@ -231,68 +234,22 @@ def assembly_bytes(info, nEl, fp32=True):
     return elem, cond, scatter
 
 
-def learned_over_jacobi(s, budget, epochs=60, lr=1e-3):
-    """FGMRES + block Jacobi with and without the network trained on that solver's own pairs:
-    the FP64 relative residual that each reaches in the same number of Krylov iterations (the
-    plastic system makes FGMRES + block Jacobi stall before tight tolerances).  The pairs come
-    from solves to 1e-2."""
-    import ctypes
+def learned_seeded_family(dims=(40, 16, 16), train=(0, 1, 2, 3), test=(4, 5), increments=14):
+    """The learned correction on the seeded J2 family (per seed sigma_y ~ U[150,350],
+    H ~ U[200,2000], nu ~ U[0.2,0.4]): trained on the Newton-iteration pairs of the `train` seeds'
+    load histories (one context, one box per seed), then the load history of the unseen `test`
+    seeds with and without it, over the block-Jacobi and the multigrid base."""
+    from edelweissfe_gb300.learned import evaluate_on_seeds, train_across_seeds
 
-    import torch
-
-    from edelweissfe_gb300 import _lib
-
-    s.enableLearnedPreconditioner(False)
-    s.setFgmresPreconditioner("jacobi")
-    saved = s.learnedParameters()
-    saved_rtol = s.linsolver.rtol
-
-    def rhs(seed):
-        b = np.random.default_rng(seed).normal(size=s.nDof)
-        b[s.dirIdxHost] = 0.0
-        return torch.as_tensor(b, device="cuda")
-
-    def capped(seed):
-        o = s.linsolver
-        opts = _lib.EfSolveOpts(_lib.EF_SOLVE_FGMRES, 1, 1e-8, o.innerRtol, budget, o.restart, o.maxRefine, 0)
-        info = _lib.EfSolveInfo()
-        b = rhs(seed)
-        x = torch.empty_like(b)
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        st = s.lib.ef_solve(s.ctx, ctypes.byref(opts), b.data_ptr(), x.data_ptr(), ctypes.byref(info),
-                            s._stream())  # fmt: skip
-        torch.cuda.synchronize()
-        if st not in (_lib.EF_OK, _lib.EF_NOT_CONVERGED):
-            _lib.check(st, "ef_solve")
-        return info.relResidual, info.iterations, time.perf_counter() - t
-
-    try:
-        off_r, off_k, off_s = capped(100)
-        s.clearTrainingPairs()
-        s.initLearnedPreconditioner(seed=1, maxSamples=32)
-        s.linsolver.rtol = 1e-2
-        s.collectTrainingPairs(every=10, maxPerSolve=8, kind="iterates")
-        for k in range(4):
-            s.linearSolve(rhs(k))
-        s.collectTrainingPairs(0, 0)
-        torch.cuda.synchronize()
-        t0 = time.time()
-        lf, ll = s.trainLearnedPreconditioner(epochs=epochs, lr=lr, norm="energy")
-        torch.cuda.synchronize()
-        train_s = time.time() - t0
-        s.enableLearnedPreconditioner(True)
-        on_r, on_k, on_s = capped(100)
-        return {"base": "block Jacobi", "krylov_budget": budget, "pairs": s.numTrainingPairs(), "epochs": epochs,
-                "loss_first": lf, "loss_last": ll, "train_s": train_s, "off_relres": off_r, "on_relres": on_r,
-                "off_krylov": off_k, "on_krylov": on_k, "off_s": off_s, "on_s": on_s}  # fmt: skip
-    except Exception as ex:  # reported, not fatal to the bench
-        return {"base": "block Jacobi", "krylov_budget": budget, "error": f"{type(ex).__name__}: {ex}"}
-    finally:
-        s.linsolver.rtol = saved_rtol
-        s.enableLearnedPreconditioner(False)
-        s.setFgmresPreconditioner("multigrid")
-        s.setLearnedParameters(*saved)
+    out = {"box": "x".join(map(str, dims)), "increments": increments}
+    for base in ("jacobi", "multigrid"):
+        try:
+            params, scales, rec = train_across_seeds(list(train), dims, increments, base=base, epochs=100)
+            ev = evaluate_on_seeds(list(test), dims, increments, params, scales, base=base)
+            out[base] = {"train": rec, "unseen": ev}
+        except Exception as ex:  # reported, not fatal to the bench
+            out[base] = {"error": f"{type(ex).__name__}: {ex}"}
+    return out
 
 
 def run_ours(a):
@@ -313,7 +270,8 @@ def run_ours(a):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     t0 = time.time()
-    s = build_solver(a, LinSolverOptions(method="fgmres", rtol=1e-8, restart=a.restart, innerRtol=a.inner_rtol))
+    s = build_solver(a, LinSolverOptions(method="fgmres", rtol=1e-8, restart=a.restart, innerRtol=a.inner_rtol,
+                                         precondReuse=a.precond_reuse))  # fmt: skip
     setup_s = time.time() - t0
     info = s.info
     lib = s.lib
@@ -409,7 +367,7 @@ def run_ours(a):
             x = orig(R)
             i = s.lastSolveInfo
             infos.append((i.kernelMs, i.iterations, i.kernelLaunches, i.spmvMs, i.spmvLaunches, i.precondMs,
-                          i.orthoMs, i.reorths, i.refinements, 1))
+                          i.orthoMs, i.reorths, i.refinements, 1, i.setupMs))
             return x
 
         s.linsolver.profile = True
@@ -419,9 +377,9 @@ def run_ours(a):
         finally:
             s.linearSolve = orig
             s.linsolver.profile = False
-        return [sum(x[i] for x in infos) for i in range(10)]
+        return [sum(x[i] for x in infos) for i in range(11)]
 
-    fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth, n_refine, n_solves = profiled_step()
+    fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth, n_refine, n_solves, setup_ms = profiled_step()
 
     # comparison arm: block-Jacobi PCG on the same load step
     s.linsolver.method = "pcg"
@@ -484,11 +442,21 @@ def run_ours(a):
         Uh, _, _, nh = s.solveIncrement(U_n, dU_n.clone(), s._vec(), target, prev, step)
         parity = fp64_parity(a, s, U_n, dU_n, target, prev, step, Uh, nh)
 
-    # the learned correction over the block-Jacobi base on this model's last Newton system: pairs
-    # from the plain FGMRES + block-Jacobi solves of random right-hand sides, GPU training, then
-    # one solve of a new right-hand side with and without the trained network
-    if learned and not a.no_learned_jacobi:
-        learned_info["over_jacobi"] = learned_over_jacobi(s, a.learned_jacobi_budget)
+    # the learned correction trained across seeds of the J2 family and used on unseen seeds
+    if learned and not a.no_learned_family:
+        learned_info["seeded_family"] = learned_seeded_family()
+
+    # the other two workloads of the suite, each in its own context: the tied hex20 | hex8 box and
+    # the batch of 1024 cubes (one whole load history); their records are nested in this line
+    others = None
+    if not a.no_other_workloads and rank == 0:
+        others = {}
+        for key, fn, args in (("tied", measure_tied, (3, 3)), ("cubes", measure_cubes, (1, 1))):
+            try:
+                others[key] = fn(*args)
+            except Exception as ex:  # reported, not fatal to the headline
+                others[key] = {"error": f"{type(ex).__name__}: {ex}"}
+            torch.cuda.synchronize()
 
     peaks, peak_kind = measured_peaks()
     sb = spmv_bytes(info)
@@ -520,7 +488,7 @@ def run_ours(a):
         "dtype": "f64 residual/return map, f32 stiffness + Krylov inner, f64 refinement",
         "data": "synthetic (structured box mesh, seeded parameters)",
         "config": workload(a),
-        "solver": f"FGMRES({a.restart}) + {multigrid_description()} ({stage})",
+        "solver": f"FGMRES({a.restart}) + {multigrid_description(a.precond_reuse)} ({stage})",
         "newton_iterations_per_step": newton,
         "krylov_iterations_per_step": krylov,
         "comparison": {"jacobi_pcg_step_s": pcg_s, "speedup_vs_jacobi_pcg": pcg_s / t_step,
@@ -538,7 +506,8 @@ def run_ours(a):
                            "spmv_ms_per_iteration": sp_ms / fg_it if fg_it else None,
                            "ortho_ms_per_iteration": orth_ms / fg_it if fg_it else None,
                            "reorthogonalised_columns": int(n_reorth), "solves": int(n_solves),
-                           "refinement_sweeps": int(n_refine), "restart": a.restart, "inner_rtol": a.inner_rtol},
+                           "refinement_sweeps": int(n_refine), "restart": a.restart, "inner_rtol": a.inner_rtol,
+                           "preconditioner_setup_ms": setup_ms},
         "dof_iterations_per_s": info.nDof * fg_it / (fg_kms * 1e-3) if fg_kms > 0 else None,
         "setup_s": setup_s,
         "history_s": history_s,
@@ -554,6 +523,7 @@ def run_ours(a):
         "clocks": clk,
         "cpu_baseline": cpu,
         "parity": parity,
+        "other_workloads": others,
         "history_newton": history,
     }  # fmt: skip
     if rank == 0:
@@ -565,17 +535,23 @@ def run_ours(a):
 def run_cubes(a):
     """1024 independent J2 hex8 cubes (edge n ~ U{4..16}, random sigma_y, H, nu per cube; base
     clamped, top pulled by 1 % in 10 increments): one step = the whole load history of the batch."""
+    from edelweissfe_gb300 import build as b
+
+    b.build()
+    print(json.dumps(measure_cubes(a.steps, a.warmup)), flush=True)
+
+
+def measure_cubes(steps, warmup):
+    """The cube batch's JSON record (see run_cubes)."""
     import torch
 
-    from edelweissfe_gb300 import build as b
     from edelweissfe_gb300.batch import BatchNISTGPU, cube_batch_spec
     from edelweissfe_gb300.solver import Step
 
-    b.build()
     spec = cube_batch_spec(1024, 0)
     step = Step(maxInc=0.1, minInc=1e-6, maxIter=25)
     s = BatchNISTGPU(spec)
-    for _ in range(max(1, a.warmup)):
+    for _ in range(max(1, warmup)):
         s.problemHistory.clear()
         s.krylovPerProblem[:] = 0
         s.solveStepBatch(step)
@@ -585,7 +561,7 @@ def run_cubes(a):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = s.lib.ef_kernel_launches()
     e0.record()
-    for _ in range(a.steps):
+    for _ in range(steps):
         s.problemHistory.clear()
         s.krylovPerProblem[:] = 0
         s.solveStepBatch(step)
@@ -593,7 +569,7 @@ def run_cubes(a):
     torch.cuda.synchronize()
     launches = s.lib.ef_kernel_launches() - l0
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3 / a.steps
+    t = e0.elapsed_time(e1) / 1e3 / steps
     # batched-PCG roofline from one eager profiled run: bytes per problem-iteration = its blocks
     # (72 B values + 4 B column) + row pointers + 10 vector passes of its DOFs
     prof = BatchNISTGPU(spec, graph=False, tile=s.tile)
@@ -611,7 +587,7 @@ def run_cubes(a):
     nEl = int(s.nElProb.sum())
     line = {
         "metric": "batched J2 cubes: load-history s (1024 cubes, 10 increments)",
-        "value": t, "unit": "s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3,
+        "value": t, "unit": "s", "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": t * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (state, stiffness, PCG)", "data": "synthetic (seeded cube sizes and materials)",
         "config": {"workload": "1024 J2 hex8 cubes, n ~ U{4..16}, sigma_y ~ U[150,350], H ~ U[200,2000], "
@@ -628,22 +604,28 @@ def run_cubes(a):
                      "solve_s": solve_s, "bytes": total_bytes},
         "clocks": clk,
     }  # fmt: skip
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_tied(a):
     """60x30x30 box (h = 1/30): x < 30 C3D20TL, x >= 30 C3D8TL, NeoHookeWa [80, 200], tied
     interface, x = 0 clamped, x = 60 face compressed to 30 % over 40 increments.  A step is one
     load increment (all Newton iterations, state accepted); warm-up increments run first."""
+    from edelweissfe_gb300 import build as b
+
+    b.build()
+    print(json.dumps(measure_tied(a.steps, a.warmup)), flush=True)
+
+
+def measure_tied(steps, warmup):
+    """The tied box's JSON record (see run_tied)."""
     import torch
 
     from edelweissfe_gb300 import _lib
-    from edelweissfe_gb300 import build as b
     from edelweissfe_gb300.mesh import tied_box_mesh
     from edelweissfe_gb300.model import DirichletBC, ElementGroup, Model
     from edelweissfe_gb300.solver import AdaptiveTimeStepper, LinSolverOptions, NISTGPU, Step
 
-    b.build()
     h = 1.0 / 30.0
     m = tied_box_mesh(30, 30, 30, 30, 30 * h, 30 * h, 30 * h, 30 * h)
     p = np.array([80.0, 200.0])
@@ -668,7 +650,7 @@ def run_tied(a):
         U, prev = Unp, ts
         return it, sum(s.krylovIterations)
 
-    for _ in range(max(3, a.warmup)):
+    for _ in range(max(3, warmup)):
         increment()
     clocks = ClockSampler()
     clocks.start()
@@ -676,16 +658,16 @@ def run_tied(a):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = s.lib.ef_kernel_launches()
     e0.record()
-    its = [increment() for _ in range(a.steps)]
+    its = [increment() for _ in range(steps)]
     e1.record()
     torch.cuda.synchronize()
     launches = s.lib.ef_kernel_launches() - l0
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3 / a.steps
+    t = e0.elapsed_time(e1) / 1e3 / steps
     peaks, peak_kind = measured_peaks()
     line = {
         "metric": "tied hex20|hex8 NeoHookeWa box: load-increment s",
-        "value": t, "unit": "s", "n_gpus": 1, "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": t * 1e3,
+        "value": t, "unit": "s", "n_gpus": 1, "steps": steps, "warmup": max(3, warmup), "ms_per_step": t * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 kinematics/stress/residual, f32 stiffness + Krylov inner, f64 refinement",
         "data": "synthetic (structured mesh)",
@@ -696,7 +678,7 @@ def run_tied(a):
         "solver": f"FGMRES(40) + {multigrid_description()}",
         "gpu_launches": int(launches), "clocks": clk, "peak_kind": peak_kind,
     }  # fmt: skip
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def _element_sample(args):

@@ -75,6 +75,7 @@ class EfSolveInfo(ctypes.Structure):
         ("precondMs", c_dbl),
         ("orthoMs", c_dbl),
         ("reorths", c_int),
+        ("setupMs", c_dbl),
     ]
 
 
@@ -126,6 +127,7 @@ SIGNATURES = {
     "ef_pcg_noalloc_max_nodes": (c_i64, []),
     "ef_kernel_launches": (c_i64, []),
     "ef_fgmres_set_preconditioner": (c_int, [c_vp, c_int]),
+    "ef_fgmres_set_reuse": (c_int, [c_vp, c_int]),
     "ef_set_group_props": (c_int, [c_vp, c_int, c_vp, c_int, c_int, c_vp]),
     "ef_set_group_cutback": (c_int, [c_vp, c_int, c_dbl]),
     "ef_set_ties": (c_int, [c_vp, c_vp, c_vp, c_vp, c_i64]),

@@ -495,6 +495,9 @@ struct ef_ctx {
     int32_t* dRowOfBlock0 = nullptr;     // fine-level block -> block row
     float *fineX = nullptr, *fineT = nullptr;  // level-0 V-cycle work vectors
     bool amgStale = true;                // coarse values need a refresh (new system or mask)
+    bool amgMaskChanged = true;          // the Dirichlet mask changed since the coarse levels were built
+    int amgMaxReuse = 0;                 // new systems that may reuse the coarse levels (ef_fgmres_set_reuse)
+    int amgReuseLeft = 0;                // reuses left before the next rebuild
     bool nnEdgeStale = true;             // the learned correction's edge weights need a refresh
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern
@@ -1643,6 +1646,7 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
     EF_CUDA(cudaMemcpy(c->dMask, m.data(), c->nDof, cudaMemcpyHostToDevice));
     c->hMask = std::move(m);
     c->amgStale = true;
+    c->amgMaskChanged = true;
     c->nnEdgeStale = true;
     c->nnVersion++;
     return EF_OK;
@@ -2408,6 +2412,18 @@ static ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
 static ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     EF_CHECK(sell_refresh(c, s));
     if (!c->amgStale) return EF_OK;
+    if (!c->amgMaskChanged && c->amgReuseLeft > 0) {
+        // lagged coarse levels: the prolongators, coarse operators and damping of an earlier system
+        // of the same pattern and mask; the fine level (blocks, block inverses, BF16 copy) is the
+        // current system's
+        c->amgReuseLeft--;
+        if (c->dBsrValsH)
+            EF_CHECK(ef_launch_to_bf16_split(c->nBlocks, (const float*)c->dBsrVals, c->dBsrValsH, s));
+        c->amgStale = false;
+        return nn_edge_refresh(c, s);
+    }
+    c->amgReuseLeft = c->amgMaxReuse;
+    c->amgMaskChanged = false;
     const int BCo = ef_amg_coarse_dofs();
     const uint8_t* fineDead = c->hMask.data();
     for (size_t l = 0; l < c->amg.size(); ++l) {
@@ -3190,6 +3206,8 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
             PcgResultHost pr;
             if (o->method == EF_SOLVE_FGMRES) {
+                const bool timeSetup = o->profile && (c->sellStale || c->amgStale);
+                if (timeSetup) EF_CUDA(cudaEventRecord(c->ev[0], s));
                 EF_CHECK(sell_refresh(c, s));
                 if (c->fgPc == EF_FGMRES_PC_MULTIGRID) {
                     EF_CHECK(amg_build(c));
@@ -3197,6 +3215,13 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
                 } else {
                     EF_CHECK(amg_workspace(c));
                     EF_CHECK(nn_edge_refresh(c, s));
+                }
+                if (timeSetup) {
+                    EF_CUDA(cudaEventRecord(c->ev[1], s));
+                    EF_CUDA(cudaEventSynchronize(c->ev[1]));
+                    float ms = 0.f;
+                    EF_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+                    inf.setupMs += ms;
                 }
                 int its = 0;
                 const ef_status fs = run_fgmres(c, (const float*)wv[0], (float*)wv[1], o->maxIter - total,
@@ -3254,6 +3279,17 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
         }
     }
     return result;
+}
+
+ef_status ef_fgmres_set_reuse(ef_ctx* c, int maxReuse) {
+    EF_REQUIRE_FINALIZED(c);
+    if (maxReuse < 0) {
+        ef_set_error("ef_fgmres_set_reuse: maxReuse must be >= 0");
+        return EF_ERR_ARG;
+    }
+    c->amgMaxReuse = maxReuse;
+    c->amgReuseLeft = 0;  // the next new system rebuilds the coarse levels
+    return EF_OK;
 }
 
 ef_status ef_fgmres_set_preconditioner(ef_ctx* c, int kind) {

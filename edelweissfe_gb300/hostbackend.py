@@ -154,6 +154,12 @@ class HostArrayBackend:
         torch.cuda.current_stream(self.device).synchronize()
         return h.numpy().copy()
 
+    def begin_increment(self):
+        """A new increment: its first new system rebuilds the FGMRES multigrid's coarse levels, the
+        following ones reuse them (LinSolverOptions.precondReuse; ef_fgmres_set_reuse)."""
+        if self.linsolver.method == "fgmres":
+            _lib.check(self.lib.ef_fgmres_set_reuse(self.ctx, self.linsolver.precondReuse), "ef_fgmres_set_reuse")
+
     def accept_state(self):
         """acceptLastState for every element (trial -> committed state, on the device)."""
         _lib.check(self.lib.ef_accept_state(self.ctx), "ef_accept_state")

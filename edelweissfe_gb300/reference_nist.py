@@ -27,7 +27,8 @@ into the elements once, when the step ends).
 Options (``*solver`` or ``options, category=NISTSolver``; the reference's ``_updateOptions``):
 ``gpuSolver`` ("pcg" or "fgmres"), ``gpuMixed`` (1: FP32 inner iterations + FP64 refinement),
 ``gpuRtol`` (FP64 relative residual of each solve), ``gpuKeFp64`` (1: FP64 element stiffness),
-``gpuSyncStates``.
+``gpuSyncStates``, ``gpuPrecondReuse`` (Newton systems of an increment that reuse the coarse
+multigrid levels built for its first one).
 
 Supported entities: ``DisplacementElement`` and ``DisplacementTLElement`` of the 3D hexahedra
 (C3D8, C3D8R, C3D8E, C3D20, C3D20R and their TL forms) with ``LinearElasticMaterial``,
@@ -129,7 +130,7 @@ def nist_gpu_class(NIST=None, exceptions=None, backendFactory=None):
         identification = "NISTGPUSolver"
 
         NISTOptions = dict(NIST.NISTOptions, linsolver="superlu", gpuSolver="fgmres", gpuMixed=1, gpuRtol=1e-10,
-                           gpuKeFp64=0, gpuSyncStates=1)  # fmt: skip
+                           gpuKeFp64=0, gpuSyncStates=1, gpuPrecondReuse=0)  # fmt: skip
 
         def solveStep(self, step, model, fieldOutputController, outputmanagers):
             self._gpu = None
@@ -151,7 +152,8 @@ def nist_gpu_class(NIST=None, exceptions=None, backendFactory=None):
                                                           self.theDofManager.nDof)  # fmt: skip
                 o = self.options
                 ls = LinSolverOptions(method=o["gpuSolver"], mixed=bool(o["gpuMixed"]), rtol=o["gpuRtol"],
-                                      restart=64 if o["gpuSolver"] == "fgmres" else 40)  # fmt: skip
+                                      restart=64 if o["gpuSolver"] == "fgmres" else 40,
+                                      precondReuse=int(o["gpuPrecondReuse"]))  # fmt: skip
                 self._gpu = backendFactory(self.theDofManager.nDof, X, groups, bool(o["gpuKeFp64"]), ls)
                 self._gpuMembers = members
             return self._gpu
@@ -167,6 +169,8 @@ def nist_gpu_class(NIST=None, exceptions=None, backendFactory=None):
 
         # ---- the Newton iteration's hot path ---------------------------------------------------
         def solveIncrement(self, *args, **kwargs):
+            if self._gpu is not None and hasattr(self._gpu, "begin_increment"):
+                self._gpu.begin_increment()
             out = super().solveIncrement(*args, **kwargs)
             self._gpu.accept_state()
             if self.options["gpuSyncStates"]:

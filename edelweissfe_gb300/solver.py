@@ -114,6 +114,7 @@ class LinSolverOptions:
     restart: int = 40
     maxRefine: int = 30
     profile: bool = False
+    precondReuse: int = 0  # FGMRES: Newton systems of an increment that reuse its first one's coarse multigrid levels
 
 
 class NISTGPU:
@@ -403,6 +404,8 @@ class NISTGPU:
         ddU = None
         dU, isExtrapolated = self.extrapolateLastIncrement(step.extrapolation, timeStep, dU, prevTimeStep)
         PExt = self._externalLoads(timeStep)
+        if self.linsolver.method == "fgmres":
+            _lib.check(self.lib.ef_fgmres_set_reuse(self.ctx, self.linsolver.precondReuse), "ef_fgmres_set_reuse")
         while True:
             torch.add(U_n, dU, out=U_np)
             P, F = self.computeElements(U_np, dU, P, F, timeStep)

@@ -81,6 +81,7 @@ typedef struct ef_solve_info {
     double precondMs;    /* FGMRES: summed duration of the preconditioner applications (profile = 1) */
     double orthoMs;      /* FGMRES: summed duration of the Gram-Schmidt steps (profile = 1) */
     int reorths;         /* FGMRES: columns that the DGKS test re-orthogonalised (profile = 1) */
+    double setupMs;      /* FGMRES: duration of the preconditioner set-up for a new system (profile = 1) */
 } ef_solve_info;
 
 int ef_abi_version(void);
@@ -312,6 +313,15 @@ ef_status ef_batch_norms(ef_ctx* ctx, const double* R, const double* F, const do
 #define EF_FGMRES_PC_MULTIGRID 0
 #define EF_FGMRES_PC_JACOBI 1
 ef_status ef_fgmres_set_preconditioner(ef_ctx* ctx, int kind);
+
+/* Lagged multigrid for the Newton iterations of one increment (inexact Newton-Krylov: the
+ * preconditioner may lag the tangent, the FP64 refinement against the exact tangent decides the
+ * solution): after this call the next newly assembled system rebuilds the coarse levels
+ * (smoothed prolongators, Galerkin operators, damping estimates), and up to maxReuse systems
+ * after it reuse them; the fine level (blocks, block inverses, BF16 copy) is always the current
+ * system's, and a new Dirichlet set always rebuilds.  maxReuse = 0 (the default) rebuilds for
+ * every system.  The Newton drivers call it at the start of each increment. */
+ef_status ef_fgmres_set_reuse(ef_ctx* ctx, int maxReuse);
 
 /* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----
  * The reference solves every Newton system with a direct or plain Krylov solver

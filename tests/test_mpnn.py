@@ -182,3 +182,21 @@ def test_gpu_trained_network_cuts_fgmres_iterations(gpu_lib):
     on = iterations([100, 101, 102])
     s.enableLearnedPreconditioner(False)
     assert on.mean() <= 0.6 * off.mean(), (off, on)
+
+
+@pytest.mark.gpu
+def test_gpu_network_trained_across_seeds_cuts_iterations_on_unseen_seeds(gpu_lib):
+    """The seeded J2 family (per seed sigma_y ~ U[150,350], H ~ U[200,2000], nu ~ U[0.2,0.4]):
+    pairs from the Newton iterations of four seeds' load histories (one context, one box per
+    seed), GPU training, then the load history of two unseen seeds with FGMRES + block Jacobi
+    with and without the trained network: the same Newton iteration counts and displacements
+    (1e-6), and fewer Krylov iterations with the network."""
+    from edelweissfe_gb300.learned import evaluate_on_seeds, train_across_seeds
+
+    dims = (12, 6, 6)
+    params, scales, rec = train_across_seeds([0, 1, 2, 3], dims, increments=14, base="jacobi", epochs=100)
+    assert rec["pairs"] > 16 and rec["loss_last"] < rec["loss_first"], rec
+    ev = evaluate_on_seeds([4, 5], dims, increments=14, params=params, scales=scales, base="jacobi")
+    assert ev["newton_on"] == ev["newton_off"], ev
+    assert ev["max_rel_dU"] <= 1e-6, ev
+    assert ev["krylov_on"] <= 0.8 * ev["krylov_off"], ev
