@@ -14,8 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libefgpu.so")
-SOURCES = ["capi.cu", "elements.cu", "elements_tl.cu", "assembly.cu", "krylov.cu", "amg.cu", "fgmres.cu", "mpnn.cu", "batch.cu",
-           "sell.cu"]
+SOURCES = ["capi.cu", "system.cu", "precond.cu", "solve.cu", "learned_api.cu", "batch_api.cu", "elements.cu",
+           "elements_tl.cu", "assembly.cu", "krylov.cu", "amg.cu", "fgmres.cu", "mpnn.cu", "batch.cu", "sell.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
 
