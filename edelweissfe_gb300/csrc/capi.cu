@@ -509,6 +509,10 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         g.nPair = h.nNodes * (h.nNodes + 1) / 2;
         g.mat = h.mat;
         g.tl = h.tl;
+        // FP64 <-> FP32-pair conversions by integer operations (off the FP64 pipe; the element pass
+        // 0.62 -> 0.54 ms at 160k hex8 J2 elements, same results to the fixtures' tolerances);
+        // EF_ELEM_INTCONV=0 uses the FP64 conversion instructions
+        g.intConv = 1;
         if (const char* e = getenv("EF_ELEM_INTCONV")) g.intConv = atoi(e) != 0;
         g.cutback = (float)h.cutback;
         g.nState = 12 + ((h.mat == MAT_VON_MISES || h.mat == MAT_NEOHOOKE_WA) ? 1 : 0);

@@ -365,6 +365,7 @@ struct ef_ctx {
     bool amgMaskChanged = true;          // the Dirichlet mask changed since the coarse levels were built
     int amgMaxReuse = 0;                 // new systems that may reuse the coarse levels (ef_fgmres_set_reuse)
     int amgReuseLeft = 0;                // reuses left before the next rebuild
+    bool amgPowerDue = true;             // the next build re-estimates the damping (power iterations)
     bool nnEdgeStale = true;             // the learned correction's edge weights need a refresh
     std::vector<uint8_t> hMask;
     std::vector<int32_t> hRowPtr0, hColIdx0;  // host copy of the fine block pattern

@@ -699,6 +699,10 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
         fineDead = L.hDead.data();
     }
     if (c->amgSmoothed) EF_CHECK(amg_power_alloc(c));
+    // with reuse enabled, the damping estimates (lambda_max of D^-1 A per level) come from the
+    // increment's first build; the later builds of the increment keep them
+    const bool power = c->amgPowerDue || c->amgMaxReuse == 0;
+    c->amgPowerDue = false;
     for (size_t l = 0; l < c->amg.size(); ++l) {
         AmgLevel& L = c->amg[l];
         const bool fine = l == 0;
@@ -710,7 +714,7 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
             // smoothed prolongator P = P_t - 4 / (3 lambda) D^-1 A P_t of the finer level (its lambda
             // from the power iteration on the device), then A P and P^T A P
             const float* fBinv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
-            EF_CHECK(amg_power(c, (int)l, s));
+            if (power) EF_CHECK(amg_power(c, (int)l, s));
             EF_CHECK(ef_launch_sa_damping(c->amgNorms + 3 * ((int)l * kPowerSteps + kPowerSteps - 1), L.saW, s));
             EF_CHECK(ef_launch_sa_setup(fine ? 3 : BCo, L.saNP, L.saPRow, L.saPCol, L.saPSeg, L.saPSrc, L.saNAP,
                                         L.saApRow, L.saApSeg, L.saApK, L.saApP, fCol, fVals, fMask, L.offs, L.agg,
@@ -727,10 +731,12 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
     EF_CHECK(ef_launch_coarsest_inverse(C.nN, C.rowPtr, C.colIdx, C.vals, c->amgCoarsestInv, s));
     if (c->dBsrValsH)
         EF_CHECK(ef_launch_to_bf16_split(c->nBlocks, (const float*)c->dBsrVals, c->dBsrValsH, s));
-    if (c->amgSmoothed) {
-        EF_CHECK(amg_damping_finish(c, s));  // every level's power iteration ran above
-    } else {
-        EF_CHECK(amg_damping(c, s));
+    if (power) {
+        if (c->amgSmoothed) {
+            EF_CHECK(amg_damping_finish(c, s));  // every level's power iteration ran above
+        } else {
+            EF_CHECK(amg_damping(c, s));
+        }
     }
     c->amgStale = false;
     return nn_edge_refresh(c, s);

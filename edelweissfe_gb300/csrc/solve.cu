@@ -418,7 +418,8 @@ ef_status ef_fgmres_set_reuse(ef_ctx* c, int maxReuse) {
         return EF_ERR_ARG;
     }
     c->amgMaxReuse = maxReuse;
-    c->amgReuseLeft = 0;  // the next new system rebuilds the coarse levels
+    c->amgReuseLeft = 0;    // the next new system rebuilds the coarse levels
+    c->amgPowerDue = true;  // and re-estimates the damping
     return EF_OK;
 }
 

@@ -100,6 +100,7 @@ ef_status ef_set_dirichlet(ef_ctx* c, const int64_t* dofs, int64_t n) {
     c->hMask = std::move(m);
     c->amgStale = true;
     c->amgMaskChanged = true;
+    c->amgPowerDue = true;
     c->nnEdgeStale = true;
     c->nnVersion++;
     return EF_OK;

@@ -319,8 +319,10 @@ ef_status ef_fgmres_set_preconditioner(ef_ctx* ctx, int kind);
  * solution): after this call the next newly assembled system rebuilds the coarse levels
  * (smoothed prolongators, Galerkin operators, damping estimates), and up to maxReuse systems
  * after it reuse them; the fine level (blocks, block inverses, BF16 copy) is always the current
- * system's, and a new Dirichlet set always rebuilds.  maxReuse = 0 (the default) rebuilds for
- * every system.  The Newton drivers call it at the start of each increment. */
+ * system's, and a new Dirichlet set always rebuilds.  With maxReuse > 0 the rebuilds inside the
+ * increment also keep the damping estimates (power iterations on D^-1 A) of its first build.
+ * maxReuse = 0 (the default) rebuilds everything for every system.  The Newton drivers call it
+ * at the start of each increment. */
 ef_status ef_fgmres_set_reuse(ef_ctx* ctx, int maxReuse);
 
 /* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----

@@ -393,10 +393,12 @@ def test_element_kernel_other_integration_rules_match_reference_fixture(gpu_lib,
 
 @pytest.mark.parametrize("elType,mat", [("C3D8", "vonmises"), ("C3D8", "vonmisesexp"), ("C3D20", "vonmises"),
                                         ("C3D8R", "vonmises")])  # fmt: skip
-def test_element_kernel_integer_conversions_match_reference_fixture(gpu_lib, elType, mat, monkeypatch):
+@pytest.mark.parametrize("intconv", ["1", "0"])
+def test_element_kernel_integer_conversions_match_reference_fixture(gpu_lib, elType, mat, intconv, monkeypatch):
     """The element kernel with its FP64 <-> FP32-pair conversions and NaN tests done by integer
-    operations (EF_ELEM_INTCONV=1, csrc/dfloat_bits.h) against the reference's fixtures, as above."""
-    monkeypatch.setenv("EF_ELEM_INTCONV", "1")
+    operations (EF_ELEM_INTCONV=1, the default, csrc/dfloat_bits.h) and by the FP64 conversion
+    instructions (EF_ELEM_INTCONV=0) against the reference's fixtures, as above."""
+    monkeypatch.setenv("EF_ELEM_INTCONV", intconv)
     test_element_kernel_matches_reference_fixture(gpu_lib, elType, mat, False)
 
 
