@@ -37,9 +37,11 @@ sys.path.insert(0, ROOT)
 
 PROPS = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
 METRIC = "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s"
-# DRAM bytes of one spmv_f32_kernel launch on the 100x40x40 box (509,343 DOF, 4,406,941 blocks),
-# measured with ncu (launch list in the FGMRES profile summary): equal to the algorithmic bytes
-SPMV_TRAFFIC_BYTES = 181.53e6
+# DRAM bytes (read + write) per launch of the two fine-level kernels of the FGMRES solve on the
+# 100x40x40 box (509,343 DOF, 4,406,941 blocks), from one ncu capture of bench.py --profile
+# (profiles/sell_kernels_hex8_J2_100x40x40.md)
+SWEEP_TRAFFIC_BYTES = 106.28e6
+PRODUCT_TRAFFIC_BYTES = 185.74e6
 # Newton iterations of the timed increment (13) of the 100x40x40 model: the same in the all-FP64
 # and the mixed-precision GPU solves; the CPU arms charge this many element passes and solves
 PCG_NEWTON_PER_STEP = 8
@@ -205,12 +207,6 @@ def ctypes_state_size(s, gid):
     nQP, nState = ctypes.c_int(), ctypes.c_int()
     s.lib.ef_get_state_size(s.ctx, gid, ctypes.byref(nQP), ctypes.byref(nState))
     return nQP.value, nState.value
-
-
-def spmv_bytes(info):
-    """Algorithmic DRAM bytes of one FP32 BSR(3x3) SpMV y = K x on the free DOFs."""
-    nb, nn, nd = info.nBlocks, info.nNodes, info.nDof
-    return nb * (9 * 4 + 4) + (nn + 1) * 4 + nd * 4 + nd * 4 + nd  # blocks + columns, row pointers, x, y, mask
 
 
 def pcg_bytes_per_iteration(info, fp32=True):
@@ -380,6 +376,11 @@ def run_ours(a):
         return [sum(x[i] for x in infos) for i in range(11)]
 
     fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth, n_refine, n_solves, setup_ms = profiled_step()
+    # the fine-level kernels timed live on the timed increment's last system (CUDA events, same stream)
+    import ctypes
+
+    fk_ms, fk_bytes = (ctypes.c_double * 2)(), (ctypes.c_double * 2)()
+    fk_ok = lib.ef_fine_kernel_profile(s.ctx, 50, fk_ms, fk_bytes, stream.cuda_stream) == _lib.EF_OK
 
     # comparison arm: block-Jacobi PCG on the same load step
     s.linsolver.method = "pcg"
@@ -459,9 +460,21 @@ def run_ours(a):
             torch.cuda.synchronize()
 
     peaks, peak_kind = measured_peaks()
-    sb = spmv_bytes(info)
-    sp_avg = sp_ms / sp_n if sp_n else None
-    achieved = sb / (sp_avg * 1e-3) / 1e9 if sp_avg else None
+    full = a.nx * a.ny * a.nz == 160000
+    roofline = None
+    if fk_ok:
+        sw_gbs = fk_bytes[0] / (fk_ms[0] * 1e-3) / 1e9
+        pr_gbs = fk_bytes[1] / (fk_ms[1] * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "sell_level3_bf16_kernel (fine multigrid sweep / residual from the "
+                                              "sliced-ELL BF16 blocks; two launches per FGMRES iteration)",
+                    "achieved": sw_gbs, "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
+                    "frac": sw_gbs / peaks["hbm_gbs"], "traffic": SWEEP_TRAFFIC_BYTES if full else None,
+                    "traffic_source": "ncu (dram__bytes_read.sum + dram__bytes_write.sum per launch) of bench.py "
+                                      "--profile --method fgmres",
+                    "bytes_per_launch": fk_bytes[0], "avg_launch_ms": fk_ms[0], "timing": "CUDA events, 50 launches",
+                    "second": {"kernel": "sell_spmv3_kernel (FGMRES product K z, FP32 sliced-ELL)", "achieved": pr_gbs,
+                               "frac": pr_gbs / peaks["hbm_gbs"], "bytes_per_launch": fk_bytes[1],
+                               "avg_launch_ms": fk_ms[1], "traffic": PRODUCT_TRAFFIC_BYTES if full else None}}  # fmt: skip
     pcg_bpi = pcg_bytes_per_iteration(info)
     pcg_gbs = pcg_bpi * pcg_it / (pcg_kms * 1e-3) / 1e9 if pcg_kms > 0 else None
     cpu = None
@@ -513,13 +526,7 @@ def run_ours(a):
         "history_s": history_s,
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.nDof, "d2h_bytes_per_step": 2 * 8 * s.nDof},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "spmv_f32_kernel (fine-level BSR SpMV of FGMRES)", "achieved": achieved,
-                     "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"] if achieved else None,
-                     "traffic": SPMV_TRAFFIC_BYTES if a.nx * a.ny * a.nz == 160000 else None,
-                     "traffic_source": "ncu launch list of bench.py --profile --method fgmres (dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum of spmv_f32_kernel, per launch)",
-                     "bytes_per_launch": sb, "launches": sp_n, "avg_launch_ms": sp_avg},
+        "roofline": roofline,
         "clocks": clk,
         "cpu_baseline": cpu,
         "parity": parity,

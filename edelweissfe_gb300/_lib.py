@@ -128,6 +128,7 @@ SIGNATURES = {
     "ef_kernel_launches": (c_i64, []),
     "ef_fgmres_set_preconditioner": (c_int, [c_vp, c_int]),
     "ef_fgmres_set_reuse": (c_int, [c_vp, c_int]),
+    "ef_fine_kernel_profile": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp]),
     "ef_set_group_props": (c_int, [c_vp, c_int, c_vp, c_int, c_int, c_vp]),
     "ef_set_group_cutback": (c_int, [c_vp, c_int, c_dbl]),
     "ef_set_ties": (c_int, [c_vp, c_vp, c_vp, c_vp, c_i64]),

@@ -411,6 +411,45 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     return result;
 }
 
+ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes, void* stream) {
+    EF_REQUIRE_FINALIZED(c);
+    if (reps < 1 || !ms || !bytes) return EF_ERR_ARG;
+    if (c->sellMode != 1 || !c->dSellV8 || !c->vcIn || !c->vcOut || !c->fineX || !c->fineT || !c->fgZ) {
+        ef_set_error("ef_fine_kernel_profile: needs an FGMRES solve with the sliced-ELL fine level first");
+        return EF_ERR_STATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nN = (int)c->nNodes;
+    const float omega = c->levelOmega.empty() ? c->amgOmega : c->levelOmega[0];
+    auto sweep = [&]() {
+        return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
+                                          c->dSellV1, c->fineX, c->vcIn, c->dMask, c->fineT, (const float*)c->dBinv,
+                                          omega, s);
+    };
+    auto product = [&]() {
+        return ef_launch_sell_spmv3(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV9, c->vcOut,
+                                    c->dMask, c->fineT, c->fgZ, s);
+    };
+    for (int k = 0; k < 2; ++k) {
+        auto run = [&]() { return k == 0 ? sweep() : product(); };
+        EF_CHECK(run());  // warm-up
+        EF_CUDA(cudaEventRecord(c->ev[0], s));
+        for (int i = 0; i < reps; ++i) EF_CHECK(run());
+        EF_CUDA(cudaEventRecord(c->ev[1], s));
+        EF_CUDA(cudaEventSynchronize(c->ev[1]));
+        float t = 0.f;
+        EF_CUDA(cudaEventElapsedTime(&t, c->ev[0], c->ev[1]));
+        ms[k] = (double)t / reps;
+    }
+    // algorithmic DRAM bytes per launch: the real blocks (values and column indices; the slices'
+    // padding is layout overhead, 3.9 % on the structured box) and the per-row vectors
+    const double nb = (double)c->nBlocks, nn = (double)nN, ns = (double)c->sellSlices;
+    bytes[0] = nb * (16 + 2 + 4) + nn * (3 * 4 /*x*/ + 3 * 4 /*r*/ + 9 * 4 /*D^-1*/ + 3 /*mask*/ + 3 * 4 /*out*/) +
+               (ns + 1) * 8;
+    bytes[1] = nb * (9 * 4 + 4) + nn * (3 * 4 /*x*/ + 3 /*mask*/ + 3 * 4 /*y*/ + 3 * 4 /*copy*/) + (ns + 1) * 8;
+    return EF_OK;
+}
+
 ef_status ef_fgmres_set_reuse(ef_ctx* c, int maxReuse) {
     EF_REQUIRE_FINALIZED(c);
     if (maxReuse < 0) {
