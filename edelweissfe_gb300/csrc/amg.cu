@@ -183,6 +183,50 @@ __global__ void sa_prolong_kernel(int nF, const int32_t* __restrict__ pRowPtr, c
     sa_prolong_row<BF>(m, pRowPtr, pCol, Pv, xc, mask, x, alpha);
 }
 
+// two-stage transfers (amg_sa_body.h): one P block per thread, then sums per coarse node (a warp,
+// lanes over its transpose list, fixed shuffle tree) or per finer row (a thread)
+template <int BF>
+__global__ void sa_restrict_contrib_kernel(int64_t nP, const int32_t* __restrict__ pRow, const float* __restrict__ Pv,
+                                           const float* __restrict__ t, float* __restrict__ c) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nP) sa_restrict_contrib<BF>(b, pRow, Pv, t, c);
+}
+
+__global__ void sa_restrict_sum_kernel(int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ tIdx,
+                                       const float* __restrict__ c, const uint8_t* __restrict__ coarseDead,
+                                       float* __restrict__ rc) {
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= nC) return;
+    float a[BC];
+    sa_restrict_sum_partial(I, lane, 32, tPtr, tIdx, c, a);
+#pragma unroll
+    for (int j = 0; j < BC; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+    if (lane < BC) {
+        float v = a[0];
+#pragma unroll
+        for (int j = 1; j < BC; ++j)
+            if (lane == j) v = a[j];
+        rc[BC * I + lane] = coarseDead[BC * I + lane] ? 0.f : v;
+    }
+}
+
+template <int BF>
+__global__ void sa_prolong_contrib_kernel(int64_t nP, const int32_t* __restrict__ pCol, const float* __restrict__ Pv,
+                                          const float* __restrict__ xc, float* __restrict__ q) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nP) sa_prolong_contrib<BF>(b, pCol, Pv, xc, q);
+}
+
+template <int BF>
+__global__ void sa_prolong_apply_kernel(int nF, const int32_t* __restrict__ pRowPtr, const float* __restrict__ q,
+                                        const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nF) sa_prolong_apply<BF>(m, pRowPtr, q, mask, x, alpha);
+}
+
 // *wP = 4 / (3 lambda) with lambda = sqrt(*n2), the prolongator damping from the power iteration
 __global__ void sa_damping_kernel(const double* __restrict__ n2, float* __restrict__ wP) {
     const double v = *n2;
@@ -992,6 +1036,39 @@ ef_status ef_launch_sa_restrict(int bf, int nC, const int32_t* tPtr, const int32
     else
         sa_restrict_kernel<6><<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, tPtr, tIdx, pRow, Pv, t,
                                                                                       coarseDead, rc);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// two-stage restriction rc = P^T t through c [nP][6] and prolongation x += alpha P xc through
+// c [nP][bf] (the same scratch of the level)
+ef_status ef_launch_sa_restrict2(int bf, int nC, int64_t nP, const int32_t* tPtr, const int32_t* tIdx,
+                                 const int32_t* pRow, const float* Pv, const float* t, const uint8_t* coarseDead,
+                                 float* c, float* rc, cudaStream_t s) {
+    if (nP > 0) {
+        if (bf == 3)
+            sa_restrict_contrib_kernel<3><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pRow, Pv, t, c);
+        else
+            sa_restrict_contrib_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pRow, Pv, t, c);
+    }
+    sa_restrict_sum_kernel<<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, tPtr, tIdx, c, coarseDead, rc);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_prolong2(int bf, int nF, int64_t nP, const int32_t* pRowPtr, const int32_t* pCol,
+                                const float* Pv, const float* xc, const uint8_t* mask, float* c, float* x, float alpha,
+                                cudaStream_t s) {
+    if (nP > 0) {
+        if (bf == 3)
+            sa_prolong_contrib_kernel<3><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pCol, Pv, xc, c);
+        else
+            sa_prolong_contrib_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pCol, Pv, xc, c);
+    }
+    if (bf == 3)
+        sa_prolong_apply_kernel<3><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, c, mask, x, alpha);
+    else
+        sa_prolong_apply_kernel<6><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, c, mask, x, alpha);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -246,6 +246,76 @@ EF_SA_HD void sa_prolong_row(int m, const int32_t* __restrict__ pRowPtr, const i
         if (!(mask && mask[BF * (int64_t)m + i])) x[BF * (int64_t)m + i] += alpha * s[i];
 }
 
+// Two-stage forms of the restriction and the prolongation, coalesced over the P blocks: stage 1
+// maps one P block to one thread -- consecutive threads read consecutive blocks -- and stores the
+// block's product (6 values for the restriction, BF for the prolongation); stage 2 sums the
+// products of each coarse node over its transpose list (in the list's fixed order) or of each
+// finer row over its contiguous blocks.
+
+// restriction, stage 1: c[b][j] = sum_i P_b[i][j] t[row(b)][i]
+template <int BF>
+EF_SA_HD void sa_restrict_contrib(int64_t b, const int32_t* __restrict__ pRow, const float* __restrict__ Pv,
+                                  const float* __restrict__ t, float* __restrict__ c) {
+    const int64_t m = pRow[b];
+    const float* P = Pv + b * BF * BC;
+    float ti[BF];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) ti[i] = t[BF * m + i];
+    EF_SA_UNROLL
+    for (int j = 0; j < BC; ++j) {
+        float a = 0.f;
+        EF_SA_UNROLL
+        for (int i = 0; i < BF; ++i) a += P[i * BC + j] * ti[i];
+        c[b * BC + j] = a;
+    }
+}
+
+// restriction, stage 2: one lane's share of coarse node I, a[j] = sum of c[tIdx[k]][j] over
+// k = tPtr[I] + lane, + nLanes, ...
+EF_SA_HD void sa_restrict_sum_partial(int I, int lane, int nLanes, const int32_t* __restrict__ tPtr,
+                                      const int32_t* __restrict__ tIdx, const float* __restrict__ c, float a[BC]) {
+    EF_SA_UNROLL
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    for (int k = tPtr[I] + lane; k < tPtr[I + 1]; k += nLanes) {
+        const float* q = c + (int64_t)tIdx[k] * BC;
+        EF_SA_UNROLL
+        for (int j = 0; j < BC; ++j) a[j] += q[j];
+    }
+}
+
+// prolongation, stage 1: q[b][i] = sum_j P_b[i][j] xc[col(b)][j]
+template <int BF>
+EF_SA_HD void sa_prolong_contrib(int64_t b, const int32_t* __restrict__ pCol, const float* __restrict__ Pv,
+                                 const float* __restrict__ xc, float* __restrict__ q) {
+    const float* P = Pv + b * BF * BC;
+    const float* cv = xc + BC * (int64_t)pCol[b];
+    float x[BC];
+    EF_SA_UNROLL
+    for (int j = 0; j < BC; ++j) x[j] = cv[j];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) {
+        float s = 0.f;
+        EF_SA_UNROLL
+        for (int j = 0; j < BC; ++j) s += P[i * BC + j] * x[j];
+        q[b * BF + i] = s;
+    }
+}
+
+// prolongation, stage 2: x[m] += alpha sum over row m's blocks of q[b] on the free DOFs
+template <int BF>
+EF_SA_HD void sa_prolong_apply(int m, const int32_t* __restrict__ pRowPtr, const float* __restrict__ q,
+                               const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
+    float s[BF];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) s[i] = 0.f;
+    for (int b = pRowPtr[m]; b < pRowPtr[m + 1]; ++b)
+        EF_SA_UNROLL
+        for (int i = 0; i < BF; ++i) s[i] += q[(int64_t)b * BF + i];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i)
+        if (!(mask && mask[BF * (int64_t)m + i])) x[BF * (int64_t)m + i] += alpha * s[i];
+}
+
 }  // namespace ef
 
 #undef EF_SA_HD

@@ -62,6 +62,12 @@ ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int3
 ef_status ef_launch_sa_restrict(int bf, int nC, const int32_t* tPtr, const int32_t* tIdx, const int32_t* pRow,
                                 const float* Pv, const float* t, const uint8_t* coarseDead, float* rc,
                                 cudaStream_t s);
+ef_status ef_launch_sa_restrict2(int bf, int nC, int64_t nP, const int32_t* tPtr, const int32_t* tIdx,
+                                 const int32_t* pRow, const float* Pv, const float* t, const uint8_t* coarseDead,
+                                 float* c, float* rc, cudaStream_t s);
+ef_status ef_launch_sa_prolong2(int bf, int nF, int64_t nP, const int32_t* pRowPtr, const int32_t* pCol,
+                                const float* Pv, const float* xc, const uint8_t* mask, float* c, float* x, float alpha,
+                                cudaStream_t s);
 ef_status ef_launch_sa_prolong(int bf, int nF, const int32_t* pRowPtr, const int32_t* pCol, const float* Pv,
                                const float* xc, const uint8_t* mask, float* x, float alpha, cudaStream_t s);
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
@@ -263,6 +269,7 @@ struct AmgLevel {
     int32_t *saCP = nullptr, *saCAP = nullptr;
     int64_t *saPSeg = nullptr, *saApSeg = nullptr, *saCSeg = nullptr;
     float *saPv = nullptr, *saAPv = nullptr, *saW = nullptr;
+    float* saC = nullptr;  // [saNP][6] block products of the two-stage restriction / prolongation
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
 
@@ -273,7 +280,7 @@ struct AmgLevel {
                         (void*)x, (void*)x2, (void*)valsH, (void*)r, (void*)t, (void*)saPRowPtr, (void*)saPCol,
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
-                        (void*)saPv, (void*)saAPv, (void*)saW})
+                        (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC})
             if (p) cudaFree(p);
     }
 };
@@ -390,6 +397,7 @@ struct ef_ctx {
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
     bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)
+    bool saTwoStage = true;                 // SA transfers as block products + sums (EF_SA_TWOSTAGE=0: one stage)
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
     int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel

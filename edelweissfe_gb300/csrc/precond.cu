@@ -154,6 +154,7 @@ ef_status sell_refresh(ef_ctx* c, cudaStream_t s) {
 ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
     if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
+    if (const char* e = getenv("EF_SA_TWOSTAGE")) c->saTwoStage = atoi(e) != 0;
     // smoothed prolongators: one sweep before and after, V-cycle (the fastest cfg 2 load step of
     // 1/1, 2/2 x V, W on level 1); plain aggregation: two sweeps and a W-cycle on level 1
     if (c->amgSmoothed) {
@@ -317,7 +318,8 @@ ef_status amg_build(ef_ctx* c) {
             L.saPv = dalloc<float>((size_t)std::max<int64_t>(1, L.saNP) * bfL * BCo, &st);
             L.saAPv = dalloc<float>((size_t)std::max<int64_t>(1, L.saNAP) * bfL * BCo, &st);
             L.saW = dalloc<float>(1, &st);
-            if (!L.saPv || !L.saAPv || !L.saW) return st;
+            L.saC = dalloc<float>((size_t)std::max<int64_t>(1, L.saNP) * BCo, &st);
+            if (!L.saPv || !L.saAPv || !L.saW || !L.saC) return st;
         }
         L.vals = dalloc<float>((size_t)L.nBlocks * BCo * BCo, &st);
         L.binv = dalloc<float>((size_t)nC * BCo * BCo, &st);
@@ -843,12 +845,18 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
             EF_CHECK(ef_launch_coarse_cycle(c->dCoarseOps, c->nCoarseOps, s));
             continue;
         }
-        if (c->amgSmoothed)
+        if (c->amgSmoothed && c->saTwoStage)
+            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t, Cn.dead,
+                                            Cn.saC, Cn.r, s));
+        else if (c->amgSmoothed)
             EF_CHECK(ef_launch_sa_restrict(bs, Cn.nN, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t, Cn.dead, Cn.r, s));
         else
             EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        if (c->amgSmoothed)
+        if (c->amgSmoothed && c->saTwoStage)
+            EF_CHECK(ef_launch_sa_prolong2(bs, nN, Cn.saNP, Cn.saPRowPtr, Cn.saPCol, Cn.saPv, Cn.x, mask, Cn.saC, cur,
+                                           c->amgAlpha, s));
+        else if (c->amgSmoothed)
             EF_CHECK(ef_launch_sa_prolong(bs, nN, Cn.saPRowPtr, Cn.saPCol, Cn.saPv, Cn.x, mask, cur, c->amgAlpha, s));
         else
             EF_CHECK(ef_launch_prolong(bs, nN, Cn.agg, Cn.offs, Cn.x, mask, cur, s, c->amgAlpha));

@@ -219,6 +219,20 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (int m = 0; m < nF; ++m)
         ef::sa_prolong_row<BF>(m, S.pRowPtr.data(), S.pCol.data(), Pv.data(), xcf.data(), fm, xf.data(), alpha);
+    // the two-stage forms: block products, then per coarse node / per finer row sums
+    std::vector<float> cb((size_t)nP * BC), rc2(nc), xf2(x0.begin(), x0.end());
+    for (int64_t b = 0; b < nP; ++b) ef::sa_restrict_contrib<BF>(b, S.pRow.data(), Pv.data(), tf.data(), cb.data());
+    for (int I = 0; I < nC; ++I) {
+        double sum[BC] = {};
+        for (int lane = 0; lane < 32; ++lane) {
+            float a[BC];
+            ef::sa_restrict_sum_partial(I, lane, 32, S.tPtr.data(), S.tIdx.data(), cb.data(), a);
+            for (int j = 0; j < BC; ++j) sum[j] += a[j];
+        }
+        for (int j = 0; j < BC; ++j) rc2[BC * I + j] = dead[BC * I + j] ? 0.f : (float)sum[j];
+    }
+    for (int64_t b = 0; b < nP; ++b) ef::sa_prolong_contrib<BF>(b, S.pCol.data(), Pv.data(), xcf.data(), cb.data());
+    for (int m = 0; m < nF; ++m) ef::sa_prolong_apply<BF>(m, S.pRowPtr.data(), cb.data(), fm, xf2.data(), alpha);
     // ---- compare (FP32 arithmetic against FP64: relative to each product's largest entry) ----
     double eP = 0, eAP = 0, eC = 0, eR = 0, eX = 0, oP = 0, oAP = 0, oC = 0;
     std::vector<uint8_t> seenP((size_t)n * nc, 0), seenAP((size_t)n * nc, 0), seenC((size_t)nc * nc, 0);
@@ -252,12 +266,16 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (size_t i = 0; i < Acd.size(); ++i)
         if (!seenC[i]) oC = std::fmax(oC, std::fabs(Acd[i]));
+    double eR2 = 0, eX2 = 0;
     for (int i = 0; i < nc; ++i) eR = std::fmax(eR, std::fabs(rc[i] - rcd[i]));
     for (int i = 0; i < n; ++i) eX = std::fmax(eX, std::fabs(xf[i] - xd[i]));
+    for (int i = 0; i < nc; ++i) eR2 = std::fmax(eR2, std::fabs(rc2[i] - rcd[i]));
+    for (int i = 0; i < n; ++i) eX2 = std::fmax(eX2, std::fabs(xf2[i] - xd[i]));
     const double sP = max_abs(Ps), sAP = max_abs(APd), sC = max_abs(Acd), sR = max_abs(rcd), sX = max_abs(xd);
     const double tol = 2e-6;
     int fails = 0;
     fails += !(eP <= tol * sP) + !(eAP <= tol * sAP) + !(eC <= tol * sC) + !(eR <= tol * sR) + !(eX <= tol * sX);
+    fails += !(eR2 <= tol * sR) + !(eX2 <= tol * sX);
     fails += (oP != 0.0) + (oAP != 0.0) + (oC != 0.0);
     // masked finer rows: P exactly zero
     for (int m = 0; m < nF; ++m)
@@ -267,9 +285,9 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
                 for (int j = 0; j < BC; ++j) fails += Pv[(size_t)b * BF * BC + a * BC + j] != 0.f;
         }
     std::printf("%s: P %lld blocks, AP %lld, coarse %lld; rel diff P %.1e AP %.1e Ac %.1e restrict %.1e "
-                "prolong %.1e; outside patterns %.1e %.1e %.1e; failures %d\n",
+                "prolong %.1e (two-stage %.1e %.1e); outside patterns %.1e %.1e %.1e; failures %d\n",
                 name, (long long)nP, (long long)nAP, (long long)nCb, eP / sP, eAP / sAP, eC / sC, eR / sR, eX / sX,
-                oP, oAP, oC, fails);
+                eR2 / sR, eX2 / sX, oP, oAP, oC, fails);
     return fails;
 }
 
