@@ -24,9 +24,8 @@
 
 namespace ef {
 
-constexpr int kSellThreads = 128;  // four warps per CTA
-constexpr int kSellSplit = 2;      // warps per slice: each takes half of the slice's entries
-constexpr int kSellSlicesPerCta = kSellThreads / (32 * kSellSplit);
+constexpr int kSellThreads = 128;  // four slices per CTA
+constexpr int kSellSlicesPerCta = kSellThreads / 32;
 
 __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src, const float* __restrict__ bsr,
                                     float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1) {
@@ -53,44 +52,6 @@ __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src,
     }
 }
 
-// The slice and entry range of this warp: warp h of a slice takes entries [j0, j1) of its width,
-// h = 0 the first half (rounded up).  Returns false past the last slice.
-struct SellPart {
-    int sl, h, lane, j0, j1;
-    int64_t e0;
-};
-__device__ __forceinline__ bool sell_part(int nSlices, const int64_t* __restrict__ off, SellPart& p) {
-    p.lane = threadIdx.x & 31;
-    const int wi = threadIdx.x >> 5;
-    p.sl = blockIdx.x * kSellSlicesPerCta + wi / kSellSplit;
-    p.h = wi % kSellSplit;
-    if (p.sl >= nSlices) return false;
-    p.e0 = off[p.sl];
-    const int w = (int)((off[p.sl + 1] - p.e0) >> 5);
-    const int half = (w + 1) >> 1;
-    p.j0 = p.h ? half : 0;
-    p.j1 = p.h ? w : half;
-    return true;
-}
-
-// the second warp's partial sums of a slice go through shared memory to the first one, which adds
-// them after its own (a fixed order: deterministic)
-__device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, float& y0, float& y1, float& y2) {
-    __shared__ float part[kSellSlicesPerCta][3][32];
-    const int ls = (threadIdx.x >> 5) / kSellSplit;
-    if (active && p.h == 1) {
-        part[ls][0][p.lane] = y0;
-        part[ls][1][p.lane] = y1;
-        part[ls][2][p.lane] = y2;
-    }
-    __syncthreads();
-    if (!active || p.h != 0) return false;
-    y0 += part[ls][0][p.lane];
-    y1 += part[ls][1][p.lane];
-    y2 += part[ls][2][p.lane];
-    return true;
-}
-
 // y = K x on the free DOFs (0 on masked rows); COPY: xcopy = x as well
 template <bool COPY>
 __global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nSlices, const int64_t* __restrict__ off,
@@ -100,27 +61,27 @@ __global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nS
                                                                   const float* __restrict__ x,
                                                                   const uint8_t* __restrict__ mask,
                                                                   float* __restrict__ y, float* __restrict__ xcopy) {
-    SellPart p;
-    const bool active = sell_part(nSlices, off, p);
+    const int lane = threadIdx.x & 31;
+    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
+    if (sl >= nSlices) return;
+    const int64_t e0 = off[sl];
+    const int w = (int)((off[sl + 1] - e0) >> 5);
+    const int32_t* cs = col + e0 + lane;
+    const float* vs = v9 + 9 * e0 + lane;
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-    if (active) {
-        const int32_t* cs = col + p.e0 + p.lane;
-        const float* vs = v9 + 9 * p.e0 + p.lane;
 #pragma unroll 3
-        for (int j = p.j0; j < p.j1; ++j) {
-            const int c3 = 3 * __ldcs(cs + 32 * j);
-            const float* vv = vs + 288 * j;
-            const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
-            const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
-            const float a6 = __ldcs(vv + 192), a7 = __ldcs(vv + 224), a8 = __ldcs(vv + 256);
-            const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
-            y0 += a0 * x0 + a1 * x1 + a2 * x2;
-            y1 += a3 * x0 + a4 * x1 + a5 * x2;
-            y2 += a6 * x0 + a7 * x1 + a8 * x2;
-        }
+    for (int j = 0; j < w; ++j) {
+        const int c3 = 3 * __ldcs(cs + 32 * j);
+        const float* vv = vs + 288 * j;
+        const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
+        const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
+        const float a6 = __ldcs(vv + 192), a7 = __ldcs(vv + 224), a8 = __ldcs(vv + 256);
+        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+        y0 += a0 * x0 + a1 * x1 + a2 * x2;
+        y1 += a3 * x0 + a4 * x1 + a5 * x2;
+        y2 += a6 * x0 + a7 * x1 + a8 * x2;
     }
-    if (!sell_combine(p, active, y0, y1, y2)) return;
-    const int r = p.sl * 32 + p.lane;
+    const int r = sl * 32 + lane;
     if (r >= nN) return;
     const int m = perm ? perm[r] : r;
     const int d = 3 * m;
@@ -141,29 +102,29 @@ __global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
     const float* __restrict__ binv, float omega) {
-    SellPart p;
-    const bool active = sell_part(nSlices, off, p);
+    const int lane = threadIdx.x & 31;
+    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
+    if (sl >= nSlices) return;
+    const int64_t e0 = off[sl];
+    const int w = (int)((off[sl + 1] - e0) >> 5);
+    const int32_t* cs = col + e0 + lane;
+    const uint4* qs = v8 + e0 + lane;
+    const __nv_bfloat16* ws = v1 + e0 + lane;
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-    if (active) {
-        const int32_t* cs = col + p.e0 + p.lane;
-        const uint4* qs = v8 + p.e0 + p.lane;
-        const __nv_bfloat16* ws = v1 + p.e0 + p.lane;
 #pragma unroll 4
-        for (int j = p.j0; j < p.j1; ++j) {
-            const int c3 = 3 * __ldcs(cs + 32 * j);
-            const uint4 q = __ldcs(qs + 32 * j);
-            const float w8 = __bfloat162float(ws[32 * j]);
-            const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
-            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
-            const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
-            const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
-            y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
-            y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
-            y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
-        }
+    for (int j = 0; j < w; ++j) {
+        const int c3 = 3 * __ldcs(cs + 32 * j);
+        const uint4 q = __ldcs(qs + 32 * j);
+        const float w8 = __bfloat162float(ws[32 * j]);
+        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+        const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
+        const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
+        y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
+        y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
+        y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
     }
-    if (!sell_combine(p, active, y0, y1, y2)) return;
-    const int rr = p.sl * 32 + p.lane;
+    const int rr = sl * 32 + lane;
     if (rr >= nN) return;
     const int m = perm ? perm[rr] : rr;
     const int d = 3 * m;

@@ -114,7 +114,9 @@ class LinSolverOptions:
     restart: int = 40
     maxRefine: int = 30
     profile: bool = False
-    precondReuse: int = 0  # FGMRES: Newton systems of an increment that reuse its first one's coarse multigrid levels
+    # FGMRES: Newton systems of an increment that reuse the coarse multigrid levels built for the one
+    # before (1: rebuilt every other system; measured best on the 160k-element J2 box)
+    precondReuse: int = 1
 
 
 class NISTGPU:
