@@ -230,19 +230,20 @@ def assembly_bytes(info, nEl, fp32=True):
     return elem, cond, scatter
 
 
-def learned_seeded_family(dims=(40, 16, 16), train=(0, 1, 2, 3), test=(4, 5), increments=14):
+def learned_seeded_family(train=(0, 1, 2, 3), test=(4, 5), increments=14):
     """The learned correction on the seeded J2 family (per seed sigma_y ~ U[150,350],
     H ~ U[200,2000], nu ~ U[0.2,0.4]): trained on the Newton-iteration pairs of the `train` seeds'
     load histories (one context, one box per seed), then the load history of the unseen `test`
-    seeds with and without it, over the block-Jacobi and the multigrid base."""
+    seeds with and without it, over the block-Jacobi base (16x8x8 boxes: FGMRES + block Jacobi
+    stalls on the plastic systems of larger boxes) and over the multigrid base (40x16x16 boxes)."""
     from edelweissfe_gb300.learned import evaluate_on_seeds, train_across_seeds
 
-    out = {"box": "x".join(map(str, dims)), "increments": increments}
-    for base in ("jacobi", "multigrid"):
+    out = {"increments": increments}
+    for base, dims in (("jacobi", (16, 8, 8)), ("multigrid", (40, 16, 16))):
         try:
             params, scales, rec = train_across_seeds(list(train), dims, increments, base=base, epochs=100)
             ev = evaluate_on_seeds(list(test), dims, increments, params, scales, base=base)
-            out[base] = {"train": rec, "unseen": ev}
+            out[base] = {"box": "x".join(map(str, dims)), "train": rec, "unseen": ev}
         except Exception as ex:  # reported, not fatal to the bench
             out[base] = {"error": f"{type(ex).__name__}: {ex}"}
     return out

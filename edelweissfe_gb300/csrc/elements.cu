@@ -470,6 +470,120 @@ __global__ void __launch_bounds__(kBlock) small_strain_apply_kernel(int nEl, con
     }
 }
 
+// The same product with the contractions in double-float arithmetic on the FP32 pipe (the FP64
+// pipe of this GPU executes 2 lanes per SM and cycle): x split once into FP32 pairs, the
+// geometry read from the split cache, H = sum_a x_a (x) g_a and y_a = sum_q sigma_q . g_qa as
+// double-float sums (about 48 significant bits, as the element kernel's strain increment and
+// residual), the Gauss-point stress from the FP64 tangent in FP64.
+template <int NN, int NQ>
+struct ApplyDFShared {
+    static constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    static constexpr int EPB = kBlock / TPE;
+    float2 xv[EPB][NN * 3 + 1];
+    float2 g[EPB][NQ * NN * 3 + 1];
+    float2 sw[EPB][NQ * 6 + 1];
+};
+
+template <int NN, int NQ>
+__global__ void __launch_bounds__(kBlock) small_strain_apply_df_kernel(int nEl, const int32_t* __restrict__ nodeDof,
+                                                                       const float2* __restrict__ geoS,
+                                                                       const double* __restrict__ x,
+                                                                       const double* __restrict__ tang,
+                                                                       double* __restrict__ ye, int intConv) {
+    constexpr int TPE = (NQ <= 8) ? 8 : 32;
+    constexpr int EPB = kBlock / TPE;
+    constexpr int ND = 3 * NN;
+    constexpr int NG = 3 * NN + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ApplyDFShared<NN, NQ>& sh = *reinterpret_cast<ApplyDFShared<NN, NQ>*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int le = tid / TPE;
+    const int lane = tid % TPE;
+    const int e = blockIdx.x * EPB + le;
+    const bool valid = e < nEl;
+    if (valid) {
+        for (int a = lane; a < NN; a += TPE) {
+            const int d = nodeDof[(int64_t)e * NN + a];
+            sh.xv[le][3 * a + 0] = df_split_sel(x[d + 0], intConv);
+            sh.xv[le][3 * a + 1] = df_split_sel(x[d + 1], intConv);
+            sh.xv[le][3 * a + 2] = df_split_sel(x[d + 2], intConv);
+        }
+    }
+    __syncthreads();
+    if (valid && lane < NQ) {
+        const int q = lane;
+        const float2* gq = geoS + ((int64_t)e * NQ + q) * NG;
+        DF H[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) H[i][j] = DF{0.f, 0.f};
+#pragma unroll 4
+        for (int a = 0; a < NN; ++a) {
+            float2 ga[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ga[c] = gq[3 * a + c];
+                sh.g[le][(q * NN + a) * 3 + c] = ga[c];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float2 u = sh.xv[le][3 * a + i];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) df_fma(H[i][j], u, ga[j]);
+            }
+        }
+        const double ep[6] = {df_value_sel(H[0][0], intConv), df_value_sel(H[1][1], intConv),
+                              df_value_sel(H[2][2], intConv),
+                              df_value_sel(H[0][1], intConv) + df_value_sel(H[1][0], intConv),
+                              df_value_sel(H[0][2], intConv) + df_value_sel(H[2][0], intConv),
+                              df_value_sel(H[1][2], intConv) + df_value_sel(H[2][1], intConv)};
+        const int64_t nQPtot = (int64_t)nEl * NQ;
+        const int64_t qi = (int64_t)e * NQ + q;
+        const double lt = tang[qi], mt = tang[nQPtot + qi], c1 = tang[2 * nQPtot + qi];
+        const double tr = ep[0] + ep[1] + ep[2];
+        double ne = 0.0, n[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) n[i] = 0.0;
+        if (c1 != 0.0) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                n[i] = tang[(3 + i) * nQPtot + qi];
+                ne += n[i] * ep[i];
+            }
+        }
+        // sigma = (lt 1x1 + 2 mt I_s - c1 n x n) eps   (weights already in lt, mt, c1)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sh.sw[le][6 * q + i] = df_split_sel(lt * tr + 2.0 * mt * ep[i] - c1 * n[i] * ne, intConv);
+#pragma unroll
+        for (int i = 3; i < 6; ++i) sh.sw[le][6 * q + i] = df_split_sel(mt * ep[i] - c1 * n[i] * ne, intConv);
+    }
+    __syncthreads();
+    if (!valid) return;
+    for (int a = lane; a < NN; a += TPE) {
+        DF f0{0.f, 0.f}, f1{0.f, 0.f}, f2{0.f, 0.f};
+#pragma unroll 2
+        for (int q = 0; q < NQ; ++q) {
+            const float2* sq = &sh.sw[le][6 * q];
+            const float2* gg = &sh.g[le][(q * NN + a) * 3];
+            const float2 gx = gg[0], gy = gg[1], gz = gg[2];
+            df_fma(f0, sq[0], gx);
+            df_fma(f0, sq[3], gy);
+            df_fma(f0, sq[4], gz);
+            df_fma(f1, sq[3], gx);
+            df_fma(f1, sq[1], gy);
+            df_fma(f1, sq[5], gz);
+            df_fma(f2, sq[4], gx);
+            df_fma(f2, sq[5], gy);
+            df_fma(f2, sq[2], gz);
+        }
+        double* o = ye + (int64_t)e * ND + 3 * a;
+        o[0] = df_value_sel(f0, intConv);
+        o[1] = df_value_sel(f1, intConv);
+        o[2] = df_value_sel(f2, intConv);
+    }
+}
+
 // Consistent body force of a constant load vector (element.py:348-371): Pe[a,c] = load_c sum_q N_qa detJ_q w_q
 template <int NN, int NQ>
 __global__ void body_force_kernel(const ElemTables* __restrict__ T, int nEl, const double* __restrict__ geo,
@@ -539,6 +653,18 @@ static ef_status launch_apply(const Group& g, const double* x, const double* tan
     constexpr int EPB = ApplyShared<NN, NQ>::EPB;
     const int grid = (g.nEl + EPB - 1) / EPB;
     if (grid == 0) return EF_OK;
+    static const bool fp64 = [] {
+        const char* e = getenv("EF_APPLY_FP64");
+        return e && atoi(e) != 0;
+    }();
+    if (g.geoS && !fp64) {  // double-float contractions (default); EF_APPLY_FP64=1: the FP64 kernel
+        const size_t smemDF = sizeof(ApplyDFShared<NN, NQ>);
+        auto kd = small_strain_apply_df_kernel<NN, NQ>;
+        EF_CUDA(cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemDF));
+        kd<<<grid, kBlock, smemDF, ef::counted(s)>>>(g.nEl, g.nodeDof, g.geoS, x, tang, ye, g.intConv);
+        EF_CUDA(cudaGetLastError());
+        return EF_OK;
+    }
     const size_t smem = sizeof(ApplyShared<NN, NQ>);
     auto k = small_strain_apply_kernel<NN, NQ>;
     EF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

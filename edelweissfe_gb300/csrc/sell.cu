@@ -24,8 +24,12 @@
 
 namespace ef {
 
-constexpr int kSellThreads = 128;  // four slices per CTA
-constexpr int kSellSlicesPerCta = kSellThreads / 32;
+constexpr int kSellThreads = 128;  // four warps per CTA
+constexpr int kSellSlicesPerCta = kSellThreads / 32;  // the product: a warp per slice
+// the BF16 sweep: two warps per slice, each taking half of the slice's entries (measured faster
+// for the sweep, 28.4 -> 26.6 us at 160k hex8; slower for the FP32 product, 36 -> 45 us)
+constexpr int kSellSplit = 2;
+constexpr int kSellSplitSlicesPerCta = kSellThreads / (32 * kSellSplit);
 
 __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src, const float* __restrict__ bsr,
                                     float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1) {
@@ -95,6 +99,44 @@ __global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nS
     }
 }
 
+// The slice and entry range of this warp: warp h of a slice takes entries [j0, j1) of its width,
+// h = 0 the first half (rounded up).  Returns false past the last slice.
+struct SellPart {
+    int sl, h, lane, j0, j1;
+    int64_t e0;
+};
+__device__ __forceinline__ bool sell_part(int nSlices, const int64_t* __restrict__ off, SellPart& p) {
+    p.lane = threadIdx.x & 31;
+    const int wi = threadIdx.x >> 5;
+    p.sl = blockIdx.x * kSellSplitSlicesPerCta + wi / kSellSplit;
+    p.h = wi % kSellSplit;
+    if (p.sl >= nSlices) return false;
+    p.e0 = off[p.sl];
+    const int w = (int)((off[p.sl + 1] - p.e0) >> 5);
+    const int half = (w + 1) >> 1;
+    p.j0 = p.h ? half : 0;
+    p.j1 = p.h ? w : half;
+    return true;
+}
+
+// the second warp's partial sums of a slice go through shared memory to the first one, which adds
+// them after its own (a fixed order: deterministic)
+__device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, float& y0, float& y1, float& y2) {
+    __shared__ float part[kSellSplitSlicesPerCta][3][32];
+    const int ls = (threadIdx.x >> 5) / kSellSplit;
+    if (active && p.h == 1) {
+        part[ls][0][p.lane] = y0;
+        part[ls][1][p.lane] = y1;
+        part[ls][2][p.lane] = y2;
+    }
+    __syncthreads();
+    if (!active || p.h != 0) return false;
+    y0 += part[ls][0][p.lane];
+    y1 += part[ls][1][p.lane];
+    y2 += part[ls][2][p.lane];
+    return true;
+}
+
 // t = r - K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
 // t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy
 __global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
@@ -102,29 +144,29 @@ __global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
     const float* __restrict__ binv, float omega) {
-    const int lane = threadIdx.x & 31;
-    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
-    if (sl >= nSlices) return;
-    const int64_t e0 = off[sl];
-    const int w = (int)((off[sl + 1] - e0) >> 5);
-    const int32_t* cs = col + e0 + lane;
-    const uint4* qs = v8 + e0 + lane;
-    const __nv_bfloat16* ws = v1 + e0 + lane;
+    SellPart p;
+    const bool active = sell_part(nSlices, off, p);
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    if (active) {
+        const int32_t* cs = col + p.e0 + p.lane;
+        const uint4* qs = v8 + p.e0 + p.lane;
+        const __nv_bfloat16* ws = v1 + p.e0 + p.lane;
 #pragma unroll 4
-    for (int j = 0; j < w; ++j) {
-        const int c3 = 3 * __ldcs(cs + 32 * j);
-        const uint4 q = __ldcs(qs + 32 * j);
-        const float w8 = __bfloat162float(ws[32 * j]);
-        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
-        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
-        const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
-        const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
-        y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
-        y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
-        y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
+        for (int j = p.j0; j < p.j1; ++j) {
+            const int c3 = 3 * __ldcs(cs + 32 * j);
+            const uint4 q = __ldcs(qs + 32 * j);
+            const float w8 = __bfloat162float(ws[32 * j]);
+            const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+            const float2 a01 = __bfloat1622float2(h[0]), a23 = __bfloat1622float2(h[1]);
+            const float2 a45 = __bfloat1622float2(h[2]), a67 = __bfloat1622float2(h[3]);
+            y0 += a01.x * x0 + a01.y * x1 + a23.x * x2;
+            y1 += a23.y * x0 + a45.x * x1 + a45.y * x2;
+            y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
+        }
     }
-    const int rr = sl * 32 + lane;
+    if (!sell_combine(p, active, y0, y1, y2)) return;
+    const int rr = p.sl * 32 + p.lane;
     if (rr >= nN) return;
     const int m = perm ? perm[rr] : rr;
     const int d = 3 * m;
@@ -181,7 +223,8 @@ ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, co
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
-    sell_level3_bf16_kernel<<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(
+    sell_level3_bf16_kernel<<<(unsigned)((nSlices + kSellSplitSlicesPerCta - 1) / kSellSplitSlicesPerCta), kSellThreads,
+                              0, ef::counted(s)>>>(
         nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
