@@ -109,6 +109,9 @@ def _oracle_backed(cls, model, dirichlets, nodeforces, elements, elDofs, **kw):
     s.iterationHistory = []
     s.krylovIterations = []
     s.lastSolveInfo = None
+    from edelweissfe_gb300.solver import LinSolverOptions
+
+    s.linsolver = LinSolverOptions()
     for k, v in kw.items():
         setattr(s, k, v)
     return s
