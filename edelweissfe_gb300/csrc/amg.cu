@@ -188,6 +188,7 @@ __global__ void sa_prolong_kernel(int nF, const int32_t* __restrict__ pRowPtr, c
 template <int BF>
 __global__ void sa_restrict_contrib_kernel(int64_t nP, const int32_t* __restrict__ pRow, const float* __restrict__ Pv,
                                            const float* __restrict__ t, float* __restrict__ c) {
+    ef::dep_entry();
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nP) sa_restrict_contrib<BF>(b, pRow, Pv, t, c);
 }
@@ -195,6 +196,7 @@ __global__ void sa_restrict_contrib_kernel(int64_t nP, const int32_t* __restrict
 __global__ void sa_restrict_sum_kernel(int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ tIdx,
                                        const float* __restrict__ c, const uint8_t* __restrict__ coarseDead,
                                        float* __restrict__ rc) {
+    ef::dep_entry();
     const int lane = threadIdx.x & 31;
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (I >= nC) return;
@@ -216,6 +218,7 @@ __global__ void sa_restrict_sum_kernel(int nC, const int32_t* __restrict__ tPtr,
 template <int BF>
 __global__ void sa_prolong_contrib_kernel(int64_t nP, const int32_t* __restrict__ pCol, const float* __restrict__ Pv,
                                           const float* __restrict__ xc, float* __restrict__ q) {
+    ef::dep_entry();
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nP) sa_prolong_contrib<BF>(b, pCol, Pv, xc, q);
 }
@@ -223,8 +226,74 @@ __global__ void sa_prolong_contrib_kernel(int64_t nP, const int32_t* __restrict_
 template <int BF>
 __global__ void sa_prolong_apply_kernel(int nF, const int32_t* __restrict__ pRowPtr, const float* __restrict__ q,
                                         const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
+    ef::dep_entry();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m < nF) sa_prolong_apply<BF>(m, pRowPtr, q, mask, x, alpha);
+}
+
+// one-pass transfers (amg_sa_body.h)
+template <int BF>
+__global__ void sa_block_copy_kernel(int64_t nP, const int32_t* __restrict__ tIdx, const float* __restrict__ Pv,
+                                     float* __restrict__ dst) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nP) sa_block_copy<BF>(k, tIdx, Pv, dst);
+}
+
+// restriction: a CTA per coarse node, a thread per P block of its column (consecutive blocks of
+// the transpose-order copy), sums in a fixed order (each thread's blocks, a shuffle tree per warp,
+// the warps in order)
+constexpr int kSaRestrictThreads = 128;
+template <int BF>
+__global__ void __launch_bounds__(kSaRestrictThreads) sa_restrict_onepass_kernel(
+    int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ rowT,
+    const float* __restrict__ PT, const float* __restrict__ t, const uint8_t* __restrict__ coarseDead,
+    float* __restrict__ rc) {
+    ef::dep_entry();
+    __shared__ float red[kSaRestrictThreads / 32][BC];
+    const int I = blockIdx.x;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    float a[BC];
+    sa_restrict_onepass_partial<BF>(I, threadIdx.x, kSaRestrictThreads, tPtr, rowT, PT, t, a);
+#pragma unroll
+    for (int j = 0; j < BC; ++j) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+        if (lane == 0) red[wp][j] = a[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < BC) {
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < kSaRestrictThreads / 32; ++w) v += red[w][threadIdx.x];
+        rc[BC * I + threadIdx.x] = coarseDead[BC * I + threadIdx.x] ? 0.f : v;
+    }
+}
+
+// prolongation: a CTA per kSaProlongRows consecutive finer rows; a thread per P block of those
+// rows (row order) leaves the block's product in shared memory, then
+// thread r sums row r's products in block order.  cap >= the block count of every such group of
+// rows (checked on the host when the copy is built); a group above it is skipped.
+constexpr int kSaProlongThreads = 256;
+constexpr int kSaProlongRows = 64;
+template <int BF>
+__global__ void __launch_bounds__(kSaProlongThreads) sa_prolong_onepass_kernel(
+    int nF, int cap, const int32_t* __restrict__ pRowPtr, const int32_t* __restrict__ pCol,
+    const float* __restrict__ Pv, const float* __restrict__ xc, const uint8_t* __restrict__ mask,
+    float* __restrict__ x, float alpha) {
+    ef::dep_entry();
+    extern __shared__ float saQ[];  // [cap][BF]
+    const int r0 = blockIdx.x * kSaProlongRows;
+    const int r1 = min(r0 + kSaProlongRows, nF);
+    const int64_t b0 = pRowPtr[r0], b1 = pRowPtr[r1];
+    if (b1 - b0 > cap) return;  // the same for the whole CTA
+    for (int64_t b = b0 + threadIdx.x; b < b1; b += kSaProlongThreads) {
+        float v[BF];
+        sa_prolong_onepass_block<BF>(b, pCol, Pv, xc, v);
+#pragma unroll
+        for (int i = 0; i < BF; ++i) saQ[(b - b0) * BF + i] = v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < r1 - r0) sa_prolong_onepass_row<BF>(r0 + threadIdx.x, b0, pRowPtr, saQ, mask, x, alpha);
 }
 
 // *wP = 4 / (3 lambda) with lambda = sqrt(*n2), the prolongator damping from the power iteration
@@ -297,6 +366,7 @@ __device__ __forceinline__ void bj_row(int m, const float* __restrict__ binv, co
 template <int BS>
 __global__ void bj_apply_kernel(int nN, const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega,
                                 const float* __restrict__ r, float* __restrict__ x, int accumulate) {
+    ef::dep_entry();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nN) return;
     bj_row<BS, false>(m, binv, mask, omega, r, x, accumulate);
@@ -330,6 +400,7 @@ __global__ void __launch_bounds__(256) level_residual_kernel(int nN, const int32
                                                               const float* __restrict__ x, const float* __restrict__ r,
                                                               const uint8_t* __restrict__ mask, float* __restrict__ t,
                                                               const float* __restrict__ binv, float omega) {
+    ef::dep_entry();
     const int lane = threadIdx.x & 7;
     const int m0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
     const int m = m0 < nN ? m0 : nN - 1;
@@ -463,6 +534,7 @@ __global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int3
                                                                const uint8_t* __restrict__ mask, float* __restrict__ t,
                                                                const float* __restrict__ binv, float omega,
                                                                const uint32_t* __restrict__ valsH) {
+    ef::dep_entry();
     const int lane = threadIdx.x & 31;
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (m >= nN) return;
@@ -641,6 +713,7 @@ __device__ __forceinline__ void coarsest_row(int i, int lane, int n, const float
 
 __global__ void coarsest_apply_kernel(int n, const float* __restrict__ inv, const float* __restrict__ r,
                                       const uint8_t* __restrict__ dead, float* __restrict__ x) {
+    ef::dep_entry();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n) return;
     coarsest_row<false>(i, threadIdx.x & 31, n, inv, r, dead, x);
@@ -971,9 +1044,9 @@ ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals,
 ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
                              float* x, int accumulate, cudaStream_t s) {
     if (bs == 3)
-        bj_apply_kernel<3><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, omega, r, x, accumulate);
+        EF_CUDA(ef::launch_dep(bj_apply_kernel<3>, nb_(nN, 256), 256, 0, s, nN, binv, mask, omega, r, x, accumulate));
     else
-        bj_apply_kernel<6><<<nb_(nN, 256), 256, 0, ef::counted(s)>>>(nN, binv, mask, omega, r, x, accumulate);
+        EF_CUDA(ef::launch_dep(bj_apply_kernel<6>, nb_(nN, 256), 256, 0, s, nN, binv, mask, omega, r, x, accumulate));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -983,11 +1056,11 @@ ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const 
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
                                    const float* binv, float omega, const void* valsH) {
     if (bs == 3)
-        level_residual_kernel<3><<<nb_((int64_t)nN * 8, 256), 256, 0, ef::counted(s)>>>(nN, rowPtr, colIdx, vals, x, r,
-                                                                                        mask, t, binv, omega);
+        EF_CUDA(ef::launch_dep(level_residual_kernel<3>, nb_((int64_t)nN * 8, 256), 256, 0, s, nN, rowPtr, colIdx, vals,
+                x, r, mask, t, binv, omega));
     else
-        level_residual6_kernel<<<nb_((int64_t)nN * 32, 256), 256, 0, ef::counted(s)>>>(
-            nN, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, (const uint32_t*)valsH);
+        EF_CUDA(ef::launch_dep(level_residual6_kernel, nb_((int64_t)nN * 32, 256), 256, 0, s, nN, rowPtr, colIdx, vals,
+                x, r, mask, t, binv, omega, (const uint32_t*)valsH));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -1047,11 +1120,12 @@ ef_status ef_launch_sa_restrict2(int bf, int nC, int64_t nP, const int32_t* tPtr
                                  float* c, float* rc, cudaStream_t s) {
     if (nP > 0) {
         if (bf == 3)
-            sa_restrict_contrib_kernel<3><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pRow, Pv, t, c);
+            EF_CUDA(ef::launch_dep(sa_restrict_contrib_kernel<3>, nb_(nP, 256), 256, 0, s, nP, pRow, Pv, t, c));
         else
-            sa_restrict_contrib_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pRow, Pv, t, c);
+            EF_CUDA(ef::launch_dep(sa_restrict_contrib_kernel<6>, nb_(nP, 256), 256, 0, s, nP, pRow, Pv, t, c));
     }
-    sa_restrict_sum_kernel<<<nb_((int64_t)nC * 32, 256), 256, 0, ef::counted(s)>>>(nC, tPtr, tIdx, c, coarseDead, rc);
+    EF_CUDA(ef::launch_dep(sa_restrict_sum_kernel, nb_((int64_t)nC * 32, 256), 256, 0, s, nC, tPtr, tIdx, c, coarseDead,
+            rc));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -1061,15 +1135,57 @@ ef_status ef_launch_sa_prolong2(int bf, int nF, int64_t nP, const int32_t* pRowP
                                 cudaStream_t s) {
     if (nP > 0) {
         if (bf == 3)
-            sa_prolong_contrib_kernel<3><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pCol, Pv, xc, c);
+            EF_CUDA(ef::launch_dep(sa_prolong_contrib_kernel<3>, nb_(nP, 256), 256, 0, s, nP, pCol, Pv, xc, c));
         else
-            sa_prolong_contrib_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, pCol, Pv, xc, c);
+            EF_CUDA(ef::launch_dep(sa_prolong_contrib_kernel<6>, nb_(nP, 256), 256, 0, s, nP, pCol, Pv, xc, c));
     }
     if (bf == 3)
-        sa_prolong_apply_kernel<3><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, c, mask, x, alpha);
+        EF_CUDA(ef::launch_dep(sa_prolong_apply_kernel<3>, nb_(nF, 256), 256, 0, s, nF, pRowPtr, c, mask, x, alpha));
     else
-        sa_prolong_apply_kernel<6><<<nb_(nF, 256), 256, 0, ef::counted(s)>>>(nF, pRowPtr, c, mask, x, alpha);
+        EF_CUDA(ef::launch_dep(sa_prolong_apply_kernel<6>, nb_(nF, 256), 256, 0, s, nF, pRowPtr, c, mask, x, alpha));
     EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// transpose-order copy of P for the one-pass restriction
+ef_status ef_launch_sa_block_copy(int bf, int64_t nP, const int32_t* tIdx, const float* Pv, float* dst,
+                                  cudaStream_t s) {
+    if (nP <= 0) return EF_OK;
+    if (bf == 3)
+        sa_block_copy_kernel<3><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, tIdx, Pv, dst);
+    else
+        sa_block_copy_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, tIdx, Pv, dst);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+size_t ef_sa_prolong_onepass_smem(int bf, int cap) { return (size_t)cap * bf * sizeof(float); }
+int ef_sa_prolong_onepass_rows() { return kSaProlongRows; }
+
+ef_status ef_launch_sa_restrict_onepass(int bf, int nC, const int32_t* tPtr, const int32_t* rowT, const float* PT,
+                                        const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s) {
+    if (nC <= 0) return EF_OK;
+    if (bf == 3)
+        EF_CUDA(ef::launch_dep(sa_restrict_onepass_kernel<3>, nC, kSaRestrictThreads, 0, s, nC, tPtr, rowT, PT, t,
+                               coarseDead, rc));
+    else
+        EF_CUDA(ef::launch_dep(sa_restrict_onepass_kernel<6>, nC, kSaRestrictThreads, 0, s, nC, tPtr, rowT, PT, t,
+                               coarseDead, rc));
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_prolong_onepass(int bf, int nF, int cap, const int32_t* pRowPtr, const int32_t* pCol,
+                                       const float* Pv, const float* xc, const uint8_t* mask, float* x, float alpha,
+                                       cudaStream_t s) {
+    if (nF <= 0) return EF_OK;
+    const int grid = nb_(nF, kSaProlongRows);
+    const size_t smem = ef_sa_prolong_onepass_smem(bf, cap);
+    if (bf == 3)
+        EF_CUDA(ef::launch_dep(sa_prolong_onepass_kernel<3>, grid, kSaProlongThreads, smem, s, nF, cap, pRowPtr, pCol,
+                               Pv, xc, mask, x, alpha));
+    else
+        EF_CUDA(ef::launch_dep(sa_prolong_onepass_kernel<6>, grid, kSaProlongThreads, smem, s, nF, cap, pRowPtr, pCol,
+                               Pv, xc, mask, x, alpha));
     return EF_OK;
 }
 
@@ -1118,7 +1234,7 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
 
 ef_status ef_launch_coarsest_apply(int n, const float* inv, const float* r, const uint8_t* dead, float* x,
                                    cudaStream_t s) {
-    coarsest_apply_kernel<<<nb_((int64_t)n * 32, 256), 256, 0, ef::counted(s)>>>(n, inv, r, dead, x);
+    EF_CUDA(ef::launch_dep(coarsest_apply_kernel, nb_((int64_t)n * 32, 256), 256, 0, s, n, inv, r, dead, x));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -316,6 +316,105 @@ EF_SA_HD void sa_prolong_apply(int m, const int32_t* __restrict__ pRowPtr, const
         if (!(mask && mask[BF * (int64_t)m + i])) x[BF * (int64_t)m + i] += alpha * s[i];
 }
 
+// One-pass transfers.  The prolongation reads P in its row order (Pv); the restriction reads a
+// copy of P in the transpose order (slot k holds block tIdx[k], rowT[k] = pRow[tIdx[k]]), so the
+// blocks of one coarse column are consecutive.  A thread takes one block: the BF x BC values are
+// contiguous (72 bytes for BF = 3, 144 for BF = 6) and load as 8- or 16-byte words.
+
+// the values of one block (8-byte aligned for BF = 3, 16-byte aligned for BF = 6)
+template <int BF>
+EF_SA_HD void sa_load_block(const float* __restrict__ src, float P[BF * BC]) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (BF == 6) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        EF_SA_UNROLL
+        for (int q = 0; q < BF * BC / 4; ++q) {
+            const float4 v = __ldg(s4 + q);
+            P[4 * q] = v.x;
+            P[4 * q + 1] = v.y;
+            P[4 * q + 2] = v.z;
+            P[4 * q + 3] = v.w;
+        }
+    } else {
+        const float2* s2 = reinterpret_cast<const float2*>(src);
+        EF_SA_UNROLL
+        for (int q = 0; q < BF * BC / 2; ++q) {
+            const float2 v = __ldg(s2 + q);
+            P[2 * q] = v.x;
+            P[2 * q + 1] = v.y;
+        }
+    }
+#else
+    for (int p = 0; p < BF * BC; ++p) P[p] = src[p];
+#endif
+}
+
+// transpose-order copy, slot k: dst[k] = Pv[tIdx[k]] (BF x BC values)
+template <int BF>
+EF_SA_HD void sa_block_copy(int64_t k, const int32_t* __restrict__ tIdx, const float* __restrict__ Pv,
+                            float* __restrict__ dst) {
+    const int64_t b = tIdx[k];
+    EF_SA_UNROLL
+    for (int p = 0; p < BF * BC; ++p) dst[k * BF * BC + p] = Pv[b * BF * BC + p];
+}
+
+// restriction, one thread's share of coarse node I from the transpose-order copy PT:
+// a[j] = sum over k = tPtr[I] + lane, + nLanes, ... of sum_i PT_k[i][j] t[rowT[k]][i]
+template <int BF>
+EF_SA_HD void sa_restrict_onepass_partial(int I, int lane, int nLanes, const int32_t* __restrict__ tPtr,
+                                          const int32_t* __restrict__ rowT, const float* __restrict__ PT,
+                                          const float* __restrict__ t, float a[BC]) {
+    EF_SA_UNROLL
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    for (int64_t k = tPtr[I] + lane; k < tPtr[I + 1]; k += nLanes) {
+        float P[BF * BC];
+        sa_load_block<BF>(PT + k * BF * BC, P);
+        const int64_t m = rowT[k];
+        float ti[BF];
+        EF_SA_UNROLL
+        for (int i = 0; i < BF; ++i) ti[i] = t[BF * m + i];
+        EF_SA_UNROLL
+        for (int i = 0; i < BF; ++i)
+            EF_SA_UNROLL
+            for (int j = 0; j < BC; ++j) a[j] += P[i * BC + j] * ti[i];
+    }
+}
+
+// prolongation product of block b (row order): q[i] = sum_j P_b[i][j] xc[col(b)][j]
+template <int BF>
+EF_SA_HD void sa_prolong_onepass_block(int64_t b, const int32_t* __restrict__ pCol, const float* __restrict__ Pv,
+                                       const float* __restrict__ xc, float q[BF]) {
+    float P[BF * BC];
+    sa_load_block<BF>(Pv + b * BF * BC, P);
+    const float* cv = xc + BC * (int64_t)pCol[b];
+    float x[BC];
+    EF_SA_UNROLL
+    for (int j = 0; j < BC; ++j) x[j] = cv[j];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) {
+        float s = 0.f;
+        EF_SA_UNROLL
+        for (int j = 0; j < BC; ++j) s += P[i * BC + j] * x[j];
+        q[i] = s;
+    }
+}
+
+// prolongation sum of finer row m from the block products q of the blocks b0, b0 + 1, ... (stride
+// BF): x[m] += alpha sum over row m's blocks, on the free DOFs
+template <int BF>
+EF_SA_HD void sa_prolong_onepass_row(int m, int64_t b0, const int32_t* __restrict__ pRowPtr, const float* q,
+                                     const uint8_t* __restrict__ mask, float* __restrict__ x, float alpha) {
+    float s[BF];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) s[i] = 0.f;
+    for (int64_t b = pRowPtr[m]; b < pRowPtr[m + 1]; ++b)
+        EF_SA_UNROLL
+        for (int i = 0; i < BF; ++i) s[i] += q[(b - b0) * BF + i];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i)
+        if (!(mask && mask[BF * (int64_t)m + i])) x[BF * (int64_t)m + i] += alpha * s[i];
+}
+
 }  // namespace ef
 
 #undef EF_SA_HD

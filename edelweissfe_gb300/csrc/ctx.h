@@ -68,6 +68,18 @@ ef_status ef_launch_sa_restrict2(int bf, int nC, int64_t nP, const int32_t* tPtr
 ef_status ef_launch_sa_prolong2(int bf, int nF, int64_t nP, const int32_t* pRowPtr, const int32_t* pCol,
                                 const float* Pv, const float* xc, const uint8_t* mask, float* c, float* x, float alpha,
                                 cudaStream_t s);
+// one-pass transfers: the restriction from a transpose-order copy of P, the prolongation from P
+// in groups of ef_sa_prolong_onepass_rows() consecutive finer rows with
+// ef_sa_prolong_onepass_smem(bf, cap) bytes of shared memory, cap >= the P blocks of every group
+ef_status ef_launch_sa_block_copy(int bf, int64_t nP, const int32_t* tIdx, const float* Pv, float* dst,
+                                  cudaStream_t s);
+size_t ef_sa_prolong_onepass_smem(int bf, int cap);
+int ef_sa_prolong_onepass_rows();
+ef_status ef_launch_sa_restrict_onepass(int bf, int nC, const int32_t* tPtr, const int32_t* rowT, const float* PT,
+                                        const float* t, const uint8_t* coarseDead, float* rc, cudaStream_t s);
+ef_status ef_launch_sa_prolong_onepass(int bf, int nF, int cap, const int32_t* pRowPtr, const int32_t* pCol,
+                                       const float* Pv, const float* xc, const uint8_t* mask, float* x, float alpha,
+                                       cudaStream_t s);
 ef_status ef_launch_sa_prolong(int bf, int nF, const int32_t* pRowPtr, const int32_t* pCol, const float* Pv,
                                const float* xc, const uint8_t* mask, float* x, float alpha, cudaStream_t s);
 ef_status ef_launch_restrict(int bf, int nC, const int32_t* aggPtr, const int32_t* aggIdx, const float* offs,
@@ -270,6 +282,12 @@ struct AmgLevel {
     int64_t *saPSeg = nullptr, *saApSeg = nullptr, *saCSeg = nullptr;
     float *saPv = nullptr, *saAPv = nullptr, *saW = nullptr;
     float* saC = nullptr;  // [saNP][6] block products of the two-stage restriction / prolongation
+    // one-pass transfers: transpose-order copy of P with the block row of each slot; saCap bounds
+    // the blocks of a prolongation group of finer rows
+    float* saPT = nullptr;
+    int32_t* saRowT = nullptr;
+    int saCap = 0;
+    bool saOnePass = false;  // this level's transfers run in one pass
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
 
@@ -280,7 +298,8 @@ struct AmgLevel {
                         (void*)x, (void*)x2, (void*)valsH, (void*)r, (void*)t, (void*)saPRowPtr, (void*)saPCol,
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
-                        (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC})
+                        (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC, (void*)saPT,
+                        (void*)saRowT})
             if (p) cudaFree(p);
     }
 };
@@ -397,7 +416,8 @@ struct ef_ctx {
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
     bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)
-    bool saTwoStage = true;                 // SA transfers as block products + sums (EF_SA_TWOSTAGE=0: one stage)
+    int saTransfer = 2;                     // SA transfers: 0 a thread per coarse node / finer row, 1 block
+                                            // products + sums, 2 one pass, a thread per block (EF_SA_TRANSFER)
     bool amgCluster = false;                // levels below clusterLevel as one cluster launch (EF_AMG_CLUSTER=1)
     int stageCap = 0;                       // > 0: fine BF16 smoothing through shared-memory staging (EF_AMG_STAGED=1)
     int clusterLevel = -1;                  // level whose coarse correction runs in coarse_cycle_kernel

@@ -28,6 +28,34 @@ inline cudaStream_t counted(cudaStream_t s) {
     return s;
 }
 
+// Programmatic dependent launch of the kernels of the Krylov iteration and the multigrid cycle
+// (chains of short dependent kernels).  A kernel launched by launch_dep() may be scheduled while
+// the kernel before it in the stream is still running, so its launch latency and CTA
+// rasterisation overlap the predecessor's tail.  Such a kernel starts with dep_entry(): it waits
+// until the predecessor grid has completed and its writes are visible, before any load or
+// store, and then lets its own successor be scheduled.  Launched without the attribute (EF_PDL=0
+// or a predecessor that is not a kernel), both instructions return at once.
+bool dep_launch_enabled();
+__device__ __forceinline__ void dep_entry() {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = counted(s);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = dep_launch_enabled() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 enum MatKind { MAT_LINEAR_ELASTIC = 0, MAT_VON_MISES = 1, MAT_NEOHOOKE_WA = 2 };
 
 // Constant tables of one element type (shape-function derivatives at the B/J

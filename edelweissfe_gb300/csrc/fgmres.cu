@@ -204,6 +204,7 @@ __global__ void __launch_bounds__(kFB, 4) multidot_partial_kernel(int64_t n, int
                                                                 double* __restrict__ part,
                                                                 const double* __restrict__ gate, int gateNv,
                                                                 double eta2) {
+    ef::dep_entry();
     if (gate && !dgks_reorth(gate, gateNv, eta2)) return;
     __shared__ float red[kFB / 32][kMaxBasis];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(kFB, 4) multidot_partial_kernel(int64_t n, int
 __global__ void __launch_bounds__(kFB) multidot_final_kernel(int nPart, int nv, const double* __restrict__ part,
                                                               double* __restrict__ h, const double* __restrict__ gate,
                                                               int gateNv, double eta2) {
+    ef::dep_entry();
     if (gate && !dgks_reorth(gate, gateNv, eta2)) return;
     __shared__ double red[kFB / 32];
     const int k = blockIdx.x;
@@ -267,6 +269,7 @@ __global__ void __launch_bounds__(kFB) cgs_axpy_kernel(int64_t n, int nv, const 
                                                         const double* __restrict__ h, float* __restrict__ w,
                                                         double* __restrict__ partN, const double* __restrict__ gate,
                                                         double eta2) {
+    ef::dep_entry();
     if (gate && !dgks_reorth(gate, nv, eta2)) return;
     __shared__ float hs[kMaxBasis];
     __shared__ float red[kFB / 32];
@@ -301,6 +304,7 @@ __global__ void __launch_bounds__(kFB) cgs_axpy_kernel(int64_t n, int nv, const 
 // hAcc = hG + hTmp when the DGKS test on hG fired, else hG (k < nv)
 __global__ void cgs_accumulate_kernel(int nv, const double* __restrict__ hG, const double* __restrict__ hTmp,
                                       double* __restrict__ hAcc, double eta2) {
+    ef::dep_entry();
     const bool re = dgks_reorth(hG, nv, eta2);
     for (int k = threadIdx.x; k < nv; k += blockDim.x) hAcc[k] = re ? hG[k] + hTmp[k] : hG[k];
 }
@@ -315,6 +319,7 @@ __global__ void __launch_bounds__(kFB) normalize_kernel(int64_t n, float* __rest
                                                          const double* __restrict__ hAcc, int nv,
                                                          volatile double* hostOut, int slotNorm,
                                                          const double* __restrict__ gate, double eta2) {
+    ef::dep_entry();
     __shared__ double red[kFB / 32];
     double t = 0.0;
     for (int c = threadIdx.x; c < nParts; c += kFB) t += np[c];
@@ -425,18 +430,18 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
     }
     float* w = V + (int64_t)nv * ldv;
     const bool re = eta2 > 0.0;
-    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv + 1, V, ldv, w, part, nullptr, 0, 0.0);
-    multidot_final_kernel<<<nv + 1, kFB, 0, ef::counted(s)>>>(nPart, nv + 1, part, hG, nullptr, 0, 0.0);
-    cgs_axpy_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, hG, w, partN, nullptr, 0.0);
+    EF_CUDA(ef::launch_dep(multidot_partial_kernel, nPart, kFB, 0, s, n, nv + 1, V, ldv, w, part, nullptr, 0, 0.0));
+    EF_CUDA(ef::launch_dep(multidot_final_kernel, nv + 1, kFB, 0, s, nPart, nv + 1, part, hG, nullptr, 0, 0.0));
+    EF_CUDA(ef::launch_dep(cgs_axpy_kernel, nPart, kFB, 0, s, n, nv, V, ldv, hG, w, partN, nullptr, 0.0));
     if (re) {
-        multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, w, part, hG, nv, eta2);
-        multidot_final_kernel<<<nv, kFB, 0, ef::counted(s)>>>(nPart, nv, part, hTmp, hG, nv, eta2);
-        cgs_axpy_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, nv, V, ldv, hTmp, w, partN, hG, eta2);
-        cgs_accumulate_kernel<<<1, kMaxBasis, 0, ef::counted(s)>>>(nv, hG, hTmp, hAcc, eta2);
+        EF_CUDA(ef::launch_dep(multidot_partial_kernel, nPart, kFB, 0, s, n, nv, V, ldv, w, part, hG, nv, eta2));
+        EF_CUDA(ef::launch_dep(multidot_final_kernel, nv, kFB, 0, s, nPart, nv, part, hTmp, hG, nv, eta2));
+        EF_CUDA(ef::launch_dep(cgs_axpy_kernel, nPart, kFB, 0, s, n, nv, V, ldv, hTmp, w, partN, hG, eta2));
+        EF_CUDA(ef::launch_dep(cgs_accumulate_kernel, 1, kMaxBasis, 0, s, nv, hG, hTmp, hAcc, eta2));
     }
     // every normalisation CTA sums all nPart parts: a quarter of the CTAs
-    normalize_kernel<<<std::max(1, nPart / 4), kFB, 0, ef::counted(s)>>>(
-        n, w, w2, partN, nPart, re ? hAcc : hG, nv, hostOut, slotNorm, re ? hG : nullptr, eta2);
+    EF_CUDA(ef::launch_dep(normalize_kernel, std::max(1, nPart / 4), kFB, 0, s, n, w, w2, partN, nPart, re ? hAcc : hG,
+            nv, hostOut, slotNorm, re ? hG : nullptr, eta2));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -444,9 +449,9 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
 // w /= |w| with |w|^2 from a one-vector multidot (the restart vector); w2 = w; |w|^2 to hostOut
 ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
                                     int slotNorm, cudaStream_t s) {
-    multidot_partial_kernel<<<nPart, kFB, 0, ef::counted(s)>>>(n, 1, w, n, w, part, nullptr, 0, 0.0);
-    normalize_kernel<<<std::max(1, nPart / 4), kFB, 0, ef::counted(s)>>>(n, w, w2, part, nPart, nullptr, 0, hostOut,
-                                                                         slotNorm, nullptr, 0.0);
+    EF_CUDA(ef::launch_dep(multidot_partial_kernel, nPart, kFB, 0, s, n, 1, w, n, w, part, nullptr, 0, 0.0));
+    EF_CUDA(ef::launch_dep(normalize_kernel, std::max(1, nPart / 4), kFB, 0, s, n, w, w2, part, nPart, nullptr, 0,
+            hostOut, slotNorm, nullptr, 0.0));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

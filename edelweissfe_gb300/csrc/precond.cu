@@ -154,7 +154,8 @@ ef_status sell_refresh(ef_ctx* c, cudaStream_t s) {
 ef_status amg_build(ef_ctx* c) {
     if (!c->amg.empty()) return EF_OK;
     if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
-    if (const char* e = getenv("EF_SA_TWOSTAGE")) c->saTwoStage = atoi(e) != 0;
+    if (const char* e = getenv("EF_SA_TWOSTAGE")) c->saTransfer = atoi(e) != 0 ? 1 : 0;
+    if (const char* e = getenv("EF_SA_TRANSFER")) c->saTransfer = std::min(2, std::max(0, atoi(e)));
     // smoothed prolongators: one sweep before and after, V-cycle (the fastest cfg 2 load step of
     // 1/1, 2/2 x V, W on level 1); plain aggregation: two sweeps and a W-cycle on level 1
     if (c->amgSmoothed) {
@@ -164,12 +165,12 @@ ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_OMEGA")) c->amgOmega = (float)atof(e);
     if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
     c->amgPre = c->amgPost = c->amgSweeps;
-    if (const char* e = getenv("EF_AMG_PRE")) c->amgPre = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_PRE")) c->amgPre = std::max(0, atoi(e));  // 0: no pre-smoothing
     if (const char* e = getenv("EF_AMG_POST")) c->amgPost = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_WLEVELS")) c->amgWLevels = std::max(0, atoi(e));
     c->amgPreC = c->amgPre;
     c->amgPostC = c->amgPost;
-    if (const char* e = getenv("EF_AMG_PRE_COARSE")) c->amgPreC = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_PRE_COARSE")) c->amgPreC = std::max(0, atoi(e));
     if (const char* e = getenv("EF_AMG_POST_COARSE")) c->amgPostC = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
@@ -320,6 +321,23 @@ ef_status amg_build(ef_ctx* c) {
             L.saW = dalloc<float>(1, &st);
             L.saC = dalloc<float>((size_t)std::max<int64_t>(1, L.saNP) * BCo, &st);
             if (!L.saPv || !L.saAPv || !L.saW || !L.saC) return st;
+            if (c->saTransfer == 2 && L.saNP > 0) {
+                // one-pass transfers where the prolongation's block products of a group of
+                // consecutive finer rows fit the shared memory
+                const int G = ef_sa_prolong_onepass_rows();
+                int cap = 0;
+                for (int r0 = 0; r0 < nFine; r0 += G)
+                    cap = std::max(cap, SA.pRowPtr[std::min(r0 + G, nFine)] - SA.pRowPtr[r0]);
+                if (ef_sa_prolong_onepass_smem(bfL, cap) <= 48 * 1024) {
+                    std::vector<int32_t> rowT(L.saNP);
+                    for (int64_t k = 0; k < L.saNP; ++k) rowT[k] = SA.pRow[SA.tIdx[k]];
+                    EF_CHECK(upload(&L.saRowT, rowT));
+                    L.saPT = dalloc<float>((size_t)L.saNP * bfL * BCo, &st);
+                    if (!L.saPT) return st;
+                    L.saCap = cap;
+                    L.saOnePass = true;
+                }
+            }
         }
         L.vals = dalloc<float>((size_t)L.nBlocks * BCo * BCo, &st);
         L.binv = dalloc<float>((size_t)nC * BCo * BCo, &st);
@@ -458,7 +476,7 @@ static ef_status amg_prepare_cluster(ef_ctx* c) {
     c->clusterLevel = -1;
     c->nCoarseOps = 0;
     const int nL = (int)c->amg.size();
-    if (!c->amgCluster || c->amgCheb || c->amgSmoothed) return EF_OK;
+    if (!c->amgCluster || c->amgCheb || c->amgSmoothed || c->amgPreC < 1) return EF_OK;
     int lc = -1;
     for (int l = 1; l < nL; ++l)
         if (c->amg[l].nN <= kClusterMaxNodes) {
@@ -722,6 +740,7 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
                                         L.saApRow, L.saApSeg, L.saApK, L.saApP, fCol, fVals, fMask, L.offs, L.agg,
                                         fBinv, L.saW, L.saPv, L.saAPv, L.nBlocks, L.saCSeg, L.saCP, L.saCAP,
                                         L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+            if (L.saOnePass) EF_CHECK(ef_launch_sa_block_copy(fine ? 3 : BCo, L.saNP, L.saTIdx, L.saPv, L.saPT, s));
         } else {
             EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
                                         L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
@@ -811,13 +830,16 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
     };
     // The sweeps (the first from zero) alternate between x and a second vector; the first goes
     // to the second vector when their total count is even, so that the last one lands in x.
+    // Without pre-smoothing the iterate starts as zeros in the vector the first sweep would write.
     float* x2 = fine ? c->fineX : c->amg[l - 1].x2;
     const int nPre = fine ? c->amgPre : c->amgPreC, nPost = fine ? c->amgPost : c->amgPostC;
     float* cur = x;
-    if (!c->amgCheb) cur = ((nPre + nPost) & 1) ? x : x2;
+    if (!c->amgCheb) cur = ((std::max(nPre, 1) + nPost) & 1) ? x : x2;
     // pre-smoothing from zero
     if (c->amgCheb) {
         EF_CHECK(chebyshev(true));
+    } else if (nPre == 0) {
+        EF_CUDA(cudaMemsetAsync(cur, 0, sizeof(float) * (size_t)bs * nN, s));
     } else {
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, cur, 0, s));
         for (int k = 1; k < nPre; ++k) {
@@ -829,7 +851,10 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
     for (int rep = 0; rep < reps; ++rep) {
-        if (!c->amgCheb) {
+        const float* res = t;  // the residual the restriction reads: r itself while the iterate is zero
+        if (!c->amgCheb && nPre == 0 && rep == 0) {
+            res = r;
+        } else if (!c->amgCheb) {
             EF_CHECK(fineH ? fine_bf16(cur, t, nullptr, 0.f)
                                           : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s,
                                                                      nullptr, 0.f, valsH));
@@ -845,15 +870,21 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
             EF_CHECK(ef_launch_coarse_cycle(c->dCoarseOps, c->nCoarseOps, s));
             continue;
         }
-        if (c->amgSmoothed && c->saTwoStage)
-            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t, Cn.dead,
-                                            Cn.saC, Cn.r, s));
+        if (c->amgSmoothed && Cn.saOnePass)
+            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, res, Cn.dead, Cn.r, s));
+        else if (c->amgSmoothed && c->saTransfer >= 1)
+            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, res,
+                                            Cn.dead, Cn.saC, Cn.r, s));
         else if (c->amgSmoothed)
-            EF_CHECK(ef_launch_sa_restrict(bs, Cn.nN, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t, Cn.dead, Cn.r, s));
+            EF_CHECK(ef_launch_sa_restrict(bs, Cn.nN, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, res, Cn.dead, Cn.r,
+                                           s));
         else
-            EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, t, Cn.dead, Cn.r, s));
+            EF_CHECK(ef_launch_restrict(bs, Cn.nN, Cn.aggPtr, Cn.aggIdx, Cn.offs, res, Cn.dead, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        if (c->amgSmoothed && c->saTwoStage)
+        if (c->amgSmoothed && Cn.saOnePass)
+            EF_CHECK(ef_launch_sa_prolong_onepass(bs, nN, Cn.saCap, Cn.saPRowPtr, Cn.saPCol, Cn.saPv, Cn.x, mask, cur,
+                                                  c->amgAlpha, s));
+        else if (c->amgSmoothed && c->saTransfer >= 1)
             EF_CHECK(ef_launch_sa_prolong2(bs, nN, Cn.saNP, Cn.saPRowPtr, Cn.saPCol, Cn.saPv, Cn.x, mask, Cn.saC, cur,
                                            c->amgAlpha, s));
         else if (c->amgSmoothed)

@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nS
                                                                   const float* __restrict__ x,
                                                                   const uint8_t* __restrict__ mask,
                                                                   float* __restrict__ y, float* __restrict__ xcopy) {
+    ef::dep_entry();
     const int lane = threadIdx.x & 31;
     const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
     if (sl >= nSlices) return;
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
     const float* __restrict__ binv, float omega) {
+    ef::dep_entry();
     SellPart p;
     const bool active = sell_part(nSlices, off, p);
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
@@ -210,11 +212,11 @@ ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const in
                                cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
     if (xcopy)
-        sell_spmv3_kernel<true><<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(nN, nSlices, off, perm, col,
-                                                                                          v9, x, mask, y, xcopy);
+        EF_CUDA(ef::launch_dep(sell_spmv3_kernel<true>, sell_grid(nSlices), kSellThreads, 0, s, nN, nSlices, off, perm,
+                col, v9, x, mask, y, xcopy));
     else
-        sell_spmv3_kernel<false><<<sell_grid(nSlices), kSellThreads, 0, ef::counted(s)>>>(nN, nSlices, off, perm, col,
-                                                                                           v9, x, mask, y, nullptr);
+        EF_CUDA(ef::launch_dep(sell_spmv3_kernel<false>, sell_grid(nSlices), kSellThreads, 0, s, nN, nSlices, off, perm,
+                col, v9, x, mask, y, nullptr));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -223,9 +225,9 @@ ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, co
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
-    sell_level3_bf16_kernel<<<(unsigned)((nSlices + kSellSplitSlicesPerCta - 1) / kSellSplitSlicesPerCta), kSellThreads,
-                              0, ef::counted(s)>>>(
-        nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega);
+    EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel,
+            (unsigned)((nSlices + kSellSplitSlicesPerCta - 1) / kSellSplitSlicesPerCta), kSellThreads, 0, s, nN,
+            nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -10,6 +10,7 @@
 // Build: g++ -O2 -std=c++17 -ffp-contract=off amg_sa_check.cpp
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstdio>
 #include <random>
 #include <utility>
@@ -233,6 +234,32 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (int64_t b = 0; b < nP; ++b) ef::sa_prolong_contrib<BF>(b, S.pCol.data(), Pv.data(), xcf.data(), cb.data());
     for (int m = 0; m < nF; ++m) ef::sa_prolong_apply<BF>(m, S.pRowPtr.data(), cb.data(), fm, xf2.data(), alpha);
+    // the one-pass forms: the restriction from the transpose-order copy of P over 128 threads per
+    // coarse node, the prolongation in groups of 64 consecutive finer rows, as the kernels run them
+    std::vector<float> PT((size_t)nP * BF * BC), rc3(nc), xf3(x0.begin(), x0.end());
+    std::vector<int32_t> rowT(nP);
+    for (int64_t k = 0; k < nP; ++k) {
+        rowT[k] = S.pRow[S.tIdx[k]];
+        ef::sa_block_copy<BF>(k, S.tIdx.data(), Pv.data(), PT.data());
+    }
+    for (int I = 0; I < nC; ++I) {
+        double sum[BC] = {};
+        for (int lane = 0; lane < 128; ++lane) {
+            float a[BC];
+            ef::sa_restrict_onepass_partial<BF>(I, lane, 128, S.tPtr.data(), rowT.data(), PT.data(), tf.data(), a);
+            for (int j = 0; j < BC; ++j) sum[j] += a[j];
+        }
+        for (int j = 0; j < BC; ++j) rc3[BC * I + j] = dead[BC * I + j] ? 0.f : (float)sum[j];
+    }
+    for (int r0 = 0; r0 < nF; r0 += 64) {
+        const int r1 = std::min(r0 + 64, nF);
+        const int64_t b0 = S.pRowPtr[r0], b1 = S.pRowPtr[r1];
+        std::vector<float> q((size_t)(b1 - b0) * BF);
+        for (int64_t b = b0; b < b1; ++b)
+            ef::sa_prolong_onepass_block<BF>(b, S.pCol.data(), Pv.data(), xcf.data(), &q[(size_t)(b - b0) * BF]);
+        for (int m = r0; m < r1; ++m)
+            ef::sa_prolong_onepass_row<BF>(m, b0, S.pRowPtr.data(), q.data(), fm, xf3.data(), alpha);
+    }
     // ---- compare (FP32 arithmetic against FP64: relative to each product's largest entry) ----
     double eP = 0, eAP = 0, eC = 0, eR = 0, eX = 0, oP = 0, oAP = 0, oC = 0;
     std::vector<uint8_t> seenP((size_t)n * nc, 0), seenAP((size_t)n * nc, 0), seenC((size_t)nc * nc, 0);
@@ -266,16 +293,19 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (size_t i = 0; i < Acd.size(); ++i)
         if (!seenC[i]) oC = std::fmax(oC, std::fabs(Acd[i]));
-    double eR2 = 0, eX2 = 0;
+    double eR2 = 0, eX2 = 0, eR3 = 0, eX3 = 0;
     for (int i = 0; i < nc; ++i) eR = std::fmax(eR, std::fabs(rc[i] - rcd[i]));
     for (int i = 0; i < n; ++i) eX = std::fmax(eX, std::fabs(xf[i] - xd[i]));
     for (int i = 0; i < nc; ++i) eR2 = std::fmax(eR2, std::fabs(rc2[i] - rcd[i]));
     for (int i = 0; i < n; ++i) eX2 = std::fmax(eX2, std::fabs(xf2[i] - xd[i]));
+    for (int i = 0; i < nc; ++i) eR3 = std::fmax(eR3, std::fabs(rc3[i] - rcd[i]));
+    for (int i = 0; i < n; ++i) eX3 = std::fmax(eX3, std::fabs(xf3[i] - xd[i]));
     const double sP = max_abs(Ps), sAP = max_abs(APd), sC = max_abs(Acd), sR = max_abs(rcd), sX = max_abs(xd);
     const double tol = 2e-6;
     int fails = 0;
     fails += !(eP <= tol * sP) + !(eAP <= tol * sAP) + !(eC <= tol * sC) + !(eR <= tol * sR) + !(eX <= tol * sX);
     fails += !(eR2 <= tol * sR) + !(eX2 <= tol * sX);
+    fails += !(eR3 <= tol * sR) + !(eX3 <= tol * sX);
     fails += (oP != 0.0) + (oAP != 0.0) + (oC != 0.0);
     // masked finer rows: P exactly zero
     for (int m = 0; m < nF; ++m)
@@ -285,9 +315,9 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
                 for (int j = 0; j < BC; ++j) fails += Pv[(size_t)b * BF * BC + a * BC + j] != 0.f;
         }
     std::printf("%s: P %lld blocks, AP %lld, coarse %lld; rel diff P %.1e AP %.1e Ac %.1e restrict %.1e "
-                "prolong %.1e (two-stage %.1e %.1e); outside patterns %.1e %.1e %.1e; failures %d\n",
+                "prolong %.1e (two-stage %.1e %.1e, one-pass %.1e %.1e); outside patterns %.1e %.1e %.1e; failures %d\n",
                 name, (long long)nP, (long long)nAP, (long long)nCb, eP / sP, eAP / sAP, eC / sC, eR / sR, eX / sX,
-                eR2 / sR, eX2 / sX, oP, oAP, oC, fails);
+                eR2 / sR, eX2 / sX, eR3 / sR, eX3 / sX, oP, oAP, oC, fails);
     return fails;
 }
 

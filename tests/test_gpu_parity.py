@@ -572,15 +572,16 @@ def test_sliced_ell_fine_level_matches_the_csr_kernels(gpu_lib, monkeypatch, cas
     assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
 
 
-def test_two_stage_sa_transfers_match_one_stage(gpu_lib, monkeypatch):
-    """The smoothed-aggregation restriction and prolongation as block products + sums (the
-    default) against the one-stage kernels (EF_SA_TWOSTAGE=0): the same 1e-8 solution in about
-    the same number of FGMRES iterations (the summation order differs), and the same bits when the
-    solve is repeated."""
+def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
+    """The three forms of the smoothed-aggregation restriction and prolongation: one pass from
+    plane-major copies of P (the default, EF_SA_TRANSFER=2), block products + sums (1) and the
+    one-stage kernels over the block-major P (0): the same 1e-8 solution in about the same number
+    of FGMRES iterations (the summation orders differ), and the same bits when the default's solve
+    is repeated."""
     rng = np.random.default_rng(17)
     out = {}
-    for two in ("0", "1"):
-        monkeypatch.setenv("EF_SA_TWOSTAGE", two)
+    for mode in ("0", "1", "2"):
+        monkeypatch.setenv("EF_SA_TRANSFER", mode)
         s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
         if "b" not in out:
             b = rng.normal(size=s.nDof)
@@ -591,10 +592,12 @@ def test_two_stage_sa_transfers_match_one_stage(gpu_lib, monkeypatch):
         s.linsolver.rtol = 1e-8
         x = s.linearSolve(R).cpu().numpy()
         assert s.lastSolveInfo.relResidual <= 1e-8
-        out[two] = (x, s.lastSolveInfo.iterations)
-        if two == "1":
+        out[mode] = (x, s.lastSolveInfo.iterations)
+        if mode == "2":
             assert np.array_equal(s.linearSolve(R).cpu().numpy(), x)
         del s
-    (x0, i0), (x1, i1) = out["0"], out["1"]
-    assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0))
-    assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
+    x0, i0 = out["0"]
+    for mode in ("1", "2"):
+        x1, i1 = out[mode]
+        assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0)), mode
+        assert abs(i1 - i0) <= max(2, i0 // 10), (mode, i0, i1)
