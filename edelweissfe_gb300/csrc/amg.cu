@@ -136,6 +136,45 @@ __global__ void sa_ap_kernel(int64_t nAP, const int32_t* __restrict__ apRow, con
     sa_ap_block<BF>(a, apRow, apSeg, apK, apP, fineCol, fineVals, fineMask, Pv, APv);
 }
 
+// AP by groups of kSaApRows finer rows: a thread per pair (coalesced pair lists) leaves the pair's
+// product in shared memory, then a thread per value of an AP block of the group sums it over the
+// block's pairs in list order.
+// cap >= the pairs of every group (checked on the host); a group above it is skipped.
+constexpr int kSaApThreads = 256;
+constexpr int kSaApRows = 2;
+template <int BF>
+__global__ void __launch_bounds__(kSaApThreads) sa_ap_rows_kernel(
+    int nF, int cap, const int32_t* __restrict__ apRowPtr, const int64_t* __restrict__ apSeg,
+    const int32_t* __restrict__ apK, const int32_t* __restrict__ apP, const int32_t* __restrict__ fineCol,
+    const float* __restrict__ fineVals, const uint8_t* __restrict__ fineMask, const float* __restrict__ Pv,
+    float* __restrict__ APv) {
+    extern __shared__ float apC[];  // [cap][BF * BC]
+    const int m0 = blockIdx.x * kSaApRows;
+    const int m1 = min(m0 + kSaApRows, nF);
+    const int64_t a0 = apRowPtr[m0], a1 = apRowPtr[m1];
+    const int64_t t0 = apSeg[a0], t1 = apSeg[a1];
+    if (t1 - t0 > cap) return;  // the same for the whole CTA
+    for (int64_t t = t0 + threadIdx.x; t < t1; t += kSaApThreads) {
+        int m = m0;
+        while (m + 1 < m1 && apSeg[apRowPtr[m + 1]] <= t) ++m;
+        float c[BF * BC];
+        sa_ap_pair<BF>(t, m, apK, apP, fineCol, fineVals, fineMask, Pv, c);
+        float* d = apC + (t - t0) * (BF * BC);
+#pragma unroll
+        for (int p = 0; p < BF * BC; ++p) d[p] = c[p];
+    }
+    __syncthreads();
+    // a thread per (AP block, value): the block's pairs in list order
+    const int nTask = (int)(a1 - a0) * (BF * BC);
+    for (int task = threadIdx.x; task < nTask; task += kSaApThreads) {
+        const int64_t a = a0 + task / (BF * BC);
+        const int p = task % (BF * BC);
+        float acc = 0.f;
+        for (int64_t t = apSeg[a]; t < apSeg[a + 1]; ++t) acc += apC[(t - t0) * (BF * BC) + p];
+        APv[a * (BF * BC) + p] = acc;
+    }
+}
+
 // one coarse block per thread
 template <int BF>
 __global__ void sa_galerkin_kernel(int64_t nC, const int64_t* __restrict__ cSeg, const int32_t* __restrict__ cP,
@@ -657,16 +696,31 @@ __global__ void coarsest_inverse_kernel(int nN, const int32_t* __restrict__ rowP
     for (int i = tid; i < n; i += nt) drop[i] = 0;
     __syncthreads();
     for (int col = 0; col < n; ++col) {
-        if (tid == 0) {
-            int p = col;
-            float best = fabsf(A(col, col));
-            for (int r = col + 1; r < n; ++r)
-                if (fabsf(A(r, col)) > best) {
-                    best = fabsf(A(r, col));
+        if (threadIdx.y == 0) {
+            // partial pivoting by the first warp: the largest |A(r, col)|, r >= col, the smallest
+            // such r on ties (the row a serial scan with a strict comparison keeps)
+            int p = -1;
+            float best = -1.f;
+            for (int r = col + threadIdx.x; r < n; r += 32) {
+                const float v = fabsf(A(r, col));
+                if (v > best) {
+                    best = v;
                     p = r;
                 }
-            piv = best > 1e-6f * dmax ? p : -1;
-            if (piv < 0) drop[col] = 1;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int op = __shfl_xor_sync(0xffffffffu, p, o);
+                if (ob > best || (ob == best && op >= 0 && (p < 0 || op < p))) {
+                    best = ob;
+                    p = op;
+                }
+            }
+            if (threadIdx.x == 0) {
+                piv = best > 1e-6f * dmax ? p : -1;
+                if (piv < 0) drop[col] = 1;
+            }
         }
         __syncthreads();
         if (piv < 0) continue;
@@ -1013,6 +1067,9 @@ __global__ void to_bf16_split_kernel(int64_t nb, const float* __restrict__ src, 
 
 using namespace ef;
 
+size_t ef_sa_ap_rows_smem(int bf, int cap) { return (size_t)cap * bf * BC * sizeof(float); }
+int ef_sa_ap_rows() { return kSaApRows; }
+
 static inline int nb_(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
 int ef_amg_coarse_dofs() { return BC; }
@@ -1078,14 +1135,19 @@ ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int3
                              const uint8_t* fineMask, const float* offs, const int32_t* agg, const float* binv,
                              const float* wP, float* Pv, float* APv, int64_t nC, const int64_t* cSeg,
                              const int32_t* cP, const int32_t* cAP, const int32_t* coarseRowOfBlock,
-                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals,
-                             cudaStream_t s) {
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals, int nF,
+                             const int32_t* apRowPtr, int apCap, cudaStream_t s) {
 #define EF_SA(BF_)                                                                                             \
     sa_prolongator_kernel<BF_><<<nb_(nP, 128), 128, 0, ef::counted(s)>>>(nP, pRow, pCol, pSeg, pSrc, fineCol, \
                                                                         fineVals, fineMask, offs, agg, binv,  \
                                                                         wP, Pv);                              \
-    sa_ap_kernel<BF_><<<nb_(nAP, 128), 128, 0, ef::counted(s)>>>(nAP, apRow, apSeg, apK, apP, fineCol,        \
-                                                                fineVals, fineMask, Pv, APv);                 \
+    if (apRowPtr)                                                                                              \
+        sa_ap_rows_kernel<BF_><<<nb_(nF, kSaApRows), kSaApThreads, ef_sa_ap_rows_smem(BF_, apCap),            \
+                                 ef::counted(s)>>>(nF, apCap, apRowPtr, apSeg, apK, apP, fineCol, fineVals,    \
+                                                   fineMask, Pv, APv);                                         \
+    else                                                                                                       \
+        sa_ap_kernel<BF_><<<nb_(nAP, 128), 128, 0, ef::counted(s)>>>(nAP, apRow, apSeg, apK, apP, fineCol,    \
+                                                                    fineVals, fineMask, Pv, APv);             \
     sa_galerkin_kernel<BF_><<<nb_(nC, 64), 64, 0, ef::counted(s)>>>(nC, cSeg, cP, cAP, Pv, APv,               \
                                                                    coarseRowOfBlock, coarseCol, coarseDead,   \
                                                                    coarseVals)

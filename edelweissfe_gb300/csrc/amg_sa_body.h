@@ -158,6 +158,33 @@ EF_SA_HD void sa_ap_block(int64_t a, const int32_t* __restrict__ apRow, const in
         for (int j = 0; j < BC; ++j) out[i * BC + j] = acc[i][j];
 }
 
+// AP pair t (finer block k = apK[t] of row m, P block apP[t] of row col(k)): c = A_k P_apP[t], rows
+// of masked finer DOFs of row m and columns of masked finer DOFs of col(k) dropped.  Summed over
+// the pairs of an AP block in their listed order this is the block of sa_ap_block (with the
+// products of one pair rounded together).
+template <int BF>
+EF_SA_HD void sa_ap_pair(int64_t t, int m, const int32_t* __restrict__ apK, const int32_t* __restrict__ apP,
+                         const int32_t* __restrict__ fineCol, const float* __restrict__ fineVals,
+                         const uint8_t* __restrict__ fineMask, const float* __restrict__ Pv, float c[BF * BC]) {
+    const int32_t k = apK[t];
+    const int n = fineCol[k];
+    const float* v = fineVals + (int64_t)k * BF * BF;
+    const float* P = Pv + (int64_t)apP[t] * BF * BC;
+    EF_SA_UNROLL
+    for (int p = 0; p < BF * BC; ++p) c[p] = 0.f;
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) {
+        if (fineMask && fineMask[BF * (int64_t)m + i]) continue;
+        EF_SA_UNROLL
+        for (int q = 0; q < BF; ++q) {
+            if (fineMask && fineMask[BF * (int64_t)n + q]) continue;
+            const float av = v[i * BF + q];
+            EF_SA_UNROLL
+            for (int j = 0; j < BC; ++j) c[i * BC + j] += av * P[q * BC + j];
+        }
+    }
+}
+
 // coarse block S = (I, J): sum over the pairs (P block (m, I), AP block (m, J)) listed in
 // cP / cAP[cSeg[S] .. cSeg[S+1]) of P^T AP, TwoSum-compensated; dead coarse DOFs get identity
 // rows and columns

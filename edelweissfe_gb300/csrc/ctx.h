@@ -57,8 +57,12 @@ ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int3
                              const uint8_t* fineMask, const float* offs, const int32_t* agg, const float* binv,
                              const float* wP, float* Pv, float* APv, int64_t nC, const int64_t* cSeg,
                              const int32_t* cP, const int32_t* cAP, const int32_t* coarseRowOfBlock,
-                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals,
-                             cudaStream_t s);
+                             const int32_t* coarseCol, const uint8_t* coarseDead, float* coarseVals, int nF,
+                             const int32_t* apRowPtr, int apCap, cudaStream_t s);
+// AP by groups of ef_sa_ap_rows() finer rows (apRowPtr non-null in ef_launch_sa_setup) needs
+// ef_sa_ap_rows_smem(bf, apCap) bytes of shared memory, apCap >= the pairs of every group
+size_t ef_sa_ap_rows_smem(int bf, int cap);
+int ef_sa_ap_rows();
 ef_status ef_launch_sa_restrict(int bf, int nC, const int32_t* tPtr, const int32_t* tIdx, const int32_t* pRow,
                                 const float* Pv, const float* t, const uint8_t* coarseDead, float* rc,
                                 cudaStream_t s);
@@ -287,6 +291,8 @@ struct AmgLevel {
     float* saPT = nullptr;
     int32_t* saRowT = nullptr;
     int saCap = 0;
+    int32_t* saApRowPtr = nullptr;  // AP row pointer, for the AP product by groups of rows (null: a thread
+    int saApCap = 0;                // per AP block); saApCap bounds the pairs of a group
     bool saOnePass = false;  // this level's transfers run in one pass
     std::vector<int32_t> hRowPtr, hColIdx, hAgg, hAggPtr, hAggIdx;
     std::vector<uint8_t> hDead;
@@ -299,7 +305,7 @@ struct AmgLevel {
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
                         (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC, (void*)saPT,
-                        (void*)saRowT})
+                        (void*)saRowT, (void*)saApRowPtr})
             if (p) cudaFree(p);
     }
 };

@@ -176,17 +176,21 @@ __device__ __forceinline__ bool dgks_reorth(const double* __restrict__ h, int nv
 // FP32 inside a CTA (the vectors themselves are FP32) and in FP64 only across CTAs, where the
 // sums are long.  All orders are fixed.
 
-// fixed-order FP64 sum over the CTA of one value per thread (every thread gets it)
-__device__ __forceinline__ double cta_sum_fixed(double v, double* red) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
+// fixed-order FP64 sum of v[0..n) over the CTA, returned to thread 0: thread-strided partial sums
+// (their loads in flight together), a shuffle tree per warp, the warps' sums in order by thread 0
+// (the other threads' FP64 work ends at their warp's tree)
+__device__ __forceinline__ double cta_sum_fixed(const double* __restrict__ v, int n, double* red) {
     double t = 0.0;
+    for (int c = threadIdx.x; c < n; c += kFB) t += v[c];
 #pragma unroll
-    for (int q = 0; q < kFB / 32; ++q) t += red[q];
-    return t;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < kFB / 32; ++q) s += red[q];
+    return s;
 }
 
 // fixed-order FP32 sum over a warp (every lane gets it)
@@ -256,9 +260,7 @@ __global__ void __launch_bounds__(kFB) multidot_final_kernel(int nPart, int nv, 
     __shared__ double red[kFB / 32];
     const int k = blockIdx.x;
     if (k >= nv) return;
-    double s = 0.0;
-    for (int c = threadIdx.x; c < nPart; c += kFB) s += part[(int64_t)k * nPart + c];
-    s = cta_sum_fixed(s, red);
+    const double s = cta_sum_fixed(part + (int64_t)k * nPart, nPart, red);
     if (threadIdx.x == 0) h[k] = s;
 }
 
@@ -320,19 +322,22 @@ __global__ void __launch_bounds__(kFB) normalize_kernel(int64_t n, float* __rest
                                                          volatile double* hostOut, int slotNorm,
                                                          const double* __restrict__ gate, double eta2) {
     ef::dep_entry();
+    // |w|^2 over the CTA, 1/|w| by thread 0 (FP64), handed to the CTA through shared memory
     __shared__ double red[kFB / 32];
-    double t = 0.0;
-    for (int c = threadIdx.x; c < nParts; c += kFB) t += np[c];
-    t = cta_sum_fixed(t, red);
-    const float inv = t > 0.0 ? (float)(1.0 / sqrt(t)) : 0.f;
-    if (blockIdx.x == 0 && hostOut) {
-        if (threadIdx.x == 0) {
+    __shared__ float sInv;
+    const double t = cta_sum_fixed(np, nParts, red);
+    if (threadIdx.x == 0) {
+        sInv = t > 0.0 ? (float)(1.0 / sqrt(t)) : 0.f;
+        if (blockIdx.x == 0 && hostOut) {
             hostOut[slotNorm] = t;
             if (gate) hostOut[slotNorm - 1] = dgks_reorth(gate, nv, eta2) ? 1.0 : 0.0;
         }
-        if (hAcc)
-            for (int k = threadIdx.x; k < nv; k += kFB) hostOut[k] = hAcc[k];
     }
+    if (blockIdx.x == 0 && hostOut && hAcc)
+        for (int k = threadIdx.x; k < nv; k += kFB) hostOut[k] = hAcc[k];
+    __syncthreads();
+    const float inv = sInv;
+#pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * kFB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kFB) {
         const float v = w[i] * inv;
         w[i] = v;
@@ -439,8 +444,8 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
         EF_CUDA(ef::launch_dep(cgs_axpy_kernel, nPart, kFB, 0, s, n, nv, V, ldv, hTmp, w, partN, hG, eta2));
         EF_CUDA(ef::launch_dep(cgs_accumulate_kernel, 1, kMaxBasis, 0, s, nv, hG, hTmp, hAcc, eta2));
     }
-    // every normalisation CTA sums all nPart parts: a quarter of the CTAs
-    EF_CUDA(ef::launch_dep(normalize_kernel, std::max(1, nPart / 4), kFB, 0, s, n, w, w2, partN, nPart, re ? hAcc : hG,
+    // every normalisation CTA sums all nPart parts (from L2) and scales its share of w
+    EF_CUDA(ef::launch_dep(normalize_kernel, nPart, kFB, 0, s, n, w, w2, partN, nPart, re ? hAcc : hG,
             nv, hostOut, slotNorm, re ? hG : nullptr, eta2));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
@@ -450,7 +455,7 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
 ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
                                     int slotNorm, cudaStream_t s) {
     EF_CUDA(ef::launch_dep(multidot_partial_kernel, nPart, kFB, 0, s, n, 1, w, n, w, part, nullptr, 0, 0.0));
-    EF_CUDA(ef::launch_dep(normalize_kernel, std::max(1, nPart / 4), kFB, 0, s, n, w, w2, part, nPart, nullptr, 0,
+    EF_CUDA(ef::launch_dep(normalize_kernel, nPart, kFB, 0, s, n, w, w2, part, nPart, nullptr, 0,
             hostOut, slotNorm, nullptr, 0.0));
     EF_CUDA(cudaGetLastError());
     return EF_OK;

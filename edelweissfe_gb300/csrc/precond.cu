@@ -321,6 +321,17 @@ ef_status amg_build(ef_ctx* c) {
             L.saW = dalloc<float>(1, &st);
             L.saC = dalloc<float>((size_t)std::max<int64_t>(1, L.saNP) * BCo, &st);
             if (!L.saPv || !L.saAPv || !L.saW || !L.saC) return st;
+            {
+                // AP by groups of finer rows where their pair products fit the shared memory
+                const int G = ef_sa_ap_rows();
+                int64_t cap = 0;
+                for (int r0 = 0; r0 < nFine; r0 += G)
+                    cap = std::max(cap, SA.apSeg[SA.apRowPtr[std::min(r0 + G, nFine)]] - SA.apSeg[SA.apRowPtr[r0]]);
+                if (cap > 0 && ef_sa_ap_rows_smem(bfL, (int)std::min<int64_t>(cap, 1 << 20)) <= 48 * 1024) {
+                    EF_CHECK(upload(&L.saApRowPtr, SA.apRowPtr));
+                    L.saApCap = (int)cap;
+                }
+            }
             if (c->saTransfer == 2 && L.saNP > 0) {
                 // one-pass transfers where the prolongation's block products of a group of
                 // consecutive finer rows fit the shared memory
@@ -734,12 +745,13 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
             // smoothed prolongator P = P_t - 4 / (3 lambda) D^-1 A P_t of the finer level (its lambda
             // from the power iteration on the device), then A P and P^T A P
             const float* fBinv = fine ? (const float*)c->dBinv : c->amg[l - 1].binv;
+            const int nFiner = fine ? (int)c->nNodes : c->amg[l - 1].nN;
             if (power) EF_CHECK(amg_power(c, (int)l, s));
             EF_CHECK(ef_launch_sa_damping(c->amgNorms + 3 * ((int)l * kPowerSteps + kPowerSteps - 1), L.saW, s));
             EF_CHECK(ef_launch_sa_setup(fine ? 3 : BCo, L.saNP, L.saPRow, L.saPCol, L.saPSeg, L.saPSrc, L.saNAP,
                                         L.saApRow, L.saApSeg, L.saApK, L.saApP, fCol, fVals, fMask, L.offs, L.agg,
                                         fBinv, L.saW, L.saPv, L.saAPv, L.nBlocks, L.saCSeg, L.saCP, L.saCAP,
-                                        L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
+                                        L.rowOfBlock, L.colIdx, L.dead, L.vals, nFiner, L.saApRowPtr, L.saApCap, s));
             if (L.saOnePass) EF_CHECK(ef_launch_sa_block_copy(fine ? 3 : BCo, L.saNP, L.saTIdx, L.saPv, L.saPT, s));
         } else {
             EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,

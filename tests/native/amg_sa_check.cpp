@@ -205,6 +205,15 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     for (int64_t a = 0; a < nAP; ++a)
         ef::sa_ap_block<BF>(a, apRow.data(), S.apSeg.data(), S.apK.data(), S.apP.data(), colIdx.data(), vals.data(), fm,
                             Pv.data(), APv.data());
+    // AP by pairs (the row-group kernel): each pair's product, then the sums of each AP block's pairs
+    std::vector<float> APv2(nAP * BF * BC, 0.f);
+    for (int m = 0; m < nF; ++m)
+        for (int32_t a = S.apRowPtr[m]; a < S.apRowPtr[m + 1]; ++a)
+            for (int64_t t = S.apSeg[a]; t < S.apSeg[a + 1]; ++t) {
+                float cpair[BF * BC];
+                ef::sa_ap_pair<BF>(t, m, S.apK.data(), S.apP.data(), colIdx.data(), vals.data(), fm, Pv.data(), cpair);
+                for (int p = 0; p < BF * BC; ++p) APv2[(size_t)a * BF * BC + p] += cpair[p];
+            }
     for (int64_t c = 0; c < nCb; ++c)
         ef::sa_galerkin_block<BF>(c, S.cSeg.data(), S.cP.data(), S.cAP.data(), Pv.data(), APv.data(), cRob.data(),
                                   S.cCol.data(), dead.data(), Acv.data());
@@ -293,7 +302,14 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (size_t i = 0; i < Acd.size(); ++i)
         if (!seenC[i]) oC = std::fmax(oC, std::fabs(Acd[i]));
-    double eR2 = 0, eX2 = 0, eR3 = 0, eX3 = 0;
+    double eR2 = 0, eX2 = 0, eR3 = 0, eX3 = 0, eAP2 = 0;
+    for (int m = 0; m < nF; ++m)
+        for (int b = S.apRowPtr[m]; b < S.apRowPtr[m + 1]; ++b)
+            for (int a = 0; a < BF; ++a)
+                for (int j = 0; j < BC; ++j) {
+                    const size_t di = (size_t)(BF * m + a) * nc + BC * S.apCol[b] + j;
+                    eAP2 = std::fmax(eAP2, std::fabs(APv2[(size_t)b * BF * BC + a * BC + j] - APd[di]));
+                }
     for (int i = 0; i < nc; ++i) eR = std::fmax(eR, std::fabs(rc[i] - rcd[i]));
     for (int i = 0; i < n; ++i) eX = std::fmax(eX, std::fabs(xf[i] - xd[i]));
     for (int i = 0; i < nc; ++i) eR2 = std::fmax(eR2, std::fabs(rc2[i] - rcd[i]));
@@ -305,7 +321,7 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     int fails = 0;
     fails += !(eP <= tol * sP) + !(eAP <= tol * sAP) + !(eC <= tol * sC) + !(eR <= tol * sR) + !(eX <= tol * sX);
     fails += !(eR2 <= tol * sR) + !(eX2 <= tol * sX);
-    fails += !(eR3 <= tol * sR) + !(eX3 <= tol * sX);
+    fails += !(eR3 <= tol * sR) + !(eX3 <= tol * sX) + !(eAP2 <= tol * sAP);
     fails += (oP != 0.0) + (oAP != 0.0) + (oC != 0.0);
     // masked finer rows: P exactly zero
     for (int m = 0; m < nF; ++m)
@@ -314,9 +330,10 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
             for (int b = S.pRowPtr[m]; b < S.pRowPtr[m + 1]; ++b)
                 for (int j = 0; j < BC; ++j) fails += Pv[(size_t)b * BF * BC + a * BC + j] != 0.f;
         }
-    std::printf("%s: P %lld blocks, AP %lld, coarse %lld; rel diff P %.1e AP %.1e Ac %.1e restrict %.1e "
+    std::printf("%s: P %lld blocks, AP %lld, coarse %lld; rel diff P %.1e AP %.1e (pairs %.1e) Ac %.1e restrict %.1e "
                 "prolong %.1e (two-stage %.1e %.1e, one-pass %.1e %.1e); outside patterns %.1e %.1e %.1e; failures %d\n",
-                name, (long long)nP, (long long)nAP, (long long)nCb, eP / sP, eAP / sAP, eC / sC, eR / sR, eX / sX,
+                name, (long long)nP, (long long)nAP, (long long)nCb, eP / sP, eAP / sAP, eAP2 / sAP, eC / sC, eR / sR,
+                eX / sX,
                 eR2 / sR, eX2 / sX, eR3 / sR, eX3 / sX, oP, oAP, oC, fails);
     return fails;
 }
