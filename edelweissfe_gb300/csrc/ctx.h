@@ -171,11 +171,12 @@ ef_status ef_launch_newton_first(int64_t n, const double* P, const double* PExt,
 ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
                                  cudaStream_t s);
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
-                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
                                cudaStream_t s);
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
-                                     const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s);
+                                     const uint8_t* mask, float* t, const float* binv, float omega, int split,
+                                     cudaStream_t s);
 
 using namespace ef;
 
@@ -407,6 +408,8 @@ struct ef_ctx {
     int sellSlices = 0;
     int64_t sellE = 0;                     // slots (32 x the sum of the slice widths)
     int64_t* dSellOff = nullptr;           // [sellSlices + 1] first slot of each slice
+    int sellSplit = 4;                     // warps per slice of the BF16 sweep: 1, 2, 4 or 8 (EF_SELL_SPLIT)
+    int sellSplitProduct = 1;              // the same for the FP32 product (EF_SELL_SPLIT_PRODUCT)
     int32_t* dSellPerm = nullptr;          // [nNodes] block row of each SELL row (null: identity)
     int32_t* dSellCol = nullptr;           // [sellE] block column (padding: the row itself)
     int32_t* dSellSrc = nullptr;           // [sellE] source block in the BSR values (-1: padding)

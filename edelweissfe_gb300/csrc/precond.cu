@@ -69,6 +69,13 @@ static ef_status sell_build(ef_ctx* c) {
     c->sellMode = 0;
     if (const char* e = getenv("EF_SELL"))
         if (atoi(e) == 0) return EF_OK;
+    auto split = [](const char* e, int dflt) {
+        if (!e) return dflt;
+        const int k = atoi(e);
+        return (k == 1 || k == 2 || k == 4 || k == 8) ? k : dflt;
+    };
+    c->sellSplit = split(getenv("EF_SELL_SPLIT"), c->sellSplit);
+    c->sellSplitProduct = split(getenv("EF_SELL_SPLIT_PRODUCT"), c->sellSplitProduct);
     const int n0 = (int)c->nNodes;
     const std::vector<int32_t>& rp = c->hRowPtr0;
     const std::vector<int32_t>& ci = c->hColIdx0;
@@ -166,12 +173,12 @@ ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_SWEEPS")) c->amgSweeps = std::max(1, atoi(e));
     c->amgPre = c->amgPost = c->amgSweeps;
     if (const char* e = getenv("EF_AMG_PRE")) c->amgPre = std::max(0, atoi(e));  // 0: no pre-smoothing
-    if (const char* e = getenv("EF_AMG_POST")) c->amgPost = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_POST")) c->amgPost = std::max(0, atoi(e));  // 0: no post-smoothing
     if (const char* e = getenv("EF_AMG_WLEVELS")) c->amgWLevels = std::max(0, atoi(e));
     c->amgPreC = c->amgPre;
     c->amgPostC = c->amgPost;
     if (const char* e = getenv("EF_AMG_PRE_COARSE")) c->amgPreC = std::max(0, atoi(e));
-    if (const char* e = getenv("EF_AMG_POST_COARSE")) c->amgPostC = std::max(1, atoi(e));
+    if (const char* e = getenv("EF_AMG_POST_COARSE")) c->amgPostC = std::max(0, atoi(e));
     if (const char* e = getenv("EF_AMG_ALPHA")) c->amgAlpha = (float)atof(e);
     if (const char* e = getenv("EF_AMG_CYCLE")) c->amgCycle = std::max(1, atoi(e));
     if (const char* e = getenv("EF_AMG_BF16")) c->amgBf16 = atoi(e) != 0;
@@ -487,7 +494,7 @@ static ef_status amg_prepare_cluster(ef_ctx* c) {
     c->clusterLevel = -1;
     c->nCoarseOps = 0;
     const int nL = (int)c->amg.size();
-    if (!c->amgCluster || c->amgCheb || c->amgSmoothed || c->amgPreC < 1) return EF_OK;
+    if (!c->amgCluster || c->amgCheb || c->amgSmoothed || c->amgPreC < 1 || c->amgPostC < 1) return EF_OK;
     int lc = -1;
     for (int l = 1; l < nL; ++l)
         if (c->amg[l].nN <= kClusterMaxNodes) {
@@ -802,7 +809,7 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
     auto fine_bf16 = [&](const float* xin, float* out, const float* bj, float om) -> ef_status {
         if (c->sellMode == 1)
             return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
-                                              c->dSellV1, xin, r, mask, out, bj, om, s);
+                                              c->dSellV1, xin, r, mask, out, bj, om, c->sellSplit, s);
         if (c->stageCap > 0)
             return ef_launch_level_residual_bf16_staged(c->nSM, c->stageCap, nN, c->nBlocks, rowPtr, colIdx,
                                                         c->dBsrValsH, xin, r, mask, out, s, bj, om);

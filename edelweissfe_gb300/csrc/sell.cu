@@ -26,10 +26,8 @@ namespace ef {
 
 constexpr int kSellThreads = 128;  // four warps per CTA
 constexpr int kSellSlicesPerCta = kSellThreads / 32;  // the product: a warp per slice
-// the BF16 sweep: two warps per slice, each taking half of the slice's entries (measured faster
-// for the sweep, 28.4 -> 26.6 us at 160k hex8; slower for the FP32 product, 36 -> 45 us)
-constexpr int kSellSplit = 2;
-constexpr int kSellSplitSlicesPerCta = kSellThreads / (32 * kSellSplit);
+// Split slices: S warps per slice, each taking a contiguous share of the slice's entries, four
+// warps per CTA up to S = 4 and S warps (one slice) above
 
 __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src, const float* __restrict__ bsr,
                                     float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1) {
@@ -56,37 +54,84 @@ __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src,
     }
 }
 
-// y = K x on the free DOFs (0 on masked rows); COPY: xcopy = x as well
-template <bool COPY>
-__global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nSlices, const int64_t* __restrict__ off,
-                                                                  const int32_t* __restrict__ perm,
-                                                                  const int32_t* __restrict__ col,
-                                                                  const float* __restrict__ v9,
-                                                                  const float* __restrict__ x,
-                                                                  const uint8_t* __restrict__ mask,
-                                                                  float* __restrict__ y, float* __restrict__ xcopy) {
-    ef::dep_entry();
-    const int lane = threadIdx.x & 31;
-    const int sl = blockIdx.x * kSellSlicesPerCta + (threadIdx.x >> 5);
-    if (sl >= nSlices) return;
-    const int64_t e0 = off[sl];
-    const int w = (int)((off[sl + 1] - e0) >> 5);
-    const int32_t* cs = col + e0 + lane;
-    const float* vs = v9 + 9 * e0 + lane;
-    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-#pragma unroll 3
-    for (int j = 0; j < w; ++j) {
-        const int c3 = 3 * __ldcs(cs + 32 * j);
-        const float* vv = vs + 288 * j;
-        const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
-        const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
-        const float a6 = __ldcs(vv + 192), a7 = __ldcs(vv + 224), a8 = __ldcs(vv + 256);
-        const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
-        y0 += a0 * x0 + a1 * x1 + a2 * x2;
-        y1 += a3 * x0 + a4 * x1 + a5 * x2;
-        y2 += a6 * x0 + a7 * x1 + a8 * x2;
+// The slice and entry range of this warp: warp h of the S warps of a slice takes entries
+// [j0, j1) = [ceil(h w / S), ceil((h + 1) w / S)) of its width w.  Returns false past the last
+// slice.
+struct SellPart {
+    int sl, h, lane, j0, j1;
+    int64_t e0;
+};
+constexpr int sell_split_threads(int S) { return S <= 4 ? kSellThreads : 32 * S; }
+template <int S>
+__device__ __forceinline__ bool sell_part(int nSlices, const int64_t* __restrict__ off, SellPart& p) {
+    constexpr int spc = sell_split_threads(S) / (32 * S);
+    p.lane = threadIdx.x & 31;
+    const int wi = threadIdx.x >> 5;
+    p.sl = blockIdx.x * spc + wi / S;
+    p.h = wi % S;
+    if (p.sl >= nSlices) return false;
+    p.e0 = off[p.sl];
+    const int w = (int)((off[p.sl + 1] - p.e0) >> 5);
+    p.j0 = (p.h * w + S - 1) / S;
+    p.j1 = ((p.h + 1) * w + S - 1) / S;
+    return true;
+}
+
+// the partial sums of warps 1..S-1 of a slice go through shared memory to warp 0, which adds them
+// after its own in warp order (a fixed order: deterministic)
+template <int S>
+__device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, float& y0, float& y1, float& y2) {
+    if constexpr (S == 1) {
+        return active;
+    } else {
+        constexpr int spc = sell_split_threads(S) / (32 * S);
+        __shared__ float part[spc][S - 1][3][32];
+        const int ls = (threadIdx.x >> 5) / S;
+        if (active && p.h > 0) {
+            part[ls][p.h - 1][0][p.lane] = y0;
+            part[ls][p.h - 1][1][p.lane] = y1;
+            part[ls][p.h - 1][2][p.lane] = y2;
+        }
+        __syncthreads();
+        if (!active || p.h != 0) return false;
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            y0 += part[ls][q][0][p.lane];
+            y1 += part[ls][q][1][p.lane];
+            y2 += part[ls][q][2][p.lane];
+        }
+        return true;
     }
-    const int r = sl * 32 + lane;
+}
+
+// y = K x on the free DOFs (0 on masked rows); COPY: xcopy = x as well; S warps per slice
+template <bool COPY, int S>
+__global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
+    int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
+    const int32_t* __restrict__ col, const float* __restrict__ v9, const float* __restrict__ x,
+    const uint8_t* __restrict__ mask, float* __restrict__ y, float* __restrict__ xcopy) {
+    ef::dep_entry();
+    SellPart p;
+    const bool active = sell_part<S>(nSlices, off, p);
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    if (active) {
+        const int32_t* cs = col + p.e0 + p.lane;
+        const float* vs = v9 + 9 * p.e0 + p.lane;
+#pragma unroll 3
+        for (int j = p.j0; j < p.j1; ++j) {
+            const int c3 = 3 * __ldcs(cs + 32 * j);
+            const float* vv = vs + 288 * j;
+            const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
+            const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
+            const float a6 = __ldcs(vv + 192), a7 = __ldcs(vv + 224), a8 = __ldcs(vv + 256);
+            const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
+            y0 += a0 * x0 + a1 * x1 + a2 * x2;
+            y1 += a3 * x0 + a4 * x1 + a5 * x2;
+            y2 += a6 * x0 + a7 * x1 + a8 * x2;
+        }
+    }
+    if (!sell_combine<S>(p, active, y0, y1, y2)) return;
+    const int r = p.sl * 32 + p.lane;
     if (r >= nN) return;
     const int m = perm ? perm[r] : r;
     const int d = 3 * m;
@@ -100,54 +145,17 @@ __global__ void __launch_bounds__(kSellThreads) sell_spmv3_kernel(int nN, int nS
     }
 }
 
-// The slice and entry range of this warp: warp h of a slice takes entries [j0, j1) of its width,
-// h = 0 the first half (rounded up).  Returns false past the last slice.
-struct SellPart {
-    int sl, h, lane, j0, j1;
-    int64_t e0;
-};
-__device__ __forceinline__ bool sell_part(int nSlices, const int64_t* __restrict__ off, SellPart& p) {
-    p.lane = threadIdx.x & 31;
-    const int wi = threadIdx.x >> 5;
-    p.sl = blockIdx.x * kSellSplitSlicesPerCta + wi / kSellSplit;
-    p.h = wi % kSellSplit;
-    if (p.sl >= nSlices) return false;
-    p.e0 = off[p.sl];
-    const int w = (int)((off[p.sl + 1] - p.e0) >> 5);
-    const int half = (w + 1) >> 1;
-    p.j0 = p.h ? half : 0;
-    p.j1 = p.h ? w : half;
-    return true;
-}
-
-// the second warp's partial sums of a slice go through shared memory to the first one, which adds
-// them after its own (a fixed order: deterministic)
-__device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, float& y0, float& y1, float& y2) {
-    __shared__ float part[kSellSplitSlicesPerCta][3][32];
-    const int ls = (threadIdx.x >> 5) / kSellSplit;
-    if (active && p.h == 1) {
-        part[ls][0][p.lane] = y0;
-        part[ls][1][p.lane] = y1;
-        part[ls][2][p.lane] = y2;
-    }
-    __syncthreads();
-    if (!active || p.h != 0) return false;
-    y0 += part[ls][0][p.lane];
-    y1 += part[ls][1][p.lane];
-    y2 += part[ls][2][p.lane];
-    return true;
-}
-
 // t = r - K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
-// t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy
-__global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
+// t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy; S warps per slice
+template <int S>
+__global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
     const float* __restrict__ binv, float omega) {
     ef::dep_entry();
     SellPart p;
-    const bool active = sell_part(nSlices, off, p);
+    const bool active = sell_part<S>(nSlices, off, p);
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
     if (active) {
         const int32_t* cs = col + p.e0 + p.lane;
@@ -167,7 +175,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_level3_bf16_kernel(
             y2 += a67.x * x0 + a67.y * x1 + w8 * x2;
         }
     }
-    if (!sell_combine(p, active, y0, y1, y2)) return;
+    if (!sell_combine<S>(p, active, y0, y1, y2)) return;
     const int rr = p.sl * 32 + p.lane;
     if (rr >= nN) return;
     const int m = perm ? perm[rr] : rr;
@@ -197,6 +205,10 @@ using namespace ef;
 static inline unsigned sell_grid(int nSlices) {
     return (unsigned)((nSlices + kSellSlicesPerCta - 1) / kSellSlicesPerCta);
 }
+static inline unsigned sell_split_grid(int nSlices, int S) {
+    const int spc = sell_split_threads(S) / (32 * S);
+    return (unsigned)((nSlices + spc - 1) / spc);
+}
 
 ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
                                  cudaStream_t s) {
@@ -208,26 +220,50 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
 }
 
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
-                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy,
+                               const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
                                cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
-    if (xcopy)
-        EF_CUDA(ef::launch_dep(sell_spmv3_kernel<true>, sell_grid(nSlices), kSellThreads, 0, s, nN, nSlices, off, perm,
-                col, v9, x, mask, y, xcopy));
-    else
-        EF_CUDA(ef::launch_dep(sell_spmv3_kernel<false>, sell_grid(nSlices), kSellThreads, 0, s, nN, nSlices, off, perm,
-                col, v9, x, mask, y, nullptr));
+#define EF_SPMV3(C_, S_)                                                                                           \
+    EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
+                           nN, nSlices, off, perm, col, v9, x, mask, y, xcopy))
+#define EF_SPMV3_S(C_)      \
+    if (split == 2)         \
+        EF_SPMV3(C_, 2);    \
+    else if (split == 4)    \
+        EF_SPMV3(C_, 4);    \
+    else if (split == 8)    \
+        EF_SPMV3(C_, 8);    \
+    else                    \
+        EF_SPMV3(C_, 1)
+    if (xcopy) {
+        EF_SPMV3_S(true);
+    } else {
+        EF_SPMV3_S(false);
+    }
+#undef EF_SPMV3_S
+#undef EF_SPMV3
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
-                                     const uint8_t* mask, float* t, const float* binv, float omega, cudaStream_t s) {
+                                     const uint8_t* mask, float* t, const float* binv, float omega, int split,
+                                     cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
-    EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel,
-            (unsigned)((nSlices + kSellSplitSlicesPerCta - 1) / kSellSplitSlicesPerCta), kSellThreads, 0, s, nN,
-            nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega));
+#define EF_L3(S_)                                                                                                   \
+    EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel<S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
+                           nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t,   \
+                           binv, omega))
+    if (split == 1)
+        EF_L3(1);
+    else if (split == 2)
+        EF_L3(2);
+    else if (split == 8)
+        EF_L3(8);
+    else
+        EF_L3(4);
+#undef EF_L3
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

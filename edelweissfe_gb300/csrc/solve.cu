@@ -151,7 +151,8 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         // w = K z_j straight into the next basis slot; z_j kept in Z
         if (c->sellMode == 1)
             EF_CHECK(ef_launch_sell_spmv3((int)c->nNodes, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol,
-                                          c->dSellV9, pz, c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
+                                          c->dSellV9, pz, c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n,
+                                          c->sellSplitProduct, s));
         else if (c->spCap > 0)
             EF_CHECK(ef_launch_spmv_f32_staged(c->nSM, c->spCap, (int)c->nNodes, c->dRowPtr, c->dColIdx,
                                                (const float*)c->dBsrVals, pz, c->dMask, V + (int64_t)(j + 1) * n,
@@ -428,11 +429,11 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
     auto sweep = [&]() {
         return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
                                           c->dSellV1, c->fineX, c->vcIn, c->dMask, c->fineT, (const float*)c->dBinv,
-                                          omega, s);
+                                          omega, c->sellSplit, s);
     };
     auto product = [&]() {
         return ef_launch_sell_spmv3(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV9, c->vcOut,
-                                    c->dMask, c->fineT, c->fgZ, s);
+                                    c->dMask, c->fineT, c->fgZ, c->sellSplitProduct, s);
     };
     for (int k = 0; k < 2; ++k) {
         auto run = [&]() { return k == 0 ? sweep() : product(); };
