@@ -343,6 +343,33 @@ EF_SA_HD void sa_prolong_apply(int m, const int32_t* __restrict__ pRowPtr, const
         if (!(mask && mask[BF * (int64_t)m + i])) x[BF * (int64_t)m + i] += alpha * s[i];
 }
 
+// Fused fine-level post-smoothing.  With one damped block-Jacobi sweep before and after the coarse
+// correction and the cycle started from zero, x1 = w D^-1 r, t = r - A x1, and after the coarse
+// correction e,
+//     x3 = x1 + a P e + w D^-1 (r - A (x1 + a P e)) = w D^-1 (r + t) + C e,
+//     C  = a (P - w D^-1 A P) = a (I - w D^-1 A) P     (the pattern of AP),
+// so the prolongation and the post-sweep become one product with C.  Block a = (m, J) of C from
+// AP block a and P block b = apToP[a] = (m, J) (or -1 when P has no such block).
+template <int BF>
+EF_SA_HD void sa_post_block(int64_t a, const int32_t* __restrict__ apRow, const int32_t* __restrict__ apToP,
+                            const float* __restrict__ Pv, const float* __restrict__ APv,
+                            const float* __restrict__ binv, float omega, float alpha, float C[BF * BC]) {
+    const int64_t m = apRow[a];
+    const int32_t b = apToP[a];
+    const float* B = binv + m * BF * BF;
+    const float* Q = APv + a * BF * BC;
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i)
+        EF_SA_UNROLL
+        for (int j = 0; j < BC; ++j) {
+            float z = 0.f;
+            EF_SA_UNROLL
+            for (int q = 0; q < BF; ++q) z += B[i * BF + q] * Q[q * BC + j];
+            const float p = b >= 0 ? Pv[(int64_t)b * BF * BC + i * BC + j] : 0.f;
+            C[i * BC + j] = alpha * (p - omega * z);
+        }
+}
+
 // One-pass transfers.  The prolongation reads P in its row order (Pv); the restriction reads a
 // copy of P in the transpose order (slot k holds block tIdx[k], rowT[k] = pRow[tIdx[k]]), so the
 // blocks of one coarse column are consecutive.  A thread takes one block: the BF x BC values are

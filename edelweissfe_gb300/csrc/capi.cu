@@ -238,6 +238,13 @@ void ef_destroy(ef_ctx* c) {
     F(c->dSellV9);
     F(c->dSellV8);
     F(c->dSellV1);
+    F(c->dPostOff);
+    F(c->dPostCol);
+    F(c->dPostSrc);
+    F(c->dPostApToP);
+    F(c->dPostQ0);
+    F(c->dPostQ1);
+    F(c->dPostQ2);
     F(c->dNodeDof);
     F(c->dCondPtr);
     F(c->dCondSrc);

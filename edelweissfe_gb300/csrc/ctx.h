@@ -178,6 +178,16 @@ ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, co
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
                                      cudaStream_t s);
 
+// fused fine-level post-smoothing x = w D^-1 (r + t) + C e with C = a (I - w D^-1 A) P (sell.cu):
+// C blocks per slot from the AP / P blocks, then the product
+ef_status ef_launch_sa_post_setup(int64_t nSlot, const int32_t* src, const int32_t* apRow, const int32_t* apToP,
+                                  const float* Pv, const float* APv, const float* binv, float omega, float alpha,
+                                  void* q0, void* q1, void* q2, cudaStream_t s);
+ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* col, const void* q0,
+                                  const void* q1, const void* q2, const float* e, const float* r, const float* t,
+                                  const float* binv, const uint8_t* mask, float omega, float* x, int split,
+                                  cudaStream_t s);
+
 using namespace ef;
 
 // error message of the calling thread (ef_last_error)
@@ -408,6 +418,13 @@ struct ef_ctx {
     int sellSlices = 0;
     int64_t sellE = 0;                     // slots (32 x the sum of the slice widths)
     int64_t* dSellOff = nullptr;           // [sellSlices + 1] first slot of each slice
+    // fused fine-level post-smoothing (EF_AMG_FUSED_POST): sliced layout of C over the fine rows
+    bool postFused = true;
+    int postSlices = 0;
+    int64_t postSlots = 0;
+    int64_t* dPostOff = nullptr;
+    int32_t *dPostCol = nullptr, *dPostSrc = nullptr, *dPostApToP = nullptr;
+    void *dPostQ0 = nullptr, *dPostQ1 = nullptr, *dPostQ2 = nullptr;
     int sellSplit = 4;                     // warps per slice of the BF16 sweep: 1, 2, 4 or 8 (EF_SELL_SPLIT)
     int sellSplitProduct = 1;              // the same for the FP32 product (EF_SELL_SPLIT_PRODUCT)
     int32_t* dSellPerm = nullptr;          // [nNodes] block row of each SELL row (null: identity)

@@ -163,6 +163,7 @@ ef_status amg_build(ef_ctx* c) {
     if (const char* e = getenv("EF_AMG_SMOOTHED")) c->amgSmoothed = atoi(e) != 0;
     if (const char* e = getenv("EF_SA_TWOSTAGE")) c->saTransfer = atoi(e) != 0 ? 1 : 0;
     if (const char* e = getenv("EF_SA_TRANSFER")) c->saTransfer = std::min(2, std::max(0, atoi(e)));
+    if (const char* e = getenv("EF_AMG_FUSED_POST")) c->postFused = atoi(e) != 0;
     // smoothed prolongators: one sweep before and after, V-cycle (the fastest cfg 2 load step of
     // 1/1, 2/2 x V, W on level 1); plain aggregation: two sweeps and a W-cycle on level 1
     if (c->amgSmoothed) {
@@ -338,6 +339,47 @@ ef_status amg_build(ef_ctx* c) {
                     EF_CHECK(upload(&L.saApRowPtr, SA.apRowPtr));
                     L.saApCap = (int)cap;
                 }
+            }
+            if (c->amg.empty() && c->postFused && c->sellMode == 1 && L.saNAP > 0) {
+                // fused fine-level post-smoothing: C in the pattern of AP, sliced over the fine rows
+                // (slices of 32 rows, column-major slots), and for each AP block its P block
+                const int nS = (nFine + 31) / 32;
+                std::vector<int64_t> poff(nS + 1, 0);
+                for (int sl = 0; sl < nS; ++sl) {
+                    int w = 0;
+                    for (int r = 32 * sl; r < std::min(32 * sl + 32, nFine); ++r)
+                        w = std::max(w, SA.apRowPtr[r + 1] - SA.apRowPtr[r]);
+                    poff[sl + 1] = poff[sl] + 32 * (int64_t)w;
+                }
+                const int64_t nSlot = poff[nS];
+                std::vector<int32_t> pcol(nSlot, 0), psrc(nSlot, -1), apToP(L.saNAP, -1);
+                for (int sl = 0; sl < nS; ++sl) {
+                    const int w = (int)((poff[sl + 1] - poff[sl]) / 32);
+                    for (int i = 0; i < 32; ++i) {
+                        const int m = 32 * sl + i;
+                        if (m >= nFine) continue;
+                        for (int j = 0; j < w; ++j) {
+                            const int64_t a = SA.apRowPtr[m] + j;
+                            if (a >= SA.apRowPtr[m + 1]) break;
+                            const int64_t t = poff[sl] + 32 * (int64_t)j + i;
+                            pcol[t] = SA.apCol[a];
+                            psrc[t] = (int32_t)a;
+                        }
+                    }
+                }
+                for (int m = 0; m < nFine; ++m)
+                    for (int32_t a = SA.apRowPtr[m]; a < SA.apRowPtr[m + 1]; ++a)
+                        apToP[a] = (int32_t)sa_find(SA.pCol, SA.pRowPtr[m], SA.pRowPtr[m + 1], SA.apCol[a]);
+                EF_CHECK(upload(&c->dPostOff, poff));
+                EF_CHECK(upload(&c->dPostCol, pcol));
+                EF_CHECK(upload(&c->dPostSrc, psrc));
+                EF_CHECK(upload(&c->dPostApToP, apToP));
+                c->dPostQ0 = dalloc<uint4>((size_t)nSlot, &st);
+                c->dPostQ1 = dalloc<uint4>((size_t)nSlot, &st);
+                c->dPostQ2 = dalloc<uint32_t>((size_t)nSlot, &st);
+                if (!c->dPostQ0 || !c->dPostQ1 || !c->dPostQ2) return st;
+                c->postSlices = nS;
+                c->postSlots = nSlot;
             }
             if (c->saTransfer == 2 && L.saNP > 0) {
                 // one-pass transfers where the prolongation's block products of a group of
@@ -778,6 +820,15 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
             EF_CHECK(amg_damping(c, s));
         }
     }
+    if (c->postSlots > 0) {
+        // C = a (I - w D^-1 A) P of the fine level for the fused post-smoothing (with the damping
+        // of this build; lagged, like P, when later systems reuse the coarse levels)
+        const AmgLevel& F0 = c->amg[0];
+        const float w0 = c->levelOmega.empty() ? c->amgOmega : c->levelOmega[0];
+        EF_CHECK(ef_launch_sa_post_setup(c->postSlots, c->dPostSrc, F0.saApRow, c->dPostApToP, F0.saPv, F0.saAPv,
+                                         (const float*)c->dBinv, w0, c->amgAlpha, c->dPostQ0, c->dPostQ1,
+                                         c->dPostQ2, s));
+    }
     c->amgStale = false;
     return nn_edge_refresh(c, s);
 }
@@ -866,6 +917,21 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;
         }
+    }
+    // fused fine-level cycle: x1 = w D^-1 r (above), t = r - A x1, the coarse correction e of the
+    // restricted t, then x = w D^-1 (r + t) + C e in one pass (the prolongation and the
+    // post-sweep of the same cycle)
+    if (fine && c->postSlots > 0 && fineH && c->sellMode == 1 && !c->amgCheb && nPre == 1 && nPost == 1 &&
+        c->amgSmoothed) {
+        EF_CHECK(fine_bf16(cur, t, nullptr, 0.f));
+        if (Cn.saOnePass)
+            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
+        else
+            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
+                                            Cn.dead, Cn.saC, Cn.r, s));
+        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
+        return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostCol, c->dPostQ0, c->dPostQ1,
+                                       c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
     }
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;

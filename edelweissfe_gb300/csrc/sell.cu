@@ -20,6 +20,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include "amg_sa_body.h"
 #include "ef_common.cuh"
 
 namespace ef {
@@ -198,6 +199,88 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel
     t[d + 2] = k2 ? x2 : x2 + omega * z2;
 }
 
+// ---- fused fine-level post-smoothing x = w D^-1 (r + t) + C e (amg_sa_body.h) ----------------
+//
+// C (3 x 6 blocks, the pattern of A P) in BF16, sliced like the fine system: slices of 32 finer
+// rows, slot e0 + 32 j + i holding row i's j-th block (padding: zero block, column 0); per slot
+// one 16-byte word with values 0..7, one with values 8..15 and one 4-byte word with 16..17.
+
+__device__ __forceinline__ uint32_t bf16x2_bits(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// slot t: C of AP block src[t] (or zeros)
+__global__ void sa_post_setup_kernel(int64_t nSlot, const int32_t* __restrict__ src, const int32_t* __restrict__ apRow,
+                                     const int32_t* __restrict__ apToP, const float* __restrict__ Pv,
+                                     const float* __restrict__ APv, const float* __restrict__ binv, float omega,
+                                     float alpha, uint4* __restrict__ q0, uint4* __restrict__ q1,
+                                     uint32_t* __restrict__ q2) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nSlot) return;
+    float C[18];
+    const int64_t a = src[t];
+    if (a >= 0) {
+        sa_post_block<3>(a, apRow, apToP, Pv, APv, binv, omega, alpha, C);
+    } else {
+#pragma unroll
+        for (int p = 0; p < 18; ++p) C[p] = 0.f;
+    }
+    q0[t] = make_uint4(bf16x2_bits(C[0], C[1]), bf16x2_bits(C[2], C[3]), bf16x2_bits(C[4], C[5]),
+                       bf16x2_bits(C[6], C[7]));
+    q1[t] = make_uint4(bf16x2_bits(C[8], C[9]), bf16x2_bits(C[10], C[11]), bf16x2_bits(C[12], C[13]),
+                       bf16x2_bits(C[14], C[15]));
+    q2[t] = bf16x2_bits(C[16], C[17]);
+}
+
+__device__ __forceinline__ float2 bf16x2_floats(uint32_t v) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v));
+}
+
+// x = w D^-1 (r + t) + sum over the row's C blocks of C e[col] (masked DOFs 0); S warps per slice
+template <int S>
+__global__ void __launch_bounds__(sell_split_threads(S)) sa_post_fused_kernel(
+    int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ col,
+    const uint4* __restrict__ q0, const uint4* __restrict__ q1, const uint32_t* __restrict__ q2,
+    const float* __restrict__ e, const float* __restrict__ r, const float* __restrict__ t,
+    const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega, float* __restrict__ x) {
+    ef::dep_entry();
+    SellPart p;
+    const bool active = sell_part<S>(nSlices, off, p);
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    if (active) {
+        const int32_t* cs = col + p.e0 + p.lane;
+        const uint4* a0 = q0 + p.e0 + p.lane;
+        const uint4* a1 = q1 + p.e0 + p.lane;
+        const uint32_t* a2 = q2 + p.e0 + p.lane;
+#pragma unroll 2
+        for (int j = p.j0; j < p.j1; ++j) {
+            const float* ev = e + 6 * (int64_t)__ldcs(cs + 32 * j);
+            const uint4 u = __ldcs(a0 + 32 * j), v = __ldcs(a1 + 32 * j);
+            const uint32_t w2 = __ldcs(a2 + 32 * j);
+            const float e0 = ev[0], e1 = ev[1], e2 = ev[2], e3 = ev[3], e4 = ev[4], e5 = ev[5];
+            const float2 c01 = bf16x2_floats(u.x), c23 = bf16x2_floats(u.y), c45 = bf16x2_floats(u.z);
+            const float2 c67 = bf16x2_floats(u.w), c89 = bf16x2_floats(v.x), cab = bf16x2_floats(v.y);
+            const float2 ccd = bf16x2_floats(v.z), cef = bf16x2_floats(v.w), cgh = bf16x2_floats(w2);
+            y0 += c01.x * e0 + c01.y * e1 + c23.x * e2 + c23.y * e3 + c45.x * e4 + c45.y * e5;
+            y1 += c67.x * e0 + c67.y * e1 + c89.x * e2 + c89.y * e3 + cab.x * e4 + cab.y * e5;
+            y2 += ccd.x * e0 + ccd.y * e1 + cef.x * e2 + cef.y * e3 + cgh.x * e4 + cgh.y * e5;
+        }
+    }
+    if (!sell_combine<S>(p, active, y0, y1, y2)) return;
+    const int m = p.sl * 32 + p.lane;
+    if (m >= nN) return;
+    const int d = 3 * m;
+    const float s0 = r[d] + t[d], s1 = r[d + 1] + t[d + 1], s2 = r[d + 2] + t[d + 2];
+    const float* B = binv + 9 * (int64_t)m;
+    const float z0 = B[0] * s0 + B[1] * s1 + B[2] * s2;
+    const float z1 = B[3] * s0 + B[4] * s1 + B[5] * s2;
+    const float z2 = B[6] * s0 + B[7] * s1 + B[8] * s2;
+    x[d] = mask[d] ? 0.f : omega * z0 + y0;
+    x[d + 1] = mask[d + 1] ? 0.f : omega * z1 + y1;
+    x[d + 2] = mask[d + 2] ? 0.f : omega * z2 + y2;
+}
+
 }  // namespace ef
 
 using namespace ef;
@@ -264,6 +347,38 @@ ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, co
     else
         EF_L3(4);
 #undef EF_L3
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_post_setup(int64_t nSlot, const int32_t* src, const int32_t* apRow, const int32_t* apToP,
+                                  const float* Pv, const float* APv, const float* binv, float omega, float alpha,
+                                  void* q0, void* q1, void* q2, cudaStream_t s) {
+    if (nSlot <= 0) return EF_OK;
+    sa_post_setup_kernel<<<(unsigned)((nSlot + 255) / 256), 256, 0, ef::counted(s)>>>(
+        nSlot, src, apRow, apToP, Pv, APv, binv, omega, alpha, (uint4*)q0, (uint4*)q1, (uint32_t*)q2);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* col, const void* q0,
+                                  const void* q1, const void* q2, const float* e, const float* r, const float* t,
+                                  const float* binv, const uint8_t* mask, float omega, float* x, int split,
+                                  cudaStream_t s) {
+    if (nSlices <= 0) return EF_OK;
+#define EF_POST(S_)                                                                                              \
+    EF_CUDA(ef::launch_dep(sa_post_fused_kernel<S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
+                           nN, nSlices, off, col, (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, e, r, t, \
+                           binv, mask, omega, x))
+    if (split == 1)
+        EF_POST(1);
+    else if (split == 2)
+        EF_POST(2);
+    else if (split == 8)
+        EF_POST(8);
+    else
+        EF_POST(4);
+#undef EF_POST
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -302,6 +302,30 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     }
     for (size_t i = 0; i < Acd.size(); ++i)
         if (!seenC[i]) oC = std::fmax(oC, std::fabs(Acd[i]));
+    // fused post-smoothing blocks C = alpha (P - omega D^-1 A P) in the pattern of AP
+    double eCp = 0, sCp = 0;
+    {
+        const float om = 0.7f, al = 0.9f;
+        std::vector<int32_t> apToP(nAP, -1);
+        for (int m = 0; m < nF; ++m)
+            for (int32_t a = S.apRowPtr[m]; a < S.apRowPtr[m + 1]; ++a)
+                apToP[a] = (int32_t)ef::sa_find(S.pCol, S.pRowPtr[m], S.pRowPtr[m + 1], S.apCol[a]);
+        for (int m = 0; m < nF; ++m)
+            for (int32_t a = S.apRowPtr[m]; a < S.apRowPtr[m + 1]; ++a) {
+                float C[BF * BC];
+                ef::sa_post_block<BF>(a, apRow.data(), apToP.data(), Pv.data(), APv.data(), binv.data(), om, al, C);
+                for (int i = 0; i < BF; ++i)
+                    for (int j = 0; j < BC; ++j) {
+                        const size_t col = BC * (size_t)S.apCol[a] + j;
+                        double z = 0.0;
+                        for (int q = 0; q < BF; ++q)
+                            z += (double)binv[(size_t)m * BF * BF + BF * i + q] * APd[(size_t)(BF * m + q) * nc + col];
+                        const double cd = al * (Ps[(size_t)(BF * m + i) * nc + col] - om * z);
+                        eCp = std::fmax(eCp, std::fabs(C[i * BC + j] - cd));
+                        sCp = std::fmax(sCp, std::fabs(cd));
+                    }
+            }
+    }
     double eR2 = 0, eX2 = 0, eR3 = 0, eX3 = 0, eAP2 = 0;
     for (int m = 0; m < nF; ++m)
         for (int b = S.apRowPtr[m]; b < S.apRowPtr[m + 1]; ++b)
@@ -321,7 +345,7 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
     int fails = 0;
     fails += !(eP <= tol * sP) + !(eAP <= tol * sAP) + !(eC <= tol * sC) + !(eR <= tol * sR) + !(eX <= tol * sX);
     fails += !(eR2 <= tol * sR) + !(eX2 <= tol * sX);
-    fails += !(eR3 <= tol * sR) + !(eX3 <= tol * sX) + !(eAP2 <= tol * sAP);
+    fails += !(eR3 <= tol * sR) + !(eX3 <= tol * sX) + !(eAP2 <= tol * sAP) + !(eCp <= tol * sCp);
     fails += (oP != 0.0) + (oAP != 0.0) + (oC != 0.0);
     // masked finer rows: P exactly zero
     for (int m = 0; m < nF; ++m)
@@ -331,10 +355,10 @@ static int check_level(const char* name, int gx, int gy, int gz, uint64_t seed, 
                 for (int j = 0; j < BC; ++j) fails += Pv[(size_t)b * BF * BC + a * BC + j] != 0.f;
         }
     std::printf("%s: P %lld blocks, AP %lld, coarse %lld; rel diff P %.1e AP %.1e (pairs %.1e) Ac %.1e restrict %.1e "
-                "prolong %.1e (two-stage %.1e %.1e, one-pass %.1e %.1e); outside patterns %.1e %.1e %.1e; failures %d\n",
+                "prolong %.1e (two-stage %.1e %.1e, one-pass %.1e %.1e); post C %.1e; outside patterns %.1e %.1e "
+                "%.1e; failures %d\n",
                 name, (long long)nP, (long long)nAP, (long long)nCb, eP / sP, eAP / sAP, eAP2 / sAP, eC / sC, eR / sR,
-                eX / sX,
-                eR2 / sR, eX2 / sX, eR3 / sR, eX3 / sX, oP, oAP, oC, fails);
+                eX / sX, eR2 / sR, eX2 / sX, eR3 / sR, eX3 / sX, eCp / sCp, oP, oAP, oC, fails);
     return fails;
 }
 

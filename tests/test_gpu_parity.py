@@ -572,6 +572,34 @@ def test_sliced_ell_fine_level_matches_the_csr_kernels(gpu_lib, monkeypatch, cas
     assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
 
 
+def test_fused_post_smoothing_matches_the_separate_kernels(gpu_lib, monkeypatch):
+    """The fine level's prolongation and post-sweep as one product x = w D^-1 (r + t) + C e with
+    C = a (I - w D^-1 A) P (the default) against the separate prolongation and BF16 sweep
+    (EF_AMG_FUSED_POST=0): the same 1e-8 solution in about the same number of FGMRES iterations
+    (C is rounded to BF16, the sweep's A likewise), and the same bits when the solve is repeated."""
+    rng = np.random.default_rng(23)
+    out = {}
+    for fused in ("0", "1"):
+        monkeypatch.setenv("EF_AMG_FUSED_POST", fused)
+        s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
+        if "b" not in out:
+            b = rng.normal(size=s.nDof)
+            b[s.dirIdxHost] = 1e-3 * rng.normal(size=s.dirIdxHost.size)
+            out["b"] = b
+        R = torch.as_tensor(out["b"], device="cuda")
+        s.linsolver.method = "fgmres"
+        s.linsolver.rtol = 1e-8
+        x = s.linearSolve(R).cpu().numpy()
+        assert s.lastSolveInfo.relResidual <= 1e-8
+        out[fused] = (x, s.lastSolveInfo.iterations)
+        if fused == "1":
+            assert np.array_equal(s.linearSolve(R).cpu().numpy(), x)
+        del s
+    (x0, i0), (x1, i1) = out["0"], out["1"]
+    assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0))
+    assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
+
+
 def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
     """The three forms of the smoothed-aggregation restriction and prolongation: one pass from
     plane-major copies of P (the default, EF_SA_TRANSFER=2), block products + sums (1) and the
