@@ -583,6 +583,59 @@ __global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int3
         resid6_row<false, false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega);
 }
 
+// Fused post-smoothing of a 6-DOF level (amg_sa_body.h): C = a (I - w D^-1 A) P in the pattern of
+// A P (FP32, rows in order), then x = w D^-1 (r + t) + C e with e the coarser level's correction.
+__global__ void sa_post6_setup_kernel(int64_t nAP, const int32_t* __restrict__ apRow,
+                                      const int32_t* __restrict__ apToP, const float* __restrict__ Pv,
+                                      const float* __restrict__ APv, const float* __restrict__ binv, float omega,
+                                      float alpha, float* __restrict__ C) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nAP) return;
+    float c[BC * BC];
+    sa_post_block<BC>(a, apRow, apToP, Pv, APv, binv, omega, alpha, c);
+#pragma unroll
+    for (int p = 0; p < BC * BC; ++p) C[a * BC * BC + p] = c[p];
+}
+
+// a warp per row m; lanes 6 k + i (k < 5) take component i of the row's blocks k, k + 5, ...;
+// the five partial sums of a component are added in a fixed order, then lanes i < 6 form
+// x[m][i] = w (D_m^-1 (r + t)_m)[i] + y[i] (dead DOFs 0)
+__global__ void __launch_bounds__(256) sa_post6_fused_kernel(int nN, const int32_t* __restrict__ rowPtr,
+                                                             const int32_t* __restrict__ col,
+                                                             const float* __restrict__ C, const float* __restrict__ e,
+                                                             const float* __restrict__ r, const float* __restrict__ t,
+                                                             const float* __restrict__ binv,
+                                                             const uint8_t* __restrict__ dead, float omega,
+                                                             float* __restrict__ x) {
+    ef::dep_entry();
+    const int lane = threadIdx.x & 31;
+    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (m >= nN) return;  // whole warps
+    const int k0 = lane / BC, i = lane % BC;
+    float y = 0.f;
+    if (k0 < 5)
+        for (int a = rowPtr[m] + k0; a < rowPtr[m + 1]; a += 5) {
+            const float* cr = C + (int64_t)a * BC * BC + i * BC;
+            const float* ev = e + BC * (int64_t)col[a];
+#pragma unroll
+            for (int j = 0; j < BC; ++j) y += cr[j] * ev[j];
+        }
+    // lane i gathers lanes i + 6, i + 12, i + 18, i + 24 in that order
+    float s = y;
+#pragma unroll
+    for (int k = 1; k < 5; ++k) {
+        const float v = __shfl_sync(0xffffffffu, y, (i + BC * k) & 31);
+        if (k0 == 0) s += v;
+    }
+    if (lane < BC) {
+        const float* B = binv + (int64_t)m * BC * BC + i * BC;
+        float z = 0.f;
+#pragma unroll
+        for (int q = 0; q < BC; ++q) z += B[q] * (r[BC * (int64_t)m + q] + t[BC * (int64_t)m + q]);
+        x[BC * (int64_t)m + i] = dead[BC * (int64_t)m + i] ? 0.f : omega * z + s;
+    }
+}
+
 // BF16 copy of FP32 values (coarse-level blocks for the smoothing residuals)
 __global__ void to_bf16_kernel(int64_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1119,6 +1172,25 @@ ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const 
         EF_CUDA(ef::launch_dep(level_residual6_kernel, nb_((int64_t)nN * 32, 256), 256, 0, s, nN, rowPtr, colIdx, vals,
                 x, r, mask, t, binv, omega, (const uint32_t*)valsH));
     EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_post6_setup(int64_t nAP, const int32_t* apRow, const int32_t* apToP, const float* Pv,
+                                   const float* APv, const float* binv, float omega, float alpha, float* C,
+                                   cudaStream_t s) {
+    if (nAP <= 0) return EF_OK;
+    sa_post6_setup_kernel<<<nb_(nAP, 128), 128, 0, ef::counted(s)>>>(nAP, apRow, apToP, Pv, APv, binv, omega, alpha,
+                                                                     C);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_post6_fused(int nN, const int32_t* rowPtr, const int32_t* col, const float* C, const float* e,
+                                   const float* r, const float* t, const float* binv, const uint8_t* dead,
+                                   float omega, float* x, cudaStream_t s) {
+    if (nN <= 0) return EF_OK;
+    EF_CUDA(ef::launch_dep(sa_post6_fused_kernel, nb_((int64_t)nN * 32, 256), 256, 0, s, nN, rowPtr, col, C, e, r, t,
+                           binv, dead, omega, x));
     return EF_OK;
 }
 

@@ -178,6 +178,13 @@ ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, co
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
                                      cudaStream_t s);
 
+// the same on a 6-DOF level (amg.cu): C FP32 in the pattern of A P, a warp per row
+ef_status ef_launch_sa_post6_setup(int64_t nAP, const int32_t* apRow, const int32_t* apToP, const float* Pv,
+                                   const float* APv, const float* binv, float omega, float alpha, float* C,
+                                   cudaStream_t s);
+ef_status ef_launch_sa_post6_fused(int nN, const int32_t* rowPtr, const int32_t* col, const float* C, const float* e,
+                                   const float* r, const float* t, const float* binv, const uint8_t* dead,
+                                   float omega, float* x, cudaStream_t s);
 // fused fine-level post-smoothing x = w D^-1 (r + t) + C e with C = a (I - w D^-1 A) P (sell.cu):
 // C blocks per slot from the AP / P blocks, then the product
 ef_status ef_launch_sa_post_setup(int64_t nSlot, const int32_t* src, const int32_t* apRow, const int32_t* apToP,
@@ -302,6 +309,10 @@ struct AmgLevel {
     float* saPT = nullptr;
     int32_t* saRowT = nullptr;
     int saCap = 0;
+    // fused post-smoothing of the finer level when it has 6 DOFs: C = a (I - w D^-1 A) P in the
+    // pattern of A P (rows, columns, C values, the P block of each AP block)
+    int32_t *postRowPtr = nullptr, *postCol = nullptr, *postApToP = nullptr;
+    float* postC = nullptr;
     int32_t* saApRowPtr = nullptr;  // AP row pointer, for the AP product by groups of rows (null: a thread
     int saApCap = 0;                // per AP block); saApCap bounds the pairs of a group
     bool saOnePass = false;  // this level's transfers run in one pass
@@ -316,7 +327,8 @@ struct AmgLevel {
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
                         (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC, (void*)saPT,
-                        (void*)saRowT, (void*)saApRowPtr})
+                        (void*)saRowT, (void*)saApRowPtr, (void*)postRowPtr, (void*)postCol,
+                        (void*)postApToP, (void*)postC})
             if (p) cudaFree(p);
     }
 };

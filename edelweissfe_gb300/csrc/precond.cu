@@ -381,6 +381,18 @@ ef_status amg_build(ef_ctx* c) {
                 c->postSlices = nS;
                 c->postSlots = nSlot;
             }
+            if (!c->amg.empty() && c->postFused && L.saNAP > 0) {
+                // fused post-smoothing of this 6-DOF finer level
+                std::vector<int32_t> apToP(L.saNAP, -1);
+                for (int m = 0; m < nFine; ++m)
+                    for (int32_t a = SA.apRowPtr[m]; a < SA.apRowPtr[m + 1]; ++a)
+                        apToP[a] = (int32_t)sa_find(SA.pCol, SA.pRowPtr[m], SA.pRowPtr[m + 1], SA.apCol[a]);
+                EF_CHECK(upload(&L.postRowPtr, SA.apRowPtr));
+                EF_CHECK(upload(&L.postCol, SA.apCol));
+                EF_CHECK(upload(&L.postApToP, apToP));
+                L.postC = dalloc<float>((size_t)L.saNAP * BCo * BCo, &st);
+                if (!L.postC) return st;
+            }
             if (c->saTransfer == 2 && L.saNP > 0) {
                 // one-pass transfers where the prolongation's block products of a group of
                 // consecutive finer rows fit the shared memory
@@ -829,6 +841,13 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
                                          (const float*)c->dBinv, w0, c->amgAlpha, c->dPostQ0, c->dPostQ1,
                                          c->dPostQ2, s));
     }
+    for (size_t l = 1; l < c->amg.size(); ++l) {  // the same for the 6-DOF levels
+        const AmgLevel& L = c->amg[l];
+        if (!L.postC) continue;
+        const float wl = l < c->levelOmega.size() ? c->levelOmega[l] : c->amgOmega;
+        EF_CHECK(ef_launch_sa_post6_setup(L.saNAP, L.saApRow, L.postApToP, L.saPv, L.saAPv, c->amg[l - 1].binv, wl,
+                                          c->amgAlpha, L.postC, s));
+    }
     c->amgStale = false;
     return nn_edge_refresh(c, s);
 }
@@ -933,8 +952,22 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
         return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostCol, c->dPostQ0, c->dPostQ1,
                                        c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
     }
+    // the same fusion on a 6-DOF level
+    const int repsC = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
+    if (!fine && Cn.postC && !c->amgCheb && nPre == 1 && nPost == 1 && repsC == 1 && c->amgSmoothed &&
+        l != c->clusterLevel) {
+        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s, nullptr, 0.f, valsH));
+        if (Cn.saOnePass)
+            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
+        else
+            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
+                                            Cn.dead, Cn.saC, Cn.r, s));
+        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
+        return ef_launch_sa_post6_fused(nN, Cn.postRowPtr, Cn.postCol, Cn.postC, Cn.x, r, t, binv, mask, omega, x,
+                                        s);
+    }
     // coarse correction (repeated for a W-cycle below the finest level)
-    const int reps = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
+    const int reps = repsC;
     for (int rep = 0; rep < reps; ++rep) {
         const float* res = t;  // the residual the restriction reads: r itself while the iterate is zero
         if (!c->amgCheb && nPre == 0 && rep == 0) {
