@@ -510,7 +510,7 @@ __device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __res
                                            const int32_t* __restrict__ colIdx, const float* __restrict__ vals,
                                            const float* x, const float* r, const uint8_t* __restrict__ mask, float* t,
                                            const float* __restrict__ binv, float omega,
-                                           const uint32_t* __restrict__ valsH = nullptr) {
+                                           const uint32_t* __restrict__ valsH = nullptr, float ys = 1.f) {
     const int g = lane / BC, ri = lane - BC * g;
     float acc = 0.f;
     if (g < 5) {
@@ -561,7 +561,7 @@ __device__ __forceinline__ void resid6_row(int m, int lane, const int32_t* __res
             smooth_row<BC, CG>(m, lane, y, x, r, mask, binv, omega, t);
         } else {
             const int d = BC * m + lane;
-            stv<CG>(t + d, (mask && mask[d]) ? 0.f : ldv<CG>(r + d) - yi);
+            stv<CG>(t + d, (mask && mask[d]) ? 0.f : ldv<CG>(r + d) - ys * yi);
         }
     }
 }
@@ -572,15 +572,38 @@ __global__ void __launch_bounds__(256) level_residual6_kernel(int nN, const int3
                                                                const float* __restrict__ x, const float* __restrict__ r,
                                                                const uint8_t* __restrict__ mask, float* __restrict__ t,
                                                                const float* __restrict__ binv, float omega,
-                                                               const uint32_t* __restrict__ valsH) {
+                                                               const uint32_t* __restrict__ valsH, float ys) {
     ef::dep_entry();
     const int lane = threadIdx.x & 31;
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (m >= nN) return;
     if (valsH)
-        resid6_row<false, true>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, valsH);
+        resid6_row<false, true>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, valsH, ys);
     else
-        resid6_row<false, false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega);
+        resid6_row<false, false>(m, lane, rowPtr, colIdx, vals, x, r, mask, t, binv, omega, nullptr, ys);
+}
+
+// B = A (M D^-1) on a 6-DOF level: block k of A times the block inverse of its column node with
+// the rows of dead DOFs zeroed (the block-Jacobi sweep from zero, x1 = w M D^-1 r, then has the
+// residual r - A x1 = r - w B r)
+__global__ void scale_blocks6_kernel(int64_t nB, const int32_t* __restrict__ colIdx, const float* __restrict__ vals,
+                                     const float* __restrict__ binv, const uint8_t* __restrict__ dead,
+                                     float* __restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nB) return;
+    const int64_t c = colIdx[k];
+    const float* A = vals + k * BC * BC;
+    const float* D = binv + c * BC * BC;
+    float* O = out + k * BC * BC;
+#pragma unroll
+    for (int i = 0; i < BC; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            float z = 0.f;
+#pragma unroll
+            for (int q = 0; q < BC; ++q) z += dead[BC * c + q] ? 0.f : A[i * BC + q] * D[q * BC + j];
+            O[i * BC + j] = z;
+        }
 }
 
 // Fused post-smoothing of a 6-DOF level (amg_sa_body.h): C = a (I - w D^-1 A) P in the pattern of
@@ -1164,13 +1187,26 @@ ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* m
 // binv == nullptr: t = r - A x; otherwise one smoothing sweep t = x + omega D^-1 (r - A x)
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
-                                   const float* binv, float omega, const void* valsH) {
-    if (bs == 3)
+                                   const float* binv, float omega, const void* valsH, float ys) {
+    if (bs == 3) {
+        if (ys != 1.f) {
+            ef_set_error("level residual: a scaled product is implemented for 6-DOF levels only");
+            return EF_ERR_ARG;
+        }
         EF_CUDA(ef::launch_dep(level_residual_kernel<3>, nb_((int64_t)nN * 8, 256), 256, 0, s, nN, rowPtr, colIdx, vals,
                 x, r, mask, t, binv, omega));
-    else
+    } else {
         EF_CUDA(ef::launch_dep(level_residual6_kernel, nb_((int64_t)nN * 32, 256), 256, 0, s, nN, rowPtr, colIdx, vals,
-                x, r, mask, t, binv, omega, (const uint32_t*)valsH));
+                x, r, mask, t, binv, omega, (const uint32_t*)valsH, ys));
+    }
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_scale_blocks6(int64_t nB, const int32_t* colIdx, const float* vals, const float* binv,
+                                  const uint8_t* dead, float* out, cudaStream_t s) {
+    if (nB <= 0) return EF_OK;
+    scale_blocks6_kernel<<<nb_(nB, 128), 128, 0, ef::counted(s)>>>(nB, colIdx, vals, binv, dead, out);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

@@ -46,9 +46,14 @@ ef_status ef_launch_galerkin(int bf, int64_t nCoarseBlocks, const int64_t* seg, 
 ef_status ef_launch_bj6_setup(int nN, const int64_t* diagPos, const float* vals, float* inv, cudaStream_t s);
 ef_status ef_launch_bj_apply(int bs, int nN, const float* binv, const uint8_t* mask, float omega, const float* r,
                              float* x, int accumulate, cudaStream_t s);
+// binv null: t = r - ys A x (ys != 1 on 6-DOF levels only); else one sweep t = x + omega D^-1 (r - A x)
 ef_status ef_launch_level_residual(int bs, int nN, const int32_t* rowPtr, const int32_t* colIdx, const float* vals,
                                    const float* x, const float* r, const uint8_t* mask, float* t, cudaStream_t s,
-                                   const float* binv = nullptr, float omega = 0.f, const void* valsH = nullptr);
+                                   const float* binv = nullptr, float omega = 0.f, const void* valsH = nullptr,
+                                   float ys = 1.f);
+// out = A (M D^-1) blockwise on a 6-DOF level (M: dead DOFs of the column node zeroed)
+ef_status ef_launch_scale_blocks6(int64_t nB, const int32_t* colIdx, const float* vals, const float* binv,
+                                  const uint8_t* dead, float* out, cudaStream_t s);
 ef_status ef_launch_to_bf16(int64_t n, const float* src, void* dst, cudaStream_t s);
 ef_status ef_launch_sa_damping(const double* n2, float* wP, cudaStream_t s);
 ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int32_t* pCol, const int64_t* pSeg,
@@ -169,14 +174,14 @@ ef_status ef_launch_newton_check(int64_t n, const double* P, const double* PExt,
 ef_status ef_launch_newton_first(int64_t n, const double* P, const double* PExt, int64_t nDir, const int64_t* dofs,
                                  const double* values, double* R, cudaStream_t s);
 ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
-                                 cudaStream_t s);
+                                 const int32_t* col, const float* binv, const uint8_t* mask, cudaStream_t s);
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
                                cudaStream_t s);
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
-                                     cudaStream_t s);
+                                     cudaStream_t s, float ys = 1.f);
 
 // the same on a 6-DOF level (amg.cu): C FP32 in the pattern of A P, a warp per row
 ef_status ef_launch_sa_post6_setup(int64_t nAP, const int32_t* apRow, const int32_t* apToP, const float* Pv,
@@ -296,6 +301,7 @@ struct AmgLevel {
     float *x = nullptr, *r = nullptr, *t = nullptr;  // V-cycle work vectors of this level
     float* x2 = nullptr;                             // second smoothing iterate (sweeps alternate)
     uint16_t* valsH = nullptr;                       // BF16 copy of vals for the smoothing residuals
+    float* valsB = nullptr;  // A (M D^-1) blockwise, for the fused cycle's residual without a pre-sweep launch
     // smoothed aggregation (transition from the finer level to this one): index maps and values
     int64_t saNP = 0, saNAP = 0;
     int32_t *saPRowPtr = nullptr, *saPCol = nullptr, *saPRow = nullptr, *saPSrc = nullptr;
@@ -327,7 +333,7 @@ struct AmgLevel {
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
                         (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC, (void*)saPT,
-                        (void*)saRowT, (void*)saApRowPtr, (void*)postRowPtr, (void*)postCol,
+                        (void*)saRowT, (void*)saApRowPtr, (void*)postRowPtr, (void*)postCol, (void*)valsB,
                         (void*)postApToP, (void*)postC})
             if (p) cudaFree(p);
     }
@@ -432,6 +438,7 @@ struct ef_ctx {
     int64_t* dSellOff = nullptr;           // [sellSlices + 1] first slot of each slice
     // fused fine-level post-smoothing (EF_AMG_FUSED_POST): sliced layout of C over the fine rows
     bool postFused = true;
+    bool sellScaled = false;  // the BF16 fine copy holds K (M D^-1) (fused cycle: no pre-sweep launch)
     int postSlices = 0;
     int64_t postSlots = 0;
     int64_t* dPostOff = nullptr;

@@ -153,7 +153,8 @@ ef_status sell_refresh(ef_ctx* c, cudaStream_t s) {
     EF_CHECK(sell_build(c));
     if (c->sellMode != 1 || !c->sellStale) return EF_OK;
     EF_CHECK(ef_launch_sell_refresh(c->sellE, c->dSellSrc, (const float*)c->dBsrVals, c->dSellV9, c->dSellV8,
-                                    c->dSellV1, s));
+                                    c->dSellV1, c->dSellCol, c->sellScaled ? (const float*)c->dBinv : nullptr,
+                                    c->dMask, s));
     c->sellStale = false;
     return EF_OK;
 }
@@ -443,6 +444,19 @@ ef_status amg_build(ef_ctx* c) {
     const int nc = BCo * c->amg.back().nN;
     c->amgCoarsestInv = dalloc<float>((size_t)nc * nc, &st);
     if (!c->amgCoarsestInv) return st;
+    // fused cycles without a pre-sweep launch: the fine BF16 copy scaled to K (M D^-1), and
+    // B = A (M D^-1) beside each 6-DOF level whose cycle is fused (EF_AMG_SCALED=0: keep the sweep)
+    bool scaled = true;
+    if (const char* e = getenv("EF_AMG_SCALED")) scaled = atoi(e) != 0;
+    const bool oneOne = c->amgPre == 1 && c->amgPost == 1 && !c->amgCheb && c->amgSmoothed;
+    c->sellScaled = scaled && oneOne && c->postSlots > 0 && c->amgBf16 && c->sellMode == 1;
+    c->sellStale = true;
+    if (scaled && c->amgPreC == 1 && c->amgPostC == 1 && !c->amgCheb && c->amgSmoothed)
+        for (size_t k = 0; k + 1 < c->amg.size(); ++k)
+            if (c->amg[k + 1].postC) {
+                c->amg[k].valsB = dalloc<float>((size_t)c->amg[k].nBlocks * BCo * BCo, &st);
+                if (!c->amg[k].valsB) return st;
+            }
     EF_CHECK(amg_workspace(c));
     c->amgStale = true;
     return EF_OK;
@@ -819,6 +833,7 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
                                         L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
         }
         EF_CHECK(ef_launch_bj6_setup(L.nN, L.diagPos, L.vals, L.binv, s));
+        if (L.valsB) EF_CHECK(ef_launch_scale_blocks6(L.nBlocks, L.colIdx, L.vals, L.binv, L.dead, L.valsB, s));
         if (L.valsH) EF_CHECK(ef_launch_to_bf16(L.nBlocks * BCo * BCo, L.vals, L.valsH, s));
     }
     const AmgLevel& C = c->amg.back();
@@ -924,6 +939,42 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
     const int nPre = fine ? c->amgPre : c->amgPreC, nPost = fine ? c->amgPost : c->amgPostC;
     float* cur = x;
     if (!c->amgCheb) cur = ((std::max(nPre, 1) + nPost) & 1) ? x : x2;
+    // Fused cycle (one sweep before and after, from zero): x1 = w M D^-1 r, t = r - A x1, the
+    // coarse correction e of the restricted t, then x = w D^-1 (r + t) + C e in one pass (the
+    // prolongation and the post-sweep).  With B = A (M D^-1) kept beside A (a scaled BF16 copy on
+    // the fine level, FP32 on a 6-DOF level) t = r - w B r needs no pre-sweep launch.
+    const int repsC = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
+    const bool fusedFine = fine && c->postSlots > 0 && fineH && c->sellMode == 1 && !c->amgCheb && nPre == 1 &&
+                           nPost == 1 && c->amgSmoothed;
+    const bool fusedCoarse = !fine && Cn.postC && !c->amgCheb && nPre == 1 && nPost == 1 && repsC == 1 &&
+                             c->amgSmoothed && l != c->clusterLevel;
+    if (fusedFine || fusedCoarse) {
+        const float* valsB = fine ? nullptr : c->amg[l - 1].valsB;
+        if (fusedFine && c->sellScaled) {
+            EF_CHECK(ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol,
+                                                c->dSellV8, c->dSellV1, r, r, mask, t, nullptr, 0.f, c->sellSplit, s,
+                                                omega));
+        } else if (fusedCoarse && valsB) {
+            EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, valsB, r, r, mask, t, s, nullptr, 0.f, nullptr,
+                                              omega));
+        } else {
+            EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, omega, r, x2, 0, s));
+            EF_CHECK(fusedFine ? fine_bf16(x2, t, nullptr, 0.f)
+                               : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x2, r, mask, t, s, nullptr,
+                                                          0.f, valsH));
+        }
+        if (Cn.saOnePass)
+            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
+        else
+            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
+                                            Cn.dead, Cn.saC, Cn.r, s));
+        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
+        if (fusedFine)
+            return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostCol, c->dPostQ0, c->dPostQ1,
+                                           c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
+        return ef_launch_sa_post6_fused(nN, Cn.postRowPtr, Cn.postCol, Cn.postC, Cn.x, r, t, binv, mask, omega, x,
+                                        s);
+    }
     // pre-smoothing from zero
     if (c->amgCheb) {
         EF_CHECK(chebyshev(true));
@@ -936,35 +987,6 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
             EF_CHECK(sweep(cur, nxt));
             cur = nxt;
         }
-    }
-    // fused fine-level cycle: x1 = w D^-1 r (above), t = r - A x1, the coarse correction e of the
-    // restricted t, then x = w D^-1 (r + t) + C e in one pass (the prolongation and the
-    // post-sweep of the same cycle)
-    if (fine && c->postSlots > 0 && fineH && c->sellMode == 1 && !c->amgCheb && nPre == 1 && nPost == 1 &&
-        c->amgSmoothed) {
-        EF_CHECK(fine_bf16(cur, t, nullptr, 0.f));
-        if (Cn.saOnePass)
-            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
-        else
-            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
-                                            Cn.dead, Cn.saC, Cn.r, s));
-        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostCol, c->dPostQ0, c->dPostQ1,
-                                       c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
-    }
-    // the same fusion on a 6-DOF level
-    const int repsC = (l > 0 && l <= c->amgWLevels && c->amgCycle > 1) ? c->amgCycle : 1;
-    if (!fine && Cn.postC && !c->amgCheb && nPre == 1 && nPost == 1 && repsC == 1 && c->amgSmoothed &&
-        l != c->clusterLevel) {
-        EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, cur, r, mask, t, s, nullptr, 0.f, valsH));
-        if (Cn.saOnePass)
-            EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
-        else
-            EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
-                                            Cn.dead, Cn.saC, Cn.r, s));
-        EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
-        return ef_launch_sa_post6_fused(nN, Cn.postRowPtr, Cn.postCol, Cn.postC, Cn.x, r, t, binv, mask, omega, x,
-                                        s);
     }
     // coarse correction (repeated for a W-cycle below the finest level)
     const int reps = repsC;

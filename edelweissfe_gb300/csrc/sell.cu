@@ -30,8 +30,13 @@ constexpr int kSellSlicesPerCta = kSellThreads / 32;  // the product: a warp per
 // Split slices: S warps per slice, each taking a contiguous share of the slice's entries, four
 // warps per CTA up to S = 4 and S warps (one slice) above
 
+// FP32 planes of K; the BF16 copy holds K, or with binv the blocks of K (M D^-1) (the block
+// inverse of the slot's column node with the rows of masked DOFs zeroed), for the residual of the
+// block-Jacobi sweep from zero: r - K (w M D^-1 r) = r - w (K M D^-1) r
 __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src, const float* __restrict__ bsr,
-                                    float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1) {
+                                    float* __restrict__ v9, uint4* __restrict__ v8, __nv_bfloat16* __restrict__ v1,
+                                    const int32_t* __restrict__ col, const float* __restrict__ binv,
+                                    const uint8_t* __restrict__ mask) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nE) return;
     const int64_t b = src[t];
@@ -47,6 +52,22 @@ __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src,
     float* d = v9 + 9 * (t - i) + i;
 #pragma unroll
     for (int k = 0; k < 9; ++k) d[32 * k] = a[k];
+    if (v8 && binv) {
+        const int64_t c = col[t];
+        const float* D = binv + 9 * c;
+        float sa[9];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                float z = 0.f;
+#pragma unroll
+                for (int u = 0; u < 3; ++u) z += mask[3 * c + u] ? 0.f : a[3 * p + u] * D[3 * u + q];
+                sa[3 * p + q] = z;
+            }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = sa[k];
+    }
     if (v8) {
         __nv_bfloat162 h[4] = {__floats2bfloat162_rn(a[0], a[1]), __floats2bfloat162_rn(a[2], a[3]),
                                __floats2bfloat162_rn(a[4], a[5]), __floats2bfloat162_rn(a[6], a[7])};
@@ -146,14 +167,14 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     }
 }
 
-// t = r - K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
+// t = r - ys K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
 // t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy; S warps per slice
 template <int S>
 __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
-    const float* __restrict__ binv, float omega) {
+    const float* __restrict__ binv, float omega, float ys) {
     ef::dep_entry();
     SellPart p;
     const bool active = sell_part<S>(nSlices, off, p);
@@ -182,7 +203,8 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel
     const int m = perm ? perm[rr] : rr;
     const int d = 3 * m;
     const bool k0 = mask[d], k1 = mask[d + 1], k2 = mask[d + 2];
-    const float t0 = k0 ? 0.f : r[d] - y0, t1 = k1 ? 0.f : r[d + 1] - y1, t2 = k2 ? 0.f : r[d + 2] - y2;
+    const float t0 = k0 ? 0.f : r[d] - ys * y0, t1 = k1 ? 0.f : r[d + 1] - ys * y1,
+                t2 = k2 ? 0.f : r[d + 2] - ys * y2;
     if (!binv) {
         t[d] = t0;
         t[d + 1] = t1;
@@ -294,10 +316,10 @@ static inline unsigned sell_split_grid(int nSlices, int S) {
 }
 
 ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bsr, float* v9, void* v8, void* v1,
-                                 cudaStream_t s) {
+                                 const int32_t* col, const float* binv, const uint8_t* mask, cudaStream_t s) {
     if (nE <= 0) return EF_OK;
     sell_refresh_kernel<<<(unsigned)((nE + 255) / 256), 256, 0, ef::counted(s)>>>(
-        nE, src, bsr, v9, (uint4*)v8, (__nv_bfloat16*)v1);
+        nE, src, bsr, v9, (uint4*)v8, (__nv_bfloat16*)v1, col, binv, mask);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
@@ -332,12 +354,12 @@ ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const in
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
-                                     cudaStream_t s) {
+                                     cudaStream_t s, float ys) {
     if (nSlices <= 0) return EF_OK;
 #define EF_L3(S_)                                                                                                   \
     EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel<S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
                            nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t,   \
-                           binv, omega))
+                           binv, omega, ys))
     if (split == 1)
         EF_L3(1);
     else if (split == 2)

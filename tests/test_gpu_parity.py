@@ -573,14 +573,17 @@ def test_sliced_ell_fine_level_matches_the_csr_kernels(gpu_lib, monkeypatch, cas
 
 
 def test_fused_post_smoothing_matches_the_separate_kernels(gpu_lib, monkeypatch):
-    """The fine level's prolongation and post-sweep as one product x = w D^-1 (r + t) + C e with
-    C = a (I - w D^-1 A) P (the default) against the separate prolongation and BF16 sweep
-    (EF_AMG_FUSED_POST=0): the same 1e-8 solution in about the same number of FGMRES iterations
-    (C is rounded to BF16, the sweep's A likewise), and the same bits when the solve is repeated."""
+    """Each level's prolongation and post-sweep as one product x = w D^-1 (r + t) + C e with
+    C = a (I - w D^-1 A) P, and the pre-sweep folded into the residual t = r - w A (M D^-1) r (the
+    default), against the fused post-smoothing with a pre-sweep launch (EF_AMG_SCALED=0) and the
+    separate prolongation and sweeps (EF_AMG_FUSED_POST=0): the same 1e-8 solution in about the
+    same number of FGMRES iterations (C and the fine blocks are rounded to BF16), and the same bits
+    when the default's solve is repeated."""
     rng = np.random.default_rng(23)
     out = {}
-    for fused in ("0", "1"):
-        monkeypatch.setenv("EF_AMG_FUSED_POST", fused)
+    for fused in ("0", "2", "1"):
+        monkeypatch.setenv("EF_AMG_FUSED_POST", "0" if fused == "0" else "1")
+        monkeypatch.setenv("EF_AMG_SCALED", "1" if fused == "1" else "0")
         s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
         if "b" not in out:
             b = rng.normal(size=s.nDof)
@@ -595,9 +598,11 @@ def test_fused_post_smoothing_matches_the_separate_kernels(gpu_lib, monkeypatch)
         if fused == "1":
             assert np.array_equal(s.linearSolve(R).cpu().numpy(), x)
         del s
-    (x0, i0), (x1, i1) = out["0"], out["1"]
-    assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0))
-    assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
+    x0, i0 = out["0"]
+    for fused in ("2", "1"):
+        x1, i1 = out[fused]
+        assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0)), fused
+        assert abs(i1 - i0) <= max(2, i0 // 10), (fused, i0, i1)
 
 
 def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
