@@ -8,15 +8,17 @@ assembly, Krylov solve, repeated until the reference's convergence test passes):
   plastic increment from the same committed state (the trial state is not accepted).
   Inputs are resident and larger than L2 (BSR system 159 MB FP32, element state 266 MB).
 
-value     : load-step seconds with FGMRES(64) preconditioned by the rigid-body aggregation
-            multigrid cycle plus the learned message-passing correction (trained on pairs from
-            the plain solves of the load history; a validation solve keeps it only if it makes
-            the step faster), FP32 inner iterations with FP64 refinement to 1e-8
+value     : load-step seconds with FGMRES(64) preconditioned by the smoothed-aggregation
+            multigrid cycle (fused one-pass kernels per level) plus the learned message-passing
+            correction when a validation solve shows that it makes the step faster (trained on
+            pairs from the plain solves of the load history), FP32 inner iterations with FP64
+            refinement to 1e-8
 comparison: the same load step with block-Jacobi PCG (same system, same tolerance)
 e2e       : the same as value through the public Python API with the step's inputs (U_n, dU)
             copied from pinned host memory and the results (U, P) read back every step
-roofline  : the fine-level FP32 BSR SpMV of FGMRES (the dominant kind of pass: every fine
-            smoothing residual and every Krylov product streams the same 159 MB of blocks)
+roofline  : the FGMRES product (the largest kernel of the step: FP32 sliced-ELL blocks, one
+            launch per iteration), timed live with CUDA events; the fused fine post-smoothing and
+            the fine residual (one launch each per iteration) beside it
 cpu_baseline: the numpy oracle (restatement of the reference's CPU path) on a bounded sample
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nx 100 --ny 40 --nz 40]
@@ -37,11 +39,12 @@ sys.path.insert(0, ROOT)
 
 PROPS = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
 METRIC = "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s"
-# DRAM bytes (read + write) per launch of the two fine-level kernels of the FGMRES solve on the
+# DRAM bytes (read + write) per launch of the fine-level kernels of the FGMRES solve on the
 # 100x40x40 box (509,343 DOF, 4,406,941 blocks), from one ncu capture of bench.py --profile
 # (profiles/sell_kernels_hex8_J2_100x40x40.md)
-SWEEP_TRAFFIC_BYTES = 106.28e6
-PRODUCT_TRAFFIC_BYTES = 185.74e6
+SWEEP_TRAFFIC_BYTES = 102.97e6
+PRODUCT_TRAFFIC_BYTES = 182.95e6
+POST_TRAFFIC_BYTES = 93.84e6
 # Newton iterations of the timed increment (13) of the 100x40x40 model: the same in the all-FP64
 # and the mixed-precision GPU solves; the CPU arms charge this many element passes and solves
 PCG_NEWTON_PER_STEP = 8
@@ -380,7 +383,7 @@ def run_ours(a):
     # the fine-level kernels timed live on the timed increment's last system (CUDA events, same stream)
     import ctypes
 
-    fk_ms, fk_bytes = (ctypes.c_double * 2)(), (ctypes.c_double * 2)()
+    fk_ms, fk_bytes = (ctypes.c_double * 3)(), (ctypes.c_double * 3)()
     fk_ok = lib.ef_fine_kernel_profile(s.ctx, 50, fk_ms, fk_bytes, stream.cuda_stream) == _lib.EF_OK
 
     # comparison arm: block-Jacobi PCG on the same load step
@@ -464,18 +467,24 @@ def run_ours(a):
     full = a.nx * a.ny * a.nz == 160000
     roofline = None
     if fk_ok:
-        sw_gbs = fk_bytes[0] / (fk_ms[0] * 1e-3) / 1e9
-        pr_gbs = fk_bytes[1] / (fk_ms[1] * 1e-3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "sell_level3_bf16_kernel (fine multigrid sweep / residual from the "
-                                              "sliced-ELL BF16 blocks; two launches per FGMRES iteration)",
-                    "achieved": sw_gbs, "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
-                    "frac": sw_gbs / peaks["hbm_gbs"], "traffic": SWEEP_TRAFFIC_BYTES if full else None,
-                    "traffic_source": "ncu (dram__bytes_read.sum + dram__bytes_write.sum per launch) of bench.py "
-                                      "--profile --method fgmres",
-                    "bytes_per_launch": fk_bytes[0], "avg_launch_ms": fk_ms[0], "timing": "CUDA events, 50 launches",
-                    "second": {"kernel": "sell_spmv3_kernel (FGMRES product K z, FP32 sliced-ELL)", "achieved": pr_gbs,
-                               "frac": pr_gbs / peaks["hbm_gbs"], "bytes_per_launch": fk_bytes[1],
-                               "avg_launch_ms": fk_ms[1], "traffic": PRODUCT_TRAFFIC_BYTES if full else None}}  # fmt: skip
+        def entry(k, kernel, traffic):
+            gbs = fk_bytes[k] / (fk_ms[k] * 1e-3) / 1e9
+            return {"kernel": kernel, "achieved": gbs, "frac": gbs / peaks["hbm_gbs"], "bytes_per_launch": fk_bytes[k],
+                    "avg_launch_ms": fk_ms[k], "traffic": traffic if full else None}
+
+        # the dominant kernel of the load step: the FGMRES product (one launch per iteration, the
+        # largest); the fused post-smoothing and the fine residual (one launch each per iteration) beside
+        roofline = entry(1, "sell_spmv3_kernel (FGMRES product K z, FP32 sliced-ELL; one launch per iteration)",
+                         PRODUCT_TRAFFIC_BYTES)
+        roofline.update({"bound": "hbm", "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
+                         "traffic_source": "ncu (dram__bytes_read.sum + dram__bytes_write.sum per launch) of "
+                                           "bench.py --profile --method fgmres",
+                         "timing": "CUDA events, 50 launches"})
+        if fk_ms[2] > 0:
+            roofline["second"] = entry(2, "sa_post_fused_kernel (fine prolongation + post-smoothing x = w D^-1 (r + t)"
+                                          " + C e, C in BF16)", POST_TRAFFIC_BYTES)
+        roofline["third"] = entry(0, "sell_level3_bf16_kernel (fine residual t = r - w K M D^-1 r, BF16 "
+                                     "sliced-ELL)", SWEEP_TRAFFIC_BYTES)
     pcg_bpi = pcg_bytes_per_iteration(info)
     pcg_gbs = pcg_bpi * pcg_it / (pcg_kms * 1e-3) / 1e9 if pcg_kms > 0 else None
     cpu = None

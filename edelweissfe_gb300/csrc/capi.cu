@@ -239,6 +239,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->dSellV8);
     F(c->dSellV1);
     F(c->dPostOff);
+    F(c->dPostPerm);
     F(c->dPostCol);
     F(c->dPostSrc);
     F(c->dPostApToP);

@@ -195,10 +195,10 @@ ef_status ef_launch_sa_post6_fused(int nN, const int32_t* rowPtr, const int32_t*
 ef_status ef_launch_sa_post_setup(int64_t nSlot, const int32_t* src, const int32_t* apRow, const int32_t* apToP,
                                   const float* Pv, const float* APv, const float* binv, float omega, float alpha,
                                   void* q0, void* q1, void* q2, cudaStream_t s);
-ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* col, const void* q0,
-                                  const void* q1, const void* q2, const float* e, const float* r, const float* t,
-                                  const float* binv, const uint8_t* mask, float omega, float* x, int split,
-                                  cudaStream_t s);
+ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                                  const void* q0, const void* q1, const void* q2, const float* e, const float* r,
+                                  const float* t, const float* binv, const uint8_t* mask, float omega, float* x,
+                                  int split, cudaStream_t s);
 
 using namespace ef;
 
@@ -442,6 +442,7 @@ struct ef_ctx {
     int postSlices = 0;
     int64_t postSlots = 0;
     int64_t* dPostOff = nullptr;
+    int32_t* dPostPerm = nullptr;  // fine row of each slot row (rows sorted by length within windows)
     int32_t *dPostCol = nullptr, *dPostSrc = nullptr, *dPostApToP = nullptr;
     void *dPostQ0 = nullptr, *dPostQ1 = nullptr, *dPostQ2 = nullptr;
     int sellSplit = 4;                     // warps per slice of the BF16 sweep: 1, 2, 4 or 8 (EF_SELL_SPLIT)

@@ -343,13 +343,19 @@ ef_status amg_build(ef_ctx* c) {
             }
             if (c->amg.empty() && c->postFused && c->sellMode == 1 && L.saNAP > 0) {
                 // fused fine-level post-smoothing: C in the pattern of AP, sliced over the fine rows
-                // (slices of 32 rows, column-major slots), and for each AP block its P block
+                // (slices of 32 rows, column-major slots; rows sorted by length within windows of
+                // 4096, as the A P rows run from 1 to 27 blocks), and for each AP block its P block
                 const int nS = (nFine + 31) / 32;
+                auto apLen = [&](int m) { return SA.apRowPtr[m + 1] - SA.apRowPtr[m]; };
+                std::vector<int32_t> pperm(nFine);
+                for (int m = 0; m < nFine; ++m) pperm[m] = m;
+                for (int w0 = 0; w0 < nFine; w0 += 4096)
+                    std::stable_sort(pperm.begin() + w0, pperm.begin() + std::min(w0 + 4096, nFine),
+                                     [&](int a, int b) { return apLen(a) > apLen(b); });
                 std::vector<int64_t> poff(nS + 1, 0);
                 for (int sl = 0; sl < nS; ++sl) {
                     int w = 0;
-                    for (int r = 32 * sl; r < std::min(32 * sl + 32, nFine); ++r)
-                        w = std::max(w, SA.apRowPtr[r + 1] - SA.apRowPtr[r]);
+                    for (int r = 32 * sl; r < std::min(32 * sl + 32, nFine); ++r) w = std::max(w, apLen(pperm[r]));
                     poff[sl + 1] = poff[sl] + 32 * (int64_t)w;
                 }
                 const int64_t nSlot = poff[nS];
@@ -357,8 +363,8 @@ ef_status amg_build(ef_ctx* c) {
                 for (int sl = 0; sl < nS; ++sl) {
                     const int w = (int)((poff[sl + 1] - poff[sl]) / 32);
                     for (int i = 0; i < 32; ++i) {
-                        const int m = 32 * sl + i;
-                        if (m >= nFine) continue;
+                        if (32 * sl + i >= nFine) continue;
+                        const int m = pperm[32 * sl + i];
                         for (int j = 0; j < w; ++j) {
                             const int64_t a = SA.apRowPtr[m] + j;
                             if (a >= SA.apRowPtr[m + 1]) break;
@@ -372,6 +378,7 @@ ef_status amg_build(ef_ctx* c) {
                     for (int32_t a = SA.apRowPtr[m]; a < SA.apRowPtr[m + 1]; ++a)
                         apToP[a] = (int32_t)sa_find(SA.pCol, SA.pRowPtr[m], SA.pRowPtr[m + 1], SA.apCol[a]);
                 EF_CHECK(upload(&c->dPostOff, poff));
+                EF_CHECK(upload(&c->dPostPerm, pperm));
                 EF_CHECK(upload(&c->dPostCol, pcol));
                 EF_CHECK(upload(&c->dPostSrc, psrc));
                 EF_CHECK(upload(&c->dPostApToP, apToP));
@@ -970,8 +977,8 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
                                             Cn.dead, Cn.saC, Cn.r, s));
         EF_CHECK(amg_vcycle(c, l + 1, Cn.r, Cn.x, s));
         if (fusedFine)
-            return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostCol, c->dPostQ0, c->dPostQ1,
-                                           c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
+            return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostPerm, c->dPostCol, c->dPostQ0,
+                                           c->dPostQ1, c->dPostQ2, Cn.x, r, t, binv, mask, omega, x, c->sellSplit, s);
         return ef_launch_sa_post6_fused(nN, Cn.postRowPtr, Cn.postCol, Cn.postC, Cn.x, r, t, binv, mask, omega, x,
                                         s);
     }

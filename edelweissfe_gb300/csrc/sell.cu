@@ -224,8 +224,9 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel
 // ---- fused fine-level post-smoothing x = w D^-1 (r + t) + C e (amg_sa_body.h) ----------------
 //
 // C (3 x 6 blocks, the pattern of A P) in BF16, sliced like the fine system: slices of 32 finer
-// rows, slot e0 + 32 j + i holding row i's j-th block (padding: zero block, column 0); per slot
-// one 16-byte word with values 0..7, one with values 8..15 and one 4-byte word with 16..17.
+// rows (in the order perm: sorted by length within windows), slot e0 + 32 j + i holding slice row
+// i's j-th block (padding: zero block, column 0); per slot one 16-byte word with values 0..7, one
+// with values 8..15 and one 4-byte word with 16..17.
 
 __device__ __forceinline__ uint32_t bf16x2_bits(float a, float b) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -262,7 +263,8 @@ __device__ __forceinline__ float2 bf16x2_floats(uint32_t v) {
 // x = w D^-1 (r + t) + sum over the row's C blocks of C e[col] (masked DOFs 0); S warps per slice
 template <int S>
 __global__ void __launch_bounds__(sell_split_threads(S)) sa_post_fused_kernel(
-    int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ col,
+    int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
+    const int32_t* __restrict__ col,
     const uint4* __restrict__ q0, const uint4* __restrict__ q1, const uint32_t* __restrict__ q2,
     const float* __restrict__ e, const float* __restrict__ r, const float* __restrict__ t,
     const float* __restrict__ binv, const uint8_t* __restrict__ mask, float omega, float* __restrict__ x) {
@@ -290,8 +292,9 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sa_post_fused_kernel(
         }
     }
     if (!sell_combine<S>(p, active, y0, y1, y2)) return;
-    const int m = p.sl * 32 + p.lane;
-    if (m >= nN) return;
+    const int rr = p.sl * 32 + p.lane;
+    if (rr >= nN) return;
+    const int m = perm ? perm[rr] : rr;
     const int d = 3 * m;
     const float s0 = r[d] + t[d], s1 = r[d + 1] + t[d + 1], s2 = r[d + 2] + t[d + 2];
     const float* B = binv + 9 * (int64_t)m;
@@ -383,15 +386,15 @@ ef_status ef_launch_sa_post_setup(int64_t nSlot, const int32_t* src, const int32
     return EF_OK;
 }
 
-ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* col, const void* q0,
-                                  const void* q1, const void* q2, const float* e, const float* r, const float* t,
-                                  const float* binv, const uint8_t* mask, float omega, float* x, int split,
-                                  cudaStream_t s) {
+ef_status ef_launch_sa_post_fused(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
+                                  const void* q0, const void* q1, const void* q2, const float* e, const float* r,
+                                  const float* t, const float* binv, const uint8_t* mask, float omega, float* x,
+                                  int split, cudaStream_t s) {
     if (nSlices <= 0) return EF_OK;
 #define EF_POST(S_)                                                                                              \
     EF_CUDA(ef::launch_dep(sa_post_fused_kernel<S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
-                           nN, nSlices, off, col, (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, e, r, t, \
-                           binv, mask, omega, x))
+                           nN, nSlices, off, perm, col, (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, e, r, \
+                           t, binv, mask, omega, x))
     if (split == 1)
         EF_POST(1);
     else if (split == 2)

@@ -426,7 +426,13 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
     cudaStream_t s = (cudaStream_t)stream;
     const int nN = (int)c->nNodes;
     const float omega = c->levelOmega.empty() ? c->amgOmega : c->levelOmega[0];
+    // the fine residual as the cycle runs it: t = r - w K (M D^-1) r from the scaled copy, or a
+    // damped sweep from the plain one
     auto sweep = [&]() {
+        if (c->sellScaled)
+            return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
+                                              c->dSellV1, c->vcIn, c->vcIn, c->dMask, c->fineT, nullptr, 0.f,
+                                              c->sellSplit, s, omega);
         return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
                                           c->dSellV1, c->fineX, c->vcIn, c->dMask, c->fineT, (const float*)c->dBinv,
                                           omega, c->sellSplit, s);
@@ -435,8 +441,16 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
         return ef_launch_sell_spmv3(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV9, c->vcOut,
                                     c->dMask, c->fineT, c->fgZ, c->sellSplitProduct, s);
     };
-    for (int k = 0; k < 2; ++k) {
-        auto run = [&]() { return k == 0 ? sweep() : product(); };
+    const bool post = c->postSlots > 0 && !c->amg.empty() && c->amg[0].x;
+    auto fused = [&]() {
+        return ef_launch_sa_post_fused(nN, c->postSlices, c->dPostOff, c->dPostPerm, c->dPostCol, c->dPostQ0,
+                                       c->dPostQ1, c->dPostQ2, c->amg[0].x, c->vcIn, c->fineT, (const float*)c->dBinv,
+                                       c->dMask, omega, c->fineX, c->sellSplit, s);
+    };
+    for (int k = 0; k < 3; ++k) {
+        ms[k] = 0.0;
+        if (k == 2 && !post) continue;
+        auto run = [&]() { return k == 0 ? sweep() : (k == 1 ? product() : fused()); };
         EF_CHECK(run());  // warm-up
         EF_CUDA(cudaEventRecord(c->ev[0], s));
         for (int i = 0; i < reps; ++i) EF_CHECK(run());
@@ -451,7 +465,14 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
     const double nb = (double)c->nBlocks, nn = (double)nN, ns = (double)c->sellSlices;
     bytes[0] = nb * (16 + 2 + 4) + nn * (3 * 4 /*x*/ + 3 * 4 /*r*/ + 9 * 4 /*D^-1*/ + 3 /*mask*/ + 3 * 4 /*out*/) +
                (ns + 1) * 8;
+    if (c->sellScaled) bytes[0] -= nn * (3 * 4 /*x*/ + 9 * 4 /*D^-1*/);  // x is r, no D^-1 in the residual
     bytes[1] = nb * (9 * 4 + 4) + nn * (3 * 4 /*x*/ + 3 /*mask*/ + 3 * 4 /*y*/ + 3 * 4 /*copy*/) + (ns + 1) * 8;
+    // the fused post-smoothing: C blocks (18 BF16 values and a column) of the pattern of A P, the
+    // per-row r, t, D^-1, mask and output (the coarse correction e, 40 k values, is read from cache)
+    bytes[2] = post ? (double)c->amg[0].saNAP * (18 * 2 + 4) +
+                          nn * (3 * 4 /*r*/ + 3 * 4 /*t*/ + 9 * 4 /*D^-1*/ + 3 /*mask*/ + 3 * 4 /*out*/) +
+                          (double)(c->postSlices + 1) * 8
+                    : 0.0;
     return EF_OK;
 }
 

@@ -325,12 +325,14 @@ ef_status ef_fgmres_set_preconditioner(ef_ctx* ctx, int kind);
  * at the start of each increment. */
 ef_status ef_fgmres_set_reuse(ef_ctx* ctx, int maxReuse);
 
-/* Diagnostics of the FGMRES solve's two fine-level kernels on the last assembled system (after
- * an FGMRES solve with the sliced-ELL fine level): each is launched once, then `reps` times back
- * to back on `stream` between two CUDA events.  ms (host [2]) receives the average duration of
- * one launch of the BF16 smoothing sweep and of the FP32 product, bytes (host [2]) their
- * algorithmic DRAM bytes per launch (the real blocks' values and column indices, the per-row
- * vectors).  Overwrites the multigrid's fine work vectors.  Synchronises `stream`. */
+/* Diagnostics of the FGMRES solve's fine-level kernels on the last assembled system (after an
+ * FGMRES solve with the sliced-ELL fine level): each is launched once, then `reps` times back to
+ * back on `stream` between two CUDA events.  ms (host [3]) receives the average duration of one
+ * launch of [0] the BF16 fine residual / smoothing sweep as the multigrid cycle runs it, [1] the
+ * FP32 product, [2] the fused prolongation + post-smoothing (0 when the cycle does not use it);
+ * bytes (host [3]) their algorithmic DRAM bytes per launch (the real blocks' values and column
+ * indices, the per-row vectors).  Overwrites the multigrid's fine work vectors.  Synchronises
+ * `stream`. */
 ef_status ef_fine_kernel_profile(ef_ctx* ctx, int reps, double* ms, double* bytes, void* stream);
 
 /* ---- learned preconditioner correction for the FGMRES solve (EF_SOLVE_FGMRES) ----
