@@ -461,6 +461,7 @@ struct ef_ctx {
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
+    bool amgDeadValid = false;  // the levels' dead-DOF masks match the current Dirichlet mask
     bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)
     int saTransfer = 2;                     // SA transfers: 0 a thread per coarse node / finer row, 1 block
                                             // products + sums, 2 one pass, a thread per block (EF_SA_TRANSFER)

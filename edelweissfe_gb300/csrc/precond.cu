@@ -802,15 +802,19 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
         return nn_edge_refresh(c, s);
     }
     c->amgReuseLeft = c->amgMaxReuse;
-    c->amgMaskChanged = false;
     const int BCo = ef_amg_coarse_dofs();
-    const uint8_t* fineDead = c->hMask.data();
-    for (size_t l = 0; l < c->amg.size(); ++l) {
-        AmgLevel& L = c->amg[l];
-        amg_dead_mask(L, l == 0 ? 3 : BCo, fineDead, L.hDead);
-        EF_CUDA(cudaMemcpyAsync(L.dead, L.hDead.data(), L.hDead.size(), cudaMemcpyHostToDevice, s));
-        fineDead = L.hDead.data();
+    if (c->amgMaskChanged || !c->amgDeadValid) {
+        // the dead coarse DOFs depend on the Dirichlet mask and the (fixed) aggregation only
+        const uint8_t* fineDead = c->hMask.data();
+        for (size_t l = 0; l < c->amg.size(); ++l) {
+            AmgLevel& L = c->amg[l];
+            amg_dead_mask(L, l == 0 ? 3 : BCo, fineDead, L.hDead);
+            EF_CUDA(cudaMemcpyAsync(L.dead, L.hDead.data(), L.hDead.size(), cudaMemcpyHostToDevice, s));
+            fineDead = L.hDead.data();
+        }
+        c->amgDeadValid = true;
     }
+    c->amgMaskChanged = false;
     if (c->amgSmoothed) EF_CHECK(amg_power_alloc(c));
     // with reuse enabled, the damping estimates (lambda_max of D^-1 A per level) come from the
     // increment's first build; the later builds of the increment keep them

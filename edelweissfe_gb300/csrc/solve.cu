@@ -295,9 +295,16 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
     inf.status = EF_OK;
     double bb = 0.0;
     EF_CHECK(dot_host(c, b, b, &bb, s));
-    // Dirichlet part: x_d = b on Dirichlet DOFs; lifted RHS b~ = b_f - K_fd x_d
+    // Dirichlet part: x_d = b on Dirichlet DOFs; lifted RHS b~ = b_f - K_fd x_d (when x_d = 0, as in
+    // every Newton system after an increment's first, b~ is b on the free DOFs: the same bits
+    // without the operator application)
     EF_CHECK(ef_launch_masked_copy(n, b, c->dMask, 1, 1.0, xd, 1, s));
-    EF_CHECK(residual64(c, xd, b, r64, s));
+    double dd = 0.0;
+    EF_CHECK(dot_host(c, xd, xd, &dd, s));
+    if (dd == 0.0)
+        EF_CHECK(ef_launch_masked_copy(n, b, c->dMask, 0, 1.0, r64, 1, s));
+    else
+        EF_CHECK(residual64(c, xd, b, r64, s));
     EF_CUDA(cudaMemsetAsync(xf, 0, sizeof(double) * n, s));
     if (!(bb > 0.0)) {
         EF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
