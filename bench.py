@@ -380,6 +380,42 @@ def run_ours(a):
         return [sum(x[i] for x in infos) for i in range(11)]
 
     fg_kms, fg_it, _, sp_ms, sp_n, pre_ms, orth_ms, n_reorth, n_refine, n_solves, setup_ms = profiled_step()
+
+    def phase_step():
+        # wall time of each Newton-loop phase over one step (synchronised around each call, so the
+        # phases do not overlap; the rest of the step is the driver's own work)
+        names = ("computeElements", "assembleStiffnessCSR", "newtonResidual", "linearSolve")
+        acc = {k: 0.0 for k in names}
+        origs = {k: getattr(s, k) for k in names}
+
+        def timed_call(k):
+            def f(*args, **kw):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                out = origs[k](*args, **kw)
+                torch.cuda.synchronize()
+                acc[k] += time.perf_counter() - t0
+                return out
+
+            return f
+
+        for k in names:
+            setattr(s, k, timed_call(k))
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            one_step()
+            torch.cuda.synchronize()
+            total = time.perf_counter() - t0
+        finally:
+            for k in names:
+                setattr(s, k, origs[k])
+        out = {k: 1e3 * v for k, v in acc.items()}
+        out["step"] = 1e3 * total
+        out["rest"] = out["step"] - sum(out[k] for k in names)
+        return out
+
+    phase_ms = phase_step()
     # the fine-level kernels timed live on the timed increment's last system (CUDA events, same stream)
     import ctypes
 
@@ -523,6 +559,7 @@ def run_ours(a):
         "assembly": {"elements_ms": t_el * 1e3, "bsr_scatter_ms": t_as * 1e3, "GBps": asm_gbs,
                      "frac_hbm": asm_gbs / peaks["hbm_gbs"], "bytes": b_elem + b_cond + b_scat,
                      "elements_per_s": nEl / (t_el + t_as)},
+        "phase_ms": phase_ms,
         "fgmres_profile": {"iterations": fg_it, "kernel_ms": fg_kms,
                            "ms_per_iteration": fg_kms / fg_it if fg_it else None,
                            "precond_ms_per_iteration": pre_ms / fg_it if fg_it else None,

@@ -308,6 +308,72 @@ __global__ void __launch_bounds__(kSaRestrictThreads) sa_restrict_onepass_kernel
     }
 }
 
+// BF16 form of the fine level's transpose-order copy (3 x 6 blocks): per slot one 16-byte word with
+// values 0..7, one with 8..15 and one 4-byte word with 16..17 (three arrays, consecutive slots
+// consecutive), for the restriction, which then streams 36 instead of 72 bytes per block
+__device__ __forceinline__ uint32_t sa_pack_bf16x2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ float2 sa_unpack_bf16x2(uint32_t v) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v));
+}
+
+__global__ void sa_block_copy_h_kernel(int64_t nP, const int32_t* __restrict__ tIdx, const float* __restrict__ Pv,
+                                       uint4* __restrict__ q0, uint4* __restrict__ q1, uint32_t* __restrict__ q2) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nP) return;
+    const float* P = Pv + (int64_t)tIdx[k] * 18;
+    q0[k] = make_uint4(sa_pack_bf16x2(P[0], P[1]), sa_pack_bf16x2(P[2], P[3]), sa_pack_bf16x2(P[4], P[5]),
+                       sa_pack_bf16x2(P[6], P[7]));
+    q1[k] = make_uint4(sa_pack_bf16x2(P[8], P[9]), sa_pack_bf16x2(P[10], P[11]), sa_pack_bf16x2(P[12], P[13]),
+                       sa_pack_bf16x2(P[14], P[15]));
+    q2[k] = sa_pack_bf16x2(P[16], P[17]);
+}
+
+// the restriction of sa_restrict_onepass_kernel<3> from the BF16 copy
+__global__ void __launch_bounds__(kSaRestrictThreads) sa_restrict_onepass_h_kernel(
+    int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ rowT, const uint4* __restrict__ q0,
+    const uint4* __restrict__ q1, const uint32_t* __restrict__ q2, const float* __restrict__ t,
+    const uint8_t* __restrict__ coarseDead, float* __restrict__ rc) {
+    ef::dep_entry();
+    __shared__ float red[kSaRestrictThreads / 32][BC];
+    const int I = blockIdx.x;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    float a[BC];
+#pragma unroll
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    for (int64_t k = tPtr[I] + threadIdx.x; k < tPtr[I + 1]; k += kSaRestrictThreads) {
+        const uint4 u = q0[k], v = q1[k];
+        const uint32_t w = q2[k];
+        float P[18];
+        const uint32_t words[9] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w, w};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float2 f = sa_unpack_bf16x2(words[q]);
+            P[2 * q] = f.x;
+            P[2 * q + 1] = f.y;
+        }
+        const int64_t m = rowT[k];
+        const float t0 = t[3 * m], t1 = t[3 * m + 1], t2 = t[3 * m + 2];
+#pragma unroll
+        for (int j = 0; j < BC; ++j) a[j] += P[j] * t0 + P[BC + j] * t1 + P[2 * BC + j] * t2;
+    }
+#pragma unroll
+    for (int j = 0; j < BC; ++j) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+        if (lane == 0) red[wp][j] = a[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < BC) {
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < kSaRestrictThreads / 32; ++w) v += red[w][threadIdx.x];
+        rc[BC * I + threadIdx.x] = coarseDead[BC * I + threadIdx.x] ? 0.f : v;
+    }
+}
+
 // prolongation: a CTA per kSaProlongRows consecutive finer rows; a thread per P block of those
 // rows (row order) leaves the block's product in shared memory, then
 // thread r sums row r's products in block order.  cap >= the block count of every such group of
@@ -1326,6 +1392,24 @@ ef_status ef_launch_sa_block_copy(int bf, int64_t nP, const int32_t* tIdx, const
     else
         sa_block_copy_kernel<6><<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, tIdx, Pv, dst);
     EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_block_copy_h(int64_t nP, const int32_t* tIdx, const float* Pv, void* q0, void* q1, void* q2,
+                                    cudaStream_t s) {
+    if (nP <= 0) return EF_OK;
+    sa_block_copy_h_kernel<<<nb_(nP, 256), 256, 0, ef::counted(s)>>>(nP, tIdx, Pv, (uint4*)q0, (uint4*)q1,
+                                                                      (uint32_t*)q2);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+ef_status ef_launch_sa_restrict_onepass_h(int nC, const int32_t* tPtr, const int32_t* rowT, const void* q0,
+                                          const void* q1, const void* q2, const float* t, const uint8_t* coarseDead,
+                                          float* rc, cudaStream_t s) {
+    if (nC <= 0) return EF_OK;
+    EF_CUDA(ef::launch_dep(sa_restrict_onepass_h_kernel, nC, kSaRestrictThreads, 0, s, nC, tPtr, rowT,
+                           (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, t, coarseDead, rc));
     return EF_OK;
 }
 

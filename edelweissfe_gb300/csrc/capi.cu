@@ -321,6 +321,7 @@ void ef_destroy(ef_ctx* c) {
         for (int e = 0; e < 4; ++e)
             if (c->fgEv[k][e]) cudaEventDestroy(c->fgEv[k][e]);
     }
+    if (c->fgNormDone) cudaEventDestroy(c->fgNormDone);
     F(c->fgV);
     F(c->fgZ);
     F(c->fgW);
@@ -497,6 +498,11 @@ ef_status ef_finalize(ef_ctx* c, int options) {
     c->keFp64 = (options & EF_OPT_KE_FP64) ? 1 : 0;
     c->scalar = !(options & EF_OPT_NO_SCALAR_CSR) && c->hTieS.empty();  // the reference CSR has no ties
     if (const char* e = getenv("EF_ELEM_GRAPH")) c->elemGraphs = atoi(e) != 0;
+    if (const char* e = getenv("EF_FGMRES_HOLD")) c->fgHold = std::max(0.0, atof(e));
+    if (const char* e = getenv("EF_REFINE_AIM")) {
+        const double v = atof(e);
+        if (v > 0.0 && v <= 1.0) c->refineAim = v;
+    }
     if (const char* e = getenv("EF_MPNN_TC")) c->nnTensorCores = atoi(e) != 0;
     const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
     ef_status st = EF_OK;

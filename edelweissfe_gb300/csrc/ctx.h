@@ -82,6 +82,12 @@ ef_status ef_launch_sa_prolong2(int bf, int nF, int64_t nP, const int32_t* pRowP
 // ef_sa_prolong_onepass_smem(bf, cap) bytes of shared memory, cap >= the P blocks of every group
 ef_status ef_launch_sa_block_copy(int bf, int64_t nP, const int32_t* tIdx, const float* Pv, float* dst,
                                   cudaStream_t s);
+// the fine level's transpose-order copy of P in BF16 (three word arrays) and its restriction
+ef_status ef_launch_sa_block_copy_h(int64_t nP, const int32_t* tIdx, const float* Pv, void* q0, void* q1, void* q2,
+                                    cudaStream_t s);
+ef_status ef_launch_sa_restrict_onepass_h(int nC, const int32_t* tPtr, const int32_t* rowT, const void* q0,
+                                          const void* q1, const void* q2, const float* t, const uint8_t* coarseDead,
+                                          float* rc, cudaStream_t s);
 size_t ef_sa_prolong_onepass_smem(int bf, int cap);
 int ef_sa_prolong_onepass_rows();
 ef_status ef_launch_sa_restrict_onepass(int bf, int nC, const int32_t* tPtr, const int32_t* rowT, const float* PT,
@@ -313,6 +319,7 @@ struct AmgLevel {
     // one-pass transfers: transpose-order copy of P with the block row of each slot; saCap bounds
     // the blocks of a prolongation group of finer rows
     float* saPT = nullptr;
+    void *saPTh0 = nullptr, *saPTh1 = nullptr, *saPTh2 = nullptr;  // BF16 form (fine level, EF_SA_PT_BF16)
     int32_t* saRowT = nullptr;
     int saCap = 0;
     // fused post-smoothing of the finer level when it has 6 DOFs: C = a (I - w D^-1 A) P in the
@@ -333,7 +340,7 @@ struct AmgLevel {
                         (void*)saPRow, (void*)saPSrc, (void*)saTPtr, (void*)saTIdx, (void*)saApRow, (void*)saApK,
                         (void*)saApP, (void*)saCP, (void*)saCAP, (void*)saPSeg, (void*)saApSeg, (void*)saCSeg,
                         (void*)saPv, (void*)saAPv, (void*)saW, (void*)saC, (void*)saPT,
-                        (void*)saRowT, (void*)saApRowPtr, (void*)postRowPtr, (void*)postCol, (void*)valsB,
+                        (void*)saRowT, (void*)saPTh0, (void*)saPTh1, (void*)saPTh2, (void*)saApRowPtr, (void*)postRowPtr, (void*)postCol, (void*)valsB,
                         (void*)postApToP, (void*)postC})
             if (p) cudaFree(p);
     }
@@ -461,6 +468,8 @@ struct ef_ctx {
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
+    double refineAim = 0.5;  // an inner solve aims at this fraction of the remaining target (EF_REFINE_AIM)
+    double fgHold = 2.0;     // FGMRES: no column enqueued ahead when the trend reaches hold x target (EF_FGMRES_HOLD)
     bool amgDeadValid = false;  // the levels' dead-DOF masks match the current Dirichlet mask
     bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)
     int saTransfer = 2;                     // SA transfers: 0 a thread per coarse node / finer row, 1 block
@@ -549,6 +558,7 @@ struct ef_ctx {
     int fgRestart = 0;
     double* fgPin = nullptr;                   // pinned host copies of two columns' coefficients
     cudaEvent_t fgDone[2] = {nullptr, nullptr};
+    cudaEvent_t fgNormDone = nullptr;  // the starting vector's norm is in host-mapped memory
     cudaEvent_t fgEv[2][4] = {};               // per column slot: iteration start/end, SpMV start/end
 };
 

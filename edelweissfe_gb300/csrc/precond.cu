@@ -412,8 +412,17 @@ ef_status amg_build(ef_ctx* c) {
                     std::vector<int32_t> rowT(L.saNP);
                     for (int64_t k = 0; k < L.saNP; ++k) rowT[k] = SA.pRow[SA.tIdx[k]];
                     EF_CHECK(upload(&L.saRowT, rowT));
-                    L.saPT = dalloc<float>((size_t)L.saNP * bfL * BCo, &st);
-                    if (!L.saPT) return st;
+                    bool h = bfL == 3;
+                    if (const char* e = getenv("EF_SA_PT_BF16")) h = h && atoi(e) != 0;
+                    if (h) {  // BF16 copy for the fine restriction
+                        L.saPTh0 = dalloc<uint4>((size_t)L.saNP, &st);
+                        L.saPTh1 = dalloc<uint4>((size_t)L.saNP, &st);
+                        L.saPTh2 = dalloc<uint32_t>((size_t)L.saNP, &st);
+                        if (!L.saPTh0 || !L.saPTh1 || !L.saPTh2) return st;
+                    } else {
+                        L.saPT = dalloc<float>((size_t)L.saNP * bfL * BCo, &st);
+                        if (!L.saPT) return st;
+                    }
                     L.saCap = cap;
                     L.saOnePass = true;
                 }
@@ -838,7 +847,10 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s) {
                                         L.saApRow, L.saApSeg, L.saApK, L.saApP, fCol, fVals, fMask, L.offs, L.agg,
                                         fBinv, L.saW, L.saPv, L.saAPv, L.nBlocks, L.saCSeg, L.saCP, L.saCAP,
                                         L.rowOfBlock, L.colIdx, L.dead, L.vals, nFiner, L.saApRowPtr, L.saApCap, s));
-            if (L.saOnePass) EF_CHECK(ef_launch_sa_block_copy(fine ? 3 : BCo, L.saNP, L.saTIdx, L.saPv, L.saPT, s));
+            if (L.saOnePass && L.saPTh0)
+                EF_CHECK(ef_launch_sa_block_copy_h(L.saNP, L.saTIdx, L.saPv, L.saPTh0, L.saPTh1, L.saPTh2, s));
+            else if (L.saOnePass)
+                EF_CHECK(ef_launch_sa_block_copy(fine ? 3 : BCo, L.saNP, L.saTIdx, L.saPv, L.saPT, s));
         } else {
             EF_CHECK(ef_launch_galerkin(fine ? 3 : BCo, L.nBlocks, L.gseg, L.gsrc, fRob, fCol, fVals, fMask, L.offs,
                                         L.rowOfBlock, L.colIdx, L.dead, L.vals, s));
@@ -974,7 +986,10 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
                                : ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, x2, r, mask, t, s, nullptr,
                                                           0.f, valsH));
         }
-        if (Cn.saOnePass)
+        if (Cn.saOnePass && Cn.saPTh0)
+            EF_CHECK(ef_launch_sa_restrict_onepass_h(Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPTh0, Cn.saPTh1, Cn.saPTh2, t,
+                                                     Cn.dead, Cn.r, s));
+        else if (Cn.saOnePass)
             EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, t, Cn.dead, Cn.r, s));
         else
             EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, t,
@@ -1021,7 +1036,10 @@ ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s)
             EF_CHECK(ef_launch_coarse_cycle(c->dCoarseOps, c->nCoarseOps, s));
             continue;
         }
-        if (c->amgSmoothed && Cn.saOnePass)
+        if (c->amgSmoothed && Cn.saOnePass && Cn.saPTh0)
+            EF_CHECK(ef_launch_sa_restrict_onepass_h(Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPTh0, Cn.saPTh1, Cn.saPTh2, res,
+                                                     Cn.dead, Cn.r, s));
+        else if (c->amgSmoothed && Cn.saOnePass)
             EF_CHECK(ef_launch_sa_restrict_onepass(bs, Cn.nN, Cn.saTPtr, Cn.saRowT, Cn.saPT, res, Cn.dead, Cn.r, s));
         else if (c->amgSmoothed && c->saTransfer >= 1)
             EF_CHECK(ef_launch_sa_restrict2(bs, Cn.nN, Cn.saNP, Cn.saTPtr, Cn.saTIdx, Cn.saPRow, Cn.saPv, res,

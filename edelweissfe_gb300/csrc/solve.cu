@@ -113,6 +113,7 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CUDA(cudaHostGetDevicePointer((void**)&c->fgPinDev, c->fgPin, 0));
         for (int k = 0; k < 2; ++k) {
             EF_CUDA(cudaEventCreateWithFlags(&c->fgDone[k], cudaEventDisableTiming));
+        if (!c->fgNormDone) EF_CUDA(cudaEventCreateWithFlags(&c->fgNormDone, cudaEventDisableTiming));
             for (int e = 0; e < 4; ++e) EF_CUDA(cudaEventCreate(&c->fgEv[k][e]));
         }
     }
@@ -123,11 +124,7 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
     EF_CUDA(cudaMemcpyAsync(V, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
     EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s));
     c->vcInStale = false;
-    EF_CUDA(cudaStreamSynchronize(s));
-    const double bnorm = sqrt(pinRestart[0]);
-    *iters = 0;
-    if (!(bnorm > 0.0)) return EF_OK;
-    double beta = bnorm;
+    EF_CUDA(cudaEventRecord(c->fgNormDone, s));
     const bool collect = c->nnInit && c->nnEvery > 0 && c->nnMaxPerSolve > 0;
     const bool snap = collect && c->nnKind == 0;
     const bool krylovSamples = collect && c->nnKind == 1;
@@ -168,15 +165,33 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CUDA(cudaEventRecord(c->fgDone[sl], s));
         return EF_OK;
     };
+    // column 0 runs while the host reads |b| (a zero b leaves every vector zero, and x = 0)
+    EF_CHECK(enqueue_column(0));
+    bool col0Queued = true;
+    EF_CUDA(cudaEventSynchronize(c->fgNormDone));
+    const double bnorm = sqrt(pinRestart[0]);
+    *iters = 0;
+    if (!(bnorm > 0.0)) {
+        EF_CUDA(cudaStreamSynchronize(s));
+        return EF_OK;
+    }
+    double beta = bnorm;
     int total = 0;
     bool converged = false;
     while (total < maxIter && !converged) {
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
-        EF_CHECK(enqueue_column(0));
+        if (!col0Queued) EF_CHECK(enqueue_column(0));
+        col0Queued = false;
+        // residual estimates after the last two columns: when the trend says column j reaches the
+        // target (within the hold factor), column j + 1 is enqueued only once column j has been
+        // read -- a short host turnaround instead of a whole column computed for nothing
+        double res1 = -1.0, res2 = -1.0;
         for (; j < m && total < maxIter; ++j) {
-            if (j + 1 < m && total + 1 < maxIter) EF_CHECK(enqueue_column(j + 1));
+            bool ahead = j + 1 < m && total + 1 < maxIter;
+            if (ahead && res1 > 0.0 && res2 > 0.0 && res1 * (res1 / res2) <= c->fgHold * rtol * bnorm) ahead = false;
+            if (ahead) EF_CHECK(enqueue_column(j + 1));
             const int sl = j & 1;
             EF_CUDA(cudaEventSynchronize(c->fgDone[sl]));
             const double* hcol = c->fgPin + sl * ldh;
@@ -238,6 +253,9 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
                 ++j;
                 break;
             }
+            if (!ahead && j + 1 < m && total < maxIter) EF_CHECK(enqueue_column(j + 1));
+            res2 = res1;
+            res1 = fabs(g[j + 1]);
         }
         // y = R^-1 g, x += Z y
         std::vector<double> y(j);
@@ -341,7 +359,7 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             const int vd = c->keFp64;
             void** wv = vd ? c->w64k : c->w32;
             EF_CHECK(ef_launch_masked_copy(n, r64, c->dMask, 0, 1.0 / rn, wv[0], vd, s));
-            const double inner = std::max(o->innerRtol, 0.5 * o->rtol * bnorm / rn);
+            const double inner = std::max(o->innerRtol, c->refineAim * o->rtol * bnorm / rn);
             PcgResultHost pr;
             if (o->method == EF_SOLVE_FGMRES) {
                 const bool timeSetup = o->profile && (c->sellStale || c->amgStale);
