@@ -328,6 +328,9 @@ void ef_destroy(ef_ctx* c) {
     F(c->fgPart);
     F(c->fgH);
     F(c->fgPartN);
+    F(c->fgPartF);
+    F(c->fgSc);
+    F(c->fgTicket);
     for (auto e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto e : c->evS)

@@ -167,7 +167,9 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
                                double* hG, double* hTmp, double* hAcc, double eta2, float* w2, double* hostOut,
                                int slotNorm, cudaStream_t s);
 ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
-                                    int slotNorm, cudaStream_t s);
+                                    int slotNorm, cudaStream_t s, float* scOut = nullptr);
+ef_status ef_launch_gs_column(int64_t n, int nv, float* V, int64_t ldv, float* part, double* partN, int nPart,
+                              float* sc, unsigned* ticket, float* w2, double* hostOut, int slotNorm, cudaStream_t s);
 int ef_sp_stage_cap(int nN, const int32_t* rowPtrHost);
 ef_status ef_launch_spmv_f32_staged(int nSM, int cap, int nN, const int32_t* rowPtr, const int32_t* colIdx,
                                     const float* vals, const float* x, const uint8_t* mask, float* y, float* xcopy,
@@ -183,7 +185,7 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
                                  const int32_t* col, const float* binv, const uint8_t* mask, cudaStream_t s);
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s);
+                               cudaStream_t s, const float* scale = nullptr);
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
@@ -550,6 +552,11 @@ struct ef_ctx {
     double* fgH = nullptr;               // device scratch: [hG | hTmp | hAcc | y], 128 each
     double* fgPartN = nullptr;           // per-CTA parts of |w|^2
     int fgNPart = 0;                     // CTAs of the orthogonalisation kernels
+    // deferred normalisation of the basis (two Gram-Schmidt kernels per column; EF_FGMRES_DEFER)
+    bool fgDefer = true;
+    float* fgPartF = nullptr;            // [kMaxBasis][nSM] per-CTA dot products
+    float* fgSc = nullptr;               // [kMaxBasis] 1 / |u_k| of the unnormalised basis vectors
+    unsigned* fgTicket = nullptr;        // last-CTA counter of gs_axpy_kernel (0 between launches)
     int spCap = 0;                       // > 0: FGMRES SpMV through shared-memory staging (EF_SPMV_STAGED=1)
     int fgPc = 0;                        // FGMRES base preconditioner: EF_FGMRES_PC_MULTIGRID / _JACOBI
     double* fgPinDev = nullptr;          // device address of fgPin

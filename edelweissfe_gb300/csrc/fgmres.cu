@@ -320,8 +320,10 @@ __global__ void __launch_bounds__(kFB) normalize_kernel(int64_t n, float* __rest
                                                          const double* __restrict__ np, int nParts,
                                                          const double* __restrict__ hAcc, int nv,
                                                          volatile double* hostOut, int slotNorm,
-                                                         const double* __restrict__ gate, double eta2) {
+                                                         const double* __restrict__ gate, double eta2,
+                                                         float* __restrict__ scOut) {
     ef::dep_entry();
+    if (scOut && blockIdx.x == 0 && threadIdx.x == 0) *scOut = 1.f;
     // |w|^2 over the CTA, 1/|w| by thread 0 (FP64), handed to the CTA through shared memory
     __shared__ double red[kFB / 32];
     __shared__ float sInv;
@@ -342,6 +344,131 @@ __global__ void __launch_bounds__(kFB) normalize_kernel(int64_t n, float* __rest
         const float v = w[i] * inv;
         w[i] = v;
         if (w2) w2[i] = v;
+    }
+}
+
+// ---- Gram-Schmidt column with deferred normalisation (two kernels per column) ---------------
+// The basis is kept as unnormalised vectors u_k with factors sc[k] = 1 / |u_k| (v_k = sc[k] u_k):
+// the new vector is never rescaled in place.  The product that makes w = K z_j applies sc[j] to
+// its result and to the stored z_j (the preconditioner is linear, so M^-1 (sc u) = sc M^-1 u).
+//   gs_dot:  part[k][cta] = u_k . w over the CTA's elements (k < nv), FP32;
+//   gs_axpy: every CTA sums part[k][0..nParts) in the same order (h_k = sc[k] sum), then
+//            w -= sum_k h_k sc[k] u_k, a copy of w to the preconditioner's input, |w|^2 parts;
+//            the last CTA to finish (an atomic ticket, no waiting) sums the |w|^2 parts in order,
+//            sets sc[nv] = 1 / |w| and publishes h and |w|^2 to host-mapped memory.
+// One CTA per SM of kGsThreads threads, so that a CTA's sum over the parts stays short.
+constexpr int kGsThreads = 1024;
+
+__global__ void __launch_bounds__(kGsThreads, 1) gs_dot_kernel(int64_t n, int nv, const float* __restrict__ V,
+                                                               int64_t ldv, const float* __restrict__ w,
+                                                               float* __restrict__ part) {
+    ef::dep_entry();
+    __shared__ float red[kGsThreads / 32][kMaxBasis];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int64_t stride = (int64_t)gridDim.x * kGsThreads;
+    for (int k0 = 0; k0 < nv; k0 += 8) {
+        const int kn = min(8, nv - k0);
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        int64_t i = (int64_t)blockIdx.x * kGsThreads + threadIdx.x;
+        for (; i + stride < n; i += 2 * stride) {
+            const float wa = w[i], wb = w[i + stride];
+            float va[8], vb[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kn) {
+                    va[k] = V[(k0 + k) * ldv + i];
+                    vb[k] = V[(k0 + k) * ldv + i + stride];
+                }
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kn) acc[k] = fmaf(vb[k], wb, fmaf(va[k], wa, acc[k]));
+        }
+        if (i < n) {
+            const float wa = w[i];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < kn) acc[k] = fmaf(V[(k0 + k) * ldv + i], wa, acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float a = warp_sum(acc[k]);
+            if (lane == 0 && k < kn) red[wp][k0 + k] = a;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nv; k += kGsThreads) {
+        float s = 0.f;
+#pragma unroll 8
+        for (int q = 0; q < kGsThreads / 32; ++q) s += red[q][k];
+        part[(int64_t)k * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kGsThreads, 1) gs_axpy_kernel(int64_t n, int nv, const float* __restrict__ V,
+                                                                int64_t ldv, const float* __restrict__ part,
+                                                                float* __restrict__ sc, float* __restrict__ w,
+                                                                float* __restrict__ w2, double* __restrict__ partN,
+                                                                unsigned* __restrict__ ticket,
+                                                                volatile double* hostOut, int slotNorm) {
+    ef::dep_entry();
+    __shared__ float hk[kMaxBasis];  // h_k (Hessenberg entries)
+    __shared__ float ck[kMaxBasis];  // h_k sc[k] (coefficients of u_k)
+    __shared__ float red[kGsThreads / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int nP = gridDim.x;
+    for (int k = wp; k < nv; k += kGsThreads / 32) {
+        float t = 0.f;
+        for (int c = lane; c < nP; c += 32) t += part[(int64_t)k * nP + c];
+        t = warp_sum(t);
+        if (lane == 0) {
+            const float f = sc[k];
+            const float h = t * f;
+            hk[k] = h;
+            ck[k] = h * f;
+        }
+    }
+    __syncthreads();
+    float nrm = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * kGsThreads + threadIdx.x; i < n; i += (int64_t)nP * kGsThreads) {
+        float s = w[i];
+        int k = 0;
+        for (; k + 8 <= nv; k += 8) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = V[(k + q) * ldv + i];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s -= ck[k + q] * v[q];
+        }
+        for (; k < nv; ++k) s -= ck[k] * V[k * ldv + i];
+        w[i] = s;
+        w2[i] = s;
+        nrm = fmaf(s, s, nrm);
+    }
+    nrm = warp_sum(nrm);
+    if (lane == 0) red[wp] = nrm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+#pragma unroll 8
+        for (int q = 0; q < kGsThreads / 32; ++q) t += red[q];
+        partN[blockIdx.x] = (double)t;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == (unsigned)nP - 1;
+    }
+    __syncthreads();
+    if (!last || wp != 0) return;
+    __threadfence();
+    double t = 0.0;
+    for (int c = lane; c < nP; c += 32) t += __ldcg(partN + c);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    for (int k = lane; k < nv; k += 32) hostOut[k] = (double)hk[k];
+    if (lane == 0) {
+        sc[nv] = t > 0.0 ? (float)(1.0 / sqrt(t)) : 0.f;
+        hostOut[slotNorm] = t;
+        hostOut[slotNorm - 1] = 0.0;  // never re-orthogonalised
+        *ticket = 0u;
     }
 }
 
@@ -446,17 +573,36 @@ ef_status ef_launch_cgs_column(int64_t n, int nv, float* V, int64_t ldv, double*
     }
     // every normalisation CTA sums all nPart parts (from L2) and scales its share of w
     EF_CUDA(ef::launch_dep(normalize_kernel, nPart, kFB, 0, s, n, w, w2, partN, nPart, re ? hAcc : hG,
-            nv, hostOut, slotNorm, re ? hG : nullptr, eta2));
+            nv, hostOut, slotNorm, re ? hG : nullptr, eta2, (float*)nullptr));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }
 
-// w /= |w| with |w|^2 from a one-vector multidot (the restart vector); w2 = w; |w|^2 to hostOut
+// One Gram-Schmidt step of column j with deferred normalisation (gs_dot_kernel, gs_axpy_kernel):
+// nv = j + 1 basis vectors u_0..u_j in V with factors sc[0..nv), the new vector w = u_nv in
+// place (already scaled by sc[j] through the product); w2 = w; sc[nv], h and |w|^2 to hostOut.
+// part: [kMaxBasis][nPart] floats, partN: [nPart], ticket: one counter, zero between launches.
+ef_status ef_launch_gs_column(int64_t n, int nv, float* V, int64_t ldv, float* part, double* partN, int nPart,
+                              float* sc, unsigned* ticket, float* w2, double* hostOut, int slotNorm, cudaStream_t s) {
+    if (nv + 1 > kMaxBasis) {
+        ef_set_error("FGMRES: basis larger than the compiled maximum");
+        return EF_ERR_ARG;
+    }
+    float* w = V + (int64_t)nv * ldv;
+    EF_CUDA(ef::launch_dep(gs_dot_kernel, nPart, kGsThreads, 0, s, n, nv, V, ldv, w, part));
+    EF_CUDA(ef::launch_dep(gs_axpy_kernel, nPart, kGsThreads, 0, s, n, nv, V, ldv, part, sc, w, w2, partN, ticket,
+                           hostOut, slotNorm));
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
+// w /= |w| with |w|^2 from a one-vector multidot (the restart vector); w2 = w; |w|^2 to hostOut;
+// scOut (optional): the vector's factor, 1
 ef_status ef_launch_normalize_first(int64_t n, float* w, double* part, int nPart, float* w2, double* hostOut,
-                                    int slotNorm, cudaStream_t s) {
+                                    int slotNorm, cudaStream_t s, float* scOut) {
     EF_CUDA(ef::launch_dep(multidot_partial_kernel, nPart, kFB, 0, s, n, 1, w, n, w, part, nullptr, 0, 0.0));
     EF_CUDA(ef::launch_dep(normalize_kernel, nPart, kFB, 0, s, n, w, w2, part, nPart, nullptr, 0,
-            hostOut, slotNorm, nullptr, 0.0));
+            hostOut, slotNorm, nullptr, 0.0, scOut));
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

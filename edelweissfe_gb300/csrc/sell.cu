@@ -126,12 +126,14 @@ __device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, flo
     }
 }
 
-// y = K x on the free DOFs (0 on masked rows); COPY: xcopy = x as well; S warps per slice
+// y = sc K x on the free DOFs (0 on masked rows); COPY: xcopy = sc x as well; sc = *scale (1 without
+// one: the FGMRES basis vector x then carries its normalisation factor); S warps per slice
 template <bool COPY, int S>
 __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const float* __restrict__ v9, const float* __restrict__ x,
-    const uint8_t* __restrict__ mask, float* __restrict__ y, float* __restrict__ xcopy) {
+    const uint8_t* __restrict__ mask, float* __restrict__ y, float* __restrict__ xcopy,
+    const float* __restrict__ scale) {
     ef::dep_entry();
     SellPart p;
     const bool active = sell_part<S>(nSlices, off, p);
@@ -157,14 +159,24 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     if (r >= nN) return;
     const int m = perm ? perm[r] : r;
     const int d = 3 * m;
-    y[d + 0] = mask[d + 0] ? 0.f : y0;
-    y[d + 1] = mask[d + 1] ? 0.f : y1;
-    y[d + 2] = mask[d + 2] ? 0.f : y2;
-    if (COPY) {
+    if (scale) {
+        const float sc = *scale;
+        y0 *= sc;
+        y1 *= sc;
+        y2 *= sc;
+        if (COPY) {
+            xcopy[d + 0] = sc * x[d + 0];
+            xcopy[d + 1] = sc * x[d + 1];
+            xcopy[d + 2] = sc * x[d + 2];
+        }
+    } else if (COPY) {
         xcopy[d + 0] = x[d + 0];
         xcopy[d + 1] = x[d + 1];
         xcopy[d + 2] = x[d + 2];
     }
+    y[d + 0] = mask[d + 0] ? 0.f : y0;
+    y[d + 1] = mask[d + 1] ? 0.f : y1;
+    y[d + 2] = mask[d + 2] ? 0.f : y2;
 }
 
 // t = r - ys K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
@@ -329,11 +341,11 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
 
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s) {
+                               cudaStream_t s, const float* scale) {
     if (nSlices <= 0) return EF_OK;
 #define EF_SPMV3(C_, S_)                                                                                           \
     EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
-                           nN, nSlices, off, perm, col, v9, x, mask, y, xcopy))
+                           nN, nSlices, off, perm, col, v9, x, mask, y, xcopy, scale))
 #define EF_SPMV3_S(C_)      \
     if (split == 2)         \
         EF_SPMV3(C_, 2);    \

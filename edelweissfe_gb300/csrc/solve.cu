@@ -92,7 +92,13 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         c->fgPartN = dalloc<double>((size_t)c->fgNPart, &st);
         c->fgH = dalloc<double>(4 * (size_t)ef_fgmres_max_basis(), &st);
         if (!c->fgW || !c->fgPart || !c->fgPartN || !c->fgH) return st;
+        c->fgPartF = dalloc<float>((size_t)c->nSM * ef_fgmres_max_basis(), &st);
+        c->fgSc = dalloc<float>((size_t)ef_fgmres_max_basis(), &st);
+        c->fgTicket = dalloc<unsigned>(1, &st);
+        if (!c->fgPartF || !c->fgSc || !c->fgTicket) return st;
+        EF_CUDA(cudaMemsetAsync(c->fgTicket, 0, sizeof(unsigned), s));
         if (const char* e = getenv("EF_FGMRES_ETA")) c->fgEta2 = atof(e) * atof(e);
+        if (const char* e = getenv("EF_FGMRES_DEFER")) c->fgDefer = atoi(e) != 0;
         bool staged = false;  // measured slower than the unstaged kernel (EF_SPMV_STAGED=1 turns it on)
         if (const char* e = getenv("EF_SPMV_STAGED")) staged = atoi(e) != 0;
         c->spCap = staged ? ef_sp_stage_cap((int)c->nNodes, c->hRowPtr0.data()) : 0;
@@ -119,13 +125,17 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
     }
     double* pinRestart = c->fgPin + 2 * ldh;
     double* pinRestartDev = c->fgPinDev + 2 * ldh;
+    const bool collect = c->nnInit && c->nnEvery > 0 && c->nnMaxPerSolve > 0;
+    // deferred normalisation: needs the sliced-ELL product (it applies the factors) and one-pass
+    // Gram-Schmidt; training samples are taken from normalised basis vectors, so not with them
+    const bool defer = c->fgDefer && c->sellMode == 1 && !(c->fgEta2 > 0.0) && !collect;
+    float* scRestart = defer ? c->fgSc : nullptr;
     EF_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, s));
     // r0 = b (x = 0); v0 = r0 / |r0| (also into the preconditioner's input)
     EF_CUDA(cudaMemcpyAsync(V, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-    EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s));
+    EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s, scRestart));
     c->vcInStale = false;
     EF_CUDA(cudaEventRecord(c->fgNormDone, s));
-    const bool collect = c->nnInit && c->nnEvery > 0 && c->nnMaxPerSolve > 0;
     const bool snap = collect && c->nnKind == 0;
     const bool krylovSamples = collect && c->nnKind == 1;
     int nKrylov = 0;
@@ -149,7 +159,7 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         if (c->sellMode == 1)
             EF_CHECK(ef_launch_sell_spmv3((int)c->nNodes, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol,
                                           c->dSellV9, pz, c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n,
-                                          c->sellSplitProduct, s));
+                                          c->sellSplitProduct, s, defer ? c->fgSc + j : nullptr));
         else if (c->spCap > 0)
             EF_CHECK(ef_launch_spmv_f32_staged(c->nSM, c->spCap, (int)c->nNodes, c->dRowPtr, c->dColIdx,
                                                (const float*)c->dBsrVals, pz, c->dMask, V + (int64_t)(j + 1) * n,
@@ -158,8 +168,12 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
             EF_CHECK(ef_launch_spmv_f32_copy((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, pz,
                                              c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n, s));
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][3], s));
-        EF_CHECK(ef_launch_cgs_column(n, j + 1, V, n, c->fgPart, c->fgPartN, c->fgNPart, hG, hTmp, hAcc, c->fgEta2,
-                                      c->vcIn, c->fgPinDev + sl * ldh, ldh - 1, s));
+        if (defer)
+            EF_CHECK(ef_launch_gs_column(n, j + 1, V, n, c->fgPartF, c->fgPartN, c->nSM, c->fgSc, c->fgTicket,
+                                         c->vcIn, c->fgPinDev + sl * ldh, ldh - 1, s));
+        else
+            EF_CHECK(ef_launch_cgs_column(n, j + 1, V, n, c->fgPart, c->fgPartN, c->fgNPart, hG, hTmp, hAcc,
+                                          c->fgEta2, c->vcIn, c->fgPinDev + sl * ldh, ldh - 1, s));
         c->vcInStale = false;
         if (prof) EF_CUDA(cudaEventRecord(c->fgEv[sl][1], s));
         EF_CUDA(cudaEventRecord(c->fgDone[sl], s));
@@ -271,7 +285,7 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         EF_CHECK(ef_launch_spmv_f32((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, x, c->dMask,
                                     c->fineT, s));
         EF_CHECK(ef_launch_sub(n, b, c->fineT, V, s));
-        EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s));
+        EF_CHECK(ef_launch_normalize_first(n, V, c->fgPart, c->fgNPart, c->vcIn, pinRestartDev, 0, s, scRestart));
         c->vcInStale = false;
         EF_CUDA(cudaStreamSynchronize(s));
         beta = sqrt(pinRestart[0]);

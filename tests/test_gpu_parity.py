@@ -605,6 +605,38 @@ def test_fused_post_smoothing_matches_the_separate_kernels(gpu_lib, monkeypatch)
         assert abs(i1 - i0) <= max(2, i0 // 10), (fused, i0, i1)
 
 
+def test_fgmres_deferred_normalisation_matches_the_normalised_basis(gpu_lib, monkeypatch):
+    """Gram-Schmidt with the basis kept unnormalised (factors 1/|u_k| applied by the product and
+    the coefficient sums; two kernels per column, the default) against the basis normalised in
+    place (EF_FGMRES_DEFER=0; four kernels per column): the same 1e-8 solution in about the same
+    number of FGMRES iterations (the roundings differ), two launches fewer per iteration, and the
+    same bits when the solve is repeated."""
+    rng = np.random.default_rng(29)
+    out = {}
+    for defer in ("0", "1"):
+        monkeypatch.setenv("EF_FGMRES_DEFER", defer)
+        s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
+        if "b" not in out:
+            b = rng.normal(size=s.nDof)
+            b[s.dirIdxHost] = 1e-3 * rng.normal(size=s.dirIdxHost.size)
+            out["b"] = b
+        R = torch.as_tensor(out["b"], device="cuda")
+        s.linsolver.method = "fgmres"
+        s.linsolver.rtol = 1e-8
+        l0 = s.lib.ef_kernel_launches()
+        x = s.linearSolve(R).cpu().numpy()
+        per_it = (s.lib.ef_kernel_launches() - l0) / s.lastSolveInfo.iterations
+        assert s.lastSolveInfo.relResidual <= 1e-8
+        out[defer] = (x, s.lastSolveInfo.iterations, per_it)
+        if defer == "1":
+            assert np.array_equal(s.linearSolve(R).cpu().numpy(), x)
+        del s
+    (x0, i0, l0), (x1, i1, l1) = out["0"], out["1"]
+    assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0))
+    assert abs(i1 - i0) <= max(2, i0 // 10), (i0, i1)
+    assert l1 < l0 - 1.5, (l0, l1)
+
+
 def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
     """The three forms of the smoothed-aggregation restriction and prolongation: one pass from
     plane-major copies of P (the default, EF_SA_TRANSFER=2), block products + sums (1) and the
