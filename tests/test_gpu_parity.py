@@ -637,6 +637,51 @@ def test_fgmres_deferred_normalisation_matches_the_normalised_basis(gpu_lib, mon
     assert l1 < l0 - 1.5, (l0, l1)
 
 
+_PDL_CHILD = """
+import sys
+import numpy as np
+import torch
+sys.path[:0] = [sys.argv[2], sys.argv[3]]
+from cases import build_gpu_solver, j2_box_spec
+from edelweissfe_gb300 import _lib
+from edelweissfe_gb300.solver import TimeStep
+
+s = build_gpu_solver(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
+_lib.check(s.lib.ef_set_dirichlet(s.ctx, s.dirIdxHost.ctypes.data, s.dirIdxHost.size), "dir")
+dU = torch.zeros(s.nDof, dtype=torch.float64, device="cuda")
+P, F = s._vec(), s._vec()
+s.computeElements(dU, dU, P, F, TimeStep(1, 0.1, 0.1, 0.1, 0.1, 0.1))
+s.assembleStiffnessCSR()
+b = np.random.default_rng(31).normal(size=s.nDof)
+b[s.dirIdxHost] = 1e-3 * np.random.default_rng(32).normal(size=s.dirIdxHost.size)
+s.linsolver.method = "fgmres"
+s.linsolver.rtol = 1e-8
+x = s.linearSolve(torch.as_tensor(b, device="cuda")).cpu().numpy()
+assert s.lastSolveInfo.relResidual <= 1e-8
+np.save(sys.argv[1], np.append(x, float(s.lastSolveInfo.iterations)))
+"""
+
+
+def test_programmatic_dependent_launch_changes_no_result(gpu_lib, tmp_path):
+    """The Krylov-iteration and multigrid kernels launched with programmatic dependent launch (the
+    default: each kernel is scheduled while its predecessor finishes and waits for it in hardware
+    before any memory access) and without it (EF_PDL=0): the same bits and iteration count of a
+    1e-8 FGMRES solve.  The setting is read once per process, so each runs in a child process."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for pdl in ("0", "1"):
+        f = str(tmp_path / f"x{pdl}.npy")
+        env = dict(os.environ, EF_PDL=pdl)
+        subprocess.run([sys.executable, "-c", _PDL_CHILD, f, os.path.join(root, "tests"), root], env=env,
+                       check=True, timeout=600)
+        out[pdl] = np.load(f)
+    assert np.array_equal(out["0"], out["1"])
+
+
 def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
     """The three forms of the smoothed-aggregation restriction and prolongation: one pass from
     plane-major copies of P (the default, EF_SA_TRANSFER=2), block products + sums (1) and the
