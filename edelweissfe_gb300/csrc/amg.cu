@@ -374,6 +374,50 @@ __global__ void __launch_bounds__(kSaRestrictThreads) sa_restrict_onepass_h_kern
     }
 }
 
+// the same restriction with a warp per coarse node (kSaRestrictWarpNodes nodes per CTA): lanes
+// stride over the node's blocks, a shuffle tree per value, no shared memory or CTA barrier
+constexpr int kSaRestrictWarpNodes = 4;
+__global__ void __launch_bounds__(32 * kSaRestrictWarpNodes) sa_restrict_warp_h_kernel(
+    int nC, const int32_t* __restrict__ tPtr, const int32_t* __restrict__ rowT, const uint4* __restrict__ q0,
+    const uint4* __restrict__ q1, const uint32_t* __restrict__ q2, const float* __restrict__ t,
+    const uint8_t* __restrict__ coarseDead, float* __restrict__ rc) {
+    ef::dep_entry();
+    const int I = blockIdx.x * kSaRestrictWarpNodes + (threadIdx.x >> 5);
+    if (I >= nC) return;
+    const int lane = threadIdx.x & 31;
+    float a[BC];
+#pragma unroll
+    for (int j = 0; j < BC; ++j) a[j] = 0.f;
+    const int k1 = tPtr[I + 1];
+#pragma unroll 2
+    for (int k = tPtr[I] + lane; k < k1; k += 32) {
+        const uint4 u = __ldcs(q0 + k), v = __ldcs(q1 + k);
+        const uint32_t w = __ldcs(q2 + k);
+        const int64_t m = __ldcs(rowT + k);
+        const float t0 = t[3 * m], t1 = t[3 * m + 1], t2 = t[3 * m + 2];
+        float P[18];
+        const uint32_t words[9] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w, w};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float2 f = sa_unpack_bf16x2(words[q]);
+            P[2 * q] = f.x;
+            P[2 * q + 1] = f.y;
+        }
+#pragma unroll
+        for (int j = 0; j < BC; ++j) a[j] += P[j] * t0 + P[BC + j] * t1 + P[2 * BC + j] * t2;
+    }
+#pragma unroll
+    for (int j = 0; j < BC; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_xor_sync(0xffffffffu, a[j], o);
+    if (lane < BC) {
+        float v = a[0];
+#pragma unroll
+        for (int j = 1; j < BC; ++j) v = lane == j ? a[j] : v;
+        rc[BC * I + lane] = coarseDead[BC * I + lane] ? 0.f : v;
+    }
+}
+
 // prolongation: a CTA per kSaProlongRows consecutive finer rows; a thread per P block of those
 // rows (row order) leaves the block's product in shared memory, then
 // thread r sums row r's products in block order.  cap >= the block count of every such group of
@@ -1408,8 +1452,15 @@ ef_status ef_launch_sa_restrict_onepass_h(int nC, const int32_t* tPtr, const int
                                           const void* q1, const void* q2, const float* t, const uint8_t* coarseDead,
                                           float* rc, cudaStream_t s) {
     if (nC <= 0) return EF_OK;
-    EF_CUDA(ef::launch_dep(sa_restrict_onepass_h_kernel, nC, kSaRestrictThreads, 0, s, nC, tPtr, rowT,
-                           (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, t, coarseDead, rc));
+    const char* e = getenv("EF_SA_RESTRICT_WARP");  // read at each launch site (the cycle is captured once)
+    const bool warp = !e || atoi(e) != 0;
+    if (warp)
+        EF_CUDA(ef::launch_dep(sa_restrict_warp_h_kernel, nb_(nC, kSaRestrictWarpNodes), 32 * kSaRestrictWarpNodes,
+                               0, s, nC, tPtr, rowT, (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, t,
+                               coarseDead, rc));
+    else
+        EF_CUDA(ef::launch_dep(sa_restrict_onepass_h_kernel, nC, kSaRestrictThreads, 0, s, nC, tPtr, rowT,
+                               (const uint4*)q0, (const uint4*)q1, (const uint32_t*)q2, t, coarseDead, rc));
     return EF_OK;
 }
 

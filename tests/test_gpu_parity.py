@@ -684,14 +684,16 @@ def test_programmatic_dependent_launch_changes_no_result(gpu_lib, tmp_path):
 
 def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
     """The three forms of the smoothed-aggregation restriction and prolongation: one pass from
-    plane-major copies of P (the default, EF_SA_TRANSFER=2), block products + sums (1) and the
+    plane-major copies of P (the default, EF_SA_TRANSFER=2; on the fine level a warp per coarse
+    node, or a CTA per coarse node with EF_SA_RESTRICT_WARP=0), block products + sums (1) and the
     one-stage kernels over the block-major P (0): the same 1e-8 solution in about the same number
     of FGMRES iterations (the summation orders differ), and the same bits when the default's solve
     is repeated."""
     rng = np.random.default_rng(17)
     out = {}
-    for mode in ("0", "1", "2"):
-        monkeypatch.setenv("EF_SA_TRANSFER", mode)
+    for mode in ("0", "1", "2c", "2"):
+        monkeypatch.setenv("EF_SA_TRANSFER", mode[0])
+        monkeypatch.setenv("EF_SA_RESTRICT_WARP", "0" if mode == "2c" else "1")
         s = _assembled(j2_box_spec(24, 10, 10, 2.4, 1.0, 1.0))
         if "b" not in out:
             b = rng.normal(size=s.nDof)
@@ -707,7 +709,7 @@ def test_sa_transfer_forms_agree(gpu_lib, monkeypatch):
             assert np.array_equal(s.linearSolve(R).cpu().numpy(), x)
         del s
     x0, i0 = out["0"]
-    for mode in ("1", "2"):
+    for mode in ("1", "2c", "2"):
         x1, i1 = out[mode]
         assert np.max(np.abs(x1 - x0)) <= 1e-6 * np.max(np.abs(x0)), mode
         assert abs(i1 - i0) <= max(2, i0 // 10), (mode, i0, i1)
