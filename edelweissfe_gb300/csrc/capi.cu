@@ -234,6 +234,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->dSellOff);
     F(c->dSellPerm);
     F(c->dSellCol);
+    F(c->dSellDia);
     F(c->dSellSrc);
     F(c->dSellV9);
     F(c->dSellV8);

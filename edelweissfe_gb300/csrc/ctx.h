@@ -185,11 +185,11 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
                                  const int32_t* col, const float* binv, const uint8_t* mask, cudaStream_t s);
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s, const float* scale = nullptr);
+                               cudaStream_t s, const float* scale = nullptr, const int32_t* dia = nullptr);
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
-                                     cudaStream_t s, float ys = 1.f);
+                                     cudaStream_t s, float ys = 1.f, const int32_t* dia = nullptr);
 
 // the same on a 6-DOF level (amg.cu): C FP32 in the pattern of A P, a warp per row
 ef_status ef_launch_sa_post6_setup(int64_t nAP, const int32_t* apRow, const int32_t* apToP, const float* Pv,
@@ -458,6 +458,10 @@ struct ef_ctx {
     int sellSplitProduct = 1;              // the same for the FP32 product (EF_SELL_SPLIT_PRODUCT)
     int32_t* dSellPerm = nullptr;          // [nNodes] block row of each SELL row (null: identity)
     int32_t* dSellCol = nullptr;           // [sellE] block column (padding: the row itself)
+    // diagonal form (EF_SELL_DIA): every slice has the same slot columns, slot column j at node
+    // offset dSellDia[j] from the row (no column array read by the fine kernels); null: off
+    int32_t* dSellDia = nullptr;
+    int sellDiaN = 0;
     int32_t* dSellSrc = nullptr;           // [sellE] source block in the BSR values (-1: padding)
     float* dSellV9 = nullptr;              // FP32 values, nine planes per slot column
     void* dSellV8 = nullptr;               // BF16 values 0..7 per slot (16-byte words)

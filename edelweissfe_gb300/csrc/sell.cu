@@ -76,6 +76,13 @@ __global__ void sell_refresh_kernel(int64_t nE, const int32_t* __restrict__ src,
     }
 }
 
+// Diagonal form of the slices (structured meshes): every block column is its row plus one of a few
+// node offsets, slot column j of every slice holding offset dia[j] (zero blocks where the row has
+// no such neighbour), so the column is computed, not loaded, and the x gathers of a warp are 32
+// consecutive nodes.  The rows are in natural order; a column outside the nodes is clamped (its
+// block is zero).
+__device__ __forceinline__ int dia_column(int row, int d, int nN) { return min(max(row + d, 0), nN - 1); }
+
 // The slice and entry range of this warp: warp h of the S warps of a slice takes entries
 // [j0, j1) = [ceil(h w / S), ceil((h + 1) w / S)) of its width w.  Returns false past the last
 // slice.
@@ -128,12 +135,12 @@ __device__ __forceinline__ bool sell_combine(const SellPart& p, bool active, flo
 
 // y = sc K x on the free DOFs (0 on masked rows); COPY: xcopy = sc x as well; sc = *scale (1 without
 // one: the FGMRES basis vector x then carries its normalisation factor); S warps per slice
-template <bool COPY, int S>
+template <bool COPY, int S, bool DIA>
 __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const float* __restrict__ v9, const float* __restrict__ x,
     const uint8_t* __restrict__ mask, float* __restrict__ y, float* __restrict__ xcopy,
-    const float* __restrict__ scale) {
+    const float* __restrict__ scale, const int32_t* __restrict__ dia) {
     ef::dep_entry();
     SellPart p;
     const bool active = sell_part<S>(nSlices, off, p);
@@ -141,9 +148,10 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     if (active) {
         const int32_t* cs = col + p.e0 + p.lane;
         const float* vs = v9 + 9 * p.e0 + p.lane;
+        const int row = p.sl * 32 + p.lane;
 #pragma unroll 3
         for (int j = p.j0; j < p.j1; ++j) {
-            const int c3 = 3 * __ldcs(cs + 32 * j);
+            const int c3 = 3 * (DIA ? dia_column(row, __ldg(dia + j), nN) : __ldcs(cs + 32 * j));
             const float* vv = vs + 288 * j;
             const float a0 = __ldcs(vv), a1 = __ldcs(vv + 32), a2 = __ldcs(vv + 64);
             const float a3 = __ldcs(vv + 96), a4 = __ldcs(vv + 128), a5 = __ldcs(vv + 160);
@@ -181,12 +189,12 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
 
 // t = r - ys K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
 // t = x + omega D^-1 (r - K x) (masked DOFs keep x), from the BF16 split copy; S warps per slice
-template <int S>
+template <int S, bool DIA>
 __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const uint4* __restrict__ v8, const __nv_bfloat16* __restrict__ v1,
     const float* __restrict__ x, const float* __restrict__ r, const uint8_t* __restrict__ mask, float* __restrict__ t,
-    const float* __restrict__ binv, float omega, float ys) {
+    const float* __restrict__ binv, float omega, float ys, const int32_t* __restrict__ dia) {
     ef::dep_entry();
     SellPart p;
     const bool active = sell_part<S>(nSlices, off, p);
@@ -195,9 +203,10 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_level3_bf16_kernel
         const int32_t* cs = col + p.e0 + p.lane;
         const uint4* qs = v8 + p.e0 + p.lane;
         const __nv_bfloat16* ws = v1 + p.e0 + p.lane;
+        const int row = p.sl * 32 + p.lane;
 #pragma unroll 4
         for (int j = p.j0; j < p.j1; ++j) {
-            const int c3 = 3 * __ldcs(cs + 32 * j);
+            const int c3 = 3 * (DIA ? dia_column(row, __ldg(dia + j), nN) : __ldcs(cs + 32 * j));
             const uint4 q = __ldcs(qs + 32 * j);
             const float w8 = __bfloat162float(ws[32 * j]);
             const float x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
@@ -341,11 +350,19 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
 
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s, const float* scale) {
+                               cudaStream_t s, const float* scale, const int32_t* dia) {
     if (nSlices <= 0) return EF_OK;
-#define EF_SPMV3(C_, S_)                                                                                           \
-    EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
-                           nN, nSlices, off, perm, col, v9, x, mask, y, xcopy, scale))
+#define EF_SPMV3(C_, S_)                                                                                              \
+    do {                                                                                                              \
+        if (dia)                                                                                                      \
+            EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_, true>, sell_split_grid(nSlices, S_),                     \
+                                   sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, v9, x, mask, y, xcopy,  \
+                                   scale, dia));                                                                      \
+        else                                                                                                          \
+            EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_, false>, sell_split_grid(nSlices, S_),                    \
+                                   sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, v9, x, mask, y, xcopy,  \
+                                   scale, dia));                                                                      \
+    } while (0)
 #define EF_SPMV3_S(C_)      \
     if (split == 2)         \
         EF_SPMV3(C_, 2);    \
@@ -369,12 +386,19 @@ ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const in
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
-                                     cudaStream_t s, float ys) {
+                                     cudaStream_t s, float ys, const int32_t* dia) {
     if (nSlices <= 0) return EF_OK;
-#define EF_L3(S_)                                                                                                   \
-    EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel<S_>, sell_split_grid(nSlices, S_), sell_split_threads(S_), 0, s, \
-                           nN, nSlices, off, perm, col, (const uint4*)v8, (const __nv_bfloat16*)v1, x, r, mask, t,   \
-                           binv, omega, ys))
+#define EF_L3(S_)                                                                                                    \
+    do {                                                                                                             \
+        if (dia)                                                                                                     \
+            EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel<S_, true>, sell_split_grid(nSlices, S_),                  \
+                                   sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, (const uint4*)v8,      \
+                                   (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega, ys, dia));                  \
+        else                                                                                                         \
+            EF_CUDA(ef::launch_dep(sell_level3_bf16_kernel<S_, false>, sell_split_grid(nSlices, S_),                 \
+                                   sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, (const uint4*)v8,      \
+                                   (const __nv_bfloat16*)v1, x, r, mask, t, binv, omega, ys, dia));                  \
+    } while (0)
     if (split == 1)
         EF_L3(1);
     else if (split == 2)

@@ -159,7 +159,7 @@ static ef_status run_fgmres(ef_ctx* c, const float* b, float* x, int maxIter, do
         if (c->sellMode == 1)
             EF_CHECK(ef_launch_sell_spmv3((int)c->nNodes, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol,
                                           c->dSellV9, pz, c->dMask, V + (int64_t)(j + 1) * n, Z + (int64_t)j * n,
-                                          c->sellSplitProduct, s, defer ? c->fgSc + j : nullptr));
+                                          c->sellSplitProduct, s, defer ? c->fgSc + j : nullptr, c->dSellDia));
         else if (c->spCap > 0)
             EF_CHECK(ef_launch_spmv_f32_staged(c->nSM, c->spCap, (int)c->nNodes, c->dRowPtr, c->dColIdx,
                                                (const float*)c->dBsrVals, pz, c->dMask, V + (int64_t)(j + 1) * n,
@@ -471,14 +471,14 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
         if (c->sellScaled)
             return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
                                               c->dSellV1, c->vcIn, c->vcIn, c->dMask, c->fineT, nullptr, 0.f,
-                                              c->sellSplit, s, omega);
+                                              c->sellSplit, s, omega, c->dSellDia);
         return ef_launch_sell_level3_bf16(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV8,
                                           c->dSellV1, c->fineX, c->vcIn, c->dMask, c->fineT, (const float*)c->dBinv,
-                                          omega, c->sellSplit, s);
+                                          omega, c->sellSplit, s, 1.f, c->dSellDia);
     };
     auto product = [&]() {
         return ef_launch_sell_spmv3(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV9, c->vcOut,
-                                    c->dMask, c->fineT, c->fgZ, c->sellSplitProduct, s);
+                                    c->dMask, c->fineT, c->fgZ, c->sellSplitProduct, s, nullptr, c->dSellDia);
     };
     const bool post = c->postSlots > 0 && !c->amg.empty() && c->amg[0].x;
     auto fused = [&]() {
@@ -501,11 +501,13 @@ ef_status ef_fine_kernel_profile(ef_ctx* c, int reps, double* ms, double* bytes,
     }
     // algorithmic DRAM bytes per launch: the real blocks (values and column indices; the slices'
     // padding is layout overhead, 3.9 % on the structured box) and the per-row vectors
+    // (the diagonal form reads no column indices: 4 bytes less per block)
     const double nb = (double)c->nBlocks, nn = (double)nN, ns = (double)c->sellSlices;
-    bytes[0] = nb * (16 + 2 + 4) + nn * (3 * 4 /*x*/ + 3 * 4 /*r*/ + 9 * 4 /*D^-1*/ + 3 /*mask*/ + 3 * 4 /*out*/) +
+    const double colB = c->dSellDia ? 0.0 : 4.0;
+    bytes[0] = nb * (16 + 2 + colB) + nn * (3 * 4 /*x*/ + 3 * 4 /*r*/ + 9 * 4 /*D^-1*/ + 3 /*mask*/ + 3 * 4 /*out*/) +
                (ns + 1) * 8;
     if (c->sellScaled) bytes[0] -= nn * (3 * 4 /*x*/ + 9 * 4 /*D^-1*/);  // x is r, no D^-1 in the residual
-    bytes[1] = nb * (9 * 4 + 4) + nn * (3 * 4 /*x*/ + 3 /*mask*/ + 3 * 4 /*y*/ + 3 * 4 /*copy*/) + (ns + 1) * 8;
+    bytes[1] = nb * (9 * 4 + colB) + nn * (3 * 4 /*x*/ + 3 /*mask*/ + 3 * 4 /*y*/ + 3 * 4 /*copy*/) + (ns + 1) * 8;
     // the fused post-smoothing: C blocks (18 BF16 values and a column) of the pattern of A P, the
     // per-row r, t, D^-1, mask and output (the coarse correction e, 40 k values, is read from cache)
     bytes[2] = post ? (double)c->amg[0].saNAP * (18 * 2 + 4) +
