@@ -584,6 +584,125 @@ __global__ void __launch_bounds__(kBlock) small_strain_apply_df_kernel(int nEl, 
     }
 }
 
+// The same product for elements with 8 Gauss points (TPE = 8 threads per element, a thread per
+// Gauss point) without the per-element geometry and stress stages in shared memory (which held
+// occupancy near a third): the Gauss-point thread keeps its stress, and for each node a forms
+// its term sigma_q . g_qa (geometry re-read from L1) as a double-float value; the 8 threads of
+// the element sum the terms by an xor butterfly of double-float additions (TwoSum of the high
+// parts: its error term is exact, so both partners of a pair get the same sum and every lane
+// ends with the same bits), and thread a keeps node a's result.  Only x is staged.
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bv = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bv)), __fsub_rn(b.hi, bv));
+    return DF{s, __fadd_rn(__fadd_rn(a.lo, b.lo), err)};
+}
+__device__ __forceinline__ DF df_shfl_xor8(DF v, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, v.hi, o, 8), __shfl_xor_sync(0xffffffffu, v.lo, o, 8)};
+}
+
+template <int NN>
+__global__ void __launch_bounds__(kBlock) small_strain_apply_df8_kernel(int nEl, const int32_t* __restrict__ nodeDof,
+                                                                        const float2* __restrict__ geoS,
+                                                                        const double* __restrict__ x,
+                                                                        const double* __restrict__ tang,
+                                                                        double* __restrict__ ye, int intConv) {
+    constexpr int NQ = 8, TPE = 8, EPB = kBlock / TPE;
+    constexpr int ND = 3 * NN;
+    constexpr int NG = 3 * NN + 1;
+    __shared__ float2 xv[EPB][ND + 1];
+    const int tid = threadIdx.x;
+    const int le = tid / TPE;
+    const int q = tid % TPE;
+    const int e0 = blockIdx.x * EPB + le;
+    const bool valid = e0 < nEl;
+    const int e = valid ? e0 : nEl - 1;  // the last element's lanes keep the shuffles full
+    for (int a = q; a < NN; a += TPE) {
+        const int d = nodeDof[(int64_t)e * NN + a];
+        xv[le][3 * a + 0] = df_split_sel(x[d + 0], intConv);
+        xv[le][3 * a + 1] = df_split_sel(x[d + 1], intConv);
+        xv[le][3 * a + 2] = df_split_sel(x[d + 2], intConv);
+    }
+    __syncthreads();
+    const float2* gq = geoS + ((int64_t)e * NQ + q) * NG;
+    DF H[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) H[i][j] = DF{0.f, 0.f};
+#pragma unroll 4
+    for (int a = 0; a < NN; ++a) {
+        float2 ga[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ga[c] = gq[3 * a + c];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float2 u = xv[le][3 * a + i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) df_fma(H[i][j], u, ga[j]);
+        }
+    }
+    const double ep[6] = {df_value_sel(H[0][0], intConv), df_value_sel(H[1][1], intConv),
+                          df_value_sel(H[2][2], intConv),
+                          df_value_sel(H[0][1], intConv) + df_value_sel(H[1][0], intConv),
+                          df_value_sel(H[0][2], intConv) + df_value_sel(H[2][0], intConv),
+                          df_value_sel(H[1][2], intConv) + df_value_sel(H[2][1], intConv)};
+    const int64_t nQPtot = (int64_t)nEl * NQ;
+    const int64_t qi = (int64_t)e * NQ + q;
+    const double lt = tang[qi], mt = tang[nQPtot + qi], c1 = tang[2 * nQPtot + qi];
+    const double tr = ep[0] + ep[1] + ep[2];
+    double ne = 0.0, n[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) n[i] = 0.0;
+    if (c1 != 0.0) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            n[i] = tang[(3 + i) * nQPtot + qi];
+            ne += n[i] * ep[i];
+        }
+    }
+    float2 sw[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sw[i] = df_split_sel(lt * tr + 2.0 * mt * ep[i] - c1 * n[i] * ne, intConv);
+#pragma unroll
+    for (int i = 3; i < 6; ++i) sw[i] = df_split_sel(mt * ep[i] - c1 * n[i] * ne, intConv);
+    DF own0{0.f, 0.f}, own1{0.f, 0.f}, own2{0.f, 0.f};
+#pragma unroll 2
+    for (int a = 0; a < NN; ++a) {
+        const float2 gx = gq[3 * a + 0], gy = gq[3 * a + 1], gz = gq[3 * a + 2];
+        DF f0{0.f, 0.f}, f1{0.f, 0.f}, f2{0.f, 0.f};
+        df_fma(f0, sw[0], gx);
+        df_fma(f0, sw[3], gy);
+        df_fma(f0, sw[4], gz);
+        df_fma(f1, sw[3], gx);
+        df_fma(f1, sw[1], gy);
+        df_fma(f1, sw[5], gz);
+        df_fma(f2, sw[4], gx);
+        df_fma(f2, sw[5], gy);
+        df_fma(f2, sw[2], gz);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            f0 = df_add(f0, df_shfl_xor8(f0, o));
+            f1 = df_add(f1, df_shfl_xor8(f1, o));
+            f2 = df_add(f2, df_shfl_xor8(f2, o));
+        }
+        if ((a & (TPE - 1)) == q) {
+            own0 = f0;
+            own1 = f1;
+            own2 = f2;
+        }
+        if ((a & (TPE - 1)) == TPE - 1 || a == NN - 1) {
+            const int ao = (a & ~(TPE - 1)) + q;  // the node this lane owns in this group of 8
+            if (valid && ao <= a) {
+                double* o = ye + (int64_t)e * ND + 3 * ao;
+                o[0] = df_value_sel(own0, intConv);
+                o[1] = df_value_sel(own1, intConv);
+                o[2] = df_value_sel(own2, intConv);
+            }
+        }
+    }
+}
+
 // Consistent body force of a constant load vector (element.py:348-371): Pe[a,c] = load_c sum_q N_qa detJ_q w_q
 template <int NN, int NQ>
 __global__ void body_force_kernel(const ElemTables* __restrict__ T, int nEl, const double* __restrict__ geo,
@@ -657,6 +776,16 @@ static ef_status launch_apply(const Group& g, const double* x, const double* tan
         const char* e = getenv("EF_APPLY_FP64");
         return e && atoi(e) != 0;
     }();
+    static const bool staged = [] {
+        const char* e = getenv("EF_APPLY_STAGED");
+        return e && atoi(e) != 0;
+    }();
+    if (g.geoS && !fp64 && NQ == 8 && !staged) {  // 8 Gauss points: the butterfly form (EF_APPLY_STAGED=1: staged)
+        small_strain_apply_df8_kernel<NN><<<(g.nEl + kBlock / 8 - 1) / (kBlock / 8), kBlock, 0, ef::counted(s)>>>(
+            g.nEl, g.nodeDof, g.geoS, x, tang, ye, g.intConv);
+        EF_CUDA(cudaGetLastError());
+        return EF_OK;
+    }
     if (g.geoS && !fp64) {  // double-float contractions (default); EF_APPLY_FP64=1: the FP64 kernel
         const size_t smemDF = sizeof(ApplyDFShared<NN, NQ>);
         auto kd = small_strain_apply_df_kernel<NN, NQ>;
