@@ -847,91 +847,113 @@ __global__ void prolong_kernel(int nN, const int32_t* __restrict__ agg, const fl
     prolong_row<BF, false>(m, agg, offs, xc, mask, x, alpha);
 }
 
-// dense pseudo-inverse of the coarsest operator (n = 6 nN <= kMaxCoarsestDof), FP64 Gauss-Jordan
-// with partial pivoting in shared memory, one CTA; pivots below 1e-10 of the largest diagonal
+// dense pseudo-inverse of the coarsest operator (n = 6 nN <= kMaxCoarsestDof), FP32 Gauss-Jordan
+// with partial pivoting in shared memory, one CTA; pivots below 1e-6 of the largest diagonal
 // entry mark a null direction whose rows/columns of the inverse are zero
 constexpr int kMaxCoarsestDof = 96;
 __global__ void coarsest_inverse_kernel(int nN, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
                                         const float* __restrict__ vals, float* __restrict__ inv) {
     // FP32 Gauss-Jordan on [A | I] in shared memory (one CTA; the FP64 version spent ~1.5 ms in
     // the FP64 pipe of a single SM); pivots below 1e-6 of the largest diagonal entry mark a null
-    // direction (FP32 round-off of a zero pivot is ~1e-7 of it)
+    // direction (FP32 round-off of a zero pivot is ~1e-7 of it).  Two CTA barriers per column:
+    // the pivot of column col + 1 is chosen while column col is eliminated (the thread updating
+    // entry (r, col + 1), r > col, posts (|value|, smallest row on ties) by a 64-bit atomic max),
+    // the row swap and the scaling of the pivot row are one pass, and the left block's column col,
+    // never read again, is left as it is.
     extern __shared__ float smemF[];
     const int n = BC * nN;
     const int ld = 2 * n + 1;
     auto A = [&](int r, int c) -> float& { return smemF[r * ld + c]; };
-    __shared__ int piv;
+    __shared__ unsigned long long key[2];
     __shared__ float dmax;
     __shared__ unsigned char drop[kMaxCoarsestDof];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     for (int r = threadIdx.y; r < n; r += blockDim.y)
         for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) A(r, c) = (c >= n && c - n == r) ? 1.f : 0.f;
     __syncthreads();
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int m = tid; m < nN; m += nt)
-        for (int k = rowPtr[m]; k < rowPtr[m + 1]; ++k) {
-            const int cn = colIdx[k];
-            for (int i = 0; i < BC; ++i)
-                for (int j = 0; j < BC; ++j) A(BC * m + i, BC * cn + j) = vals[(int64_t)k * BC * BC + i * BC + j];
-        }
+    // the blocks' values spread over all threads (a value per thread and step; the row of block
+    // k by a scan of the at most 16 row starts)
+    const int nnzV = rowPtr[nN] * BC * BC;
+    for (int v = tid; v < nnzV; v += nt) {
+        const int k = v / (BC * BC), ij = v - k * (BC * BC);
+        int m = 0;
+        while (m + 1 < nN && rowPtr[m + 1] <= k) ++m;
+        A(BC * m + ij / BC, BC * colIdx[k] + ij % BC) = vals[v];
+    }
     __syncthreads();
-    if (tid == 0) {
+    if (threadIdx.y == 0) {  // the largest |diagonal| by the first warp
         float d = 0.f;
-        for (int i = 0; i < n; ++i) d = fmaxf(d, fabsf(A(i, i)));
-        dmax = d;
+        for (int i = threadIdx.x; i < n; i += 32) d = fmaxf(d, fabsf(A(i, i)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+        if (threadIdx.x == 0) dmax = d;
     }
     for (int i = tid; i < n; i += nt) drop[i] = 0;
-    __syncthreads();
+    // the pivot key of an entry: |value| bits above, the complement of the row below (the larger
+    // key: the larger magnitude, then the smaller row)
+    auto pkey = [](float v, int r) -> unsigned long long {
+        return ((unsigned long long)__float_as_uint(fabsf(v)) << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)r);
+    };
+    bool searched = false;  // the current column's key was posted by the previous elimination
     for (int col = 0; col < n; ++col) {
-        if (threadIdx.y == 0) {
-            // partial pivoting by the first warp: the largest |A(r, col)|, r >= col, the smallest
-            // such r on ties (the row a serial scan with a strict comparison keeps)
-            int p = -1;
-            float best = -1.f;
-            for (int r = col + threadIdx.x; r < n; r += 32) {
-                const float v = fabsf(A(r, col));
-                if (v > best) {
-                    best = v;
-                    p = r;
-                }
-            }
+        if (!searched) {  // column 0, or the column after a dropped one: an explicit search
+            if (tid == 0) key[col & 1] = 0ull;
+            __syncthreads();
+            for (int r = col + tid; r < n; r += nt) atomicMax(&key[col & 1], pkey(A(r, col), r));
+        }
+        __syncthreads();
+        const unsigned long long kk = key[col & 1];
+        const float best = __uint_as_float((unsigned)(kk >> 32));
+        const int piv = (best > 1e-6f * dmax) ? (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) : -1;
+        if (piv < 0) {
+            if (tid == 0) drop[col] = 1;
+            searched = false;
+            continue;
+        }
+        // swap rows col and piv and scale the pivot row by 1 / d over the live columns
+        const float d = A(piv, col);
+        if (tid == 0) key[(col + 1) & 1] = 0ull;
+        for (int c = col + 1 + tid; c < 2 * n; c += nt) {
+            const float a = A(col, c), b = A(piv, c);
+            A(col, c) = b / d;
+            if (piv != col) A(piv, c) = a;
+        }
+        __syncthreads();
+        // eliminate column col from every other row (its multiplier from the unswapped column:
+        // row piv now holds the old row col, whose entry is still at (col, col)): warp w takes
+        // columns col + 1 + w + 32 k, lane l rows l + 32 i (a row stride of ld = 2 n + 1 words
+        // keeps the lanes on distinct banks); warp 0, which holds column col + 1, picks the next
+        // pivot among its rows below col by a shuffle tree
+        {
+            const int lane = threadIdx.x, w = threadIdx.y;
+            float f[kMaxCoarsestDof / 32];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int op = __shfl_xor_sync(0xffffffffu, p, o);
-                if (ob > best || (ob == best && op >= 0 && (p < 0 || op < p))) {
-                    best = ob;
-                    p = op;
+            for (int i = 0; i < kMaxCoarsestDof / 32; ++i) {
+                const int r = lane + 32 * i;
+                f[i] = (r < n && r != col) ? ((r == piv) ? A(col, col) : A(r, col)) : 0.f;
+            }
+            unsigned long long kbest = 0ull;
+            for (int c = col + 1 + w; c < 2 * n; c += 32) {
+                const float a = A(col, c);
+#pragma unroll
+                for (int i = 0; i < kMaxCoarsestDof / 32; ++i) {
+                    const int r = lane + 32 * i;
+                    if (r < n && r != col) {
+                        const float v = A(r, c) - f[i] * a;
+                        A(r, c) = v;
+                        if (c == col + 1 && r > col) kbest = max(kbest, pkey(v, r));
+                    }
                 }
             }
-            if (threadIdx.x == 0) {
-                piv = best > 1e-6f * dmax ? p : -1;
-                if (piv < 0) drop[col] = 1;
+            if (w == 0) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) kbest = max(kbest, __shfl_xor_sync(0xffffffffu, kbest, o));
+                if (lane == 0) key[(col + 1) & 1] = kbest;
             }
         }
-        __syncthreads();
-        if (piv < 0) continue;
-        if (piv != col)
-            for (int c = tid; c < 2 * n; c += nt) {
-                const float tmp = A(col, c);
-                A(col, c) = A(piv, c);
-                A(piv, c) = tmp;
-            }
-        __syncthreads();
-        const float d = A(col, col);
-        __syncthreads();
-        for (int c = tid; c < 2 * n; c += nt) A(col, c) /= d;
-        __syncthreads();
-        for (int r = threadIdx.y; r < n; r += blockDim.y) {
-            if (r == col) continue;
-            const float f = A(r, col);
-            for (int c = threadIdx.x; c < 2 * n; c += blockDim.x)
-                if (c != col) A(r, c) -= f * A(col, c);
-        }
-        __syncthreads();
-        for (int r = tid; r < n; r += nt)
-            if (r != col) A(r, col) = 0.f;
-        __syncthreads();
+        searched = true;
     }
+    __syncthreads();
     for (int i = tid; i < n * n; i += nt) {
         const int r = i / n, c = i % n;
         inv[i] = (drop[r] || drop[c]) ? 0.f : A(r, n + c);
