@@ -187,6 +187,70 @@ __global__ void sa_galerkin_kernel(int64_t nC, const int64_t* __restrict__ cSeg,
     sa_galerkin_block<BF>(S, cSeg, cP, cAP, Pv, APv, coarseRowOfBlock, coarseCol, coarseDead, coarseVals);
 }
 
+// A warp per coarse block (8 per CTA): the lanes form the products s_ij = sum_q P_qi Q_qj of up
+// to 32 pairs at once into shared memory, then lane v (and v + 32) adds value v of each pair with
+// TwoSum in list order -- the operations of sa_galerkin_block in the same order (the same bits),
+// with the pairs' loads issued by 32 lanes together instead of one thread walking them.
+constexpr int kGalWarps = 8;
+template <int BF>
+__global__ void __launch_bounds__(32 * kGalWarps) sa_galerkin_warp_kernel(
+    int64_t nC, const int64_t* __restrict__ cSeg, const int32_t* __restrict__ cP, const int32_t* __restrict__ cAP,
+    const float* __restrict__ Pv, const float* __restrict__ APv, const int32_t* __restrict__ coarseRowOfBlock,
+    const int32_t* __restrict__ coarseCol, const uint8_t* __restrict__ coarseDead, float* __restrict__ coarseVals) {
+    constexpr int NV = BC * BC;  // 36 values per coarse block
+    __shared__ float sp[kGalWarps][32][NV + 1];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t S = (int64_t)blockIdx.x * kGalWarps + wp;
+    if (S >= nC) return;  // the whole warp
+    const int64_t t0 = cSeg[S], t1 = cSeg[S + 1];
+    float hi0 = 0.f, lo0 = 0.f, hi1 = 0.f, lo1 = 0.f;
+    auto add = [](float& hi, float& lo, float v) {
+        const float tt = sa_add_rn(hi, v);
+        const float bv = sa_sub_rn(tt, hi);
+        lo = sa_add_rn(lo, sa_add_rn(sa_sub_rn(hi, sa_sub_rn(tt, bv)), sa_sub_rn(v, bv)));
+        hi = tt;
+    };
+    for (int64_t tb = t0; tb < t1; tb += 32) {
+        const int64_t t = tb + lane;
+        if (t < t1) {
+            const float* P = Pv + (int64_t)cP[t] * BF * BC;
+            const float* Q = APv + (int64_t)cAP[t] * BF * BC;
+            float pr[BF * BC], qr[BF * BC];
+#pragma unroll
+            for (int u = 0; u < BF * BC; ++u) {
+                pr[u] = P[u];
+                qr[u] = Q[u];
+            }
+#pragma unroll
+            for (int i = 0; i < BC; ++i)
+#pragma unroll
+                for (int j = 0; j < BC; ++j) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int q = 0; q < BF; ++q) s += pr[q * BC + i] * qr[q * BC + j];
+                    sp[wp][lane][i * BC + j] = s;
+                }
+        }
+        __syncwarp();
+        const int cnt = (t1 - tb < 32) ? (int)(t1 - tb) : 32;
+        for (int u = 0; u < cnt; ++u) {
+            add(hi0, lo0, sp[wp][u][lane]);
+            if (lane < NV - 32) add(hi1, lo1, sp[wp][u][lane + 32]);
+        }
+        __syncwarp();
+    }
+    const int I = coarseRowOfBlock[S], J = coarseCol[S];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int v = lane + 32 * h;
+        if (v >= NV) break;
+        const int i = v / BC, j = v % BC;
+        float a = h ? sa_add_rn(hi1, lo1) : sa_add_rn(hi0, lo0);
+        if (coarseDead[BC * (int64_t)I + i] || coarseDead[BC * (int64_t)J + j]) a = (I == J && i == j) ? 1.f : 0.f;
+        coarseVals[S * NV + v] = a;
+    }
+}
+
 // one warp per coarse node: lane partial sums over strided P blocks, fixed shuffle tree; dead
 // coarse DOFs -> 0
 template <int BF>
@@ -1388,10 +1452,16 @@ ef_status ef_launch_sa_setup(int bf, int64_t nP, const int32_t* pRow, const int3
     else                                                                                                       \
         sa_ap_kernel<BF_><<<nb_(nAP, 128), 128, 0, ef::counted(s)>>>(nAP, apRow, apSeg, apK, apP, fineCol,    \
                                                                     fineVals, fineMask, Pv, APv);             \
-    sa_galerkin_kernel<BF_><<<nb_(nC, 64), 64, 0, ef::counted(s)>>>(nC, cSeg, cP, cAP, Pv, APv,               \
-                                                                   coarseRowOfBlock, coarseCol, coarseDead,   \
-                                                                   coarseVals)
+    if (galWarp)                                                                                               \
+        sa_galerkin_warp_kernel<BF_><<<nb_(nC, kGalWarps), 32 * kGalWarps, 0, ef::counted(s)>>>(               \
+            nC, cSeg, cP, cAP, Pv, APv, coarseRowOfBlock, coarseCol, coarseDead, coarseVals);                  \
+    else                                                                                                       \
+        sa_galerkin_kernel<BF_><<<nb_(nC, 64), 64, 0, ef::counted(s)>>>(nC, cSeg, cP, cAP, Pv, APv,           \
+                                                                       coarseRowOfBlock, coarseCol, coarseDead, \
+                                                                       coarseVals)
     if (nP == 0 || nC == 0) return EF_OK;
+    const char* ge = getenv("EF_GALERKIN_WARP");  // 0: a thread per coarse block
+    const bool galWarp = !ge || atoi(ge) != 0;
     if (bf == 3) {
         EF_SA(3);
     } else {
