@@ -159,9 +159,9 @@ __global__ void __launch_bounds__(kSaApThreads) sa_ap_rows_kernel(
         while (m + 1 < m1 && apSeg[apRowPtr[m + 1]] <= t) ++m;
         float c[BF * BC];
         sa_ap_pair<BF>(t, m, apK, apP, fineCol, fineVals, fineMask, Pv, c);
-        float* d = apC + (t - t0) * (BF * BC);
+        float2* d = reinterpret_cast<float2*>(apC + (t - t0) * (BF * BC));
 #pragma unroll
-        for (int p = 0; p < BF * BC; ++p) d[p] = c[p];
+        for (int p = 0; p < BF * BC / 2; ++p) d[p] = make_float2(c[2 * p], c[2 * p + 1]);
     }
     __syncthreads();
     // a thread per (AP block, value): the block's pairs in list order
@@ -213,14 +213,9 @@ __global__ void __launch_bounds__(32 * kGalWarps) sa_galerkin_warp_kernel(
     for (int64_t tb = t0; tb < t1; tb += 32) {
         const int64_t t = tb + lane;
         if (t < t1) {
-            const float* P = Pv + (int64_t)cP[t] * BF * BC;
-            const float* Q = APv + (int64_t)cAP[t] * BF * BC;
             float pr[BF * BC], qr[BF * BC];
-#pragma unroll
-            for (int u = 0; u < BF * BC; ++u) {
-                pr[u] = P[u];
-                qr[u] = Q[u];
-            }
+            sa_load_pblock<BF>(Pv + (int64_t)cP[t] * BF * BC, pr);
+            sa_load_pblock<BF>(APv + (int64_t)cAP[t] * BF * BC, qr);
 #pragma unroll
             for (int i = 0; i < BC; ++i)
 #pragma unroll

@@ -162,6 +162,23 @@ EF_SA_HD void sa_ap_block(int64_t a, const int32_t* __restrict__ apRow, const in
 // of masked finer DOFs of row m and columns of masked finer DOFs of col(k) dropped.  Summed over
 // the pairs of an AP block in their listed order this is the block of sa_ap_block (with the
 // products of one pair rounded together).
+// the BF x BC block at d into registers: on the device as 8-byte words (a block of 18 or 36 floats
+// starts on an 8-byte boundary), the same values
+template <int BF>
+EF_SA_HD void sa_load_pblock(const float* __restrict__ d, float P[BF * BC]) {
+#if defined(__CUDA_ARCH__)
+    const float2* d2 = reinterpret_cast<const float2*>(d);
+    EF_SA_UNROLL
+    for (int u = 0; u < BF * BC / 2; ++u) {
+        const float2 w = d2[u];
+        P[2 * u] = w.x;
+        P[2 * u + 1] = w.y;
+    }
+#else
+    for (int u = 0; u < BF * BC; ++u) P[u] = d[u];
+#endif
+}
+
 template <int BF>
 EF_SA_HD void sa_ap_pair(int64_t t, int m, const int32_t* __restrict__ apK, const int32_t* __restrict__ apP,
                          const int32_t* __restrict__ fineCol, const float* __restrict__ fineVals,
@@ -169,15 +186,22 @@ EF_SA_HD void sa_ap_pair(int64_t t, int m, const int32_t* __restrict__ apK, cons
     const int32_t k = apK[t];
     const int n = fineCol[k];
     const float* v = fineVals + (int64_t)k * BF * BF;
-    const float* P = Pv + (int64_t)apP[t] * BF * BC;
+    float P[BF * BC];
+    sa_load_pblock<BF>(Pv + (int64_t)apP[t] * BF * BC, P);
+    bool mr[BF], mc[BF];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) {
+        mr[i] = fineMask && fineMask[BF * (int64_t)m + i];
+        mc[i] = fineMask && fineMask[BF * (int64_t)n + i];
+    }
     EF_SA_UNROLL
     for (int p = 0; p < BF * BC; ++p) c[p] = 0.f;
     EF_SA_UNROLL
     for (int i = 0; i < BF; ++i) {
-        if (fineMask && fineMask[BF * (int64_t)m + i]) continue;
+        if (mr[i]) continue;
         EF_SA_UNROLL
         for (int q = 0; q < BF; ++q) {
-            if (fineMask && fineMask[BF * (int64_t)n + q]) continue;
+            if (mc[q]) continue;
             const float av = v[i * BF + q];
             EF_SA_UNROLL
             for (int j = 0; j < BC; ++j) c[i * BC + j] += av * P[q * BC + j];
