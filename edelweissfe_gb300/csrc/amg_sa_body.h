@@ -45,6 +45,44 @@ EF_SA_HD float sa_sub_rn(float a, float b) {
 #endif
 }
 
+// the BF x BC block at d into registers: on the device as 8-byte words (a block of 18 or 36 floats
+// starts on an 8-byte boundary), the same values
+template <int BF>
+EF_SA_HD void sa_load_pblock(const float* __restrict__ d, float P[BF * BC]) {
+#if defined(__CUDA_ARCH__)
+    const float2* d2 = reinterpret_cast<const float2*>(d);
+    EF_SA_UNROLL
+    for (int u = 0; u < BF * BC / 2; ++u) {
+        const float2 w = d2[u];
+        P[2 * u] = w.x;
+        P[2 * u + 1] = w.y;
+    }
+#else
+    for (int u = 0; u < BF * BC; ++u) P[u] = d[u];
+#endif
+}
+
+// the BF x BF block at d into registers: 6 x 6 blocks (144 bytes, 16-byte aligned) as 16-byte words
+// on the device, 3 x 3 blocks (36 bytes, 4-byte aligned) value by value
+template <int BF>
+EF_SA_HD void sa_load_ablock(const float* __restrict__ d, float A[BF * BF]) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (BF == 6) {
+        const float4* d4 = reinterpret_cast<const float4*>(d);
+        EF_SA_UNROLL
+        for (int u = 0; u < 9; ++u) {
+            const float4 w = d4[u];
+            A[4 * u] = w.x;
+            A[4 * u + 1] = w.y;
+            A[4 * u + 2] = w.z;
+            A[4 * u + 3] = w.w;
+        }
+        return;
+    }
+#endif
+    for (int u = 0; u < BF * BF; ++u) A[u] = d[u];
+}
+
 // finer-node prolongation block, BF x 6: [I | R(d)] (BF = 3) or [I R(d) ; 0 I] (BF = 6) with
 // R(d) = [e_x x d, e_y x d, e_z x d] and d the node's offset from its aggregate centroid
 template <int BF>
@@ -85,18 +123,25 @@ EF_SA_HD void sa_prolongator_block(int64_t b, const int32_t* __restrict__ pRow, 
     for (int i = 0; i < BF; ++i)
         EF_SA_UNROLL
         for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
+    bool mr[BF];
+    EF_SA_UNROLL
+    for (int i = 0; i < BF; ++i) mr[i] = fineMask && fineMask[BF * (int64_t)m + i];
     for (int64_t t = pSeg[b]; t < pSeg[b + 1]; ++t) {
         const int32_t k = pSrc[t];
         const int n = fineCol[k];
         float Pn[BF][BC];
         pblock<BF>(offs + 3 * (int64_t)n, Pn);
-        const float* v = fineVals + (int64_t)k * BF * BF;
+        float v[BF * BF];
+        sa_load_ablock<BF>(fineVals + (int64_t)k * BF * BF, v);
+        bool mc[BF];
+        EF_SA_UNROLL
+        for (int q = 0; q < BF; ++q) mc[q] = fineMask && fineMask[BF * (int64_t)n + q];
         EF_SA_UNROLL
         for (int i = 0; i < BF; ++i) {
-            if (fineMask && fineMask[BF * (int64_t)m + i]) continue;
+            if (mr[i]) continue;
             EF_SA_UNROLL
             for (int q = 0; q < BF; ++q) {
-                if (fineMask && fineMask[BF * (int64_t)n + q]) continue;
+                if (mc[q]) continue;
                 const float a = v[i * BF + q];
                 EF_SA_UNROLL
                 for (int j = 0; j < BC; ++j) acc[i][j] += a * Pn[q][j];
@@ -162,30 +207,14 @@ EF_SA_HD void sa_ap_block(int64_t a, const int32_t* __restrict__ apRow, const in
 // of masked finer DOFs of row m and columns of masked finer DOFs of col(k) dropped.  Summed over
 // the pairs of an AP block in their listed order this is the block of sa_ap_block (with the
 // products of one pair rounded together).
-// the BF x BC block at d into registers: on the device as 8-byte words (a block of 18 or 36 floats
-// starts on an 8-byte boundary), the same values
-template <int BF>
-EF_SA_HD void sa_load_pblock(const float* __restrict__ d, float P[BF * BC]) {
-#if defined(__CUDA_ARCH__)
-    const float2* d2 = reinterpret_cast<const float2*>(d);
-    EF_SA_UNROLL
-    for (int u = 0; u < BF * BC / 2; ++u) {
-        const float2 w = d2[u];
-        P[2 * u] = w.x;
-        P[2 * u + 1] = w.y;
-    }
-#else
-    for (int u = 0; u < BF * BC; ++u) P[u] = d[u];
-#endif
-}
-
 template <int BF>
 EF_SA_HD void sa_ap_pair(int64_t t, int m, const int32_t* __restrict__ apK, const int32_t* __restrict__ apP,
                          const int32_t* __restrict__ fineCol, const float* __restrict__ fineVals,
                          const uint8_t* __restrict__ fineMask, const float* __restrict__ Pv, float c[BF * BC]) {
     const int32_t k = apK[t];
     const int n = fineCol[k];
-    const float* v = fineVals + (int64_t)k * BF * BF;
+    float v[BF * BF];
+    sa_load_ablock<BF>(fineVals + (int64_t)k * BF * BF, v);
     float P[BF * BC];
     sa_load_pblock<BF>(Pv + (int64_t)apP[t] * BF * BC, P);
     bool mr[BF], mc[BF];
