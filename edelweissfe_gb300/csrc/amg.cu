@@ -164,14 +164,21 @@ __global__ void __launch_bounds__(kSaApThreads) sa_ap_rows_kernel(
         for (int p = 0; p < BF * BC / 2; ++p) d[p] = make_float2(c[2 * p], c[2 * p + 1]);
     }
     __syncthreads();
-    // a thread per (AP block, value): the block's pairs in list order
-    const int nTask = (int)(a1 - a0) * (BF * BC);
+    // a thread per (AP block, pair of values): the block's pairs in list order (8-byte words)
+    constexpr int H = BF * BC / 2;
+    const int nTask = (int)(a1 - a0) * H;
+    const float2* apC2 = reinterpret_cast<const float2*>(apC);
+    float2* APv2 = reinterpret_cast<float2*>(APv);
     for (int task = threadIdx.x; task < nTask; task += kSaApThreads) {
-        const int64_t a = a0 + task / (BF * BC);
-        const int p = task % (BF * BC);
-        float acc = 0.f;
-        for (int64_t t = apSeg[a]; t < apSeg[a + 1]; ++t) acc += apC[(t - t0) * (BF * BC) + p];
-        APv[a * (BF * BC) + p] = acc;
+        const int64_t a = a0 + task / H;
+        const int p = task % H;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int64_t t = apSeg[a]; t < apSeg[a + 1]; ++t) {
+            const float2 v = apC2[(t - t0) * H + p];
+            acc.x += v.x;
+            acc.y += v.y;
+        }
+        APv2[a * H + p] = acc;
     }
 }
 
@@ -214,8 +221,8 @@ __global__ void __launch_bounds__(32 * kGalWarps) sa_galerkin_warp_kernel(
         const int64_t t = tb + lane;
         if (t < t1) {
             float pr[BF * BC], qr[BF * BC];
-            sa_load_pblock<BF>(Pv + (int64_t)cP[t] * BF * BC, pr);
-            sa_load_pblock<BF>(APv + (int64_t)cAP[t] * BF * BC, qr);
+            sa_load_block<BF>(Pv + (int64_t)cP[t] * BF * BC, pr);
+            sa_load_block<BF>(APv + (int64_t)cAP[t] * BF * BC, qr);
 #pragma unroll
             for (int i = 0; i < BC; ++i)
 #pragma unroll

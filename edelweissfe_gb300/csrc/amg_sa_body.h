@@ -45,20 +45,31 @@ EF_SA_HD float sa_sub_rn(float a, float b) {
 #endif
 }
 
-// the BF x BC block at d into registers: on the device as 8-byte words (a block of 18 or 36 floats
-// starts on an 8-byte boundary), the same values
+// the values of one block (8-byte aligned for BF = 3, 16-byte aligned for BF = 6)
 template <int BF>
-EF_SA_HD void sa_load_pblock(const float* __restrict__ d, float P[BF * BC]) {
+EF_SA_HD void sa_load_block(const float* __restrict__ src, float P[BF * BC]) {
 #if defined(__CUDA_ARCH__)
-    const float2* d2 = reinterpret_cast<const float2*>(d);
-    EF_SA_UNROLL
-    for (int u = 0; u < BF * BC / 2; ++u) {
-        const float2 w = d2[u];
-        P[2 * u] = w.x;
-        P[2 * u + 1] = w.y;
+    if constexpr (BF == 6) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        EF_SA_UNROLL
+        for (int q = 0; q < BF * BC / 4; ++q) {
+            const float4 v = __ldg(s4 + q);
+            P[4 * q] = v.x;
+            P[4 * q + 1] = v.y;
+            P[4 * q + 2] = v.z;
+            P[4 * q + 3] = v.w;
+        }
+    } else {
+        const float2* s2 = reinterpret_cast<const float2*>(src);
+        EF_SA_UNROLL
+        for (int q = 0; q < BF * BC / 2; ++q) {
+            const float2 v = __ldg(s2 + q);
+            P[2 * q] = v.x;
+            P[2 * q + 1] = v.y;
+        }
     }
 #else
-    for (int u = 0; u < BF * BC; ++u) P[u] = d[u];
+    for (int p = 0; p < BF * BC; ++p) P[p] = src[p];
 #endif
 }
 
@@ -216,7 +227,7 @@ EF_SA_HD void sa_ap_pair(int64_t t, int m, const int32_t* __restrict__ apK, cons
     float v[BF * BF];
     sa_load_ablock<BF>(fineVals + (int64_t)k * BF * BF, v);
     float P[BF * BC];
-    sa_load_pblock<BF>(Pv + (int64_t)apP[t] * BF * BC, P);
+    sa_load_block<BF>(Pv + (int64_t)apP[t] * BF * BC, P);
     bool mr[BF], mc[BF];
     EF_SA_UNROLL
     for (int i = 0; i < BF; ++i) {
@@ -427,34 +438,6 @@ EF_SA_HD void sa_post_block(int64_t a, const int32_t* __restrict__ apRow, const 
 // copy of P in the transpose order (slot k holds block tIdx[k], rowT[k] = pRow[tIdx[k]]), so the
 // blocks of one coarse column are consecutive.  A thread takes one block: the BF x BC values are
 // contiguous (72 bytes for BF = 3, 144 for BF = 6) and load as 8- or 16-byte words.
-
-// the values of one block (8-byte aligned for BF = 3, 16-byte aligned for BF = 6)
-template <int BF>
-EF_SA_HD void sa_load_block(const float* __restrict__ src, float P[BF * BC]) {
-#if defined(__CUDA_ARCH__)
-    if constexpr (BF == 6) {
-        const float4* s4 = reinterpret_cast<const float4*>(src);
-        EF_SA_UNROLL
-        for (int q = 0; q < BF * BC / 4; ++q) {
-            const float4 v = __ldg(s4 + q);
-            P[4 * q] = v.x;
-            P[4 * q + 1] = v.y;
-            P[4 * q + 2] = v.z;
-            P[4 * q + 3] = v.w;
-        }
-    } else {
-        const float2* s2 = reinterpret_cast<const float2*>(src);
-        EF_SA_UNROLL
-        for (int q = 0; q < BF * BC / 2; ++q) {
-            const float2 v = __ldg(s2 + q);
-            P[2 * q] = v.x;
-            P[2 * q + 1] = v.y;
-        }
-    }
-#else
-    for (int p = 0; p < BF * BC; ++p) P[p] = src[p];
-#endif
-}
 
 // transpose-order copy, slot k: dst[k] = Pv[tIdx[k]] (BF x BC values)
 template <int BF>
