@@ -40,11 +40,11 @@ sys.path.insert(0, ROOT)
 PROPS = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
 METRIC = "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembly GB/s"
 # DRAM bytes (read + write) per launch of the fine-level kernels of the FGMRES solve on the
-# 100x40x40 box (509,343 DOF, 4,406,941 blocks), from one ncu capture of bench.py --profile
-# (profiles/sell_kernels_hex8_J2_100x40x40.md)
-SWEEP_TRAFFIC_BYTES = 102.97e6
-PRODUCT_TRAFFIC_BYTES = 182.95e6
-POST_TRAFFIC_BYTES = 93.84e6
+# 100x40x40 box (509,343 DOF, 4,406,941 blocks; the slices in their diagonal form), from one ncu
+# capture of bench.py --profile --method fgmres
+SWEEP_TRAFFIC_BYTES = 87.45e6
+PRODUCT_TRAFFIC_BYTES = 170.52e6
+POST_TRAFFIC_BYTES = 95.23e6
 # Newton iterations of the timed increment (13) of the 100x40x40 model: the same in the all-FP64
 # and the mixed-precision GPU solves; the CPU arms charge this many element passes and solves
 PCG_NEWTON_PER_STEP = 8
@@ -510,7 +510,8 @@ def run_ours(a):
 
         # the dominant kernel of the load step: the FGMRES product (one launch per iteration, the
         # largest); the fused post-smoothing and the fine residual (one launch each per iteration) beside
-        roofline = entry(1, "sell_spmv3_kernel (FGMRES product K z, FP32 sliced-ELL; one launch per iteration)",
+        roofline = entry(1, "sell_spmv3_kernel (FGMRES product K z, FP32 sliced-ELL in its diagonal form: "
+                            "columns computed from 27 node offsets; one launch per iteration)",
                          PRODUCT_TRAFFIC_BYTES)
         roofline.update({"bound": "hbm", "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
                          "traffic_source": "ncu (dram__bytes_read.sum + dram__bytes_write.sum per launch) of "
@@ -520,7 +521,7 @@ def run_ours(a):
             roofline["second"] = entry(2, "sa_post_fused_kernel (fine prolongation + post-smoothing x = w D^-1 (r + t)"
                                           " + C e, C in BF16)", POST_TRAFFIC_BYTES)
         roofline["third"] = entry(0, "sell_level3_bf16_kernel (fine residual t = r - w K M D^-1 r, BF16 "
-                                     "sliced-ELL)", SWEEP_TRAFFIC_BYTES)
+                                     "sliced-ELL, diagonal form)", SWEEP_TRAFFIC_BYTES)
     pcg_bpi = pcg_bytes_per_iteration(info)
     pcg_gbs = pcg_bpi * pcg_it / (pcg_kms * 1e-3) / 1e9 if pcg_kms > 0 else None
     cpu = None
