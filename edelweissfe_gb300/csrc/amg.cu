@@ -1660,6 +1660,18 @@ ef_status ef_launch_scale_rnorm(int64_t n, float* x, const double* n2, cudaStrea
     return EF_OK;
 }
 
+// x *= *fac (a factor left on the device in FP32)
+__global__ void scale_by_kernel(int64_t n, float* __restrict__ x, const float* __restrict__ fac) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= *fac;
+}
+ef_status ef_launch_scale_by(int64_t n, float* x, const float* fac, cudaStream_t s) {
+    if (n == 0) return EF_OK;
+    scale_by_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, x, fac);
+    EF_CUDA(cudaGetLastError());
+    return EF_OK;
+}
+
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s) {
     if (n == 0) return EF_OK;
     fill_hash_kernel<<<nb_(n, 256), 256, 0, ef::counted(s)>>>(n, x);

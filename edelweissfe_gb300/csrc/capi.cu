@@ -235,6 +235,7 @@ void ef_destroy(ef_ctx* c) {
     F(c->dSellPerm);
     F(c->dSellCol);
     F(c->dSellDia);
+    F(c->amgPowFac);
     F(c->dSellSrc);
     F(c->dSellV9);
     F(c->dSellV8);

@@ -105,6 +105,7 @@ ef_status ef_launch_coarsest_inverse(int nN, const int32_t* rowPtr, const int32_
                                      float* inv, cudaStream_t s);
 ef_status ef_launch_fill_hash(int64_t n, float* x, cudaStream_t s);
 ef_status ef_launch_scale_rnorm(int64_t n, float* x, const double* n2, cudaStream_t s);
+ef_status ef_launch_scale_by(int64_t n, float* x, const float* fac, cudaStream_t s);
 ef_status ef_launch_cheb_step(int bs, int nN, const float* binv, const uint8_t* mask, float a, float b, const float* t,
                               float* d, float* x, int first, cudaStream_t s);
 ef_status ef_launch_level_residual_bf16(int nN, int64_t nBlocks, const int32_t* rowPtr, const int32_t* colIdx,
@@ -141,7 +142,7 @@ ef_status ef_launch_features(int nN, const float* Mv, const float* v, const floa
 ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s);
 ef_status ef_mpnn_refresh(int n, const float* p, void* pb, float* pf, cudaStream_t s);
 ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
-                        int nPart, double* out, cudaStream_t s);
+                        int nPart, double* out, cudaStream_t s, float* fac = nullptr);
 ef_status ef_mpnn_scale(int64_t n, float* x, float a, cudaStream_t s);
 ef_status ef_mpnn_dense_eval_host(int tc, int nN, const float* h, const float* agg, const float* W, float* q,
                                   float* hout, int* flagsOut, cudaStream_t s);
@@ -185,7 +186,8 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
                                  const int32_t* col, const float* binv, const uint8_t* mask, cudaStream_t s);
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s, const float* scale = nullptr, const int32_t* dia = nullptr);
+                               cudaStream_t s, const float* scale = nullptr, const int32_t* dia = nullptr,
+                               const float* binv = nullptr);
 ef_status ef_launch_sell_level3_bf16(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                      const void* v8, const void* v1, const float* x, const float* r,
                                      const uint8_t* mask, float* t, const float* binv, float omega, int split,
@@ -470,6 +472,7 @@ struct ef_ctx {
     float amgOmega = 1.0f;                  // upper bound of the smoothing damping
     std::vector<float> levelOmega;          // per smoothed level: amgOmega, or 4 / (3 lambda_max(D^-1 A)) when smaller
     float* amgPow[2] = {nullptr, nullptr};  // power-iteration vectors (fine size)
+    float* amgPowFac = nullptr;             // 1 / |a| of the power iteration (FP32, on the device)
     float* amgZero = nullptr;
     bool amgBf16 = true;                    // fine-level smoothing residuals from a BF16 copy of the blocks
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi

@@ -563,14 +563,20 @@ __global__ void sumsq_partial_kernel(int64_t n, int groups, const float* __restr
 }
 
 // out[g] = sum_c part[c][g], one warp per g: lane-strided sums, then a fixed shuffle tree
-__global__ void sumsq_final_kernel(int nPart, const double* __restrict__ part, double* __restrict__ out) {
+// (fac: optional, 1 / sqrt(out[0]) in FP32, 1 when out[0] is not positive -- the power
+// iteration's normalisation factor, formed once instead of per element)
+__global__ void sumsq_final_kernel(int nPart, const double* __restrict__ part, double* __restrict__ out,
+                                   float* __restrict__ fac) {
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (g >= 3) return;
     double t = 0.0;
     for (int c = lane; c < nPart; c += 32) t += part[(int64_t)c * 3 + g];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (lane == 0) out[g] = t;
+    if (lane == 0) {
+        out[g] = t;
+        if (g == 0 && fac) *fac = t > 0.0 ? (float)(1.0 / sqrt(t)) : 1.f;
+    }
 }
 
 __global__ void scale_inplace_kernel(int64_t n, float* __restrict__ x, float a) {
@@ -726,9 +732,9 @@ ef_status ef_mpnn_bf16_to_f32(int n, const void* pb, float* pf, cudaStream_t s) 
 // out[0..3) = the sums of sumsq_partial_kernel (mode `groups`); part holds nPart x 3 doubles;
 // deterministic
 ef_status ef_mpnn_sumsq(int64_t n, int groups, const float* z, const float* e, const uint8_t* mask, double* part,
-                        int nPart, double* out, cudaStream_t s) {
+                        int nPart, double* out, cudaStream_t s, float* fac) {
     sumsq_partial_kernel<<<nPart, 256, 0, ef::counted(s)>>>(n, groups, z, e, mask, part);
-    sumsq_final_kernel<<<1, 96, 0, ef::counted(s)>>>(nPart, part, out);
+    sumsq_final_kernel<<<1, 96, 0, ef::counted(s)>>>(nPart, part, out, fac);
     EF_CUDA(cudaGetLastError());
     return EF_OK;
 }

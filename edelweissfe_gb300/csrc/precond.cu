@@ -758,6 +758,7 @@ static ef_status amg_power_alloc(ef_ctx* c) {
         c->amgPow[0] = dalloc<float>(c->nDof, &st);
         c->amgPow[1] = dalloc<float>(c->nDof, &st);
         c->amgZero = dalloc<float>(c->nDof, &st);
+        c->amgPowFac = dalloc<float>(1, &st);
         if (st != EF_OK) return st;
         EF_CUDA(cudaMemset(c->amgZero, 0, sizeof(float) * c->nDof));
     }
@@ -792,12 +793,22 @@ static ef_status amg_power(ef_ctx* c, int l, cudaStream_t s) {
     const int64_t n = (int64_t)bs * nN;
     float* a = c->amgPow[0];
     float* b = c->amgPow[1];
+    // the fine level through the sliced-ELL product, which scales its input by 1 / |a| and applies
+    // the block inverses in its epilogue: b = D^-1 K (a / |a|), one launch per step
+    const bool sellStep = fine && c->sellMode == 1 && !c->sellStale;
     EF_CHECK(ef_launch_fill_hash(n, a, s));
     for (int it = 0; it < kPowerSteps; ++it) {
         double* n2 = c->amgNorms + 3 * (l * kPowerSteps + it);
-        EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, n2, s));
+        EF_CHECK(ef_mpnn_sumsq(n, 1, a, nullptr, mask, c->nnRed, c->nnPartN, n2, s, c->amgPowFac));
         if (it + 1 == kPowerSteps) break;
-        EF_CHECK(ef_launch_scale_rnorm(n, a, n2, s));
+        if (sellStep) {
+            EF_CHECK(ef_launch_sell_spmv3(nN, c->sellSlices, c->dSellOff, c->dSellPerm, c->dSellCol, c->dSellV9, a,
+                                          mask, b, nullptr, c->sellSplitProduct, s, c->amgPowFac, c->dSellDia,
+                                          binv));
+            std::swap(a, b);
+            continue;
+        }
+        EF_CHECK(ef_launch_scale_by(n, a, c->amgPowFac, s));
         EF_CHECK(ef_launch_level_residual(bs, nN, rowPtr, colIdx, vals, a, c->amgZero, mask, b, s));  // -A a
         EF_CHECK(ef_launch_bj_apply(bs, nN, binv, mask, 1.f, b, a, 0, s));                            // D^-1
     }

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
     int nN, int nSlices, const int64_t* __restrict__ off, const int32_t* __restrict__ perm,
     const int32_t* __restrict__ col, const float* __restrict__ v9, const float* __restrict__ x,
     const uint8_t* __restrict__ mask, float* __restrict__ y, float* __restrict__ xcopy,
-    const float* __restrict__ scale, const int32_t* __restrict__ dia) {
+    const float* __restrict__ scale, const int32_t* __restrict__ dia, const float* __restrict__ binv) {
     ef::dep_entry();
     SellPart p;
     const bool active = sell_part<S>(nSlices, off, p);
@@ -182,9 +182,21 @@ __global__ void __launch_bounds__(sell_split_threads(S)) sell_spmv3_kernel(
         xcopy[d + 1] = x[d + 1];
         xcopy[d + 2] = x[d + 2];
     }
-    y[d + 0] = mask[d + 0] ? 0.f : y0;
-    y[d + 1] = mask[d + 1] ? 0.f : y1;
-    y[d + 2] = mask[d + 2] ? 0.f : y2;
+    y0 = mask[d + 0] ? 0.f : y0;
+    y1 = mask[d + 1] ? 0.f : y1;
+    y2 = mask[d + 2] ? 0.f : y2;
+    if (binv) {  // y = D^-1 (K x) with the row's block inverse (the power iteration on D^-1 K)
+        const float* B = binv + 9 * (int64_t)m;
+        const float z0 = B[0] * y0 + B[1] * y1 + B[2] * y2;
+        const float z1 = B[3] * y0 + B[4] * y1 + B[5] * y2;
+        const float z2 = B[6] * y0 + B[7] * y1 + B[8] * y2;
+        y0 = mask[d + 0] ? 0.f : z0;
+        y1 = mask[d + 1] ? 0.f : z1;
+        y2 = mask[d + 2] ? 0.f : z2;
+    }
+    y[d + 0] = y0;
+    y[d + 1] = y1;
+    y[d + 2] = y2;
 }
 
 // t = r - ys K x on the fine level (0 on masked rows), or with binv a damped block-Jacobi sweep
@@ -350,18 +362,18 @@ ef_status ef_launch_sell_refresh(int64_t nE, const int32_t* src, const float* bs
 
 ef_status ef_launch_sell_spmv3(int nN, int nSlices, const int64_t* off, const int32_t* perm, const int32_t* col,
                                const float* v9, const float* x, const uint8_t* mask, float* y, float* xcopy, int split,
-                               cudaStream_t s, const float* scale, const int32_t* dia) {
+                               cudaStream_t s, const float* scale, const int32_t* dia, const float* binv) {
     if (nSlices <= 0) return EF_OK;
 #define EF_SPMV3(C_, S_)                                                                                              \
     do {                                                                                                              \
         if (dia)                                                                                                      \
             EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_, true>, sell_split_grid(nSlices, S_),                     \
                                    sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, v9, x, mask, y, xcopy,  \
-                                   scale, dia));                                                                      \
+                                   scale, dia, binv));                                                                \
         else                                                                                                          \
             EF_CUDA(ef::launch_dep(sell_spmv3_kernel<C_, S_, false>, sell_split_grid(nSlices, S_),                    \
                                    sell_split_threads(S_), 0, s, nN, nSlices, off, perm, col, v9, x, mask, y, xcopy,  \
-                                   scale, dia));                                                                      \
+                                   scale, dia, binv));                                                                \
     } while (0)
 #define EF_SPMV3_S(C_)      \
     if (split == 2)         \
