@@ -768,18 +768,25 @@ __global__ void scale_blocks6_kernel(int64_t nB, const int32_t* __restrict__ col
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nB) return;
     const int64_t c = colIdx[k];
-    const float* A = vals + k * BC * BC;
-    const float* D = binv + c * BC * BC;
-    float* O = out + k * BC * BC;
+    float A[BC * BC], D[BC * BC];
+    sa_load_ablock<BC>(vals + k * BC * BC, A);
+    sa_load_ablock<BC>(binv + c * BC * BC, D);
+    bool dq[BC];
+#pragma unroll
+    for (int q = 0; q < BC; ++q) dq[q] = dead[BC * c + q];
+    float4* O = reinterpret_cast<float4*>(out + k * BC * BC);
+    float o[BC * BC];
 #pragma unroll
     for (int i = 0; i < BC; ++i)
 #pragma unroll
         for (int j = 0; j < BC; ++j) {
             float z = 0.f;
 #pragma unroll
-            for (int q = 0; q < BC; ++q) z += dead[BC * c + q] ? 0.f : A[i * BC + q] * D[q * BC + j];
-            O[i * BC + j] = z;
+            for (int q = 0; q < BC; ++q) z += dq[q] ? 0.f : A[i * BC + q] * D[q * BC + j];
+            o[i * BC + j] = z;
         }
+#pragma unroll
+    for (int u = 0; u < BC * BC / 4; ++u) O[u] = make_float4(o[4 * u], o[4 * u + 1], o[4 * u + 2], o[4 * u + 3]);
 }
 
 // Fused post-smoothing of a 6-DOF level (amg_sa_body.h): C = a (I - w D^-1 A) P in the pattern of

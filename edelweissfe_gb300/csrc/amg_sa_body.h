@@ -420,8 +420,15 @@ EF_SA_HD void sa_post_block(int64_t a, const int32_t* __restrict__ apRow, const 
                             const float* __restrict__ binv, float omega, float alpha, float C[BF * BC]) {
     const int64_t m = apRow[a];
     const int32_t b = apToP[a];
-    const float* B = binv + m * BF * BF;
-    const float* Q = APv + a * BF * BC;
+    float B[BF * BF], Q[BF * BC], P[BF * BC];
+    sa_load_ablock<BF>(binv + m * BF * BF, B);
+    sa_load_block<BF>(APv + a * BF * BC, Q);
+    if (b >= 0) {
+        sa_load_block<BF>(Pv + (int64_t)b * BF * BC, P);
+    } else {
+        EF_SA_UNROLL
+        for (int u = 0; u < BF * BC; ++u) P[u] = 0.f;
+    }
     EF_SA_UNROLL
     for (int i = 0; i < BF; ++i)
         EF_SA_UNROLL
@@ -429,8 +436,7 @@ EF_SA_HD void sa_post_block(int64_t a, const int32_t* __restrict__ apRow, const 
             float z = 0.f;
             EF_SA_UNROLL
             for (int q = 0; q < BF; ++q) z += B[i * BF + q] * Q[q * BC + j];
-            const float p = b >= 0 ? Pv[(int64_t)b * BF * BC + i * BC + j] : 0.f;
-            C[i * BC + j] = alpha * (p - omega * z);
+            C[i * BC + j] = alpha * (P[i * BC + j] - omega * z);
         }
 }
 
