@@ -457,7 +457,7 @@ struct ef_ctx {
     int32_t *dPostCol = nullptr, *dPostSrc = nullptr, *dPostApToP = nullptr;
     void *dPostQ0 = nullptr, *dPostQ1 = nullptr, *dPostQ2 = nullptr;
     int sellSplit = 4;                     // warps per slice of the BF16 sweep: 1, 2, 4 or 8 (EF_SELL_SPLIT)
-    int sellSplitProduct = 1;              // the same for the FP32 product (EF_SELL_SPLIT_PRODUCT)
+    int sellSplitProduct = 4;              // the same for the FP32 product (EF_SELL_SPLIT_PRODUCT)
     int32_t* dSellPerm = nullptr;          // [nNodes] block row of each SELL row (null: identity)
     int32_t* dSellCol = nullptr;           // [sellE] block column (padding: the row itself)
     // diagonal form (EF_SELL_DIA): every slice has the same slot columns, slot column j at node
