@@ -43,7 +43,7 @@ METRIC = "hex8 J2 load-step s: learned-FGMRES vs Jacobi-PCG @1e-8 resid; assembl
 # 100x40x40 box (509,343 DOF, 4,406,941 blocks; the slices in their diagonal form), from one ncu
 # capture of bench.py --profile --method fgmres
 SWEEP_TRAFFIC_BYTES = 87.45e6
-PRODUCT_TRAFFIC_BYTES = 170.52e6
+PRODUCT_TRAFFIC_BYTES = 176.73e6  # each slice split over 4 warps (170.52e6 with one warp per slice)
 POST_TRAFFIC_BYTES = 95.23e6
 # Newton iterations of the timed increment (13) of the 100x40x40 model: the same in the all-FP64
 # and the mixed-precision GPU solves; the CPU arms charge this many element passes and solves
@@ -516,12 +516,22 @@ def run_ours(a):
         roofline.update({"bound": "hbm", "peak": peaks["hbm_gbs"], "peak_kind": peak_kind, "unit": "GB/s",
                          "traffic_source": "ncu (dram__bytes_read.sum + dram__bytes_write.sum per launch) of "
                                            "bench.py --profile --method fgmres",
-                         "timing": "CUDA events, 50 launches"})
+                         "timing": "CUDA events, 50 back-to-back launches on the timed increment's last system"})
+        if sp_n and sp_ms > 0:
+            # the product's own launches inside the solve: CUDA events around each one on the solve's
+            # stream, over one profiled replay of the timed increment
+            in_ms = sp_ms / sp_n
+            gbs = fk_bytes[1] / (in_ms * 1e-3) / 1e9
+            roofline.update({"back_to_back_ms": roofline["avg_launch_ms"], "back_to_back_frac": roofline["frac"],
+                             "avg_launch_ms": in_ms, "achieved": gbs, "frac": gbs / peaks["hbm_gbs"],
+                             "timing": f"CUDA events around each of the {int(sp_n)} product launches of one profiled "
+                                       "replay of the timed increment (the solve's stream); back_to_back_*: 50 "
+                                       "launches in a row on its last system"})
         if fk_ms[2] > 0:
             roofline["second"] = entry(2, "sa_post_fused_kernel (fine prolongation + post-smoothing x = w D^-1 (r + t)"
-                                          " + C e, C in BF16)", POST_TRAFFIC_BYTES)
+                                          " + C e, C in BF16; 50 back-to-back launches)", POST_TRAFFIC_BYTES)
         roofline["third"] = entry(0, "sell_level3_bf16_kernel (fine residual t = r - w K M D^-1 r, BF16 "
-                                     "sliced-ELL, diagonal form)", SWEEP_TRAFFIC_BYTES)
+                                     "sliced-ELL, diagonal form; 50 back-to-back launches)", SWEEP_TRAFFIC_BYTES)
     pcg_bpi = pcg_bytes_per_iteration(info)
     pcg_gbs = pcg_bpi * pcg_it / (pcg_kms * 1e-3) / 1e9 if pcg_kms > 0 else None
     cpu = None
