@@ -589,7 +589,7 @@ ef_status amg_refresh(ef_ctx* c, cudaStream_t s);
 ef_status amg_vcycle(ef_ctx* c, int l, const float* r, float* x, cudaStream_t s);
 ef_status amg_capture(ef_ctx* c);
 ef_status sell_refresh(ef_ctx* c, cudaStream_t s);
-ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s);
+ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s, bool force = false);
 // solve.cu
 ef_status nn_apply(ef_ctx* c, cudaStream_t s);
 ef_status nn_capture(ef_ctx* c);

@@ -78,6 +78,7 @@ ef_status nn_current_system(ef_ctx* c, cudaStream_t s, int* out) {
             if (S.sys == slot) S.sys = -1;
     }
     ef_ctx::NNSystem& Y = c->nnSystems[slot];
+    EF_CHECK(nn_edge_refresh(c, s, true));
     EF_CUDA(cudaMemcpyAsync(Y.K, c->dBsrVals, sizeof(float) * 9 * c->nBlocks, cudaMemcpyDeviceToDevice, s));
     EF_CUDA(cudaMemcpyAsync(Y.a, c->nnA, sizeof(float) * c->nBlocks, cudaMemcpyDeviceToDevice, s));
     Y.version = c->nnVersion;

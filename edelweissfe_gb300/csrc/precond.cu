@@ -855,9 +855,12 @@ static ef_status amg_damping(ef_ctx* c, cudaStream_t s) {
     return amg_damping_finish(c, s);
 }
 
-// edge weights of the learned correction for the current system
-ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s) {
+// edge weights of the learned correction for the current system; only while something reads them
+// (the correction is applied, or training pairs are collected): otherwise they stay stale and the
+// next reader refreshes them first
+ef_status nn_edge_refresh(ef_ctx* c, cudaStream_t s, bool force) {
     if (!c->nnInit || !c->nnEdgeStale) return EF_OK;
+    if (!force && !c->nnOn && !(c->nnEvery > 0 && c->nnMaxPerSolve > 0)) return EF_OK;
     EF_CHECK(ef_launch_edge_weights((int)c->nNodes, c->dRowPtr, c->dColIdx, (const float*)c->dBsrVals, c->nnA, s));
     EF_CHECK(ef_launch_gather_f32(c->nBlocks, c->nnTpos, c->nnA, c->nnAT, s));
     c->nnEdgeStale = false;

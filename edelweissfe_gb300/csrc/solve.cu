@@ -61,6 +61,7 @@ ef_status fgmres_precond(ef_ctx* c, const float* v, const float** out, cudaStrea
     EF_CHECK(apply_base(c, s));
     *out = c->vcOut;
     if (c->nnOn) {
+        EF_CHECK(nn_edge_refresh(c, s, true));
         EF_CHECK(nn_capture(c));
         ef::note_launches(c->nnGraphKernels);
         EF_CUDA(cudaGraphLaunch(c->nnGraph, s));
