@@ -71,7 +71,9 @@ def parse():
                     help="skip the learned correction's cross-seed measurement on the seeded J2 family")
     ap.add_argument("--pcg-steps", type=int, default=2, help="timed steps of the Jacobi-PCG comparison")
     ap.add_argument("--restart", type=int, default=64, help="FGMRES restart length")
-    ap.add_argument("--inner-rtol", type=float, default=1e-5, help="relative tolerance of one inner (FP32) solve")
+    ap.add_argument("--inner-rtol", type=float, default=1e-4,
+                    help="relative tolerance of the first inner (FP32) solve of a system (the later ones: 1e-2 or "
+                         "what the remaining target needs)")
     ap.add_argument("--precond-reuse", type=int, default=1,
                     help="Newton systems of an increment that reuse the coarse multigrid levels of its first one")
     ap.add_argument("--method", default="fgmres", choices=["pcg", "fgmres"], help="solver of --profile")

@@ -508,6 +508,10 @@ ef_status ef_finalize(ef_ctx* c, int options) {
         const double v = atof(e);
         if (v > 0.0 && v <= 1.0) c->refineAim = v;
     }
+    if (const char* e = getenv("EF_REFINE_FLOOR")) {
+        const double v = atof(e);
+        if (v >= 0.0 && v < 0.5) c->refineFloor = v;
+    }
     if (const char* e = getenv("EF_MPNN_TC")) c->nnTensorCores = atoi(e) != 0;
     const size_t ks = c->keFp64 ? sizeof(double) : sizeof(float);
     ef_status st = EF_OK;

@@ -478,6 +478,10 @@ struct ef_ctx {
     bool amgCheb = false;                   // Chebyshev smoothing (degree amgSweeps) instead of damped block Jacobi
     bool amgBf16Coarse = false;             // coarse smoothing residuals from BF16 copies (EF_AMG_BF16_COARSE)
     double refineAim = 0.5;  // an inner solve aims at this fraction of the remaining target (EF_REFINE_AIM)
+    // the tightest relative tolerance of an inner solve after the first (EF_REFINE_FLOOR; 0: none):
+    // an FP32 solve lowers the FP64 residual of its right-hand side by about 3e-3 at best (the
+    // rounding of the FP32 products), so iterating it further buys nothing
+    double refineFloor = 1e-2;
     double fgHold = 2.0;     // FGMRES: no column enqueued ahead when the trend reaches hold x target (EF_FGMRES_HOLD)
     bool amgDeadValid = false;  // the levels' dead-DOF masks match the current Dirichlet mask
     bool amgSmoothed = true;                // smoothed-aggregation prolongators (EF_AMG_SMOOTHED=0: plain aggregation)

@@ -374,7 +374,13 @@ ef_status ef_solve(ef_ctx* c, const ef_solve_opts* o, const double* b, double* x
             const int vd = c->keFp64;
             void** wv = vd ? c->w64k : c->w32;
             EF_CHECK(ef_launch_masked_copy(n, r64, c->dMask, 0, 1.0 / rn, wv[0], vd, s));
-            const double inner = std::max(o->innerRtol, c->refineAim * o->rtol * bnorm / rn);
+            // the first inner solve to innerRtol; with the multigrid-preconditioned FGMRES the later
+            // ones no tighter than what such an FP32 solve lowers the FP64 residual by (refineFloor,
+            // measured), nor than the remaining target needs
+            const bool floored = sweep > 0 && o->method == EF_SOLVE_FGMRES &&
+                                 c->fgPc == EF_FGMRES_PC_MULTIGRID && !c->nnOn;
+            const double inner = std::max(floored ? std::max(o->innerRtol, c->refineFloor) : o->innerRtol,
+                                          c->refineAim * o->rtol * bnorm / rn);
             PcgResultHost pr;
             if (o->method == EF_SOLVE_FGMRES) {
                 const bool timeSetup = o->profile && (c->sellStale || c->amgStale);

@@ -62,7 +62,10 @@ typedef struct ef_solve_opts {
     int method;          /* EF_SOLVE_PCG or EF_SOLVE_FGMRES */
     int mixed;           /* 1: FP32 inner iterations + FP64 iterative refinement; 0: all FP64 */
     double rtol;         /* target ||b - A x||_2 / ||b||_2 in FP64 */
-    double innerRtol;    /* relative tolerance of one inner solve (mixed mode) */
+    double innerRtol;    /* relative tolerance of an inner solve (mixed mode); with FGMRES and the
+                            multigrid preconditioner the solves after the first of a system stop at
+                            max(innerRtol, 1e-2 or EF_REFINE_FLOOR, half the remaining target
+                            relative to their right-hand side) */
     int maxIter;         /* cap on the total number of Krylov iterations */
     int restart;         /* FGMRES restart length */
     int maxRefine;       /* cap on refinement sweeps (mixed mode) */
