@@ -580,6 +580,7 @@ def run_ours(a):
                            "ortho_ms_per_iteration": orth_ms / fg_it if fg_it else None,
                            "reorthogonalised_columns": int(n_reorth), "solves": int(n_solves),
                            "refinement_sweeps": int(n_refine), "restart": a.restart, "inner_rtol": a.inner_rtol,
+                           "refine_floor": float(os.environ.get("EF_REFINE_FLOOR", "1e-2")),
                            "preconditioner_setup_ms": setup_ms},
         "dof_iterations_per_s": info.nDof * fg_it / (fg_kms * 1e-3) if fg_kms > 0 else None,
         "setup_s": setup_s,
